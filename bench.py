@@ -1,0 +1,390 @@
+"""PBSM3D step throughput on GB300: element-steps per second.
+
+One "step" is one PBSM3D timestep (PBSM3D::run) over the 1M-face x 10-layer
+synthetic mesh: saltation and layer coefficients, sliced-ELL assembly of the
+suspension system, its Krylov solve to relative residual 1e-8, the column
+post, the deposition system and its solve, the erosion/deposition update.
+An element-step is one face advanced one timestep.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: device-resident forcing (uploaded before the timed region), K steps
+timed with CUDA events on the library's stream, barrier + synchronize on both
+sides, max over ranks.  e2e: the same K steps through the C ABI with host
+(pinned) forcing and host outputs, copies inside the timed region.
+--impl reference: the CPU restatement of the reference (oracle, GMRES(30) +
+ILUT, tol 1e-8) on this machine's host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from chm_gb300 import capi, synth  # noqa: E402
+
+METRIC = "PBSM3D elem-steps/sec (1M tris, 10 layers); learned vs plain at same residual"
+UNIT = "elem-steps/s"
+FALLBACK_HBM = 6800.0
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (gloo on the host: the step has
+    no data-path collective; ranks are independent replicas)."""
+
+    def __init__(self, world: int):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM, "fallback"
+
+
+class ClockSampler:
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        for r in rows:
+            for idx, name in ((5, "hw_slowdown"), (6, "hw_thermal_slowdown"), (7, "sw_thermal_slowdown"),
+                              (8, "sw_power_cap")):
+                if r[idx].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def make_workload(args, rank: int):
+    cfg = synth.CONFIGS[args.config]
+    seed = args.seed + rank  # replicas: one independent member per rank
+    w = synth.Workload(cfg["n_points"], cfg["side"], seed=seed, wind_scale=args.wind)
+    return w, cfg["nLayer"]
+
+
+def forcing_desc(arrs: dict, on_device: int, keep: list):
+    f = capi.ForcingDesc()
+    for k, a in arrs.items():
+        if on_device:
+            setattr(f, k, C.cast(C.c_void_p(a.data_ptr()), C.POINTER(C.c_double)))
+        else:
+            setattr(f, k, capi.ptr(a))
+        keep.append(a)
+    f.on_device = on_device
+    return f
+
+
+def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
+    import torch
+    torch.cuda.set_device(local_rank)
+    lib = capi.load()
+    w, L = make_workload(args, rank)
+    T = w.mesh.n_faces
+    nsteps = args.warmup + args.steps
+    host_forcing = [w.forcing(s).arrays() for s in range(nsteps)]
+    keep = []
+    desc = capi.mesh_desc(w.mesh, keep)
+    cfg = capi.default_config(lib, nLayer=L, precision=capi.MIXED if args.precision == "mixed" else capi.FP64)
+    ctx = C.c_void_p()
+    rc = lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx))
+    if rc != 0:
+        raise RuntimeError(lib.pbsm3d_last_error(None).decode())
+    lib.pbsm3d_set_profiling(ctx, 1)
+    # device-resident forcing for every step, uploaded before timing
+    dev_forcing = [{k: torch.from_numpy(a).cuda() for k, a in fs.items()} for fs in host_forcing]
+    out_names = ("Qsalt", "Qsusp", "Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "sum_drift",
+                 "pbsm_more_than_avail", "blowingsnow_probability")
+    dev_out = {k: torch.empty(T, dtype=torch.float64, device="cuda") for k in out_names}
+    o_dev = capi.Outputs()
+    for k, t in dev_out.items():
+        setattr(o_dev, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+    o_dev.on_device = 1
+    torch.cuda.synchronize()
+    st = capi.Stats()
+
+    def step(fdesc, odesc):
+        r = lib.pbsm3d_step(ctx, C.byref(fdesc), 3600.0, C.byref(odesc), C.byref(st))
+        if r != 0:
+            raise RuntimeError(f"pbsm3d_step {capi.STATUS_NAMES.get(r)}: {lib.pbsm3d_last_error(ctx).decode()}")
+        return st.as_dict()
+
+    fdescs = [forcing_desc(d, 1, keep) for d in dev_forcing]
+    for s in range(args.warmup):
+        step(fdescs[s], o_dev)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.3)
+    stats = []
+    dist.barrier()
+    torch.cuda.synchronize()
+    lib.pbsm3d_timer_mark(ctx, 0)
+    t0 = time.perf_counter()
+    for s in range(args.warmup, nsteps):
+        stats.append(step(fdescs[s], o_dev))
+    lib.pbsm3d_timer_mark(ctx, 1)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clocks = sampler.stop()
+    ms = C.c_double()
+    lib.pbsm3d_timer_elapsed(ctx, 0, 1, C.byref(ms))
+    t_dev = ms.value / 1000.0
+    t_max = dist.max(t_dev)
+    faces_total = dist.sum(float(T * args.steps))
+
+    # ---- e2e: host pinned forcing in, host outputs back, copies timed
+    pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in fs.items()} for fs in host_forcing]
+    pin_out = {k: torch.empty(T, dtype=torch.float64).pin_memory() for k in out_names}
+    o_host = capi.Outputs()
+    for k, t in pin_out.items():
+        setattr(o_host, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+    o_host.on_device = 0
+    hdescs = []
+    for d in pin_f:
+        f = capi.ForcingDesc()
+        for k, t in d.items():
+            setattr(f, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+        f.on_device = 0
+        hdescs.append(f)
+    step(hdescs[0], o_host)
+    dist.barrier()
+    torch.cuda.synchronize()
+    lib.pbsm3d_timer_mark(ctx, 2)
+    e2e_stats = []
+    for s in range(args.warmup, nsteps):
+        e2e_stats.append(step(hdescs[s], o_host))
+    lib.pbsm3d_timer_mark(ctx, 3)
+    torch.cuda.synchronize()
+    lib.pbsm3d_timer_elapsed(ctx, 2, 3, C.byref(ms))
+    t_e2e = dist.max(ms.value / 1000.0)
+    dist.barrier()
+    h2d = 8 * T * len(host_forcing[0])
+    d2h = 8 * T * len(out_names)
+
+    # ---- roofline of the dominant kernel class (events around each launch)
+    kern_ms = np.sum([s["kern_ms"] for s in stats], axis=0)
+    kern_bytes = np.sum([s["kern_bytes"] for s in stats], axis=0)
+    kern_n = np.sum([s["kern_launches"] for s in stats], axis=0)
+    top = int(np.argmax(kern_ms))
+    peak, peak_kind = measured_peak()
+    achieved = float(kern_bytes[top]) / (float(kern_ms[top]) / 1e3) / 1e9 if kern_ms[top] > 0 else 0.0
+    traffic = None
+    prof_file = ROOT / "profiles" / "traffic.json"
+    if prof_file.exists():
+        try:
+            tr = json.loads(prof_file.read_text())
+            key = f"{capi.KERNELS[top]}:{args.config}:{args.precision}"
+            if key in tr:
+                traffic = tr[key]
+        except Exception:
+            traffic = None
+    total_ms = float(np.sum(kern_ms))
+    kernels = {capi.KERNELS[k]: {"ms": round(float(kern_ms[k]), 3), "launches": int(kern_n[k]),
+                                 "GBps": round(float(kern_bytes[k]) / (float(kern_ms[k]) / 1e3) / 1e9, 1)
+                                 if kern_ms[k] > 0 else None,
+                                 "share": round(float(kern_ms[k]) / total_ms, 4) if total_ms > 0 else None}
+               for k in range(len(capi.KERNELS)) if kern_n[k] > 0}
+    alg_bytes = float(np.sum([s["bytes_moved"] for s in stats]))
+    lib.pbsm3d_destroy(ctx)
+
+    res = {
+        "metric": METRIC, "value": faces_total / t_max, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+f32",
+        "data": "synthetic (seeded Delaunay mesh and forcing of the reference's benchmark shape)",
+        "config": {"workload": f"{args.config}: {T} faces x {L} layers, hourly steps, Weibull wind scale "
+                               f"{args.wind} m/s, seed {args.seed}+rank",
+                   "faces": T, "layers": L, "precision": args.precision,
+                   "solver": "BiCGStab, column-Thomas right preconditioner, rel. residual 1e-8; deposition CG 1e-12",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "working set larger than L2 (no flush needed)"},
+        "e2e": {"value": faces_total / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(s["gpu_launches"] for s in stats)),
+        "roofline": {"bound": "hbm", "kernel": capi.KERNELS[top], "achieved": round(achieved, 1),
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic},
+        "step_roofline": {"alg_GB_per_step": round(alg_bytes / args.steps / 1e9, 3),
+                          "achieved_GBps": round(alg_bytes / t_dev / 1e9, 1),
+                          "frac": round(alg_bytes / t_dev / 1e9 / peak, 4)},
+        "kernels": kernels,
+        "solver": {"susp_iters_mean": float(np.mean([s["susp_iters"] for s in stats])),
+                   "dep_iters_mean": float(np.mean([s["dep_iters"] for s in stats])),
+                   "susp_rel_residual_max": float(np.max([s["susp_rel_residual"] for s in stats])),
+                   "ms_coefficients": float(np.mean([s["ms_coefficients"] for s in stats])),
+                   "ms_susp_solve": float(np.mean([s["ms_susp_solve"] for s in stats])),
+                   "ms_dep_solve": float(np.mean([s["ms_dep_solve"] for s in stats]))},
+        "wall_s": wall,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(w, L, args)
+    return res
+
+
+def cpu_baseline(w, L, args) -> dict:
+    """The oracle (C++ restatement of the reference, GMRES(30)+ILUT, tol 1e-8)
+    timed on this host's cores over one step of the same workload."""
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    from oracle import pyoracle
+    o = pyoracle.Oracle(w.mesh, nLayer=L, solver={"nblocks": cores})
+    f = w.forcing(args.warmup)
+    t0 = time.perf_counter()
+    _, st = o.step(f, 3600.0, want_c=False)
+    dt = time.perf_counter() - t0
+    o.close()
+    T = w.mesh.n_faces
+    return {"value": T / dt, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)), "kind": "port",
+            "sample": f"1 step of the same {T}-face x {L}-layer workload ({dt:.1f} s; GMRES(30)+ILUT over "
+                      f"{cores} blocks, {st['susp_iters']} suspension iterations)"}
+
+
+def run_reference(args, rank: int, world: int) -> dict | None:
+    if rank != 0:
+        return None
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    from oracle import pyoracle
+    w, L = make_workload(args, 0)
+    T = w.mesh.n_faces
+    o = pyoracle.Oracle(w.mesh, nLayer=L, solver={"nblocks": cores})
+    budget = args.ref_budget
+    for s in range(min(args.warmup, 1)):
+        o.step(w.forcing(s), 3600.0, want_c=False)
+    t0 = time.perf_counter()
+    done = 0
+    iters = []
+    for s in range(args.steps):
+        _, st = o.step(w.forcing(args.warmup + s), 3600.0, want_c=False)
+        iters.append(st["susp_iters"])
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    v = T * done / dt
+    sample = (f"{done} of {args.steps} steps of the {T}-face x {L}-layer workload ({dt:.1f} s, "
+              f"GMRES(30)+ILUT over {cores} blocks, mean {np.mean(iters):.1f} suspension iterations)")
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1),
+            "ms_per_step": dt / done * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{args.config}: {T} faces x {L} layers, hourly steps", "faces": T, "layers": L},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg2", choices=sorted(synth.CONFIGS))
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--wind", type=float, default=8.0)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--ref-budget", type=float, default=120.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+        if res is not None:
+            print(json.dumps(res))
+        return
+    dist = Dist(world)
+    res = run_ours(args, dist, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,734 @@
+// capi.cu -- the extern "C" boundary of libpbsm3d_cuda (declared in
+// include/pbsm3d.h): context creation (PBSM3D::PBSM3D + init + the two
+// NearestNeighborProblem constructors), the step (PBSM3D::run) and the
+// checkpoint state.  The step never falls back to the CPU: a missing or
+// failing GPU is an error returned to the caller.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pbsm3d_internal.cuh"
+
+using namespace pbsm;
+
+struct pbsm3d_ctx {
+    Ctx c;
+};
+
+static thread_local std::string g_create_error;
+
+namespace pbsm {
+
+void prof_begin(Ctx& c, cudaStream_t s) {
+    c.launches++;
+    if (!c.prof) return;
+    if ((size_t)(2 * c.pused + 2) > c.pev.size()) {
+        size_t old = c.pev.size();
+        c.pev.resize(std::max<size_t>(256, old * 2));
+        for (size_t k = old; k < c.pev.size(); ++k) cudaEventCreate(&c.pev[k]);
+    }
+    cudaEventRecord(c.pev[2 * c.pused], s);
+}
+
+void prof_end(Ctx& c, cudaStream_t s, int cat, int64_t bytes) {
+    c.bytes += bytes;
+    if (c.prof) cudaEventRecord(c.pev[2 * c.pused + 1], s);
+    if ((int)c.pcat.size() <= c.pused) {
+        c.pcat.resize(c.pused + 64);
+        c.pbytes.resize(c.pused + 64);
+    }
+    c.pcat[c.pused] = cat;
+    c.pbytes[c.pused] = bytes;
+    c.pused++;
+}
+
+// The last n launches returned at once (the solve had converged): their
+// bytes and event records are removed.
+void prof_drop(Ctx& c, int n) {
+    for (int k = 0; k < n && c.pused > 0; ++k) {
+        c.pused--;
+        c.bytes -= c.pbytes[c.pused];
+    }
+}
+
+}  // namespace pbsm
+
+namespace {
+
+template <typename T>
+T* dalloc(Ctx& c, size_t n, bool& ok) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        ok = false;
+        return nullptr;
+    }
+    c.allocations.push_back(p);
+    return static_cast<T*>(p);
+}
+
+void free_all(Ctx& c) {
+    for (void* p : c.allocations) cudaFree(p);
+    c.allocations.clear();
+    for (auto& e : c.pev) cudaEventDestroy(e);
+    c.pev.clear();
+    for (auto& e : c.ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c.user_ev)
+        if (e) cudaEventDestroy(e);
+    if (c.sc_host) cudaFreeHost(c.sc_host);
+    c.sc_host = nullptr;
+    if (c.stream) cudaStreamDestroy(c.stream);
+    c.stream = nullptr;
+}
+
+// SoA [3][Tp] from row-major [n][3]
+template <typename T>
+void to_soa3(const T* src, int64_t n, int64_t Tp, std::vector<T>& dst, T pad) {
+    dst.assign(3 * Tp, pad);
+    for (int64_t i = 0; i < n; ++i)
+        for (int j = 0; j < 3; ++j) dst[j * Tp + i] = src[3 * i + j];
+}
+
+int upload(Ctx& c, void* dst, const void* src, size_t bytes) {
+    PBSM_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c.stream));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pbsm3d_config_defaults(pbsm3d_config* cfg) {
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->abi_version = PBSM3D_ABI_VERSION;
+    cfg->nLayer = 10;
+    cfg->do_fixed_settling = 0;
+    cfg->do_sublimation = 1;
+    cfg->do_lateral_diff = 1;
+    cfg->rouault_diffusion_coef = 0;
+    cfg->enable_veg = 1;
+    cfg->iterative_subl = 0;
+    cfg->use_exp_fetch = 0;
+    cfg->use_tanh_fetch = 1;
+    cfg->use_PomLi_probability = 0;
+    cfg->z0_ustar_coupling = 0;
+    cfg->use_subgrid_topo = 0;
+    cfg->use_subgrid_topo_V2 = 0;
+    cfg->use_R94_lambda = 1;
+    cfg->debug_output = 0;
+    cfg->settling_velocity = 0.5;
+    cfg->smooth_coeff = 820;
+    cfg->min_sd_trans = 0.1;
+    cfg->cutoff = 0.3;
+    cfg->snow_diffusion_const = 0.3;
+    cfg->ustar_th_scale = 1.0;
+    cfg->z0_snow = 0.01;
+    cfg->settling_scale = 1.0;
+    cfg->solver = PBSM3D_SOLVER_BICGSTAB;
+    cfg->precision = PBSM3D_FP64;
+    cfg->warm_start = PBSM3D_X0_ZERO;
+    cfg->gmres_restart = 30;
+    cfg->susp_maxit = 1000;
+    cfg->dep_maxit = 1000;
+    cfg->susp_tol = 1e-8;
+    cfg->dep_tol = 1e-12;
+    cfg->inner_tol = 1e-5;
+    cfg->slice_width = 0;
+}
+
+const char* pbsm3d_last_error(const pbsm3d_ctx* ctx) {
+    return ctx ? ctx->c.err.c_str() : g_create_error.c_str();
+}
+
+int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbsm3d_ctx** out) {
+    if (!out) return PBSM3D_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (!mesh || !cfg_in) {
+        g_create_error = "null mesh or config";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    const pbsm3d_config& cfg = *cfg_in;
+    if (cfg.abi_version != PBSM3D_ABI_VERSION) {
+        g_create_error = "config abi_version mismatch (use pbsm3d_config_defaults)";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (mesh->n_faces <= 0 || mesh->n_faces > (int64_t)INT32_MAX / 2 || !mesh->neighbor || !mesh->edge_length ||
+        !mesh->edge_normal || !mesh->area || !mesh->center) {
+        g_create_error = "invalid mesh description";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (cfg.use_exp_fetch && cfg.use_tanh_fetch) {  // PBSM3D.cpp:132-135
+        g_create_error = "PBSM3d: Cannot specify both exp_fetch and tanh_fetch";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (!(cfg.settling_velocity >= 0)) {  // PBSM3D.cpp:237-240
+        g_create_error = "PBSM3D settling velocity must be positive";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (cfg.nLayer < 1 || cfg.nLayer > kMaxLayers) {
+        g_create_error = "nLayer must be in [1, 64]";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (cfg.iterative_subl || cfg.z0_ustar_coupling || cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2 ||
+        cfg.debug_output) {
+        g_create_error =
+            "iterative_subl, z0_ustar_coupling, use_subgrid_topo(_V2) and debug_output are not implemented";
+        return PBSM3D_ERR_UNSUPPORTED;
+    }
+    if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {
+        g_create_error = "only the BiCGStab suspension solver is implemented";
+        return PBSM3D_ERR_UNSUPPORTED;
+    }
+    if (cfg.warm_start != PBSM3D_X0_ZERO && cfg.warm_start != PBSM3D_X0_PREVIOUS) {
+        g_create_error = "learned warm start needs pbsm3d_set_mlp support";
+        return PBSM3D_ERR_UNSUPPORTED;
+    }
+    if (!(cfg.susp_tol > 0) || !(cfg.dep_tol > 0) || cfg.susp_maxit < 1 || cfg.dep_maxit < 1 ||
+        (cfg.precision == PBSM3D_MIXED && !(cfg.inner_tol > 0 && cfg.inner_tol < 1))) {
+        g_create_error = "invalid solver tolerance or iteration limit";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    const int64_t T = mesh->n_faces;
+    for (int64_t k = 0; k < 3 * T; ++k) {
+        const int32_t nb = mesh->neighbor[k];
+        if (nb < -1 || nb >= T || nb == k / 3) {
+            g_create_error = "neighbour index out of range at face " + std::to_string(k / 3);
+            return PBSM3D_ERR_BAD_MESH;
+        }
+    }
+    for (int64_t i = 0; i < T; ++i)
+        if (!(mesh->area[i] > 0) || !isfinite(mesh->area[i])) {
+            g_create_error = "face " + std::to_string(i) + " has a non-positive or non-finite area";
+            return PBSM3D_ERR_BAD_MESH;
+        }
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) {
+        g_create_error = "no CUDA device";
+        return PBSM3D_ERR_CUDA;
+    }
+
+    auto* h = new (std::nothrow) pbsm3d_ctx();
+    if (!h) return PBSM3D_ERR_OUT_OF_MEMORY;
+    Ctx& c = h->c;
+    c.cfg = cfg;
+    const int L = cfg.nLayer;
+    const int64_t Tp = (T + 255) / 256 * 256;
+    const int64_t R = Tp * L;
+    Params& P = c.P;
+    P.T = T;
+    P.Tp = Tp;
+    P.R = R;
+    P.L = L;
+    P.dz = 5.0 / (double)L;  // susp_depth / nLayer, PBSM3D.cpp:225-226
+    P.dt = 0;
+    P.use_exp_fetch = cfg.use_exp_fetch;
+    P.use_tanh_fetch = cfg.use_tanh_fetch;
+    P.use_PomLi = cfg.use_PomLi_probability;
+    P.use_R94_lambda = cfg.use_R94_lambda;
+    bool all_veg = mesh->canopy_height != nullptr;
+    if (all_veg && mesh->has_vegetation)
+        for (int64_t i = 0; i < T; ++i) all_veg = all_veg && mesh->has_vegetation[i];
+    P.enable_veg = cfg.enable_veg && all_veg;  // PBSM3D.cpp:283-325
+    P.do_fixed_settling = cfg.do_fixed_settling;
+    P.do_sublimation = cfg.do_sublimation;
+    P.do_lateral_diff = cfg.do_lateral_diff;
+    P.rouault = cfg.rouault_diffusion_coef;
+    P.settling_velocity = cfg.settling_velocity;
+    P.eps = cfg.smooth_coeff;
+    P.min_sd_trans = cfg.min_sd_trans;
+    P.cutoff = cfg.cutoff;
+    P.snow_diffusion_const = cfg.snow_diffusion_const;
+    P.uth_scale = cfg.ustar_th_scale;
+    P.z0_snow = cfg.z0_snow;
+    P.settling_scale = cfg.settling_scale;
+    P.cos_pi_4 = cos(M_PI / 4.0);
+    {
+        const double fetch_ref = 300;
+        P.Lc_tanh = 0.5 * tanh(0.1333333333e-1 * fetch_ref - 2.0) + 0.5;
+    }
+    P.log_2_0002 = log(2.0 / 0.0002);
+    P.log_zur_z0 = log(50.0 / cfg.z0_snow);
+    P.mixed = cfg.precision == PBSM3D_MIXED;
+
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+    c.grid_faces = (int)std::max<int64_t>(1, std::min<int64_t>((Tp + kBlock - 1) / kBlock, (int64_t)sms * 8));
+    c.grid_rows = c.grid_faces;
+    c.red.nblocks = c.grid_faces;
+
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "cudaStreamCreate failed";
+        delete h;
+        return PBSM3D_ERR_CUDA;
+    }
+    for (auto& e : c.ev) cudaEventCreate(&e);
+    for (auto& e : c.user_ev) cudaEventCreate(&e);
+    if (cudaMallocHost(&c.sc_host, sizeof(Scalars)) != cudaSuccess) {
+        g_create_error = "cudaMallocHost failed";
+        free_all(c);
+        delete h;
+        return PBSM3D_ERR_OUT_OF_MEMORY;
+    }
+
+    bool ok = true;
+    Faces& F = c.F;
+    F.nbr = dalloc<int32_t>(c, 3 * Tp, ok);
+    F.E = dalloc<double>(c, 3 * Tp, ok);
+    F.mx = dalloc<double>(c, 3 * Tp, ok);
+    F.my = dalloc<double>(c, 3 * Tp, ok);
+    F.area = dalloc<double>(c, Tp, ok);
+    F.zc = dalloc<double>(c, Tp, ok);
+    F.dxn = dalloc<double>(c, 3 * Tp, ok);
+    F.canopy = dalloc<double>(c, Tp, ok);
+    F.lai = dalloc<double>(c, Tp, ok);
+    F.stalkN = dalloc<double>(c, Tp, ok);
+    F.stalkD = dalloc<double>(c, Tp, ok);
+    F.water = dalloc<uint8_t>(c, Tp, ok);
+    Forcing& Fo = c.Fo;
+    double* fbuf = dalloc<double>(c, 9 * Tp, ok);
+    if (ok) {
+        Fo.UR = fbuf;
+        Fo.U2 = fbuf + Tp;
+        Fo.dir = fbuf + 2 * Tp;
+        Fo.swe = fbuf + 3 * Tp;
+        Fo.t = fbuf + 4 * Tp;
+        Fo.rh = fbuf + 5 * Tp;
+        Fo.sd = fbuf + 6 * Tp;
+        Fo.fetch = fbuf + 7 * Tp;
+        Fo.psh = fbuf + 8 * Tp;
+    }
+    FaceState& S = c.S;
+    S.saltation = dalloc<uint8_t>(c, Tp, ok);
+    double* sbuf = dalloc<double>(c, 9 * Tp, ok);
+    if (ok) {
+        S.Qsalt = sbuf;
+        S.Qsusp = sbuf + Tp;
+        S.Qsubl = sbuf + 2 * Tp;
+        S.Qsubl_mass = sbuf + 3 * Tp;
+        S.sum_subl = sbuf + 4 * Tp;
+        S.drift_mass = sbuf + 5 * Tp;
+        S.sum_drift = sbuf + 6 * Tp;
+        S.more = sbuf + 7 * Tp;
+        S.bsp = sbuf + 8 * Tp;
+    }
+    Susp& A = c.A;
+    A.band = dalloc<double>(c, 6 * R, ok);
+    A.rhs = dalloc<double>(c, R, ok);
+    A.x = dalloc<double>(c, R, ok);
+    A.u_z = dalloc<double>(c, R, ok);
+    A.csubl = dalloc<double>(c, R, ok);
+    A.fac_l = dalloc<double>(c, R, ok);
+    A.fac_ib = dalloc<double>(c, R, ok);
+    c.r = dalloc<double>(c, R, ok);
+    if (P.mixed) {
+        A.lat32 = dalloc<float>(c, 3 * R, ok);
+        A.l32 = dalloc<float>(c, R, ok);
+        A.ib32 = dalloc<float>(c, R, ok);
+        A.up32 = dalloc<float>(c, R, ok);
+        c.r32 = dalloc<float>(c, R, ok);
+        c.rh32 = dalloc<float>(c, R, ok);
+        c.p32 = dalloc<float>(c, R, ok);
+        c.v32 = dalloc<float>(c, R, ok);
+        c.s32 = dalloc<float>(c, R, ok);
+        c.t32 = dalloc<float>(c, R, ok);
+        c.zp32 = dalloc<float>(c, R, ok);
+        c.zs32 = dalloc<float>(c, R, ok);
+        c.x32 = dalloc<float>(c, R, ok);
+    } else {
+        c.rh = dalloc<double>(c, R, ok);
+        c.p = dalloc<double>(c, R, ok);
+        c.v = dalloc<double>(c, R, ok);
+        c.sv = dalloc<double>(c, R, ok);
+        c.tv = dalloc<double>(c, R, ok);
+        c.zp = dalloc<double>(c, R, ok);
+        c.zs = dalloc<double>(c, R, ok);
+    }
+    Dep& D = c.D;
+    D.diag = dalloc<double>(c, Tp, ok);
+    D.off = dalloc<double>(c, 3 * Tp, ok);
+    D.dinv = dalloc<double>(c, Tp, ok);
+    D.rhs = dalloc<double>(c, Tp, ok);
+    D.x = dalloc<double>(c, Tp, ok);
+    c.dr = dalloc<double>(c, Tp, ok);
+    c.dz_ = dalloc<double>(c, Tp, ok);
+    c.dp = dalloc<double>(c, Tp, ok);
+    c.dq = dalloc<double>(c, Tp, ok);
+    c.sc = dalloc<Scalars>(c, 4, ok);
+    c.red.partials = dalloc<double>(c, (size_t)8 * c.red.nblocks, ok);
+    c.ledger = dalloc<double>(c, 8, ok);
+    if (!ok) {
+        g_create_error = "out of device memory for " + std::to_string(T) + " faces x " + std::to_string(L) + " layers";
+        free_all(c);
+        delete h;
+        return PBSM3D_ERR_OUT_OF_MEMORY;
+    }
+
+    // ---- pack the mesh (PBSM3D.cpp:278-392) into SoA
+    int rc = 0;
+    std::vector<int32_t> nb;
+    to_soa3<int32_t>(mesh->neighbor, T, Tp, nb, -1);
+    std::vector<double> E, mx(3 * Tp, 0.0), my(3 * Tp, 0.0), tmp(Tp, 0.0), cx(Tp, 0.0), cy(Tp, 0.0);
+    to_soa3<double>(mesh->edge_length, T, Tp, E, 0.0);
+    for (int64_t i = 0; i < T; ++i)
+        for (int j = 0; j < 3; ++j) {
+            mx[j * Tp + i] = mesh->edge_normal[6 * i + 2 * j];
+            my[j * Tp + i] = mesh->edge_normal[6 * i + 2 * j + 1];
+        }
+    rc |= upload(c, F.nbr, nb.data(), nb.size() * 4);
+    rc |= upload(c, F.E, E.data(), E.size() * 8);
+    rc |= upload(c, F.mx, mx.data(), mx.size() * 8);
+    rc |= upload(c, F.my, my.data(), my.size() * 8);
+    std::vector<double> area(Tp, 1.0), zc(Tp, 0.0);
+    for (int64_t i = 0; i < T; ++i) {
+        area[i] = mesh->area[i];
+        cx[i] = mesh->center[3 * i];
+        cy[i] = mesh->center[3 * i + 1];
+        zc[i] = mesh->center[3 * i + 2];
+    }
+    rc |= upload(c, F.area, area.data(), Tp * 8);
+    rc |= upload(c, F.zc, zc.data(), Tp * 8);
+    std::vector<double> canopy(Tp, 0.0), lai(Tp, 0.0), sN(Tp, 0.0), sD(Tp, 0.0);
+    if (P.enable_veg)
+        for (int64_t i = 0; i < T; ++i) {
+            canopy[i] = mesh->canopy_height[i];
+            if (cfg.use_R94_lambda) {
+                lai[i] = mesh->lai ? mesh->lai[i] : 0.0;
+            } else {
+                sN[i] = mesh->stalk_number ? mesh->stalk_number[i] : 1.0;
+                sD[i] = mesh->stalk_diameter ? mesh->stalk_diameter[i] : 0.8;
+            }
+        }
+    rc |= upload(c, F.canopy, canopy.data(), Tp * 8);
+    rc |= upload(c, F.lai, lai.data(), Tp * 8);
+    rc |= upload(c, F.stalkN, sN.data(), Tp * 8);
+    rc |= upload(c, F.stalkD, sD.data(), Tp * 8);
+    std::vector<uint8_t> water(Tp, 0);
+    if (mesh->is_water)
+        for (int64_t i = 0; i < T; ++i) water[i] = mesh->is_water[i] ? 1 : 0;
+    rc |= upload(c, F.water, water.data(), Tp);
+    rc |= upload(c, c.dr, cx.data(), Tp * 8);
+    rc |= upload(c, c.dz_, cy.data(), Tp * 8);
+    // module state: CHM face variables start at -9999, sum_drift/sum_subl at 0
+    std::vector<double> nanv(Tp, -9999.0), zero(Tp, 0.0);
+    rc |= upload(c, S.Qsalt, nanv.data(), Tp * 8);
+    rc |= upload(c, S.Qsusp, nanv.data(), Tp * 8);
+    rc |= upload(c, S.Qsubl, nanv.data(), Tp * 8);
+    rc |= upload(c, S.Qsubl_mass, nanv.data(), Tp * 8);
+    rc |= upload(c, S.sum_subl, zero.data(), Tp * 8);
+    rc |= upload(c, S.drift_mass, nanv.data(), Tp * 8);
+    rc |= upload(c, S.sum_drift, zero.data(), Tp * 8);
+    rc |= upload(c, S.more, nanv.data(), Tp * 8);
+    rc |= upload(c, S.bsp, nanv.data(), Tp * 8);
+    rc |= upload(c, Fo.fetch, std::vector<double>(Tp, 1000.0).data(), Tp * 8);
+    rc |= upload(c, Fo.psh, zero.data(), Tp * 8);
+    if (cudaMemsetAsync(c.sc, 0, 4 * sizeof(Scalars), c.stream) != cudaSuccess) rc = 1;
+    if (cudaMemsetAsync(A.x, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
+    if (configure_solver_kernels(c)) rc = 1;
+    launch_init_static(c, c.stream);
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = 1;
+    if (rc) {
+        g_create_error = "device upload failed: " + c.err;
+        free_all(c);
+        delete h;
+        return PBSM3D_ERR_CUDA;
+    }
+    c.launches = 0;
+    c.bytes = 0;
+    *out = h;
+    return 0;
+}
+
+void pbsm3d_destroy(pbsm3d_ctx* h) {
+    if (!h) return;
+    cudaStreamSynchronize(h->c.stream);
+    free_all(h->c);
+    delete h;
+}
+
+int pbsm3d_set_profiling(pbsm3d_ctx* h, int32_t on) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    h->c.prof = on != 0;
+    return 0;
+}
+
+int pbsm3d_timer_mark(pbsm3d_ctx* h, int32_t slot) {
+    if (!h || slot < 0 || slot >= 16) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    PBSM_CUDA_TRY(cudaEventRecord(c.user_ev[slot], c.stream));
+    return 0;
+}
+
+int pbsm3d_timer_elapsed(pbsm3d_ctx* h, int32_t a, int32_t b, double* ms) {
+    if (!h || !ms || a < 0 || a >= 16 || b < 0 || b >= 16) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    PBSM_CUDA_TRY(cudaEventSynchronize(c.user_ev[b]));
+    float f = 0;
+    PBSM_CUDA_TRY(cudaEventElapsedTime(&f, c.user_ev[a], c.user_ev[b]));
+    *ms = f;
+    return 0;
+}
+
+int pbsm3d_set_mlp(pbsm3d_ctx* h, const float*, const float*, const float*, const float*, const float*,
+                   const float*, const float*, const float*, const float*, const float*, float) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    h->c.err = "learned warm start is not built into this library version";
+    return PBSM3D_ERR_UNSUPPORTED;
+}
+
+static int copy_in(Ctx& c, double* dst, const double* src, int on_device) {
+    PBSM_CUDA_TRY(cudaMemcpyAsync(dst, src, c.P.T * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c.stream));
+    return 0;
+}
+static int copy_out(Ctx& c, double* dst, const double* src, int on_device) {
+    if (!dst) return 0;
+    PBSM_CUDA_TRY(cudaMemcpyAsync(dst, src, c.P.T * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                  c.stream));
+    return 0;
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_outputs* out, pbsm3d_stats* st) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    if (!f || !f->U_R || !f->U_2m_above_srf || !f->vw_dir || !f->swe || !f->t || !f->rh || !f->snowdepthavg) {
+        c.err = "missing forcing array";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if ((c.cfg.use_exp_fetch || c.cfg.use_tanh_fetch) && !f->fetch) {
+        c.err = "fetch forcing is required by use_exp_fetch/use_tanh_fetch";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (c.cfg.use_PomLi_probability && !f->p_snow_hours) {
+        c.err = "p_snow_hours forcing is required by use_PomLi_probability";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (!(dt > 0) || !isfinite(dt)) {
+        c.err = "dt must be positive";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    cudaStream_t s = c.stream;
+    c.P.dt = dt;
+    c.launches = 0;
+    c.bytes = 0;
+    c.pused = 0;
+    c.susp_iters = c.susp_matvecs = c.susp_refinements = c.dep_iters = 0;
+    c.susp_relres = c.dep_relres = 0;
+    int rc;
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[0], s));
+    const int dev = f->on_device;
+    if ((rc = copy_in(c, c.Fo.UR, f->U_R, dev)) || (rc = copy_in(c, c.Fo.U2, f->U_2m_above_srf, dev)) ||
+        (rc = copy_in(c, c.Fo.dir, f->vw_dir, dev)) || (rc = copy_in(c, c.Fo.swe, f->swe, dev)) ||
+        (rc = copy_in(c, c.Fo.t, f->t, dev)) || (rc = copy_in(c, c.Fo.rh, f->rh, dev)) ||
+        (rc = copy_in(c, c.Fo.sd, f->snowdepthavg, dev)))
+        return rc;
+    if (f->fetch && (rc = copy_in(c, c.Fo.fetch, f->fetch, dev))) return rc;
+    if (f->p_snow_hours && (rc = copy_in(c, c.Fo.psh, f->p_snow_hours, dev))) return rc;
+    const int64_t h2d = dev ? 0 : c.P.T * 8 * (7 + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
+
+    // warm start: keep the previous solution in A.x (assembly zeroes it otherwise)
+    double* x_keep = nullptr;
+    if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS) x_keep = c.r;  // stash x before the assembly resets it
+    if (x_keep) PBSM_CUDA_TRY(cudaMemcpyAsync(x_keep, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
+    launch_assemble_suspension(c, s);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[2], s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (c.sc_host->nan_flag != 0.0) {
+        c.err = "NaN in the assembled suspension system (check the forcing)";
+        return PBSM3D_ERR_NAN_INPUT;
+    }
+    const double susp_rhs_max = c.sc_host->rhs_max;
+    c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
+    if (c.suspension_present) {
+        if (x_keep) PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, x_keep, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+        rc = solve_suspension(c, s, st);
+        PBSM_CUDA_TRY(cudaGetLastError());
+        if (rc) return rc;
+    }
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[3], s));
+    launch_post_and_assemble_deposition(c, s);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[4], s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (c.sc_host->nan_flag != 0.0) {
+        c.err = "NaN in the assembled deposition system";
+        return PBSM3D_ERR_NAN_INPUT;
+    }
+    const double dep_rhs_max = c.sc_host->rhs_max;
+    c.deposition_present = c.suspension_present && dep_rhs_max > 1e-12;  // PBSM3D.cpp:1661-1664
+    if (c.deposition_present) {
+        rc = solve_deposition(c, s, st);
+        PBSM_CUDA_TRY(cudaGetLastError());
+        if (rc) return rc;
+    }
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[5], s));
+    launch_update(c, s);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[6], s));
+    int64_t d2h = 0;
+    if (out) {
+        const int od = out->on_device;
+        double* outs[9] = {out->Qsalt, out->Qsusp, out->Qsubl, out->Qsubl_mass, out->sum_subl,
+                           out->drift_mass, out->sum_drift, out->pbsm_more_than_avail, out->blowingsnow_probability};
+        const double* srcs[9] = {c.S.Qsalt, c.S.Qsusp, c.S.Qsubl, c.S.Qsubl_mass, c.S.sum_subl,
+                                 c.S.drift_mass, c.S.sum_drift, c.S.more, c.S.bsp};
+        for (int k = 0; k < 9; ++k) {
+            if ((rc = copy_out(c, outs[k], srcs[k], od))) return rc;
+            if (outs[k] && !od) d2h += c.P.T * 8;
+        }
+        if (out->c) {
+            // layer-major with stride n_faces (the device stride is the padded Tp)
+            PBSM_CUDA_TRY(cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L,
+                                            od ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+            if (!od) d2h += c.P.T * c.P.L * 8;
+        }
+    }
+    double ledger[8] = {0};
+    PBSM_CUDA_TRY(cudaMemcpyAsync(ledger, c.ledger, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaEventRecord(c.ev[7], s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st) {
+        memset(st, 0, sizeof(*st));
+        st->suspension_present = c.suspension_present;
+        st->deposition_present = c.deposition_present;
+        st->susp_iters = c.susp_iters;
+        st->susp_matvecs = c.susp_matvecs;
+        st->susp_refinements = c.susp_refinements;
+        st->dep_iters = c.dep_iters;
+        st->susp_rel_residual = c.susp_relres;
+        st->dep_rel_residual = c.dep_relres;
+        st->susp_rhs_max = susp_rhs_max;
+        st->dep_rhs_max = dep_rhs_max;
+        st->ms_coefficients = ev_ms(c.ev[1], c.ev[2]);
+        st->ms_susp_solve = ev_ms(c.ev[2], c.ev[3]);
+        st->ms_post = ev_ms(c.ev[3], c.ev[4]);
+        st->ms_dep_assembly = 0;
+        st->ms_dep_solve = ev_ms(c.ev[4], c.ev[5]);
+        st->ms_update = ev_ms(c.ev[5], c.ev[6]);
+        st->ms_total = ev_ms(c.ev[0], c.ev[7]);
+        if (c.deposition_present) {
+            st->ledger_divergence = ledger[0];
+            st->ledger_deposited = ledger[1];
+            st->ledger_clipped = ledger[2];
+            st->ledger_residual = ledger[3];
+        }
+        st->ledger_snow_mass = ledger[4];
+        st->bytes_moved = c.bytes + h2d + d2h;
+        st->gpu_launches = c.launches;
+        if (c.prof) {
+            st->profiled = 1;
+            for (int k = 0; k < c.pused; ++k) {
+                const int cat = c.pcat[k];
+                st->kern_ms[cat] += ev_ms(c.pev[2 * k], c.pev[2 * k + 1]);
+                st->kern_bytes[cat] += c.pbytes[k];
+                st->kern_launches[cat] += 1;
+            }
+        }
+    }
+    return 0;
+}
+
+int pbsm3d_get_state(pbsm3d_ctx* h, double* sum_drift, double* sum_subl, double* drift_mass, double* more) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    int rc;
+    if ((rc = copy_out(c, sum_drift, c.S.sum_drift, 0)) || (rc = copy_out(c, sum_subl, c.S.sum_subl, 0)) ||
+        (rc = copy_out(c, drift_mass, c.S.drift_mass, 0)) || (rc = copy_out(c, more, c.S.more, 0)))
+        return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int pbsm3d_set_state(pbsm3d_ctx* h, const double* sum_drift, const double* sum_subl, const double* drift_mass,
+                     const double* more) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    int rc;
+    if ((sum_drift && (rc = copy_in(c, c.S.sum_drift, sum_drift, 0))) ||
+        (sum_subl && (rc = copy_in(c, c.S.sum_subl, sum_subl, 0))) ||
+        (drift_mass && (rc = copy_in(c, c.S.drift_mass, drift_mass, 0))) ||
+        (more && (rc = copy_in(c, c.S.more, more, 0))))
+        return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+static int export_system(Ctx& c, int which, int32_t* cols, double* vals, double* rhs, double* x) {
+    const int64_t T = c.P.T, Tp = c.P.Tp;
+    const int L = which == 0 ? c.P.L : 1;
+    const int64_t R = which == 0 ? c.P.R : Tp;
+    std::vector<int32_t> nb(3 * Tp);
+    PBSM_CUDA_TRY(cudaMemcpy(nb.data(), c.F.nbr, 3 * Tp * 4, cudaMemcpyDeviceToHost));
+    std::vector<double> band, b(R), xv(R);
+    if (which == 0) {
+        band.resize(6 * R);
+        PBSM_CUDA_TRY(cudaMemcpy(band.data(), c.A.band, 6 * R * 8, cudaMemcpyDeviceToHost));
+        PBSM_CUDA_TRY(cudaMemcpy(b.data(), c.A.rhs, R * 8, cudaMemcpyDeviceToHost));
+        PBSM_CUDA_TRY(cudaMemcpy(xv.data(), c.A.x, R * 8, cudaMemcpyDeviceToHost));
+    } else {
+        band.assign(6 * R, 0.0);
+        PBSM_CUDA_TRY(cudaMemcpy(band.data(), c.D.diag, Tp * 8, cudaMemcpyDeviceToHost));
+        PBSM_CUDA_TRY(cudaMemcpy(band.data() + R, c.D.off, 3 * Tp * 8, cudaMemcpyDeviceToHost));
+        PBSM_CUDA_TRY(cudaMemcpy(b.data(), c.D.rhs, R * 8, cudaMemcpyDeviceToHost));
+        PBSM_CUDA_TRY(cudaMemcpy(xv.data(), c.D.x, R * 8, cudaMemcpyDeviceToHost));
+    }
+    for (int z = 0; z < L; ++z)
+        for (int64_t i = 0; i < T; ++i) {
+            const int64_t rr = z * T + i;   // reference row
+            const int64_t rd = z * Tp + i;  // device row
+            int k = 0;
+            auto put = [&](int64_t col, double v) {
+                if (cols) cols[6 * rr + k] = (int32_t)col;
+                if (vals) vals[6 * rr + k] = v;
+                ++k;
+            };
+            put(rr, band[rd]);
+            for (int j = 0; j < 3; ++j) {
+                const int32_t n = nb[j * Tp + i];
+                if (n >= 0) put(z * T + n, band[(1 + j) * R + rd]);
+            }
+            if (z > 0) put(rr - T, band[4 * R + rd]);
+            if (z < L - 1) put(rr + T, band[5 * R + rd]);
+            while (k < 6) {
+                if (cols) cols[6 * rr + k] = -1;
+                if (vals) vals[6 * rr + k] = 0.0;
+                ++k;
+            }
+            if (rhs) rhs[rr] = b[rd];
+            if (x) x[rr] = xv[rd];
+        }
+    return 0;
+}
+
+int pbsm3d_export_suspension(pbsm3d_ctx* h, int32_t* cols, double* vals, double* rhs, double* x) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(h->c.stream);
+    return export_system(h->c, 0, cols, vals, rhs, x);
+}
+
+int pbsm3d_export_deposition(pbsm3d_ctx* h, int32_t* cols, double* vals, double* rhs, double* x) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    cudaStreamSynchronize(h->c.stream);
+    return export_system(h->c, 1, cols, vals, rhs, x);
+}
+
+}  // extern "C"

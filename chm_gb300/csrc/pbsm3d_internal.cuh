@@ -1,0 +1,251 @@
+// pbsm3d_internal.cuh -- device data layout and kernel entry points of
+// libpbsm3d_cuda (sm_103a).
+//
+// HBM layout (all SoA, 256-byte aligned allocations):
+//   faces      i in [0, Tp), Tp = n_faces rounded up to a multiple of 256;
+//              faces >= n_faces are padding with identity rows.
+//   rows       r = z*Tp + i (layer-major, the reference's extruded ordering
+//              row = z*n_global + gid, LinearAlgebra.cpp:46-55, with a
+//              padded stride).  R = nLayer*Tp.
+//   suspension matrix: sliced ELL, one slice per layer, 6 slots per row
+//              stored slot-major: band[k*R + r], k = 0 diag, 1..3 lateral
+//              face 0..2, 4 below (z-1), 5 above (z+1).  Column indices are
+//              implicit: lateral = z*Tp + nbr[j*Tp + i], vertical = r -/+ Tp.
+//   column preconditioner: Thomas factors of each face's tridiagonal column
+//              fac_l[r] (forward multiplier), fac_ib[r] (1/pivot); the upper
+//              band is band 5.
+//   deposition matrix: dep_diag[Tp], dep_off[j*Tp + i] (j = 0..2).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pbsm3d.h"
+
+namespace pbsm {
+
+constexpr int kBlock = 256;
+constexpr int kMaxLayers = 64;
+constexpr int kMaxTerms = 4;
+
+// Configuration scalars every kernel sees (passed by value).
+struct Params {
+    int64_t T, Tp, R;
+    int L;
+    double dz, dt;
+    int use_exp_fetch, use_tanh_fetch, use_PomLi, use_R94_lambda, enable_veg;
+    int do_fixed_settling, do_sublimation, do_lateral_diff, rouault;
+    double settling_velocity, eps, min_sd_trans, cutoff, snow_diffusion_const;
+    double uth_scale, z0_snow, settling_scale;
+    // constants computed once on the host with the C library, the way the
+    // reference computes them (compile-time or libm): cos(pi/4), the tanh
+    // fetch factor, log(2/0.0002), log(50/z0).
+    double cos_pi_4, Lc_tanh, log_2_0002, log_zur_z0;
+    int mixed;
+};
+
+// Per-face static geometry (device pointers).
+struct Faces {
+    int32_t* nbr;     // [3][Tp]
+    double* E;        // [3][Tp]
+    double* mx;       // [3][Tp]
+    double* my;       // [3][Tp]
+    double* area;     // [Tp]
+    double* zc;       // [Tp] centroid elevation
+    double* dxn;      // [3][Tp] centroid distance to neighbour j
+    double* canopy;   // [Tp]
+    double* lai;
+    double* stalkN;
+    double* stalkD;
+    uint8_t* water;   // [Tp]
+};
+
+// Per-step forcing resident in HBM.
+struct Forcing {
+    double *UR, *U2, *dir, *swe, *t, *rh, *sd, *fetch, *psh;
+};
+
+// Per-face work/state.
+struct FaceState {
+    uint8_t* saltation;
+    double *Qsalt, *Qsusp, *Qsubl, *Qsubl_mass, *sum_subl, *drift_mass, *sum_drift, *more, *bsp;
+};
+
+// Suspension system.
+struct Susp {
+    double* band;     // [6][R]
+    double* rhs;      // [R]
+    double* x;        // [R]
+    double* u_z;      // [R]
+    double* csubl;    // [R]
+    double* fac_l;    // [R]
+    double* fac_ib;   // [R]
+    // MIXED: FP32 copies of the lateral bands and the column factors
+    float* lat32;     // [3][R]
+    float* l32;       // [R]
+    float* ib32;      // [R]
+    float* up32;      // [R]
+};
+
+// Deposition system.
+struct Dep {
+    double* diag;     // [Tp]
+    double* off;      // [3][Tp]
+    double* dinv;     // [Tp]
+    double* rhs;      // [Tp]
+    double* x;        // [Tp]
+};
+
+// Device scalars of one Krylov solve (one cache line each group).
+struct Scalars {
+    double rho, alpha, omega, beta;
+    double bnorm2, rnorm2, target2, tmp;
+    double rv, ts, tt, pq;
+    double rhs_max, nan_flag, red0, red1;
+    int iter, done, maxit, status;
+    unsigned counter[8];
+};
+
+// Reduction workspace: per-block partials.
+struct ReduceWs {
+    double* partials;  // [kMaxTerms][nblocks]
+    int nblocks;
+};
+
+struct Ctx;
+
+// physics.cu
+void launch_assemble_suspension(Ctx& c, cudaStream_t s);
+void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s);
+void launch_update(Ctx& c, cudaStream_t s);
+void launch_init_static(Ctx& c, cudaStream_t s);
+
+// solver.cu
+int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
+int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
+int configure_solver_kernels(Ctx& c);
+
+struct Ctx {
+    pbsm3d_config cfg;
+    Params P;
+    Faces F;
+    Forcing Fo;
+    FaceState S;
+    Susp A;
+    Dep D;
+    // Krylov work vectors (FP64), [R] each
+    double *r, *rh, *p, *v, *sv, *tv, *zp, *zs;
+    // FP32 work vectors for MIXED, [R] each
+    float *r32, *rh32, *p32, *v32, *s32, *t32, *zp32, *zs32, *x32;
+    // deposition CG vectors [Tp]
+    double *dr, *dz_, *dp, *dq;
+    // reductions
+    Scalars* sc;       // device
+    Scalars* sc_host;  // pinned mirror
+    ReduceWs red;
+    int grid_rows, grid_faces;
+    // ledger partial sums
+    double* ledger;    // device [8]
+    cudaStream_t stream;
+    cudaEvent_t ev[16];
+    cudaEvent_t user_ev[16];
+    std::vector<void*> allocations;
+    std::string err;
+    int launches;
+    int64_t bytes;
+    // per-launch profiling (pbsm3d_set_profiling)
+    bool prof = false;
+    std::vector<cudaEvent_t> pev;
+    std::vector<int> pcat;
+    std::vector<int64_t> pbytes;
+    int pused = 0;
+    double kern_ms[16];
+    int64_t kern_bytes[16];
+    int kern_launches[16];
+    bool suspension_present, deposition_present;
+    int susp_iters, susp_matvecs, susp_refinements, dep_iters;
+    double susp_relres, dep_relres;
+};
+
+// Record the start of a kernel launch of class cat with the given algorithmic
+// bytes (profiling only).  Every launch also adds its bytes to c.bytes.
+void prof_begin(Ctx& c, cudaStream_t s);
+void prof_end(Ctx& c, cudaStream_t s, int cat, int64_t bytes);
+// Forget the last n recorded launches (no-op launches after convergence).
+void prof_drop(Ctx& c, int n);
+
+#define PBSM_CUDA_TRY(expr)                                                           \
+    do {                                                                              \
+        cudaError_t e_ = (expr);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            c.err = std::string(#expr) + ": " + cudaGetErrorString(e_);               \
+            return PBSM3D_ERR_CUDA;                                                   \
+        }                                                                             \
+    } while (0)
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Deterministic block reduction of NT values (sum), result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ void block_sum(double (&v)[NT]) {
+    __shared__ double sh[NT][kBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        double w = warp_sum(v[k]);
+        if (lane == 0) sh[k][wid] = w;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            double w = lane < (int)(blockDim.x >> 5) ? sh[k][lane] : 0.0;
+            v[k] = warp_sum(w);
+        }
+    }
+    __syncthreads();
+}
+
+// Write this block's NT partials; the last block to arrive sums all partials
+// in a fixed order (deterministic) and returns true in every thread of that
+// block with the totals in tot[] (valid in thread 0 only).
+template <int NT>
+__device__ __forceinline__ bool block_partials_last(double (&v)[NT], double* partials, unsigned* counter,
+                                                    double (&tot)[NT]) {
+    block_sum<NT>(v);
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NT; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        is_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        double s = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(&partials[k * gridDim.x + b]);
+        tot[k] = s;
+    }
+    block_sum<NT>(tot);
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
+}  // namespace pbsm

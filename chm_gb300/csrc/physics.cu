@@ -1,0 +1,599 @@
+// physics.cu -- per-face physics and system assembly of the PBSM3D step.
+//
+// Compiled with --fmad=false: every multiply and add rounds separately, in
+// the order the reference writes them, so the assembled systems agree with
+// a C++ evaluation of src/modules/PBSM3D.cpp to the last few ulps (the only
+// differences left come from CUDA's pow/log/exp/sin/cos).
+#include <math.h>
+
+#include "pbsm3d_internal.cuh"
+
+namespace pbsm {
+namespace {
+
+constexpr double kKappa = 0.4;    // PhysConst.h:31
+constexpr double kRhoIce = 917;   // PhysConst.h:39
+constexpr double kZUR = 50.0;     // Atmosphere.h:31
+
+// module_base.hpp:471-479: -9999 or NaN
+__device__ __forceinline__ bool is_nan_chm(double v) { return fabs(v - -9999.0) < 1e-5 || isnan(v); }
+// std::max(a, b) == (a < b) ? b : a (NaN in b yields a)
+__device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+// Atmosphere.cpp:32-38
+__device__ __forceinline__ double log_scale_wind(double u, double Z_in, double Z_out, double sd, double z0) {
+    return u * log((Z_out - (sd + z0)) / z0) / log((Z_in - (sd + z0)) / z0);
+}
+
+// Atmosphere.cpp:62-80 (T in K against Tfreeze = 0: the water branch for any T > 0 K)
+__device__ __forceinline__ double saturated_vapour_pressure(double T) {
+    const double TA = T - 273.15;
+    if (T >= 0.) return 611.21 * exp((17.502 * TA) / (240.97 + TA));
+    return 611.15 * exp((22.452 * TA) / (272.55 + TA));
+}
+
+// coordinates.cpp:112-131
+__device__ __forceinline__ void bearing_to_cartesian(double bearing, double& x, double& y) {
+    double h = 450. - bearing;
+    if (h > 360.) h = h - 360.;
+    const double theta = h * M_PI / 180.;
+    sincos(theta, &y, &x);
+}
+
+// MeteoIO standard atmosphere (PBSM3D.cpp:785): p(z) / (R_dry T)
+__device__ __forceinline__ double std_dry_air_density(double altitude, double temperature) {
+    const double p0 = 101325., lapse = 0.0065, T0 = 288.15, Rd = 287.058, g = 9.80665, R0 = 6356766.0;
+    const double expo = g / (lapse * Rd);
+    const double p = p0 * pow(1. - ((lapse * R0 * altitude) / (T0 * (R0 + altitude))), expo);
+    return p / (287.058 * temperature);
+}
+
+// armadillo's 3-vector dot with a zero z on one side: (a0*b0 + a2*b2) + a1*b1
+__device__ __forceinline__ double dot2(double ax, double ay, double bx, double by) {
+    double v1 = 0, v2 = 0;
+    v1 += ax * bx;
+    v2 += ay * by;
+    return v1 + v2;
+}
+
+// One face: saltation (PBSM3D.cpp:417-925), layer coefficients (:927-1233),
+// suspension rows (:1236-1404) and the Thomas factorisation of its column.
+__global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces G, Forcing F, FaceState S, Susp A,
+                                                               double* partials, Scalars* sc) {
+    double vmax = 0.0, vnan = 0.0;
+    const int64_t Tp = P.Tp, R = P.R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= P.T) {  // padding face: identity rows
+            for (int z = 0; z < P.L; ++z) {
+                const int64_t r = (int64_t)z * Tp + i;
+                A.band[r] = 1.0;
+                for (int k = 1; k < 6; ++k) A.band[k * R + r] = 0.0;
+                A.rhs[r] = 0.0;
+                A.x[r] = 0.0;
+                A.u_z[r] = 0.0;
+                A.csubl[r] = 0.0;
+                A.fac_l[r] = 0.0;
+                A.fac_ib[r] = 1.0;
+                if (P.mixed) {
+                    for (int k = 0; k < 3; ++k) A.lat32[k * R + r] = 0.f;
+                    A.l32[r] = 0.f;
+                    A.ib32[r] = 1.f;
+                    A.up32[r] = 0.f;
+                }
+            }
+            continue;
+        }
+        // ---- saltation, PBSM3D.cpp:436-925
+        double fetch = 1000;
+        if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
+        const double min_sd_trans_avg = P.min_sd_trans;
+        const double uref = F.UR[i];
+        double snow_depth = F.sd[i];
+        snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
+        const double u2 = F.U2[i];
+        const double z10 = 10. + snow_depth;
+        double u10;
+        if (z10 < kZUR)
+            u10 = log_scale_wind(uref, kZUR, z10, snow_depth, P.z0_snow);
+        else
+            u10 = uref;
+        double swe = F.swe[i];
+        swe = is_nan_chm(swe) ? 0 : swe;
+        double height_diff = smax(0.0, G.canopy[i] - snow_depth);
+        if (!P.enable_veg) height_diff = 0;
+        double ustar = 1.3;
+        double lambda = 0;
+        bool saltation = false;
+        double z0 = 0;
+        const double T_c = F.t[i];
+        double uth = 0.35 + (1.0 / 150.0) * T_c + (1.0 / 8200.0) * T_c * T_c;
+        uth = uth * P.uth_scale;
+        const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
+        if (height_diff <= P.cutoff && snow_depth >= min_sd_trans_avg && !G.water[i]) {
+            if (P.use_R94_lambda)
+                lambda = 0.5 * G.lai[i] * height_diff;
+            else
+                lambda = stalkN * stalkD * height_diff;
+            ustar = u2 * kKappa / P.log_2_0002;
+            if (ustar >= uth) {
+                saltation = true;
+                z0 = P.z0_snow;
+            }
+        }
+        if (!saltation) {
+            z0 = P.z0_snow;
+            ustar = smax(0.01, kKappa * uref / P.log_zur_z0);
+        }
+        z0 = smax(P.z0_snow, z0);
+        ustar = smax(0.01, ustar);
+        double hs = 0;
+        if (saltation) hs = 0.08436 * pow(ustar, 1.27);
+        double Qsalt = 0;
+        double c_salt = 0;
+        const double t = F.t[i] + 273.15;
+        double vx, vy;
+        bearing_to_cartesian(F.dir[i], vx, vy);
+        const double ux = -vx, uy = -vy;
+        double mx[3], my[3], Ej[3], Af[3];
+        int32_t nb[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            mx[j] = G.mx[j * Tp + i];
+            my[j] = G.my[j * Tp + i];
+            Ej[j] = G.E[j * Tp + i];
+            nb[j] = G.nbr[j * Tp + i];
+            Af[j] = Ej[j] * P.dz;
+        }
+        const double area = G.area[i];
+        if (saltation) {
+            const double rho_f = std_dry_air_density(G.zc[i], t);
+            const double Beta = 202.0, mB = 0.16;
+            const double tau_n_ratio = (mB * Beta * lambda) / (1.0 + mB * Beta * lambda);
+            c_salt = rho_f / (3.29 * ustar) * (1.0 - tau_n_ratio - (uth * uth) / (ustar * ustar));
+            if (c_salt < 0 || isnan(c_salt)) {
+                c_salt = 0;
+                saltation = false;
+            }
+            if (P.use_exp_fetch && fetch < 500) {
+                const double fetch_ref = 500, mu = 3.0;
+                c_salt *= 1.0 - exp(-mu * fetch / fetch_ref);
+            } else if (P.use_tanh_fetch && fetch <= 300.) {
+                c_salt *= P.Lc_tanh;  // 0.5*tanh(0.01333*fetch_ref - 2)+0.5 with fetch_ref = 300
+            }
+            if (P.use_PomLi) {  // PBSM3D.cpp:848-865
+                const double Ah = F.psh[i];
+                const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
+                const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
+                const double z0v = (stalkN * stalkD * height_diff) / 2.0;
+                const double us = u10 / sqrt((1 + 340.0 * z0v));
+                const double Pu10 = 1.0 / (1.0 + exp((sqrt(M_PI) * (u_mean - us)) / delta));
+                S.bsp[i] = Pu10;
+                c_salt *= Pu10;
+            }
+            const double uhs = 2.8 * uth;
+            Qsalt = c_salt * uhs * hs;
+            double mass = 0;
+            for (int j = 0; j < 3; ++j) {
+                const double udm = dot2(ux, uy, mx[j], my[j]);
+                mass += -Ej[j] * Qsalt * udm;
+            }
+            mass = mass / area * P.dt;
+            if (mass < 0 && fabs(mass) > swe) {
+                c_salt = 0;
+                Qsalt = c_salt * uhs * hs;
+            }
+        }
+        S.Qsalt[i] = Qsalt;
+        S.saltation[i] = saltation;
+
+        // ---- layers, PBSM3D.cpp:927-1404
+        const double rh = F.rh[i] / 100.;
+        const double es = saturated_vapour_pressure(t);
+        const double D = 2.06e-5 * pow(t / 273.15, 1.75);
+        const double lambda_t = 0.000063 * t + 0.00673;
+        const double Ls = 2.838e6, M = 18.01, Rg = 8313;
+        const double rho = (M * es) / (Rg * t);
+        const double V5 = area * P.dz / 5.0;
+        double prev_up = 0.0, prev_beta = 1.0;
+        for (int z = 0; z < P.L; ++z) {
+            const double cz = z * P.dz + hs + P.dz / 2.;
+            double u_z;
+            const double hz = cz + snow_depth;
+            if (saltation && cz < height_diff)
+                u_z = 2.8 * uth;
+            else if (cz < height_diff)
+                u_z = 0.01;
+            else if (hz < kZUR)
+                u_z = smax(0.01, log_scale_wind(uref, kZUR, hz, snow_depth, z0));
+            else
+                u_z = smax(0.01, uref);
+            const double rm = 4.6e-5 * pow(cz, -0.258);
+            const double mm_alpha = 4.08 + 12.6 * cz;
+            const double mm =
+                4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 / mm_alpha + 2. / (mm_alpha * mm_alpha));
+            const double r_z = pow((3.0 * mm) / (4 * M_PI * kRhoIce), 0.3333333);
+            const double xrz = 0.005 * pow(u_z, 1.36);
+            double omega = P.settling_velocity;
+            if (!P.do_fixed_settling) omega = 1.1e7 * pow(r_z, 1.8);
+            omega = omega * P.settling_scale;
+            const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
+            const double Re = 2.0 * r_z * Vr / 1.88e-5;
+            const double Nu = 1.79 + 0.606 * pow(Re, 0.5);
+            const double Sh = Nu;
+            const double sigma = (rh - 1.0) * (1.019 + 0.027 * log(cz));
+            const double Qr = 0.9 * M_PI * rm * rm * 120.0;
+            const double dmdtz =
+                Sh * rho * D * (6.283185308 * Nu * Rg * r_z * sigma * t * t * lambda_t - Ls * M * Qr + Qr * Rg * t) /
+                (D * Ls * Sh * (Ls * M - Rg * t) * rho + lambda_t * t * t * Nu * Rg);
+            double csubl = dmdtz / mm;
+            double alpha[5] = {0, 0, 0, 0, 0};
+            if (P.do_lateral_diff)
+                for (int a = 0; a < 3; ++a) {
+                    alpha[a] = Af[a];
+                    alpha[a] *= 0.00001;
+                }
+            const double l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
+            const double w = omega;
+            double diffusion_coeff = P.snow_diffusion_const;
+            if (P.rouault) diffusion_coeff = 1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar));
+            const double K34 = diffusion_coeff * ustar * l;
+            alpha[3] = area * K34 / P.dz;
+            alpha[4] = area * K34 / P.dz;
+            // wind vector scaled to u_z, then w: uvw = (ux, uy) * (u_z / |u|), -w
+            double v1 = 0, v2 = 0;
+            v1 += ux * ux;
+            v2 += uy * uy;
+            const double s = u_z / sqrt(v1 + v2);
+            const double wx = ux * s, wy = uy * s;
+            double udm[5];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) udm[j] = dot2(wx, wy, mx[j], my[j]);
+            udm[3] = -w;  // uvw . (0,0,1)
+            udm[4] = w;   // uvw . (0,0,-1)
+            const int64_t r = (int64_t)z * Tp + i;
+            if (!P.do_sublimation) csubl = 0.0;
+            A.u_z[r] = u_z;
+            A.csubl[r] = csubl;
+            double dg = 0.0, lat[3] = {0, 0, 0}, lo = 0.0, up = 0.0, b = 0.0;
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                const bool has = nb[f] >= 0;
+                if (udm[f] > 0) {
+                    if (has) {
+                        dg += (V5 * csubl - Af[f] * udm[f] - alpha[f]);
+                        lat[f] += alpha[f];
+                    } else {
+                        dg += (-0.1e-1 * alpha[f] - 1. * Af[f] * udm[f] + csubl * V5);
+                    }
+                } else {
+                    if (has) {
+                        dg += V5 * csubl - alpha[f];
+                        lat[f] += -Af[f] * udm[f] + alpha[f];
+                    } else {
+                        dg += -0.1e-1 * alpha[f] - .99 * Af[f] * udm[f] + csubl * V5;
+                    }
+                }
+            }
+            if (z == 0) {
+                const double alpha4 = area * K34 / (hs / 2.0 + P.dz / 2.0);
+                dg += V5 * csubl - area * udm[4] - alpha4;
+                b += -alpha4 * c_salt;
+                if (udm[3] > 0) {
+                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    if (P.L > 1) up += alpha[3];
+                } else {
+                    dg += V5 * csubl - alpha[3];
+                    if (P.L > 1) up += -area * udm[3] + alpha[3];
+                }
+            } else if (z == P.L - 1) {
+                const double cprecip = 0;
+                if (udm[3] > 0) {
+                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    b += -alpha[3] * cprecip;
+                } else {
+                    dg += V5 * csubl - alpha[3];
+                    b += area * cprecip * udm[3] - alpha[3] * cprecip;
+                }
+                if (udm[4] > 0) {
+                    dg += V5 * csubl - area * udm[4] - alpha[4];
+                    lo += alpha[4];
+                } else {
+                    dg += V5 * csubl - alpha[4];
+                    lo += -area * udm[4] + alpha[4];
+                }
+            } else {
+                if (udm[3] > 0) {
+                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    up += alpha[3];
+                } else {
+                    dg += V5 * csubl - alpha[3];
+                    up += -area * udm[3] + alpha[3];
+                }
+                if (udm[4] > 0) {
+                    dg += V5 * csubl - area * udm[4] - alpha[4];
+                    lo += alpha[4];
+                } else {
+                    dg += V5 * csubl - alpha[4];
+                    lo += -area * udm[4] + alpha[4];
+                }
+            }
+            A.band[r] = dg;
+            A.band[1 * R + r] = lat[0];
+            A.band[2 * R + r] = lat[1];
+            A.band[3 * R + r] = lat[2];
+            A.band[4 * R + r] = lo;
+            A.band[5 * R + r] = up;
+            A.rhs[r] = b;
+            A.x[r] = 0.0;
+            // Thomas factorisation of the column: beta_z = d_z - l_z * up_{z-1}
+            const double lz = (z == 0) ? 0.0 : lo / prev_beta;
+            const double beta = (z == 0) ? dg : dg - lz * prev_up;
+            const double ib = 1.0 / beta;
+            A.fac_l[r] = lz;
+            A.fac_ib[r] = ib;
+            if (P.mixed) {
+                A.lat32[r] = (float)lat[0];
+                A.lat32[R + r] = (float)lat[1];
+                A.lat32[2 * R + r] = (float)lat[2];
+                A.l32[r] = (float)lz;
+                A.ib32[r] = (float)ib;
+                A.up32[r] = (float)up;
+            }
+            prev_up = up;
+            prev_beta = beta;
+            vmax = fmax(vmax, fabs(b));
+            if (isnan(dg) || isnan(b) || isnan(lat[0]) || isnan(lat[1]) || isnan(lat[2]) || isnan(lo) || isnan(up) ||
+                !isfinite(ib))
+                vnan = 1.0;
+        }
+    }
+    // ||rhs||_inf and NaN flag: block max, last block finalises
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __shared__ double shm[2][kBlock / 32];
+    double a = warp_max(vmax), bn = warp_max(vnan);
+    if (lane == 0) {
+        shm[0][wid] = a;
+        shm[1][wid] = bn;
+    }
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double m0 = 0, m1 = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            m0 = fmax(m0, shm[0][k]);
+            m1 = fmax(m1, shm[1][k]);
+        }
+        partials[blockIdx.x] = m0;
+        partials[gridDim.x + blockIdx.x] = m1;
+        __threadfence();
+        last = atomicAdd(&sc->counter[0], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double m0 = 0, m1 = 0;
+        for (int k = 0; k < (int)gridDim.x; ++k) {
+            m0 = fmax(m0, __ldcg(&partials[k]));
+            m1 = fmax(m1, __ldcg(&partials[gridDim.x + k]));
+        }
+        sc->rhs_max = m0;
+        sc->nan_flag = m1;
+        sc->counter[0] = 0u;
+    }
+}
+
+// PBSM3D.cpp:1467-1503 (column post) fused with :1516-1658 (deposition rows).
+// Qsusp/Qsalt of the neighbours are needed, so the post runs first in its own
+// kernel; the deposition kernel then gathers.
+__global__ void __launch_bounds__(kBlock) k_post(Params P, Susp A, FaceState S) {
+    const int64_t Tp = P.Tp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
+        double Qsusp = 0, Qsubl = 0;
+        for (int z = 0; z < P.L; ++z) {
+            const int64_t r = (int64_t)z * Tp + i;
+            double c = A.x[r];
+            c = c < 0 || is_nan_chm(c) ? 0 : c;
+            Qsusp += c * A.u_z[r] * P.dz;
+            Qsubl += A.csubl[r] * c * P.dz;
+        }
+        S.Qsusp[i] = Qsusp;
+        S.Qsubl[i] = Qsubl;
+        const double qm = Qsubl * P.dt;
+        S.Qsubl_mass[i] = qm;
+        S.sum_subl[i] += qm;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces G, Forcing F, FaceState S, Dep D,
+                                                               double* partials, Scalars* sc) {
+    const int64_t Tp = P.Tp;
+    double vmax = 0, vnan = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= P.T) {
+            D.diag[i] = 1.0;
+            D.dinv[i] = 1.0;
+            for (int j = 0; j < 3; ++j) D.off[j * Tp + i] = 0.0;
+            D.rhs[i] = 0.0;
+            D.x[i] = 0.0;
+            continue;
+        }
+        double vx, vy;
+        bearing_to_cartesian(F.dir[i], vx, vy);
+        const double ux = -vx, uy = -vy;
+        double dg = G.area[i];  // replace, PBSM3D.cpp:1546
+        double b = 0.0;
+        const double Qs_self = S.Qsusp[i], Qa_self = S.Qsalt[i];
+        for (int j = 0; j < 3; ++j) {
+            const double udm = dot2(ux, uy, G.mx[j * Tp + i], G.my[j * Tp + i]);
+            const double Ej = G.E[j * Tp + i];
+            const int32_t nb = G.nbr[j * Tp + i];
+            double Qtj, Qsj;
+            if (udm > 0) {
+                Qtj = Qs_self;
+                Qsj = Qa_self;
+            } else if (nb >= 0) {
+                Qtj = S.Qsusp[nb];
+                Qsj = S.Qsalt[nb];
+                if (is_nan_chm(Qsj)) Qsj = 0;
+            } else {
+                Qtj = Qs_self;
+                Qsj = Qa_self;
+            }
+            double off = 0.0;
+            if (nb >= 0) {
+                const double dxj = G.dxn[j * Tp + i];
+                dg += P.eps * Ej / dxj;
+                off += -P.eps * Ej / dxj;
+            }
+            D.off[j * Tp + i] = off;
+            b += -Ej * (Qtj + Qsj) * udm;
+        }
+        D.diag[i] = dg;
+        D.dinv[i] = 1.0 / dg;
+        D.rhs[i] = b;
+        D.x[i] = 0.0;
+        vmax = fmax(vmax, fabs(b));
+        if (isnan(dg) || isnan(b)) vnan = 1.0;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __shared__ double shm[2][kBlock / 32];
+    double a = warp_max(vmax), bn = warp_max(vnan);
+    if (lane == 0) {
+        shm[0][wid] = a;
+        shm[1][wid] = bn;
+    }
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double m0 = 0, m1 = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            m0 = fmax(m0, shm[0][k]);
+            m1 = fmax(m1, shm[1][k]);
+        }
+        partials[blockIdx.x] = m0;
+        partials[gridDim.x + blockIdx.x] = m1;
+        __threadfence();
+        last = atomicAdd(&sc->counter[0], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double m0 = 0, m1 = 0;
+        for (int k = 0; k < (int)gridDim.x; ++k) {
+            m0 = fmax(m0, __ldcg(&partials[k]));
+            m1 = fmax(m1, __ldcg(&partials[gridDim.x + k]));
+        }
+        sc->rhs_max = m0;
+        sc->nan_flag = m1;
+        sc->counter[0] = 0u;
+    }
+}
+
+// PBSM3D.cpp:1710-1740 plus the FP64 mass ledger (deterministic partial sums).
+// rres holds b - A q from the solver's final residual.
+__global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F, FaceState S, Dep D, const double* rres,
+                                                   int deposition_present, double* partials, Scalars* sc,
+                                                   double* ledger) {
+    double v[4] = {0, 0, 0, 0};  // divergence, deposited, clipped, residual
+    double snow = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
+        double swe = F.swe[i];
+        swe = is_nan_chm(swe) ? 0 : swe;
+        const double area = G.area[i];
+        snow += area * swe;
+        if (!deposition_present) continue;
+        const double q = D.x[i];
+        const double qdep = is_nan_chm(q) ? 0 : q;
+        double mass = qdep * P.dt;
+        if (mass < 0 && fabs(mass) > swe) {
+            S.more[i] = 1;
+            mass = -swe;
+        }
+        if (mass < 0 && !S.saltation[i]) mass = 0;
+        S.drift_mass[i] = mass;
+        S.sum_drift[i] += mass;
+        v[0] += P.dt * D.rhs[i];
+        v[1] += P.dt * area * q;
+        v[2] += area * (mass - q * P.dt);
+        v[3] += P.dt * rres[i];
+    }
+    double w[5] = {v[0], v[1], v[2], v[3], snow};
+    __shared__ double sh[5][kBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < 5; ++k) {
+        double s = warp_sum(w[k]);
+        if (lane == 0) sh[k][wid] = s;
+    }
+    __syncthreads();
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 5; ++k) {
+            double s = 0;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh[k][q];
+            partials[k * gridDim.x + blockIdx.x] = s;
+        }
+        __threadfence();
+        last = atomicAdd(&sc->counter[1], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        for (int k = 0; k < 5; ++k) {
+            double s = 0;
+            for (int q = 0; q < (int)gridDim.x; ++q) s += __ldcg(&partials[k * gridDim.x + q]);
+            ledger[k] = s;
+        }
+        sc->counter[1] = 0u;
+    }
+}
+
+// Centroid distances to neighbours (distance_UTM, coordinates.cpp:100-106).
+__global__ void k_init_static(Params P, Faces G, const double* cx, const double* cy) {
+    const int64_t Tp = P.Tp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = G.nbr[j * Tp + i];
+            double d = 2.0;
+            if (nb >= 0 && i < P.T) {
+                const double ddx = cx[i] - cx[nb];
+                const double ddy = cy[i] - cy[nb];
+                d = sqrt(ddx * ddx + ddy * ddy);
+            }
+            G.dxn[j * Tp + i] = d;
+        }
+    }
+}
+
+}  // namespace
+
+void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
+    const int64_t T = c.P.T, rows = T * c.P.L;
+    prof_begin(c, s);
+    k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.red.partials, c.sc);
+    // per face: 8 forcing + 133 B geometry in, Qsalt + flag out; per row 12 doubles out (+6 floats MIXED)
+    prof_end(c, s, PBSM3D_K_ASSEMBLE, T * (64 + 133 + 9) + rows * (96 + (c.P.mixed ? 24 : 0)));
+}
+
+void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {
+    const int64_t T = c.P.T, rows = T * c.P.L;
+    prof_begin(c, s);
+    k_post<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.A, c.S);
+    prof_end(c, s, PBSM3D_K_POST, rows * 24 + T * 40);
+    prof_begin(c, s);
+    k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.red.partials, c.sc);
+    prof_end(c, s, PBSM3D_K_DEP_ASSEMBLE, T * 196);
+}
+
+void launch_update(Ctx& c, cudaStream_t s) {
+    prof_begin(c, s);
+    k_update<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.dr, c.deposition_present ? 1 : 0,
+                                             c.red.partials, c.sc, c.ledger);
+    prof_end(c, s, PBSM3D_K_UPDATE, c.P.T * 81);
+}
+
+// cx, cy: the centroid x/y staged in the CG work vectors by pbsm3d_create
+void launch_init_static(Ctx& c, cudaStream_t s) {
+    k_init_static<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.dr, c.dz_);
+}
+
+}  // namespace pbsm

@@ -1,0 +1,590 @@
+// solver.cu -- Krylov solves of the two PBSM3D systems on the GPU.
+//
+// Suspension (replaces the Belos GMRES(30) + Ifpack2 ILUT solve of
+// LinearAlgebra.cpp:228-252): right-preconditioned BiCGStab.  The matrix is
+// split A = B + N, B = the tridiagonal column of each face (diagonal, below,
+// above), N = the three lateral couplings.  With M = B the preconditioned
+// operator is A B^{-1} = I + N B^{-1}, so one operator application is
+//   z = B^{-1} u   (Thomas sweep down and up each column, fused into the
+//                   vector update that produces u)
+//   y = u + N z    (gather of z at the three face neighbours, fused with the
+//                   dot products that follow)
+// and the vertical bands are never re-read inside the iteration.  The true
+// residual b - A x is recomputed from all six FP64 bands at the end.
+//
+// MIXED: the same BiCGStab in FP32 (FP32 lateral bands and column factors)
+// solves A d = r to a modest tolerance inside FP64 iterative refinement;
+// residuals, x and all norms stay FP64.
+//
+// Deposition (SPD: diag(area) + eps * weighted graph Laplacian):
+// Jacobi-preconditioned CG in FP64.
+//
+// Every reduction is deterministic: fixed grid, per-block partials, the
+// last block sums them in block order.  Scalars live in device memory, so
+// iterations are launched without host synchronisation; the host polls the
+// iteration count every few iterations.
+#include <math.h>
+
+#include <algorithm>
+
+#include "pbsm3d_internal.cuh"
+
+namespace pbsm {
+namespace {
+
+template <typename V>
+struct Op {
+    const V* lat;    // [3][R]
+    const V* l;      // [R] forward multipliers
+    const V* ib;     // [R] inverse pivots
+    const V* up;     // [R] above band
+    const int32_t* nbr;  // [3][Tp]
+    int64_t Tp, R;
+    int L;
+};
+
+enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3 };
+
+// z = B^{-1} u for one column, u already in smem column g[z*bd + tid].
+template <typename V>
+__device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V* zout) {
+    const int bd = blockDim.x, tid = threadIdx.x;
+    V prev = 0;
+    for (int z = 0; z < op.L; ++z) {
+        const int64_t r = (int64_t)z * op.Tp + i;
+        V gz = g[z * bd + tid] - op.l[r] * prev;
+        g[z * bd + tid] = gz;
+        prev = gz;
+    }
+    V y = 0;
+    for (int z = op.L - 1; z >= 0; --z) {
+        const int64_t r = (int64_t)z * op.Tp + i;
+        y = (g[z * bd + tid] - op.up[r] * y) * op.ib[r];
+        zout[r] = y;
+    }
+}
+
+// p = r + beta (p - omega v); zp = B^{-1} p
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bicg_p(Op<V> op, const V* __restrict__ r, V* __restrict__ p,
+                                                   const V* __restrict__ v, V* __restrict__ zp, const Scalars* sc) {
+    if (sc->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    V* g = reinterpret_cast<V*>(smem_raw);
+    const V beta = (V)sc->beta, omega = (V)sc->omega;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int z = 0; z < op.L; ++z) {
+            const int64_t k = (int64_t)z * op.Tp + i;
+            const V pk = r[k] + beta * (p[k] - omega * v[k]);
+            p[k] = pk;
+            g[z * blockDim.x + threadIdx.x] = pk;
+        }
+        column_solve(op, i, g, zp);
+    }
+}
+
+// s = r - alpha v; zs = B^{-1} s
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, const V* __restrict__ r, const V* __restrict__ v,
+                                                   V* __restrict__ s, V* __restrict__ zs, const Scalars* sc) {
+    if (sc->done) return;
+    extern __shared__ unsigned char smem_raw[];
+    V* g = reinterpret_cast<V*>(smem_raw);
+    const V alpha = (V)sc->alpha;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int z = 0; z < op.L; ++z) {
+            const int64_t k = (int64_t)z * op.Tp + i;
+            const V sk = r[k] - alpha * v[k];
+            s[k] = sk;
+            g[z * blockDim.x + threadIdx.x] = sk;
+        }
+        column_solve(op, i, g, zs);
+    }
+}
+
+// y = u + N z, with dot products (a, y) [and (y, y)]
+template <typename V, int NT>
+__device__ __forceinline__ void lateral_apply(const Op<V>& op, const V* __restrict__ u, const V* __restrict__ zz,
+                                              V* __restrict__ y, const V* __restrict__ a, V (&acc)[2]) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+        for (int z = 0; z < op.L; ++z) {
+            const int64_t base = (int64_t)z * op.Tp;
+            const int64_t k = base + i;
+            V yk = u[k];
+            if (n0 >= 0) yk += op.lat[k] * zz[base + n0];
+            if (n1 >= 0) yk += op.lat[op.R + k] * zz[base + n1];
+            if (n2 >= 0) yk += op.lat[2 * op.R + k] * zz[base + n2];
+            y[k] = yk;
+            acc[0] += a[k] * yk;
+            if (NT > 1) acc[1] += yk * yk;
+        }
+    }
+}
+
+// v = p + N zp; rv = (rhat, v); alpha = rho / rv
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bicg_v(Op<V> op, const V* __restrict__ p, const V* __restrict__ zp,
+                                                   V* __restrict__ v, const V* __restrict__ rh, Scalars* sc,
+                                                   double* partials) {
+    if (sc->done) return;
+    V acc[2] = {0, 0};
+    lateral_apply<V, 1>(op, p, zp, v, rh, acc);
+    double d[1] = {(double)acc[0]}, tot[1];
+    if (block_partials_last<1>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        const double rv = tot[0];
+        sc->rv = rv;
+        if (rv == 0.0 || !isfinite(rv)) {
+            sc->done = DONE_BREAKDOWN;
+        } else {
+            sc->alpha = sc->rho / rv;
+        }
+    }
+}
+
+// t = s + N zs; ts = (t, s), tt = (t, t); omega = ts / tt
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bicg_t(Op<V> op, const V* __restrict__ s, const V* __restrict__ zs,
+                                                   V* __restrict__ t, Scalars* sc, double* partials) {
+    if (sc->done) return;
+    V acc[2] = {0, 0};
+    lateral_apply<V, 2>(op, s, zs, t, s, acc);
+    double d[2] = {(double)acc[0], (double)acc[1]}, tot[2];
+    if (block_partials_last<2>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->ts = tot[0];
+        sc->tt = tot[1];
+        sc->omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
+    }
+}
+
+// x += alpha zp + omega zs; r = s - omega t; rho' = (rhat, r), (r, r)
+template <typename V, typename X>
+__global__ void __launch_bounds__(kBlock) k_bicg_x(int64_t Tp, int L, X* __restrict__ x, const V* __restrict__ zp,
+                                                   const V* __restrict__ zs, const V* __restrict__ s,
+                                                   const V* __restrict__ t, V* __restrict__ r,
+                                                   const V* __restrict__ rh, Scalars* sc, double* partials) {
+    if (sc->done) return;
+    const X alpha = (X)sc->alpha, omega = (X)sc->omega;
+    const V om = (V)sc->omega;
+    V acc[2] = {0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int z = 0; z < L; ++z) {
+            const int64_t k = (int64_t)z * Tp + i;
+            x[k] = x[k] + alpha * (X)zp[k] + omega * (X)zs[k];
+            const V rk = s[k] - om * t[k];
+            r[k] = rk;
+            acc[0] += rh[k] * rk;
+            acc[1] += rk * rk;
+        }
+    }
+    double d[2] = {(double)acc[0], (double)acc[1]}, tot[2];
+    if (block_partials_last<2>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        const double rho_new = tot[0];
+        sc->rnorm2 = tot[1];
+        sc->iter += 1;
+        if (tot[1] <= sc->target2) {
+            sc->done = DONE_CONVERGED;
+        } else if (sc->omega == 0.0 || rho_new == 0.0 || !isfinite(rho_new) || !isfinite(tot[1])) {
+            sc->done = DONE_BREAKDOWN;
+        } else if (sc->iter >= sc->maxit) {
+            sc->done = DONE_MAXIT;
+        } else {
+            sc->beta = (rho_new / sc->rho) * (sc->alpha / sc->omega);
+        }
+        sc->rho = rho_new;
+    }
+}
+
+// r = b - A x with all six FP64 bands; optionally r32 = (float) r.
+// Also (r, r) and (b, b).  Resets the BiCGStab state: rhat = r, p = v = 0.
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_residual(Params P, const double* __restrict__ band,
+                                                     const int32_t* __restrict__ nbr, const double* __restrict__ x,
+                                                     const double* __restrict__ b, double* __restrict__ r,
+                                                     V* __restrict__ rv, V* __restrict__ rhv, V* __restrict__ pv,
+                                                     V* __restrict__ vv, Scalars* sc, double* partials, double tol,
+                                                     int maxit) {
+    const int64_t Tp = P.Tp, R = P.R;
+    double acc[2] = {0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
+        for (int z = 0; z < P.L; ++z) {
+            const int64_t base = (int64_t)z * Tp;
+            const int64_t k = base + i;
+            double ax = band[k] * x[k];
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                if (nb[j] >= 0) ax += band[(j + 1) * R + k] * x[base + nb[j]];
+            if (z > 0) ax += band[4 * R + k] * x[k - Tp];
+            if (z < P.L - 1) ax += band[5 * R + k] * x[k + Tp];
+            const double rk = b[k] - ax;
+            r[k] = rk;
+            if (rv) {
+                rv[k] = (V)rk;
+                rhv[k] = (V)rk;
+                pv[k] = 0;
+                vv[k] = 0;
+            }
+            acc[0] += rk * rk;
+            acc[1] += b[k] * b[k];
+        }
+    }
+    double tot[2];
+    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rnorm2 = tot[0];
+        sc->bnorm2 = tot[1];
+        sc->rho = tot[0];
+        sc->alpha = 1.0;
+        sc->omega = 1.0;
+        sc->beta = 0.0;
+        sc->target2 = tol * tol * tot[0];
+        sc->iter = 0;
+        sc->maxit = maxit;
+        sc->done = tot[0] == 0.0 ? DONE_CONVERGED : DONE_NO;
+    }
+}
+
+// x += (double) d
+__global__ void __launch_bounds__(kBlock) k_add_correction(int64_t n, double* __restrict__ x,
+                                                           const float* __restrict__ d) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        x[k] += (double)d[k];
+}
+template <typename V>
+__global__ void k_zero(int64_t n, V* __restrict__ a) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        a[k] = 0;
+}
+
+// ---------------------------------------------------------------- deposition CG
+// init: r = b, z = D^{-1} b, p = z, q = A z; (r,z), (p,q), (b,b)
+__global__ void __launch_bounds__(kBlock) k_cg_init(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
+                                                    double* zz, double* p, double* q, Scalars* sc, double* partials,
+                                                    double tol, int maxit) {
+    const int64_t Tp = P.Tp;
+    double acc[3] = {0, 0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        const double bi = D.rhs[i];
+        const double zi = D.dinv[i] * bi;
+        double qi = D.diag[i] * zi;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = nbr[j * Tp + i];
+            if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.rhs[nb]);
+        }
+        r[i] = bi;
+        zz[i] = zi;
+        p[i] = zi;
+        q[i] = qi;
+        D.x[i] = 0.0;
+        acc[0] += bi * zi;
+        acc[1] += zi * qi;
+        acc[2] += bi * bi;
+    }
+    double tot[3];
+    if (block_partials_last<3>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rho = tot[0];
+        sc->bnorm2 = tot[2];
+        sc->rnorm2 = tot[2];
+        sc->target2 = tol * tol * tot[2];
+        sc->iter = 0;
+        sc->maxit = maxit;
+        if (tot[2] == 0.0) {
+            sc->done = DONE_CONVERGED;
+        } else if (!(tot[1] > 0.0)) {
+            sc->done = DONE_BREAKDOWN;
+        } else {
+            sc->done = DONE_NO;
+            sc->alpha = tot[0] / tot[1];
+        }
+    }
+}
+
+// x += alpha p; r -= alpha q; z = D^{-1} r; (r,z), (r,r)
+__global__ void __launch_bounds__(kBlock) k_cg_x(Params P, Dep D, double* r, double* zz, const double* p,
+                                                 const double* q, Scalars* sc, double* partials) {
+    if (sc->done) return;
+    const double alpha = sc->alpha;
+    double acc[2] = {0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        D.x[i] += alpha * p[i];
+        const double ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        const double zi = D.dinv[i] * ri;
+        zz[i] = zi;
+        acc[0] += ri * zi;
+        acc[1] += ri * ri;
+    }
+    double tot[2];
+    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->iter += 1;
+        sc->rnorm2 = tot[1];
+        sc->beta = tot[0] / sc->rho;
+        sc->rho = tot[0];
+        if (tot[1] <= sc->target2) sc->done = DONE_CONVERGED;
+        else if (!isfinite(tot[1])) sc->done = DONE_BREAKDOWN;
+        else if (sc->iter >= sc->maxit) sc->done = DONE_MAXIT;
+    }
+}
+
+// p = z + beta p; q = A z + beta q; (p,q) -> alpha = rho / (p,q)
+__global__ void __launch_bounds__(kBlock) k_cg_p(Params P, Dep D, const int32_t* __restrict__ nbr, const double* zz,
+                                                 double* p, double* q, Scalars* sc, double* partials) {
+    if (sc->done) return;
+    const double beta = sc->beta;
+    const int64_t Tp = P.Tp;
+    double acc[1] = {0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        double az = D.diag[i] * zz[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = nbr[j * Tp + i];
+            if (nb >= 0) az += D.off[j * Tp + i] * zz[nb];
+        }
+        const double pi = zz[i] + beta * p[i];
+        const double qi = az + beta * q[i];
+        p[i] = pi;
+        q[i] = qi;
+        acc[0] += pi * qi;
+    }
+    double tot[1];
+    if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        if (!(tot[0] > 0.0)) sc->done = DONE_BREAKDOWN;
+        else sc->alpha = sc->rho / tot[0];
+    }
+}
+
+// r = b - A x (deposition), (r, r)
+__global__ void __launch_bounds__(kBlock) k_cg_resid(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
+                                                     Scalars* sc, double* partials) {
+    const int64_t Tp = P.Tp;
+    double acc[1] = {0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        double ax = D.diag[i] * D.x[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = nbr[j * Tp + i];
+            if (nb >= 0) ax += D.off[j * Tp + i] * D.x[nb];
+        }
+        const double ri = D.rhs[i] - ax;
+        r[i] = ri;
+        acc[0] += ri * ri;
+    }
+    double tot[1];
+    if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) sc->tmp = tot[0];
+}
+
+template <typename V>
+Op<V> make_op(Ctx& c);
+template <>
+Op<double> make_op<double>(Ctx& c) {
+    return Op<double>{c.A.band + c.P.R, c.A.fac_l, c.A.fac_ib, c.A.band + 5 * c.P.R, c.F.nbr, c.P.Tp, c.P.R, c.P.L};
+}
+template <>
+Op<float> make_op<float>(Ctx& c) {
+    return Op<float>{c.A.lat32, c.A.l32, c.A.ib32, c.A.up32, c.F.nbr, c.P.Tp, c.P.R, c.P.L};
+}
+
+int read_scalars(Ctx& c, cudaStream_t s, Scalars* dev) {
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, dev, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    return 0;
+}
+
+// Run BiCGStab iterations on the state set up by k_residual until done.
+template <typename V, typename X>
+int bicgstab_iterations(Ctx& c, cudaStream_t s, Scalars* sc, X* x, V* r, V* rh, V* p, V* v, V* sv, V* tv, V* zp,
+                        V* zs, int& iters) {
+    Op<V> op = make_op<V>(c);
+    const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
+    const int g = c.grid_faces;
+    double* part = c.red.partials;
+    const int64_t T = c.P.T, rows = T * c.P.L;
+    const int64_t sv_ = sizeof(V), sx = sizeof(X);
+    int chunk = 4;
+    int before = 0;
+    {
+        int rc = read_scalars(c, s, sc);
+        if (rc) return rc;
+        before = c.sc_host->iter;
+        if (c.sc_host->done) {
+            iters = 0;
+            return 0;
+        }
+    }
+    while (true) {
+        for (int k = 0; k < chunk; ++k) {
+            prof_begin(c, s);
+            k_bicg_p<V><<<g, kBlock, smem, s>>>(op, r, p, v, zp, sc);
+            prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
+            prof_begin(c, s);
+            k_bicg_v<V><<<g, kBlock, 0, s>>>(op, p, zp, v, rh, sc, part);
+            prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + T * 12);
+            prof_begin(c, s);
+            k_bicg_s<V><<<g, kBlock, smem, s>>>(op, r, v, sv, zs, sc);
+            prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
+            prof_begin(c, s);
+            k_bicg_t<V><<<g, kBlock, 0, s>>>(op, sv, zs, tv, sc, part);
+            prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + T * 12);
+            prof_begin(c, s);
+            k_bicg_x<V, X><<<g, kBlock, 0, s>>>(c.P.Tp, c.P.L, x, zp, zs, sv, tv, r, rh, sc, part);
+            prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
+        }
+        int rc = read_scalars(c, s, sc);
+        if (rc) return rc;
+        const int ran = c.sc_host->iter - before;
+        before = c.sc_host->iter;
+        // launches after the converging iteration returned at once: not counted
+        const int idle = chunk - ran - (c.sc_host->done == DONE_BREAKDOWN ? 1 : 0);
+        if (idle > 0) prof_drop(c, 5 * idle);
+        if (c.sc_host->done) break;
+        chunk = std::min(16, chunk * 2);
+    }
+    iters = c.sc_host->iter;
+    return 0;
+}
+
+}  // namespace
+
+// Column kernels stage L values per thread in shared memory; above 48 KB the
+// launch needs the opt-in limit raised.
+int configure_solver_kernels(Ctx& c) {
+    const int s64 = c.P.L * kBlock * 8, s32 = c.P.L * kBlock * 4;
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    return 0;
+}
+
+// Suspension solve: x0 = current contents of A.x.  Fills iteration stats.
+int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
+    (void)st;
+    const int g = c.grid_faces;
+    double* part = c.red.partials;
+    Scalars* sc0 = c.sc;      // FP64 outer / plain
+    Scalars* sc1 = c.sc + 1;  // FP32 inner
+    const double tol = c.cfg.susp_tol;
+    int total_iters = 0, sweeps = 0;
+    double bnorm2 = 0;
+    const int maxit = c.cfg.susp_maxit;
+    c.susp_relres = 0;
+    while (true) {
+        // r = b - A x, in FP64; reset the Krylov state
+        if (c.P.mixed) {
+            prof_begin(c, s);
+            k_residual<float><<<g, kBlock, 0, s>>>(c.P, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
+                                                   c.p32, c.v32, sc0, part, tol, maxit);
+            prof_end(c, s, PBSM3D_K_RESIDUAL, c.P.T * c.P.L * 88 + c.P.T * 12);
+        } else {
+            prof_begin(c, s);
+            k_residual<double><<<g, kBlock, 0, s>>>(c.P, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
+                                                    c.v, sc0, part, tol, maxit);
+            prof_end(c, s, PBSM3D_K_RESIDUAL, c.P.T * c.P.L * 96 + c.P.T * 12);
+        }
+        int rc = read_scalars(c, s, sc0);
+        if (rc) return rc;
+        if (sweeps == 0) bnorm2 = c.sc_host->bnorm2;
+        const double rn2 = c.sc_host->rnorm2;
+        c.susp_relres = bnorm2 > 0 ? sqrt(rn2 / bnorm2) : 0.0;
+        if (rn2 <= tol * tol * bnorm2) break;
+        if (total_iters >= maxit) {
+            c.susp_iters = total_iters;
+            c.err = "suspension solve failed to converge (relative residual " + std::to_string(c.susp_relres) + ")";
+            return PBSM3D_ERR_NOT_CONVERGED;
+        }
+        if (!isfinite(rn2)) {
+            c.err = "suspension solve produced a non-finite residual";
+            return PBSM3D_ERR_NOT_CONVERGED;
+        }
+        int it = 0;
+        if (c.P.mixed) {
+            // inner: A32 d = r32, d0 = 0, to inner_tol relative
+            const double itol = c.cfg.inner_tol;
+            Scalars init{};
+            init.rho = rn2;
+            init.alpha = init.omega = 1.0;
+            init.beta = 0.0;
+            init.bnorm2 = rn2;
+            init.target2 = itol * itol * rn2;
+            init.maxit = std::max(1, maxit - total_iters);
+            PBSM_CUDA_TRY(cudaMemcpyAsync(sc1, &init, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+            prof_begin(c, s);
+            k_zero<float><<<g, kBlock, 0, s>>>(c.P.R, c.x32);
+            prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 4);
+            rc = bicgstab_iterations<float, float>(c, s, sc1, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32, c.t32,
+                                                   c.zp32, c.zs32, it);
+            if (rc) return rc;
+            prof_begin(c, s);
+            k_add_correction<<<g, kBlock, 0, s>>>(c.P.R, c.A.x, c.x32);
+            prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 20);
+        } else {
+            // target relative to ||b|| (the state's target2 is relative to ||r||)
+            Scalars* h = c.sc_host;
+            h->target2 = tol * tol * bnorm2;
+            h->maxit = maxit - total_iters;
+            PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->target2, &h->target2, sizeof(double), cudaMemcpyHostToDevice, s));
+            PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->maxit, &h->maxit, sizeof(int), cudaMemcpyHostToDevice, s));
+            rc = bicgstab_iterations<double, double>(c, s, sc0, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv, c.zp, c.zs,
+                                                     it);
+            if (rc) return rc;
+        }
+        total_iters += it;
+        sweeps++;
+        if (sweeps > 64) {
+            c.err = "suspension solve: refinement did not converge";
+            return PBSM3D_ERR_NOT_CONVERGED;
+        }
+    }
+    c.susp_iters = total_iters;
+    c.susp_matvecs = 2 * total_iters + sweeps + 1;
+    c.susp_refinements = sweeps;
+    return 0;
+}
+
+int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
+    (void)st;
+    const int g = c.grid_faces;
+    double* part = c.red.partials;
+    Scalars* sc = c.sc + 2;
+    const int64_t T = c.P.T;
+    prof_begin(c, s);
+    k_cg_init<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, c.dz_, c.dp, c.dq, sc, part, c.cfg.dep_tol,
+                                   c.cfg.dep_maxit);
+    prof_end(c, s, PBSM3D_K_CG, T * 96);
+    int chunk = 8;
+    int before = 0;
+    while (true) {
+        for (int k = 0; k < chunk; ++k) {
+            prof_begin(c, s);
+            k_cg_x<<<g, kBlock, 0, s>>>(c.P, c.D, c.dr, c.dz_, c.dp, c.dq, sc, part);
+            prof_end(c, s, PBSM3D_K_CG, T * 64);
+            prof_begin(c, s);
+            k_cg_p<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dz_, c.dp, c.dq, sc, part);
+            prof_end(c, s, PBSM3D_K_CG, T * 84);
+        }
+        int rc = read_scalars(c, s, sc);
+        if (rc) return rc;
+        const int ran = c.sc_host->iter - before;
+        before = c.sc_host->iter;
+        const int idle = chunk - ran;
+        if (idle > 0) prof_drop(c, 2 * idle);
+        if (c.sc_host->done) break;
+    }
+    const int done = c.sc_host->done;
+    c.dep_iters = c.sc_host->iter;
+    const double bn2 = c.sc_host->bnorm2;
+    prof_begin(c, s);
+    k_cg_resid<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);
+    prof_end(c, s, PBSM3D_K_CG, T * 76);
+    int rc = read_scalars(c, s, sc);
+    if (rc) return rc;
+    c.dep_relres = bn2 > 0 ? sqrt(c.sc_host->tmp / bn2) : 0.0;
+    if (done != DONE_CONVERGED && !(c.sc_host->tmp <= c.cfg.dep_tol * c.cfg.dep_tol * bn2)) {
+        c.err = "deposition solve failed to converge (relative residual " + std::to_string(c.dep_relres) + ")";
+        return PBSM3D_ERR_NOT_CONVERGED;
+    }
+    return 0;
+}
+
+}  // namespace pbsm

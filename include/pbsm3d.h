@@ -1,0 +1,305 @@
+/*
+ * pbsm3d.h -- C ABI of libpbsm3d_cuda, the GB300 (sm_103a) implementation of
+ * CHM's PBSM3D blowing-snow timestep.
+ *
+ * One context owns one mesh resident in HBM.  A step runs, entirely on the
+ * GPU: saltation, suspension coefficients, the sliced-ELL assembly of the
+ * 3-D suspension advection-diffusion system, its Krylov solve, the column
+ * post-processing (Qsusp, Qsubl), the assembly and solve of the 2-D drift
+ * flux-divergence (deposition) system and the erosion/deposition update.
+ *
+ * Reference interfaces replaced (Chrismarsh/CHM):
+ *   pbsm3d_create   <- PBSM3D::PBSM3D(config_file)   src/modules/PBSM3D.cpp:103-219
+ *                      PBSM3D::init(mesh&)           src/modules/PBSM3D.cpp:221-398
+ *                      NearestNeighborProblem ctor   src/math/LinearAlgebra.cpp:31-197
+ *   pbsm3d_step     <- PBSM3D::run(mesh&)            src/modules/PBSM3D.cpp:400-1748
+ *   pbsm3d_get_state/pbsm3d_set_state
+ *                   <- PBSM3D::checkpoint / load_checkpoint
+ *                                                    src/modules/PBSM3D.cpp:1753-1773
+ *   error codes     <- CHM_THROW_EXCEPTION(module_error, ...)
+ *                                                    src/modules/PBSM3D.cpp:1447,1704
+ *
+ * Conventions
+ *   - Plain C structs, POD arrays, no exceptions across the ABI.
+ *   - Per-face arrays are indexed by the face's position in the mesh
+ *     (CHM cell_local_id == cell_global_id for a single-process mesh,
+ *     src/mesh/triangulation.cpp:300-302).  [3*n] arrays are row-major
+ *     (face, j).  neighbor[3*i+j] is the face across the edge opposite
+ *     vertex j (CGAL convention), -1 when there is none.
+ *   - Layered arrays ([nLayer*n]) are layer-major: index z*n + i, the
+ *     ordering of the reference's extruded map (LinearAlgebra.cpp:46-55).
+ *   - Return 0 on success, a negative PBSM3D_ERR_* on failure; the message
+ *     is available from pbsm3d_last_error().
+ *   - A context is not thread-safe; use one context per host thread.
+ */
+#ifndef PBSM3D_H
+#define PBSM3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBSM3D_ABI_VERSION 1
+
+enum pbsm3d_status {
+    PBSM3D_OK = 0,
+    PBSM3D_ERR_INVALID_ARG = -1,
+    PBSM3D_ERR_BAD_MESH = -2,
+    PBSM3D_ERR_NAN_INPUT = -3,
+    PBSM3D_ERR_NOT_CONVERGED = -4,
+    PBSM3D_ERR_CUDA = -5,
+    PBSM3D_ERR_UNSUPPORTED = -6,
+    PBSM3D_ERR_OUT_OF_MEMORY = -7
+};
+
+/* Krylov method of the suspension solve. */
+enum pbsm3d_solver {
+    PBSM3D_SOLVER_BICGSTAB = 0, /* right-preconditioned BiCGStab (default) */
+    PBSM3D_SOLVER_GMRES = 1     /* right-preconditioned restarted GMRES(m) */
+};
+
+/* Arithmetic of the suspension solve. */
+enum pbsm3d_precision {
+    PBSM3D_FP64 = 0,  /* FP64 matrix, preconditioner and Krylov vectors */
+    PBSM3D_MIXED = 1  /* FP32 SpMV + preconditioner inside FP64 iterative refinement */
+};
+
+/* Initial guess of the suspension solve. */
+enum pbsm3d_warm_start {
+    PBSM3D_X0_ZERO = 0,     /* x0 = 0 every step, as the reference (LinearAlgebra.cpp:199-206) */
+    PBSM3D_X0_PREVIOUS = 1, /* previous step's concentration field */
+    PBSM3D_X0_LEARNED = 2   /* per-row MLP prediction (pbsm3d_set_mlp) */
+};
+
+/*
+ * Module configuration.  Every key of the reference is here with the
+ * reference default (PBSM3D.cpp:123-145, 223-258); pbsm3d_config_defaults()
+ * fills them.  Fields after "debug_output" are this library's additions and
+ * default to the reference behaviour.
+ */
+typedef struct pbsm3d_config {
+    int32_t abi_version;            /* PBSM3D_ABI_VERSION */
+    int32_t nLayer;                 /* "nLayer" 10 */
+    int32_t do_fixed_settling;      /* "do_fixed_settling" false */
+    int32_t do_sublimation;         /* "do_sublimation" true */
+    int32_t do_lateral_diff;        /* "do_lateral_diff" true */
+    int32_t rouault_diffusion_coef; /* "rouault_diffusion_coef" false */
+    int32_t enable_veg;             /* "enable_veg" true */
+    int32_t iterative_subl;         /* "iterative_subl" false (true: UNSUPPORTED) */
+    int32_t use_exp_fetch;          /* "use_exp_fetch" false */
+    int32_t use_tanh_fetch;         /* "use_tanh_fetch" true */
+    int32_t use_PomLi_probability;  /* "use_PomLi_probability" false */
+    int32_t z0_ustar_coupling;      /* "z0_ustar_coupling" false (true: UNSUPPORTED) */
+    int32_t use_subgrid_topo;       /* "use_subgrid_topo" false (true: UNSUPPORTED) */
+    int32_t use_subgrid_topo_V2;    /* "use_subgrid_topo_V2" false (true: UNSUPPORTED) */
+    int32_t use_R94_lambda;         /* "use_R94_lambda" true */
+    int32_t debug_output;           /* "debug_output" false (true: UNSUPPORTED) */
+    double settling_velocity;       /* "settling_velocity" 0.5 m/s, must be >= 0 */
+    double smooth_coeff;            /* "smooth_coeff" 820 (Laplacian smoothing eps) */
+    double min_sd_trans;            /* "min_sd_trans" 0.1 m */
+    double cutoff;                  /* "cutoff" 0.3 m */
+    double snow_diffusion_const;    /* "snow_diffusion_const" 0.3 */
+
+    /* Parameter perturbations of an ensemble member (identity defaults). */
+    double ustar_th_scale;  /* multiplies the threshold friction velocity, 1.0 */
+    double z0_snow;         /* aerodynamic roughness of snow, 0.01 m (Snow::Z0_SNOW) */
+    double settling_scale;  /* multiplies the settling velocity, 1.0 */
+
+    /* Solver settings. */
+    int32_t solver;         /* enum pbsm3d_solver, BICGSTAB */
+    int32_t precision;      /* enum pbsm3d_precision, FP64 */
+    int32_t warm_start;     /* enum pbsm3d_warm_start, ZERO */
+    int32_t gmres_restart;  /* GMRES(m) restart length, 30 (LinearAlgebra.cpp:166) */
+    int32_t susp_maxit;     /* 1000 (LinearAlgebra.cpp:167) */
+    int32_t dep_maxit;      /* 1000 */
+    double susp_tol;        /* relative residual ||b-Ax||/||b||, 1e-8 (LinearAlgebra.cpp:168) */
+    double dep_tol;         /* deposition relative residual, 1e-12 */
+    double inner_tol;       /* MIXED: FP32 inner relative reduction per refinement sweep, 1e-5 */
+    int32_t slice_width;    /* sliced-ELL rows per slice (power of two, 32..1024), 0 = autotune */
+    int32_t reserved[7];
+} pbsm3d_config;
+
+/*
+ * Mesh description: per-face geometry as CHM's triangulation computes it.
+ *   edge_length[3*i+j]  face->edge_length(j)          triangulation.hpp:1493-1498
+ *   edge_normal[6*i+2j+{0,1}] face->edge_unit_normal(j) triangulation.hpp:1443-1463
+ *   area[i]             face->get_area()              triangulation.hpp:1830-1856
+ *   center[3*i+{0,1,2}] face->center() (centroid x, y, z)  triangulation.hpp:1577-1589
+ * Optional arrays may be NULL.  has_vegetation NULL with canopy_height
+ * non-NULL means every face has vegetation; canopy_height NULL means none.
+ * All pointers are host pointers, read during pbsm3d_create only.
+ */
+typedef struct pbsm3d_mesh_desc {
+    int64_t n_faces;
+    const int32_t* neighbor;       /* [3*n] */
+    const double* edge_length;     /* [3*n] */
+    const double* edge_normal;     /* [6*n] */
+    const double* area;            /* [n] */
+    const double* center;          /* [3*n] */
+    const uint8_t* has_vegetation; /* [n] or NULL */
+    const double* canopy_height;   /* [n] "CanopyHeight" or NULL */
+    const double* lai;             /* [n] "LAI" or NULL */
+    const double* stalk_number;    /* [n] "stalk_number" or NULL (default 1) */
+    const double* stalk_diameter;  /* [n] "stalk_diameter" or NULL (default 0.8) */
+    const uint8_t* is_water;       /* [n] landcover is_water flag or NULL */
+} pbsm3d_mesh_desc;
+
+/*
+ * Per-step forcing, SoA, n_faces doubles each (the depends list of
+ * PBSM3D.cpp:105-138).  CHM's "nan" value -9999 is accepted where the
+ * reference accepts it (swe, snowdepthavg).  fetch may be NULL when neither
+ * fetch formulation is enabled; p_snow_hours is read only by
+ * use_PomLi_probability.  on_device: 0 = host pointers (copied in by the
+ * step), 1 = device pointers already resident in HBM.
+ */
+typedef struct pbsm3d_forcing {
+    const double* U_R;
+    const double* U_2m_above_srf;
+    const double* vw_dir;
+    const double* swe;
+    const double* t;
+    const double* rh;
+    const double* snowdepthavg;
+    const double* fetch;
+    const double* p_snow_hours;
+    int32_t on_device;
+} pbsm3d_forcing;
+
+/*
+ * Per-step outputs (the provides list of PBSM3D.cpp:112-188), n_faces
+ * doubles each, NULL = not wanted.  drift_mass, sum_drift, sum_subl,
+ * pbsm_more_than_avail and blowingsnow_probability are module state held in
+ * the context and copied out every step: like the reference, drift_mass keeps
+ * its previous value in a step without deposition (PBSM3D.cpp:1742-1745) and
+ * starts at -9999.  c, when non-NULL, receives the nLayer*n_faces suspension
+ * concentrations (kg m^-3), layer-major.
+ */
+typedef struct pbsm3d_outputs {
+    double* Qsalt;
+    double* Qsusp;
+    double* Qsubl;
+    double* Qsubl_mass;
+    double* sum_subl;
+    double* drift_mass;
+    double* sum_drift;
+    double* pbsm_more_than_avail;
+    double* blowingsnow_probability;
+    double* c;
+    int32_t on_device;
+} pbsm3d_outputs;
+
+/* Step diagnostics.  Times are CUDA-event milliseconds on the context's stream. */
+typedef struct pbsm3d_stats {
+    int32_t suspension_present;  /* ||b_susp||_inf > 1e-12 (PBSM3D.cpp:1424-1427) */
+    int32_t deposition_present;  /* suspension_present && ||b_dep||_inf > 1e-12 */
+    int32_t susp_iters;          /* Krylov iterations (matrix-vector products / 2 for BiCGStab) */
+    int32_t susp_matvecs;        /* operator applications, all precisions */
+    int32_t susp_refinements;    /* MIXED: FP64 refinement sweeps */
+    int32_t dep_iters;
+    double susp_rel_residual;    /* final ||b-Ax||/||b|| in FP64 */
+    double dep_rel_residual;
+    double susp_rhs_max;
+    double dep_rhs_max;
+    double ms_coefficients;      /* saltation + layer coefficients + assembly + factorisation */
+    double ms_susp_solve;
+    double ms_post;              /* Qsusp/Qsubl column reduction */
+    double ms_dep_assembly;
+    double ms_dep_solve;
+    double ms_update;
+    double ms_total;             /* whole step on the device, incl. copies when on_device=0 */
+    /* Mass ledger of the deposition update, kg, summed in FP64 over faces. */
+    double ledger_divergence;    /* dt * sum_i b_dep[i]  (net drift flux into the faces) */
+    double ledger_deposited;     /* dt * sum_i area[i] * q[i]  (solution) */
+    double ledger_clipped;       /* sum_i area[i] * (drift_mass[i] - q[i]*dt)  (caps, no-erosion rule) */
+    double ledger_snow_mass;     /* sum_i area[i] * swe[i] before the step */
+    double ledger_residual;      /* dt * sum_i (b - A q)[i] */
+    int64_t bytes_moved;         /* algorithmic HBM bytes of the step (model of the kernels) */
+    int32_t gpu_launches;        /* kernels launched by the step */
+    int32_t profiled;            /* 1 when the kern_* fields below were measured */
+    /* Per kernel class (enum pbsm3d_kernel): CUDA-event time of the launches
+     * that did work, their count and their algorithmic HBM bytes.  Filled only
+     * when profiling is on (pbsm3d_set_profiling). */
+    double kern_ms[16];
+    int64_t kern_bytes[16];
+    int32_t kern_launches[16];
+} pbsm3d_stats;
+
+/* Kernel classes reported in pbsm3d_stats.kern_*. */
+enum pbsm3d_kernel {
+    PBSM3D_K_ASSEMBLE = 0,   /* saltation + layer coefficients + ELL rows + column factors */
+    PBSM3D_K_BICG_P = 1,     /* p update fused with the column (Thomas) preconditioner */
+    PBSM3D_K_BICG_V = 2,     /* v = p + N B^-1 p (lateral gather) + dot */
+    PBSM3D_K_BICG_S = 3,     /* s update fused with the column preconditioner */
+    PBSM3D_K_BICG_T = 4,     /* t = s + N B^-1 s + two dots */
+    PBSM3D_K_BICG_X = 5,     /* x, r update + two dots */
+    PBSM3D_K_RESIDUAL = 6,   /* FP64 true residual b - A x */
+    PBSM3D_K_POST = 7,       /* Qsusp / Qsubl column reduction */
+    PBSM3D_K_DEP_ASSEMBLE = 8,
+    PBSM3D_K_CG = 9,         /* deposition CG iterations (both kernels) */
+    PBSM3D_K_UPDATE = 10,    /* erosion/deposition update + mass ledger */
+    PBSM3D_K_OTHER = 11,
+    PBSM3D_K_COUNT = 12
+};
+
+typedef struct pbsm3d_ctx pbsm3d_ctx;
+
+/* Fill *cfg with the reference defaults. */
+void pbsm3d_config_defaults(pbsm3d_config* cfg);
+
+/* Validate the config (the checks of PBSM3D.cpp:132-135, 237-240), pack the
+ * mesh into device SoA, build the sliced-ELL pattern of both systems.
+ * Replaces PBSM3D::PBSM3D + PBSM3D::init + the two NearestNeighborProblem ctors. */
+int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, pbsm3d_ctx** out);
+
+/* One timestep of dt seconds (global_param->dt(), integer seconds in CHM).
+ * Replaces PBSM3D::run.  stats may be NULL. */
+int pbsm3d_step(pbsm3d_ctx* ctx, const pbsm3d_forcing* forcing, double dt,
+                const pbsm3d_outputs* out, pbsm3d_stats* stats);
+
+/* Module state for checkpoint/restart (host arrays of n_faces doubles, NULL = skip).
+ * The reference checkpoints sum_drift only ("PBSM3D:sum_drift", PBSM3D.cpp:1753-1773). */
+int pbsm3d_get_state(pbsm3d_ctx* ctx, double* sum_drift, double* sum_subl,
+                     double* drift_mass, double* pbsm_more_than_avail);
+int pbsm3d_set_state(pbsm3d_ctx* ctx, const double* sum_drift, const double* sum_subl,
+                     const double* drift_mass, const double* pbsm_more_than_avail);
+
+/* Sliced-ELL export of the last assembled systems in the reference row order
+ * (row = z*n_faces + face) and the reference graph's slot order: self, lateral
+ * neighbours in face order 0..2 (present ones only), below, above
+ * (LinearAlgebra.cpp:67-116).  cols/vals are [rows*6], unused slots col=-1.
+ * rhs and x (solution) are [rows].  Any pointer may be NULL. */
+int pbsm3d_export_suspension(pbsm3d_ctx* ctx, int32_t* cols, double* vals, double* rhs, double* x);
+int pbsm3d_export_deposition(pbsm3d_ctx* ctx, int32_t* cols, double* vals, double* rhs, double* x);
+
+/* Learned warm start: load the MLP (14 -> 128 -> 128 -> 128 -> 1, BF16 weights
+ * as float values, row-major [out][in]) and the feature normalisation.
+ * Used when cfg.warm_start == PBSM3D_X0_LEARNED. */
+int pbsm3d_set_mlp(pbsm3d_ctx* ctx, const float* w0, const float* b0, const float* w1, const float* b1,
+                   const float* w2, const float* b2, const float* w3, const float* b3,
+                   const float* feat_mean, const float* feat_scale, float out_scale);
+
+/* Per-launch CUDA-event timing of every kernel (off by default).  When on,
+ * the step records an event pair around each launch on the context's stream
+ * and fills pbsm3d_stats.kern_*. */
+int pbsm3d_set_profiling(pbsm3d_ctx* ctx, int32_t on);
+
+/* Device-side timing of a region on the context's stream (measurement
+ * plumbing): pbsm3d_timer_mark records CUDA event `slot` (0..15) on the
+ * stream; pbsm3d_timer_elapsed waits for both and returns the milliseconds
+ * between them. */
+int pbsm3d_timer_mark(pbsm3d_ctx* ctx, int32_t slot);
+int pbsm3d_timer_elapsed(pbsm3d_ctx* ctx, int32_t a, int32_t b, double* ms);
+
+/* Message of the last failure on this context (or of the last failed create
+ * when ctx is NULL). */
+const char* pbsm3d_last_error(const pbsm3d_ctx* ctx);
+
+void pbsm3d_destroy(pbsm3d_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBSM3D_H */
