@@ -2,7 +2,6 @@
 
 The CUDA sources are compiled in parallel, one object per translation unit,
 then linked into chm_gb300/lib/libpbsm3d_cuda.so against the CUDA runtime.
-physics.cu is compiled with --fmad=false (see its header comment).
 """
 from __future__ import annotations
 
@@ -20,7 +19,7 @@ LIB = LIBDIR / "libpbsm3d_cuda.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr"]
-PER_FILE = {"physics.cu": ["--fmad=false"]}
+PER_FILE: dict = {}
 
 
 def nvcc() -> str:

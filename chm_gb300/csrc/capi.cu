@@ -137,7 +137,7 @@ void pbsm3d_config_defaults(pbsm3d_config* cfg) {
     cfg->susp_maxit = 1000;
     cfg->dep_maxit = 1000;
     cfg->susp_tol = 1e-8;
-    cfg->dep_tol = 1e-12;
+    cfg->dep_tol = 1e-10;
     cfg->inner_tol = 1e-5;
     cfg->slice_width = 0;
 }
@@ -226,6 +226,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     P.R = R;
     P.L = L;
     P.dz = 5.0 / (double)L;  // susp_depth / nLayer, PBSM3D.cpp:225-226
+    P.inv_dz = 1.0 / P.dz;
     P.dt = 0;
     P.use_exp_fetch = cfg.use_exp_fetch;
     P.use_tanh_fetch = cfg.use_tanh_fetch;
@@ -321,6 +322,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     }
     Susp& A = c.A;
     A.band = dalloc<double>(c, 6 * R, ok);
+    A.cztab = dalloc<CzCoef>(c, kMaxLayers, ok);
     A.rhs = dalloc<double>(c, R, ok);
     A.x = dalloc<double>(c, R, ok);
     A.u_z = dalloc<double>(c, R, ok);
@@ -364,6 +366,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     c.sc = dalloc<Scalars>(c, 4, ok);
     c.red.partials = dalloc<double>(c, (size_t)8 * c.red.nblocks, ok);
     c.ledger = dalloc<double>(c, 8, ok);
+    c.gbar = dalloc<GridBar>(c, 1, ok);
     if (!ok) {
         g_create_error = "out of device memory for " + std::to_string(T) + " faces x " + std::to_string(L) + " layers";
         free_all(c);
@@ -432,6 +435,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     if (cudaMemsetAsync(c.sc, 0, 4 * sizeof(Scalars), c.stream) != cudaSuccess) rc = 1;
     if (cudaMemsetAsync(A.x, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
     if (configure_solver_kernels(c)) rc = 1;
+    if (configure_cg(c)) rc = 1;
     launch_init_static(c, c.stream);
     if (cudaStreamSynchronize(c.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) rc = 1;
     if (rc) {

@@ -35,7 +35,7 @@ constexpr int kMaxTerms = 4;
 struct Params {
     int64_t T, Tp, R;
     int L;
-    double dz, dt;
+    double dz, inv_dz, dt;
     int use_exp_fetch, use_tanh_fetch, use_PomLi, use_R94_lambda, enable_veg;
     int do_fixed_settling, do_sublimation, do_lateral_diff, rouault;
     double settling_velocity, eps, min_sd_trans, cutoff, snow_diffusion_const;
@@ -74,8 +74,14 @@ struct FaceState {
     double *Qsalt, *Qsusp, *Qsubl, *Qsubl_mass, *sum_subl, *drift_mass, *sum_drift, *more, *bsp;
 };
 
+// Height-dependent coefficients of one layer (see cz_coeffs in physics.cu).
+struct CzCoef {
+    double inv_mm, r_z, omega, Qr, sigfac, l, pad0, pad1;
+};
+
 // Suspension system.
 struct Susp {
+    CzCoef* cztab;    // [L] for faces with hs == 0
     double* band;     // [6][R]
     double* rhs;      // [R]
     double* x;        // [R]
@@ -109,6 +115,12 @@ struct Scalars {
     unsigned counter[8];
 };
 
+// Grid-wide barrier state of a persistent (cooperative) kernel.
+struct GridBar {
+    unsigned count, gen;
+    int err, pad;
+};
+
 // Reduction workspace: per-block partials.
 struct ReduceWs {
     double* partials;  // [kMaxTerms][nblocks]
@@ -127,6 +139,7 @@ void launch_init_static(Ctx& c, cudaStream_t s);
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
+int configure_cg(Ctx& c);
 
 struct Ctx {
     pbsm3d_config cfg;
@@ -149,6 +162,8 @@ struct Ctx {
     int grid_rows, grid_faces;
     // ledger partial sums
     double* ledger;    // device [8]
+    GridBar* gbar;     // device
+    int coop_blocks;   // co-resident blocks of the persistent CG kernel
     cudaStream_t stream;
     cudaEvent_t ev[16];
     cudaEvent_t user_ev[16];
@@ -201,7 +216,7 @@ __device__ __forceinline__ double warp_max(double v) {
 // Deterministic block reduction of NT values (sum), result valid in thread 0.
 template <int NT>
 __device__ __forceinline__ void block_sum(double (&v)[NT]) {
-    __shared__ double sh[NT][kBlock / 32];
+    __shared__ double sh[NT][32];  // up to 1024 threads
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < NT; ++k) {

@@ -1,9 +1,19 @@
 // physics.cu -- per-face physics and system assembly of the PBSM3D step.
 //
-// Compiled with --fmad=false: every multiply and add rounds separately, in
-// the order the reference writes them, so the assembled systems agree with
-// a C++ evaluation of src/modules/PBSM3D.cpp to the last few ulps (the only
-// differences left come from CUDA's pow/log/exp/sin/cos).
+// The assembly is bound by the FP64 pipe (GB300 issues FP64 at a small
+// fraction of its FP32 rate), so it is written to spend as few FP64
+// instructions per row as the accuracy bar allows:
+//  * x^y for x > 0 is exp(y log x), and the particle-size terms share their
+//    logarithms (relative error a few 1e-16 against a correctly rounded pow);
+//  * terms that depend only on the layer height are tabulated per layer for
+//    the faces without a saltation layer;
+//  * NaN/Inf detection, the |rhs| maximum and sign tests run on the integer
+//    pipe (bit patterns);
+//  * multiply-adds contract to FMA, except in the saltation concentration
+//    whose bracket 1 - tau - u*_th^2/u*^2 cancels near the threshold and is
+//    evaluated with explicitly rounded operations in the reference's order.
+// The assembled entries agree with a C++ evaluation of
+// src/modules/PBSM3D.cpp to ~1e-15 relative.
 #include <math.h>
 
 #include "pbsm3d_internal.cuh"
@@ -14,6 +24,19 @@ namespace {
 constexpr double kKappa = 0.4;    // PhysConst.h:31
 constexpr double kRhoIce = 917;   // PhysConst.h:39
 constexpr double kZUR = 50.0;     // Atmosphere.h:31
+
+// x^y for x > 0 (x = 0 gives 0 for y > 0): exp(y * log(x)).
+__device__ __forceinline__ double powpos(double x, double y) { return exp(y * log(x)); }
+
+// Bit-pattern tests that keep comparisons off the FP64 pipe.
+__device__ __forceinline__ bool nonfinite(double x) {
+    return ((unsigned)(__double_as_longlong(x) >> 32) & 0x7ff00000u) == 0x7ff00000u;
+}
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+// x > 0 for a non-NaN x (false for +0 and -0)
+__device__ __forceinline__ bool gt0(double x) { return __double_as_longlong(x) > 0; }
 
 // module_base.hpp:471-479: -9999 or NaN
 __device__ __forceinline__ bool is_nan_chm(double v) { return fabs(v - -9999.0) < 1e-5 || isnan(v); }
@@ -44,7 +67,7 @@ __device__ __forceinline__ void bearing_to_cartesian(double bearing, double& x, 
 __device__ __forceinline__ double std_dry_air_density(double altitude, double temperature) {
     const double p0 = 101325., lapse = 0.0065, T0 = 288.15, Rd = 287.058, g = 9.80665, R0 = 6356766.0;
     const double expo = g / (lapse * Rd);
-    const double p = p0 * pow(1. - ((lapse * R0 * altitude) / (T0 * (R0 + altitude))), expo);
+    const double p = p0 * powpos(1. - ((lapse * R0 * altitude) / (T0 * (R0 + altitude))), expo);
     return p / (287.058 * temperature);
 }
 
@@ -56,11 +79,41 @@ __device__ __forceinline__ double dot2(double ax, double ay, double bx, double b
     return v1 + v2;
 }
 
+// Height-dependent terms of one suspension layer centred at cz
+// (PBSM3D.cpp:1003-1028, 1113-1120, 1157): mean particle radius and mass,
+// radius of the mean-mass particle, settling velocity, the log(cz) factor of
+// the undersaturation, the radiation term and the mixing length.
+__device__ __forceinline__ void cz_coeffs(double cz, double z0, const Params& P, CzCoef& o) {
+    const double lcz = log(cz);
+    const double rm = 4.6e-5 * exp(-0.258 * lcz);                   // 4.6e-5 cz^-0.258
+    const double mm_alpha = 4.08 + 12.6 * cz;
+    const double mm = 4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 / mm_alpha + 2. / (mm_alpha * mm_alpha));
+    o.inv_mm = 1.0 / mm;
+    const double lq = 0.3333333 * log((3.0 * mm) / (4 * M_PI * kRhoIce));
+    o.r_z = exp(lq);                                                // (3 mm / 4 pi rho)^0.3333333
+    double omega = P.settling_velocity;
+    if (!P.do_fixed_settling) omega = 1.1e7 * exp(1.8 * lq);       // 1.1e7 r_z^1.8
+    o.omega = omega * P.settling_scale;
+    o.Qr = 0.9 * M_PI * rm * rm * 120.0;
+    o.sigfac = 1.019 + 0.027 * lcz;
+    o.l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
+}
+
+// The same terms for every layer of a face with no saltation layer (hs = 0).
+__global__ void k_cz_table(Params P, CzCoef* tab) {
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= P.L) return;
+    const double hs = 0.0;
+    const double cz = z * P.dz + hs + P.dz / 2.;
+    cz_coeffs(cz, P.z0_snow, P, tab[z]);
+}
+
 // One face: saltation (PBSM3D.cpp:417-925), layer coefficients (:927-1233),
 // suspension rows (:1236-1404) and the Thomas factorisation of its column.
-__global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces G, Forcing F, FaceState S, Susp A,
+__global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Faces G, Forcing F, FaceState S, Susp A,
                                                                double* partials, Scalars* sc) {
-    double vmax = 0.0, vnan = 0.0;
+    unsigned long long vmax_bits = 0;
+    bool bad = false;
     const int64_t Tp = P.Tp, R = P.R;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= P.T) {  // padding face: identity rows
@@ -106,8 +159,10 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
         bool saltation = false;
         double z0 = 0;
         const double T_c = F.t[i];
-        double uth = 0.35 + (1.0 / 150.0) * T_c + (1.0 / 8200.0) * T_c * T_c;
-        uth = uth * P.uth_scale;
+        // u*_th decides saltation (ustar >= u*_th) and enters the cancelling
+        // c_salt bracket: evaluated without contraction, in the reference's order
+        double uth = __dadd_rn(__dadd_rn(0.35, __dmul_rn(1.0 / 150.0, T_c)), __dmul_rn(__dmul_rn(1.0 / 8200.0, T_c), T_c));
+        uth = __dmul_rn(uth, P.uth_scale);
         const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
         if (height_diff <= P.cutoff && snow_depth >= min_sd_trans_avg && !G.water[i]) {
             if (P.use_R94_lambda)
@@ -127,7 +182,7 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
         z0 = smax(P.z0_snow, z0);
         ustar = smax(0.01, ustar);
         double hs = 0;
-        if (saltation) hs = 0.08436 * pow(ustar, 1.27);
+        if (saltation) hs = 0.08436 * powpos(ustar, 1.27);
         double Qsalt = 0;
         double c_salt = 0;
         const double t = F.t[i] + 273.15;
@@ -148,8 +203,12 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
         if (saltation) {
             const double rho_f = std_dry_air_density(G.zc[i], t);
             const double Beta = 202.0, mB = 0.16;
-            const double tau_n_ratio = (mB * Beta * lambda) / (1.0 + mB * Beta * lambda);
-            c_salt = rho_f / (3.29 * ustar) * (1.0 - tau_n_ratio - (uth * uth) / (ustar * ustar));
+            const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
+            const double tau_n_ratio = __ddiv_rn(mbl, __dadd_rn(1.0, mbl));
+            // the bracket cancels near the threshold: no contraction here
+            const double bracket =
+                __dsub_rn(__dsub_rn(1.0, tau_n_ratio), __ddiv_rn(__dmul_rn(uth, uth), __dmul_rn(ustar, ustar)));
+            c_salt = __dmul_rn(__ddiv_rn(rho_f, __dmul_rn(3.29, ustar)), bracket);
             if (c_salt < 0 || isnan(c_salt)) {
                 c_salt = 0;
                 saltation = false;
@@ -174,10 +233,10 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
             Qsalt = c_salt * uhs * hs;
             double mass = 0;
             for (int j = 0; j < 3; ++j) {
-                const double udm = dot2(ux, uy, mx[j], my[j]);
-                mass += -Ej[j] * Qsalt * udm;
+                const double udm = __dadd_rn(__dmul_rn(ux, mx[j]), __dmul_rn(uy, my[j]));
+                mass = __dadd_rn(mass, __dmul_rn(__dmul_rn(-Ej[j], Qsalt), udm));
             }
-            mass = mass / area * P.dt;
+            mass = __dmul_rn(__ddiv_rn(mass, area), P.dt);
             if (mass < 0 && fabs(mass) > swe) {
                 c_salt = 0;
                 Qsalt = c_salt * uhs * hs;
@@ -187,14 +246,33 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
         S.saltation[i] = saltation;
 
         // ---- layers, PBSM3D.cpp:927-1404
+        // Per-face factors hoisted out of the layer loop.  Division by a
+        // per-face or constant value becomes a multiplication by its
+        // reciprocal and the sublimation rate is regrouped so no division is
+        // left per row (each change moves a result by at most a few ulps).
         const double rh = F.rh[i] / 100.;
         const double es = saturated_vapour_pressure(t);
-        const double D = 2.06e-5 * pow(t / 273.15, 1.75);
+        const double D = 2.06e-5 * powpos(t / 273.15, 1.75);
         const double lambda_t = 0.000063 * t + 0.00673;
         const double Ls = 2.838e6, M = 18.01, Rg = 8313;
         const double rho = (M * es) / (Rg * t);
+        // dm/dt = Sh rho D (2 pi Nu R r sigma t^2 lt - L M Qr + Qr R t) /
+        //         (D L Sh (L M - R t) rho + lt t^2 Nu R), Sh = Nu:
+        //       = q * (c1 Nu r sigma - L M Qr + Qr R t)
+        const double Rgt = Rg * t;
+        const double c1 = 6.283185308 * Rg * (t * t * lambda_t);
+        const double q_sub = (rho * D) / (D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
+        const double LsM = Ls * M;
         const double V5 = area * P.dz / 5.0;
-        double prev_up = 0.0, prev_beta = 1.0;
+        const double areaK = area * P.inv_dz;
+        const double sdz0 = snow_depth + z0;
+        const double inv_z0 = 1.0 / z0;
+        const double inv_logden = 1.0 / log((kZUR - sdz0) * inv_z0);
+        double v1 = 0, v2 = 0;
+        v1 += ux * ux;
+        v2 += uy * uy;
+        const double inv_nrm = 1.0 / sqrt(v1 + v2);
+        double prev_up = 0.0, prev_ib = 1.0;
         for (int z = 0; z < P.L; ++z) {
             const double cz = z * P.dz + hs + P.dz / 2.;
             double u_z;
@@ -203,47 +281,39 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
                 u_z = 2.8 * uth;
             else if (cz < height_diff)
                 u_z = 0.01;
-            else if (hz < kZUR)
-                u_z = smax(0.01, log_scale_wind(uref, kZUR, hz, snow_depth, z0));
+            else if (hz < kZUR)  // log_scale_wind(uref, 50, hz, snow_depth, z0)
+                u_z = smax(0.01, uref * log((hz - sdz0) * inv_z0) * inv_logden);
             else
                 u_z = smax(0.01, uref);
-            const double rm = 4.6e-5 * pow(cz, -0.258);
-            const double mm_alpha = 4.08 + 12.6 * cz;
-            const double mm =
-                4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 / mm_alpha + 2. / (mm_alpha * mm_alpha));
-            const double r_z = pow((3.0 * mm) / (4 * M_PI * kRhoIce), 0.3333333);
-            const double xrz = 0.005 * pow(u_z, 1.36);
-            double omega = P.settling_velocity;
-            if (!P.do_fixed_settling) omega = 1.1e7 * pow(r_z, 1.8);
-            omega = omega * P.settling_scale;
+            // height-dependent particle terms: a per-layer table when the
+            // suspension layer starts at the snow surface (hs == 0)
+            CzCoef co;
+            if (hs == 0.0)
+                co = A.cztab[z];
+            else
+                cz_coeffs(cz, z0, P, co);
+            const double xrz = 0.005 * powpos(u_z, 1.36);
+            const double omega = co.omega;
             const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
-            const double Re = 2.0 * r_z * Vr / 1.88e-5;
-            const double Nu = 1.79 + 0.606 * pow(Re, 0.5);
-            const double Sh = Nu;
-            const double sigma = (rh - 1.0) * (1.019 + 0.027 * log(cz));
-            const double Qr = 0.9 * M_PI * rm * rm * 120.0;
-            const double dmdtz =
-                Sh * rho * D * (6.283185308 * Nu * Rg * r_z * sigma * t * t * lambda_t - Ls * M * Qr + Qr * Rg * t) /
-                (D * Ls * Sh * (Ls * M - Rg * t) * rho + lambda_t * t * t * Nu * Rg);
-            double csubl = dmdtz / mm;
+            const double Re = 2.0 * co.r_z * Vr * (1.0 / 1.88e-5);
+            const double Nu = 1.79 + 0.606 * sqrt(Re);
+            const double sigma = (rh - 1.0) * co.sigfac;
+            const double dmdtz = q_sub * (c1 * Nu * co.r_z * sigma - LsM * co.Qr + co.Qr * Rgt);
+            double csubl = dmdtz * co.inv_mm;
             double alpha[5] = {0, 0, 0, 0, 0};
             if (P.do_lateral_diff)
                 for (int a = 0; a < 3; ++a) {
                     alpha[a] = Af[a];
                     alpha[a] *= 0.00001;
                 }
-            const double l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
             const double w = omega;
             double diffusion_coeff = P.snow_diffusion_const;
             if (P.rouault) diffusion_coeff = 1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar));
-            const double K34 = diffusion_coeff * ustar * l;
-            alpha[3] = area * K34 / P.dz;
-            alpha[4] = area * K34 / P.dz;
+            const double K34 = diffusion_coeff * ustar * co.l;
+            alpha[3] = areaK * K34;
+            alpha[4] = alpha[3];
             // wind vector scaled to u_z, then w: uvw = (ux, uy) * (u_z / |u|), -w
-            double v1 = 0, v2 = 0;
-            v1 += ux * ux;
-            v2 += uy * uy;
-            const double s = u_z / sqrt(v1 + v2);
+            const double s = u_z * inv_nrm;
             const double wx = ux * s, wy = uy * s;
             double udm[5];
 #pragma unroll
@@ -258,7 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 const bool has = nb[f] >= 0;
-                if (udm[f] > 0) {
+                if (gt0(udm[f])) {
                     if (has) {
                         dg += (V5 * csubl - Af[f] * udm[f] - alpha[f]);
                         lat[f] += alpha[f];
@@ -274,11 +344,12 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
                     }
                 }
             }
+            const bool top_out = gt0(udm[3]), bot_out = gt0(udm[4]);
             if (z == 0) {
-                const double alpha4 = area * K34 / (hs / 2.0 + P.dz / 2.0);
+                const double alpha4 = area * K34 / (hs / 2.0 + P.dz / 2.0);  // once per face
                 dg += V5 * csubl - area * udm[4] - alpha4;
                 b += -alpha4 * c_salt;
-                if (udm[3] > 0) {
+                if (top_out) {
                     dg += V5 * csubl - area * udm[3] - alpha[3];
                     if (P.L > 1) up += alpha[3];
                 } else {
@@ -287,14 +358,14 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
                 }
             } else if (z == P.L - 1) {
                 const double cprecip = 0;
-                if (udm[3] > 0) {
+                if (top_out) {
                     dg += V5 * csubl - area * udm[3] - alpha[3];
                     b += -alpha[3] * cprecip;
                 } else {
                     dg += V5 * csubl - alpha[3];
                     b += area * cprecip * udm[3] - alpha[3] * cprecip;
                 }
-                if (udm[4] > 0) {
+                if (bot_out) {
                     dg += V5 * csubl - area * udm[4] - alpha[4];
                     lo += alpha[4];
                 } else {
@@ -302,14 +373,14 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
                     lo += -area * udm[4] + alpha[4];
                 }
             } else {
-                if (udm[3] > 0) {
+                if (top_out) {
                     dg += V5 * csubl - area * udm[3] - alpha[3];
                     up += alpha[3];
                 } else {
                     dg += V5 * csubl - alpha[3];
                     up += -area * udm[3] + alpha[3];
                 }
-                if (udm[4] > 0) {
+                if (bot_out) {
                     dg += V5 * csubl - area * udm[4] - alpha[4];
                     lo += alpha[4];
                 } else {
@@ -326,7 +397,7 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
             A.rhs[r] = b;
             A.x[r] = 0.0;
             // Thomas factorisation of the column: beta_z = d_z - l_z * up_{z-1}
-            const double lz = (z == 0) ? 0.0 : lo / prev_beta;
+            const double lz = (z == 0) ? 0.0 : lo * prev_ib;
             const double beta = (z == 0) ? dg : dg - lz * prev_up;
             const double ib = 1.0 / beta;
             A.fac_l[r] = lz;
@@ -340,14 +411,16 @@ __global__ void __launch_bounds__(kBlock) k_assemble_suspension(Params P, Faces 
                 A.up32[r] = (float)up;
             }
             prev_up = up;
-            prev_beta = beta;
-            vmax = fmax(vmax, fabs(b));
-            if (isnan(dg) || isnan(b) || isnan(lat[0]) || isnan(lat[1]) || isnan(lat[2]) || isnan(lo) || isnan(up) ||
-                !isfinite(ib))
-                vnan = 1.0;
+            prev_ib = ib;
+            vmax_bits = max(vmax_bits, abs_bits(b));
+            if (nonfinite(dg) | nonfinite(b) | nonfinite(lat[0]) | nonfinite(lat[1]) | nonfinite(lat[2]) |
+                nonfinite(lo) | nonfinite(up) | nonfinite(ib))
+                bad = true;
         }
     }
-    // ||rhs||_inf and NaN flag: block max, last block finalises
+    // ||rhs||_inf (as the bit pattern of a non-negative double, whose integer
+    // order is its numeric order) and the NaN/Inf flag: last block finalises
+    const double vmax = __longlong_as_double((long long)vmax_bits), vnan = bad ? 1.0 : 0.0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     __shared__ double shm[2][kBlock / 32];
     double a = warp_max(vmax), bn = warp_max(vnan);
@@ -593,6 +666,7 @@ void launch_update(Ctx& c, cudaStream_t s) {
 
 // cx, cy: the centroid x/y staged in the CG work vectors by pbsm3d_create
 void launch_init_static(Ctx& c, cudaStream_t s) {
+    k_cz_table<<<1, 64, 0, s>>>(c.P, c.A.cztab);
     k_init_static<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.dr, c.dz_);
 }
 

@@ -374,6 +374,183 @@ __global__ void __launch_bounds__(kBlock) k_cg_resid(Params P, Dep D, const int3
     if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) sc->tmp = tot[0];
 }
 
+// ---------------------------------------------------------------- persistent deposition CG
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
+constexpr int kCgBlock = 512;  // one block per SM keeps barrier arrivals few
+
+// Grid-wide barrier of a cooperative launch.  The wait is bounded: after
+// kBarrierLimitNs a block sets gb->err and every block leaves at its next
+// barrier, so a fault in the co-residency assumption ends in an error, never
+// in a hang.  Returns false when the kernel must exit.
+__device__ bool grid_barrier(GridBar* gb) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned gen = ld_acquire_u32(&gb->gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        ok = 1;
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_timer_ns();
+            while (ld_acquire_u32(&gb->gen) == gen) {
+                if (*(volatile int*)&gb->err) {
+                    ok = 0;
+                    break;
+                }
+                if (global_timer_ns() - t0 > kBarrierLimitNs) {
+                    atomicExch(&gb->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Totals of NT per-thread values over the whole grid, identical in every
+// block (each block sums all partials in block order).  buf alternates
+// between two partial buffers so a fast block never overwrites partials a
+// slow block is still reading.
+template <int NT>
+__device__ bool grid_totals(double (&v)[NT], double* partials, GridBar* gb, double (&tot)[NT]) {
+    __shared__ double bc[NT];
+    block_sum<NT>(v);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NT; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+    if (!grid_barrier(gb)) return false;
+    double t[NT];
+    for (int k = 0; k < NT; ++k) {
+        double acc = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&partials[k * gridDim.x + b]);
+        t[k] = acc;
+    }
+    block_sum<NT>(t);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NT; ++k) bc[k] = t[k];
+    __syncthreads();
+    for (int k = 0; k < NT; ++k) tot[k] = bc[k];
+    __syncthreads();
+    return true;
+}
+
+// Jacobi-preconditioned CG on the deposition system in one cooperative
+// launch; at 1M faces its vectors and matrix (~100 MB) stay in L2.
+__global__ void __launch_bounds__(kCgBlock) k_cg_persistent(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
+                                                          double* zz, double* p, double* q, double* partials,
+                                                          GridBar* gb, Scalars* sc, double tol, int maxit) {
+    const int64_t Tp = P.Tp;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double* bufs[2] = {partials, partials + 4 * gridDim.x};
+    int nb_buf = 0;
+    // init: r = b, z = D^-1 b, p = z, q = A z
+    double a3[3] = {0, 0, 0}, t3[3];
+    for (int64_t i = i0; i < Tp; i += stride) {
+        const double bi = D.rhs[i];
+        const double zi = D.dinv[i] * bi;
+        double qi = D.diag[i] * zi;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = nbr[j * Tp + i];
+            if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.rhs[nb]);
+        }
+        r[i] = bi;
+        zz[i] = zi;
+        p[i] = zi;
+        q[i] = qi;
+        D.x[i] = 0.0;
+        a3[0] += bi * zi;
+        a3[1] += zi * qi;
+        a3[2] += bi * bi;
+    }
+    if (!grid_totals<3>(a3, bufs[nb_buf], gb, t3)) return;
+    nb_buf ^= 1;
+    double rho = t3[0];
+    const double bb = t3[2];
+    const double target2 = tol * tol * bb;
+    int status = 0, it = 0;
+    double rr = bb;
+    if (bb == 0.0) status = 1;
+    else if (!(t3[1] > 0.0)) status = 2;
+    double alpha = status ? 0.0 : rho / t3[1];
+    while (status == 0) {
+        double a2[2] = {0, 0}, t2[2];
+        for (int64_t i = i0; i < Tp; i += stride) {
+            D.x[i] += alpha * p[i];
+            const double ri = r[i] - alpha * q[i];
+            r[i] = ri;
+            const double zi = D.dinv[i] * ri;
+            zz[i] = zi;
+            a2[0] += ri * zi;
+            a2[1] += ri * ri;
+        }
+        if (!grid_totals<2>(a2, bufs[nb_buf], gb, t2)) return;
+        nb_buf ^= 1;
+        ++it;
+        rr = t2[1];
+        if (rr <= target2) {
+            status = 1;
+            break;
+        }
+        if (!isfinite(rr)) {
+            status = 2;
+            break;
+        }
+        if (it >= maxit) {
+            status = 3;
+            break;
+        }
+        const double beta = t2[0] / rho;
+        rho = t2[0];
+        double a1[1] = {0}, t1[1];
+        for (int64_t i = i0; i < Tp; i += stride) {
+            double az = D.diag[i] * zz[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) az += D.off[j * Tp + i] * zz[nb];
+            }
+            const double pi = zz[i] + beta * p[i];
+            const double qi = az + beta * q[i];
+            p[i] = pi;
+            q[i] = qi;
+            a1[0] += pi * qi;
+        }
+        if (!grid_totals<1>(a1, bufs[nb_buf], gb, t1)) return;
+        nb_buf ^= 1;
+        if (!(t1[0] > 0.0)) {
+            status = 2;
+            break;
+        }
+        alpha = rho / t1[0];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->iter = it;
+        sc->done = status;
+        sc->rnorm2 = rr;
+        sc->bnorm2 = bb;
+    }
+}
+
 template <typename V>
 Op<V> make_op(Ctx& c);
 template <>
@@ -542,42 +719,53 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     return 0;
 }
 
+int configure_cg(Ctx& c) {
+    int per_sm = 0, dev = 0, sms = 0;
+    PBSM_CUDA_TRY(cudaGetDevice(&dev));
+    PBSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int coop = 0;
+    PBSM_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent, kCgBlock, 0));
+    const int64_t need = (c.P.Tp + kCgBlock - 1) / kCgBlock;
+    // one co-resident block per SM (at most the partials workspace's 8 x grid_faces / 7 blocks)
+    int64_t blocks = std::min<int64_t>(need, per_sm >= 1 ? (int64_t)sms : 0);
+    blocks = std::min<int64_t>(blocks, (int64_t)c.red.nblocks);
+    c.coop_blocks = coop ? (int)blocks : 0;
+    return 0;
+}
+
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     (void)st;
-    const int g = c.grid_faces;
     double* part = c.red.partials;
     Scalars* sc = c.sc + 2;
     const int64_t T = c.P.T;
-    prof_begin(c, s);
-    k_cg_init<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, c.dz_, c.dp, c.dq, sc, part, c.cfg.dep_tol,
-                                   c.cfg.dep_maxit);
-    prof_end(c, s, PBSM3D_K_CG, T * 96);
-    int chunk = 8;
-    int before = 0;
-    while (true) {
-        for (int k = 0; k < chunk; ++k) {
-            prof_begin(c, s);
-            k_cg_x<<<g, kBlock, 0, s>>>(c.P, c.D, c.dr, c.dz_, c.dp, c.dq, sc, part);
-            prof_end(c, s, PBSM3D_K_CG, T * 64);
-            prof_begin(c, s);
-            k_cg_p<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dz_, c.dp, c.dq, sc, part);
-            prof_end(c, s, PBSM3D_K_CG, T * 84);
-        }
-        int rc = read_scalars(c, s, sc);
-        if (rc) return rc;
-        const int ran = c.sc_host->iter - before;
-        before = c.sc_host->iter;
-        const int idle = chunk - ran;
-        if (idle > 0) prof_drop(c, 2 * idle);
-        if (c.sc_host->done) break;
+    if (c.coop_blocks <= 0) {
+        c.err = "the device does not support cooperative launches";
+        return PBSM3D_ERR_CUDA;
     }
+    PBSM_CUDA_TRY(cudaMemsetAsync(c.gbar, 0, sizeof(GridBar), s));
+    double tol = c.cfg.dep_tol;
+    int maxit = c.cfg.dep_maxit;
+    void* args[] = {&c.P, &c.D, &c.F.nbr, &c.dr, &c.dz_, &c.dp, &c.dq, &part, &c.gbar, &sc, &tol, &maxit};
+    prof_begin(c, s);
+    PBSM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_persistent, dim3(c.coop_blocks), dim3(kCgBlock),
+                                              args, 0, s));
+    int rc = read_scalars(c, s, sc);
+    if (rc) return rc;
     const int done = c.sc_host->done;
     c.dep_iters = c.sc_host->iter;
+    prof_end(c, s, PBSM3D_K_CG, T * 96 + (int64_t)c.dep_iters * T * 148);
+    GridBar gb;
+    PBSM_CUDA_TRY(cudaMemcpy(&gb, c.gbar, sizeof(GridBar), cudaMemcpyDeviceToHost));
+    if (gb.err) {
+        c.err = "deposition solve: grid barrier timed out";
+        return PBSM3D_ERR_CUDA;
+    }
     const double bn2 = c.sc_host->bnorm2;
     prof_begin(c, s);
-    k_cg_resid<<<g, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);
+    k_cg_resid<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);
     prof_end(c, s, PBSM3D_K_CG, T * 76);
-    int rc = read_scalars(c, s, sc);
+    rc = read_scalars(c, s, sc);
     if (rc) return rc;
     c.dep_relres = bn2 > 0 ? sqrt(c.sc_host->tmp / bn2) : 0.0;
     if (done != DONE_CONVERGED && !(c.sc_host->tmp <= c.cfg.dep_tol * c.cfg.dep_tol * bn2)) {

@@ -259,4 +259,7 @@ CONFIGS = {
     "cfg1": dict(n_points=4096, side=5000.0, nLayer=5),
     # ~1.05M faces in a 70 km square, 10 layers
     "cfg2": dict(n_points=524288, side=70000.0, nLayer=10),
+    # the same point density at a quarter of the size (~262k faces), for
+    # profiler captures that must stay small
+    "cfg2q": dict(n_points=131072, side=35000.0, nLayer=10),
 }

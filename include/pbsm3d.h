@@ -116,7 +116,7 @@ typedef struct pbsm3d_config {
     int32_t susp_maxit;     /* 1000 (LinearAlgebra.cpp:167) */
     int32_t dep_maxit;      /* 1000 */
     double susp_tol;        /* relative residual ||b-Ax||/||b||, 1e-8 (LinearAlgebra.cpp:168) */
-    double dep_tol;         /* deposition relative residual, 1e-12 */
+    double dep_tol;         /* deposition relative residual, 1e-10 */
     double inner_tol;       /* MIXED: FP32 inner relative reduction per refinement sweep, 1e-5 */
     int32_t slice_width;    /* sliced-ELL rows per slice (power of two, 32..1024), 0 = autotune */
     int32_t reserved[7];

@@ -268,7 +268,7 @@ def _fill_defaults(c):
     c.susp_maxit = 1000
     c.dep_maxit = 1000
     c.susp_tol = 1e-8
-    c.dep_tol = 1e-12
+    c.dep_tol = 1e-10
     c.inner_tol = 1e-5
 
 

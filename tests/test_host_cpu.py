@@ -1,0 +1,136 @@
+"""Host-side logic on CPU: the module/factory mirror, config parsing, the
+C-ABI library's exports, and the replica reduction of bench.py under a
+2-rank gloo group."""
+import ctypes as C
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from chm_gb300 import capi
+from chm_gb300.pbsm3d import ModuleError, ModuleNotFound, PBSM3D, create, registered_keys
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def test_factory_and_depends_provides():
+    assert "PBSM3D" in registered_keys()
+    m = create("PBSM3D", {"nLayer": "10"})
+    assert isinstance(m, PBSM3D)
+    assert m.parallel == "domain"
+    for v in ("U_2m_above_srf", "vw_dir", "swe", "t", "rh", "U_R", "fetch"):
+        assert v in m.depends
+    for v in ("Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "Qsusp", "Qsalt", "sum_drift",
+              "pbsm_more_than_avail", "blowingsnow_probability", "global_cell_id"):
+        assert v in m.provides
+    m2 = create("PBSM3D", {"use_tanh_fetch": "false"})
+    assert "p_snow_hours" in m2.depends and "fetch" not in m2.depends
+    with pytest.raises(ModuleNotFound):
+        create("NotAModule", {})
+
+
+def test_config_errors_match_reference():
+    with pytest.raises(ModuleError, match="Cannot specify both"):
+        PBSM3D({"use_exp_fetch": "true", "use_tanh_fetch": "true"})
+    with pytest.raises(ModuleError, match="positive"):
+        PBSM3D({"settling_velocity": "-1"}).init(None)
+    with pytest.raises(ModuleError):
+        PBSM3D({"use_exp_fetch": "maybe"})
+
+
+def _header_functions():
+    text = (ROOT / "include" / "pbsm3d.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pbsm3d_[a-z_]+)\s*\(", text)))
+
+
+def test_library_exports_every_header_symbol(cuda_lib):
+    names = _header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(cuda_lib, n), n
+    assert set(names) == set(capi.EXPORTS)
+
+
+def test_struct_layout_matches_header(cuda_lib):
+    """The config defaults filled by the library read back through ctypes."""
+    cfg = capi.default_config(cuda_lib)
+    assert cfg.abi_version == capi.ABI_VERSION
+    assert cfg.nLayer == 10 and cfg.use_tanh_fetch == 1 and cfg.use_R94_lambda == 1
+    assert cfg.settling_velocity == 0.5 and cfg.smooth_coeff == 820 and cfg.susp_tol == 1e-8
+    assert cfg.gmres_restart == 30 and cfg.susp_maxit == 1000 and cfg.z0_snow == 0.01
+
+
+def test_create_without_gpu_is_an_error(cuda_lib):
+    """No CPU fallback: without a device the library refuses to create a context."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    from chm_gb300 import synth
+    m = synth.make_mesh(64, 300.0, 0)
+    keep = []
+    desc = capi.mesh_desc(m, keep)
+    cfg = capi.default_config(cuda_lib)
+    ctx = C.c_void_p()
+    rc = cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx))
+    assert rc == capi.ERR_CUDA
+    assert cuda_lib.pbsm3d_last_error(None)
+
+
+def test_create_rejects_bad_configs(cuda_lib):
+    from chm_gb300 import synth
+    m = synth.make_mesh(64, 300.0, 0)
+    keep = []
+    desc = capi.mesh_desc(m, keep)
+    ctx = C.c_void_p()
+    for bad in (dict(use_exp_fetch=1, use_tanh_fetch=1), dict(settling_velocity=-0.1), dict(nLayer=0),
+                dict(abi_version=99)):
+        cfg = capi.default_config(cuda_lib, **bad)
+        assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
+    cfg = capi.default_config(cuda_lib, iterative_subl=1)
+    assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_UNSUPPORTED
+    bad_nb = m.neighbor.copy()
+    bad_nb[0, 0] = m.n_faces + 5
+    m.neighbor = bad_nb
+    desc = capi.mesh_desc(m, keep)
+    cfg = capi.default_config(cuda_lib)
+    assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_BAD_MESH
+
+
+def _replica_worker(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import sys
+    sys.path.insert(0, str(ROOT))
+    import bench
+    d = bench.Dist(world)
+    d.barrier()
+    mx = d.max(float(rank + 1))
+    tot = d.sum(float(10 * (rank + 1)))
+    q.put((rank, mx, tot))
+    d.dist.destroy_process_group()
+
+
+def test_replica_reduction_two_ranks_gloo():
+    """bench.py --gpus N runs independent replicas: time = max over ranks,
+    element-steps = sum over ranks (gloo, world size 2)."""
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_replica_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+    assert res == [(0, 2.0, 30.0), (1, 2.0, 30.0)]
