@@ -68,5 +68,25 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+SHIM = ROOT / "chm_gb300" / "shim"
+HARNESS = LIBDIR / "pbsm3d_harness"
+
+
+def build_shim(force: bool = False) -> Path:
+    """The C++ module (CHM module_base replica + PBSM3D over the C ABI) and its
+    harness executable, linked against libpbsm3d_cuda.so."""
+    lib = build_cuda()
+    srcs = [SHIM / "PBSM3D_gpu.cpp", SHIM / "harness.cpp"]
+    deps = srcs + [SHIM / "PBSM3D_gpu.hpp", SHIM / "chm_module.hpp", ROOT / "include" / "pbsm3d.h", lib]
+    if force or _stale(HARNESS, deps):
+        cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", *map(str, srcs), "-o", str(HARNESS), f"-L{LIBDIR}", "-lpbsm3d_cuda",
+               f"-Wl,-rpath,{LIBDIR}"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"shim build failed:\n{r.stdout}\n{r.stderr}")
+    return HARNESS
+
+
 if __name__ == "__main__":
     print(build_cuda(force=True, verbose=True))

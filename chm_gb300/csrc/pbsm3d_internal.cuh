@@ -76,7 +76,13 @@ struct FaceState {
 
 // Height-dependent coefficients of one layer (see cz_coeffs in physics.cu).
 struct CzCoef {
-    double inv_mm, r_z, omega, Qr, sigfac, l, pad0, pad1;
+    double inv_mm, r_z, omega, Qr, sigfac, l;
+    double rz2nu;  // 2 r_z / nu: Re = rz2nu * Vr
+    double rsig;   // r_z * sigfac
+    double lwarg;  // table only: log((cz - z0) / z0), the wind-profile numerator
+    double llw;    // table only: log(lwarg)
+    double cz;     // layer centre height above the snow surface
+    double pad0;
 };
 
 // Suspension system.

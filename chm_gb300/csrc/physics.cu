@@ -97,15 +97,27 @@ __device__ __forceinline__ void cz_coeffs(double cz, double z0, const Params& P,
     o.Qr = 0.9 * M_PI * rm * rm * 120.0;
     o.sigfac = 1.019 + 0.027 * lcz;
     o.l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
+    o.rz2nu = 2.0 * o.r_z * (1.0 / 1.88e-5);                        // Re = rz2nu * Vr
+    o.rsig = o.r_z * o.sigfac;
+    o.lwarg = 0.0;
+    o.llw = 0.0;
+    o.cz = cz;
 }
 
-// The same terms for every layer of a face with no saltation layer (hs = 0).
+// The same terms for every layer of a face with no saltation layer (hs = 0),
+// plus log((cz - z0)/z0) of the wind profile and its logarithm.
 __global__ void k_cz_table(Params P, CzCoef* tab) {
     const int z = blockIdx.x * blockDim.x + threadIdx.x;
     if (z >= P.L) return;
     const double hs = 0.0;
     const double cz = z * P.dz + hs + P.dz / 2.;
-    cz_coeffs(cz, P.z0_snow, P, tab[z]);
+    const double z0 = P.z0_snow;
+    CzCoef o;
+    cz_coeffs(cz, z0, P, o);
+    o.cz = cz;
+    o.lwarg = log((cz - z0) * (1.0 / z0));
+    o.llw = log(o.lwarg);
+    tab[z] = o;
 }
 
 // One face: saltation (PBSM3D.cpp:417-925), layer coefficients (:927-1233),
@@ -246,10 +258,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         S.saltation[i] = saltation;
 
         // ---- layers, PBSM3D.cpp:927-1404
-        // Per-face factors hoisted out of the layer loop.  Division by a
-        // per-face or constant value becomes a multiplication by its
-        // reciprocal and the sublimation rate is regrouped so no division is
-        // left per row (each change moves a result by at most a few ulps).
+        // Everything that does not change with the layer is computed once per
+        // face.  Division by a per-face or constant value becomes a product
+        // with its reciprocal and the sublimation rate is regrouped so that no
+        // division is left per row (each change moves a result by a few ulps).
         const double rh = F.rh[i] / 100.;
         const double es = saturated_vapour_pressure(t);
         const double D = 2.06e-5 * powpos(t / 273.15, 1.75);
@@ -257,134 +269,159 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         const double Ls = 2.838e6, M = 18.01, Rg = 8313;
         const double rho = (M * es) / (Rg * t);
         // dm/dt = Sh rho D (2 pi Nu R r sigma t^2 lt - L M Qr + Qr R t) /
-        //         (D L Sh (L M - R t) rho + lt t^2 Nu R), Sh = Nu:
-        //       = q * (c1 Nu r sigma - L M Qr + Qr R t)
+        //         (D L Sh (L M - R t) rho + lt t^2 Nu R),  Sh = Nu,
+        //       = q * ((c1 (rh-1)) Nu (r sigfac) - Qr (L M - R t))
         const double Rgt = Rg * t;
-        const double c1 = 6.283185308 * Rg * (t * t * lambda_t);
+        const double c1r = 6.283185308 * Rg * (t * t * lambda_t) * (rh - 1.0);
         const double q_sub = (rho * D) / (D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
-        const double LsM = Ls * M;
+        const double LR = Ls * M - Rgt;
         const double V5 = area * P.dz / 5.0;
         const double areaK = area * P.inv_dz;
         const double sdz0 = snow_depth + z0;
         const double inv_z0 = 1.0 / z0;
-        const double inv_logden = 1.0 / log((kZUR - sdz0) * inv_z0);
+        const double logden = log((kZUR - sdz0) * inv_z0);
+        const double inv_logden = 1.0 / logden;
+        // log(u_z) = log(uref) - log(logden) + log(log((cz - z0)/z0)) on the
+        // fast path (hs == 0), so u_z^1.36 costs one exp per row there
+        const double lu_face = uref > 0.0 ? log(uref) - log(logden) : 0.0;
         double v1 = 0, v2 = 0;
         v1 += ux * ux;
         v2 += uy * uy;
         const double inv_nrm = 1.0 / sqrt(v1 + v2);
+        // lateral faces: udotm_f = u_z * k_f with k_f = (u_hat . m_f) / |u_hat|
+        double Ak[3], al[3];
+        bool out_f[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const double kf = inv_nrm * dot2(ux, uy, mx[f], my[f]);
+            Ak[f] = Af[f] * kf;
+            out_f[f] = gt0(kf);
+            al[f] = P.do_lateral_diff ? Af[f] * 0.00001 : 0.0;
+        }
+        const double ust_dc = P.snow_diffusion_const * ustar;
+        // Per-face versions of the per-row branch tests (no FP64 compare per
+        // row): the canopy test cz < height_diff can only hold when
+        // height_diff > 0, and hz < 50 m holds for every layer when the top of
+        // the suspension column is below 50 m.
+        const bool fast = hs == 0.0;
+        const bool in_canopy_possible = height_diff > 0.0;
+        const bool all_below_zur = snow_depth + hs + 5.0 + P.dz < kZUR;
+        const long long b001 = __double_as_longlong(0.01);
+        const bool uref_pos = uref > 0.0;
         double prev_up = 0.0, prev_ib = 1.0;
         for (int z = 0; z < P.L; ++z) {
-            const double cz = z * P.dz + hs + P.dz / 2.;
-            double u_z;
-            const double hz = cz + snow_depth;
-            if (saltation && cz < height_diff)
-                u_z = 2.8 * uth;
-            else if (cz < height_diff)
-                u_z = 0.01;
-            else if (hz < kZUR)  // log_scale_wind(uref, 50, hz, snow_depth, z0)
-                u_z = smax(0.01, uref * log((hz - sdz0) * inv_z0) * inv_logden);
-            else
-                u_z = smax(0.01, uref);
-            // height-dependent particle terms: a per-layer table when the
-            // suspension layer starts at the snow surface (hs == 0)
             CzCoef co;
-            if (hs == 0.0)
+            double cz;
+            if (fast) {
                 co = A.cztab[z];
-            else
+                cz = co.cz;
+            } else {
+                cz = z * P.dz + hs + P.dz / 2.;
                 cz_coeffs(cz, z0, P, co);
-            const double xrz = 0.005 * powpos(u_z, 1.36);
+            }
+            double u_z, xrz;
+            if (in_canopy_possible && saltation && cz < height_diff) {
+                u_z = 2.8 * uth;
+                xrz = 0.005 * powpos(u_z, 1.36);
+            } else if (in_canopy_possible && cz < height_diff) {
+                u_z = 0.01;
+                xrz = 0.005 * powpos(u_z, 1.36);
+            } else if (all_below_zur || cz + snow_depth < kZUR) {
+                // log_scale_wind(uref, 50, hz, snow_depth, z0), clamped at 0.01 m/s
+                const double larg = fast ? co.lwarg : log((cz + snow_depth - sdz0) * inv_z0);
+                const double u_raw = uref * larg * inv_logden;
+                const long long ub = __double_as_longlong(u_raw);
+                const bool above = ub > b001 && ub <= 0x7ff0000000000000ll;  // 0.01 < u_raw, not NaN
+                u_z = above ? u_raw : 0.01;
+                xrz = (fast && above && uref_pos) ? 0.005 * exp(1.36 * (lu_face + co.llw))
+                                                  : 0.005 * powpos(u_z, 1.36);
+            } else {
+                u_z = fmax(0.01, uref);
+                xrz = 0.005 * powpos(u_z, 1.36);
+            }
             const double omega = co.omega;
             const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
-            const double Re = 2.0 * co.r_z * Vr * (1.0 / 1.88e-5);
-            const double Nu = 1.79 + 0.606 * sqrt(Re);
-            const double sigma = (rh - 1.0) * co.sigfac;
-            const double dmdtz = q_sub * (c1 * Nu * co.r_z * sigma - LsM * co.Qr + co.Qr * Rgt);
+            const double Nu = 1.79 + 0.606 * sqrt(co.rz2nu * Vr);
+            const double dmdtz = q_sub * (c1r * Nu * co.rsig - co.Qr * LR);
             double csubl = dmdtz * co.inv_mm;
-            double alpha[5] = {0, 0, 0, 0, 0};
-            if (P.do_lateral_diff)
-                for (int a = 0; a < 3; ++a) {
-                    alpha[a] = Af[a];
-                    alpha[a] *= 0.00001;
-                }
             const double w = omega;
-            double diffusion_coeff = P.snow_diffusion_const;
-            if (P.rouault) diffusion_coeff = 1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar));
-            const double K34 = diffusion_coeff * ustar * co.l;
-            alpha[3] = areaK * K34;
+            double K34;
+            if (P.rouault)
+                K34 = (1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar))) * ustar * co.l;
+            else
+                K34 = ust_dc * co.l;
+            double alpha[5] = {al[0], al[1], al[2], areaK * K34, 0.0};
             alpha[4] = alpha[3];
-            // wind vector scaled to u_z, then w: uvw = (ux, uy) * (u_z / |u|), -w
-            const double s = u_z * inv_nrm;
-            const double wx = ux * s, wy = uy * s;
             double udm[5];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) udm[j] = dot2(wx, wy, mx[j], my[j]);
             udm[3] = -w;  // uvw . (0,0,1)
             udm[4] = w;   // uvw . (0,0,-1)
             const int64_t r = (int64_t)z * Tp + i;
             if (!P.do_sublimation) csubl = 0.0;
             A.u_z[r] = u_z;
             A.csubl[r] = csubl;
+            const double V5cs = V5 * csubl;
             double dg = 0.0, lat[3] = {0, 0, 0}, lo = 0.0, up = 0.0, b = 0.0;
 #pragma unroll
             for (int f = 0; f < 3; ++f) {
                 const bool has = nb[f] >= 0;
-                if (gt0(udm[f])) {
+                const double Au = u_z * Ak[f];  // A_f * udotm_f
+                if (out_f[f]) {
                     if (has) {
-                        dg += (V5 * csubl - Af[f] * udm[f] - alpha[f]);
+                        dg += (V5cs - Au - alpha[f]);
                         lat[f] += alpha[f];
                     } else {
-                        dg += (-0.1e-1 * alpha[f] - 1. * Af[f] * udm[f] + csubl * V5);
+                        dg += (-0.1e-1 * alpha[f] - 1. * Au + V5cs);
                     }
                 } else {
                     if (has) {
-                        dg += V5 * csubl - alpha[f];
-                        lat[f] += -Af[f] * udm[f] + alpha[f];
+                        dg += V5cs - alpha[f];
+                        lat[f] += -Au + alpha[f];
                     } else {
-                        dg += -0.1e-1 * alpha[f] - .99 * Af[f] * udm[f] + csubl * V5;
+                        dg += -0.1e-1 * alpha[f] - .99 * Au + V5cs;
                     }
                 }
             }
             const bool top_out = gt0(udm[3]), bot_out = gt0(udm[4]);
             if (z == 0) {
                 const double alpha4 = area * K34 / (hs / 2.0 + P.dz / 2.0);  // once per face
-                dg += V5 * csubl - area * udm[4] - alpha4;
+                dg += V5cs - area * udm[4] - alpha4;
                 b += -alpha4 * c_salt;
                 if (top_out) {
-                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    dg += V5cs - area * udm[3] - alpha[3];
                     if (P.L > 1) up += alpha[3];
                 } else {
-                    dg += V5 * csubl - alpha[3];
+                    dg += V5cs - alpha[3];
                     if (P.L > 1) up += -area * udm[3] + alpha[3];
                 }
             } else if (z == P.L - 1) {
                 const double cprecip = 0;
                 if (top_out) {
-                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    dg += V5cs - area * udm[3] - alpha[3];
                     b += -alpha[3] * cprecip;
                 } else {
-                    dg += V5 * csubl - alpha[3];
+                    dg += V5cs - alpha[3];
                     b += area * cprecip * udm[3] - alpha[3] * cprecip;
                 }
                 if (bot_out) {
-                    dg += V5 * csubl - area * udm[4] - alpha[4];
+                    dg += V5cs - area * udm[4] - alpha[4];
                     lo += alpha[4];
                 } else {
-                    dg += V5 * csubl - alpha[4];
+                    dg += V5cs - alpha[4];
                     lo += -area * udm[4] + alpha[4];
                 }
             } else {
                 if (top_out) {
-                    dg += V5 * csubl - area * udm[3] - alpha[3];
+                    dg += V5cs - area * udm[3] - alpha[3];
                     up += alpha[3];
                 } else {
-                    dg += V5 * csubl - alpha[3];
+                    dg += V5cs - alpha[3];
                     up += -area * udm[3] + alpha[3];
                 }
                 if (bot_out) {
-                    dg += V5 * csubl - area * udm[4] - alpha[4];
+                    dg += V5cs - area * udm[4] - alpha[4];
                     lo += alpha[4];
                 } else {
-                    dg += V5 * csubl - alpha[4];
+                    dg += V5cs - alpha[4];
                     lo += -area * udm[4] + alpha[4];
                 }
             }

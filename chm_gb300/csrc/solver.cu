@@ -676,8 +676,10 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         }
         int it = 0;
         if (c.P.mixed) {
-            // inner: A32 d = r32, d0 = 0, to inner_tol relative
-            const double itol = c.cfg.inner_tol;
+            // inner: A32 d = r32, d0 = 0, to inner_tol relative -- or less when
+            // the FP64 target is closer than that (no over-solving in the last sweep)
+            const double need = 0.5 * tol * sqrt(bnorm2 / rn2);
+            const double itol = std::min(0.5, std::max(c.cfg.inner_tol, need));
             Scalars init{};
             init.rho = rn2;
             init.alpha = init.omega = 1.0;

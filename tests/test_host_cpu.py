@@ -134,3 +134,14 @@ def test_replica_reduction_two_ranks_gloo():
     for p in ps:
         p.join(timeout=60)
     assert res == [(0, 2.0, 30.0), (1, 2.0, 30.0)]
+
+
+def test_cpp_module_shim_selftest(cuda_lib):
+    """The C++ module (CHM module_base/factory replica + PBSM3D over the C
+    ABI) builds and passes its host-side checks without a GPU."""
+    import subprocess
+    from chm_gb300 import build
+    exe = build.build_shim()
+    r = subprocess.run([str(exe), "--selftest"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "selftest ok" in r.stdout
