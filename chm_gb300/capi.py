@@ -94,6 +94,7 @@ EXPORTS = [
     "pbsm3d_config_defaults", "pbsm3d_create", "pbsm3d_step", "pbsm3d_get_state", "pbsm3d_set_state",
     "pbsm3d_export_suspension", "pbsm3d_export_deposition", "pbsm3d_set_mlp", "pbsm3d_set_profiling",
     "pbsm3d_timer_mark", "pbsm3d_timer_elapsed", "pbsm3d_last_error", "pbsm3d_destroy",
+    "pbsm3d_deposition_solve_noalloc",
 ]
 
 _lib = None
@@ -130,6 +131,9 @@ def load(path: Path | None = None):
     lib.pbsm3d_timer_mark.restype = C.c_int
     lib.pbsm3d_timer_elapsed.argtypes = [vp, C.c_int32, C.c_int32, _dp]
     lib.pbsm3d_timer_elapsed.restype = C.c_int
+    lib.pbsm3d_deposition_solve_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_double, C.c_int32,
+                                                    C.POINTER(C.c_int32), _dp]
+    lib.pbsm3d_deposition_solve_noalloc.restype = C.c_int
     lib.pbsm3d_last_error.argtypes = [vp]
     lib.pbsm3d_last_error.restype = C.c_char_p
     lib.pbsm3d_destroy.argtypes = [vp]

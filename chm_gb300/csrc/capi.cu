@@ -24,6 +24,8 @@ static thread_local std::string g_create_error;
 
 namespace pbsm {
 
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+
 void prof_begin(Ctx& c, cudaStream_t s) {
     c.launches++;
     if (!c.prof) return;

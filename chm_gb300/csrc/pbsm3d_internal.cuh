@@ -146,6 +146,8 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
 int configure_cg(Ctx& c);
+// capi.cu: the message pbsm3d_last_error(NULL) returns
+void set_global_error(const std::string& msg);
 
 struct Ctx {
     pbsm3d_config cfg;

@@ -293,6 +293,27 @@ int pbsm3d_set_profiling(pbsm3d_ctx* ctx, int32_t on);
 int pbsm3d_timer_mark(pbsm3d_ctx* ctx, int32_t slot);
 int pbsm3d_timer_elapsed(pbsm3d_ctx* ctx, int32_t a, int32_t b, double* ms);
 
+/*
+ * Deposition solve without device allocation.  No counterpart in the
+ * reference: it exists for hosts that own all device memory and do not let
+ * a library call cudaMalloc (a model that reserves the GPU at start-up and
+ * forbids allocation inside its time loop, or a framework whose memory pool
+ * is the only allocator on the device).  Solves the SPD deposition system
+ *   diag[i] x[i] + sum_j off[j*n+i] x[neighbor[j*n+i]] = rhs[i]
+ * (the layout pbsm3d_step assembles: SoA, j = 0..2, neighbour -1 = none) by
+ * Jacobi-preconditioned CG to ||rhs - A x|| <= tol ||rhs||, x0 = 0.  All
+ * arrays are device pointers of the current device, owned by the caller.
+ * Work space is a fixed static device array sized for at most 1,048,576
+ * faces (32 MiB, held by every device that loads the library until exit);
+ * larger n_faces returns PBSM3D_ERR_INVALID_ARG.  The first call on a device
+ * looks up that array's address (make it before any stream capture); calls
+ * that overlap on one device race on the shared array.  Runs on the legacy
+ * default stream and returns when done.  Messages: pbsm3d_last_error(NULL).
+ */
+int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* neighbor, const double* diag,
+                                    const double* off, const double* rhs, double* x, double tol, int32_t maxit,
+                                    int32_t* iters, double* rel_residual);
+
 /* Message of the last failure on this context (or of the last failed create
  * when ctx is NULL). */
 const char* pbsm3d_last_error(const pbsm3d_ctx* ctx);
