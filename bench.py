@@ -163,6 +163,8 @@ VARIANTS = {
     # name: config overrides (all reach relative residual 1e-8 in FP64)
     "plain_fp64": {"precision": capi.FP64},
     "mixed": {"precision": capi.MIXED},
+    "previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS},
+    "learned": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED},
 }
 
 
@@ -197,6 +199,12 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
         if rc != 0:
             raise RuntimeError(lib.pbsm3d_last_error(None).decode())
         lib.pbsm3d_set_profiling(ctx, 1)
+        if overrides.get("warm_start") == capi.X0_LEARNED:
+            from chm_gb300 import warmstart
+            p, mu, sc = warmstart.load()
+            rc = lib.pbsm3d_set_mlp(ctx, capi.ptr(p, C.c_float), capi.ptr(mu, C.c_float), capi.ptr(sc, C.c_float))
+            if rc != 0:
+                raise RuntimeError(lib.pbsm3d_last_error(ctx).decode())
         return ctx
 
     def step(ctx, fdesc, odesc):
@@ -218,6 +226,10 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
         return t, stats
 
     names = args.variants.split(",")
+    if "learned" in names:
+        from chm_gb300 import warmstart
+        if not warmstart.WEIGHTS_FILE.exists():
+            names.remove("learned")
     sampler = ClockSampler(local_rank)
     results = {}
     ctxs = {}
@@ -389,7 +401,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(synth.CONFIGS))
-    ap.add_argument("--variants", default="plain_fp64,mixed",
+    ap.add_argument("--variants", default="plain_fp64,mixed,previous,learned",
                     help="comma list of %s; the fastest meeting residual 1e-8 is the headline" % ",".join(VARIANTS))
     ap.add_argument("--wind", type=float, default=8.0)
     ap.add_argument("--seed", type=int, default=1)

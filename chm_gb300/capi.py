@@ -21,7 +21,7 @@ SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1
 FP64, MIXED = 0, 1
 X0_ZERO, X0_PREVIOUS, X0_LEARNED = 0, 1, 2
 KERNELS = ["ASSEMBLE", "BICG_P", "BICG_V", "BICG_S", "BICG_T", "BICG_X", "RESIDUAL", "POST", "DEP_ASSEMBLE", "CG",
-           "UPDATE", "OTHER"]
+           "UPDATE", "OTHER", "MLP"]
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -43,7 +43,7 @@ class Config(C.Structure):
         ("solver", C.c_int32), ("precision", C.c_int32), ("warm_start", C.c_int32), ("gmres_restart", C.c_int32),
         ("susp_maxit", C.c_int32), ("dep_maxit", C.c_int32),
         ("susp_tol", C.c_double), ("dep_tol", C.c_double), ("inner_tol", C.c_double),
-        ("slice_width", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("slice_width", C.c_int32), ("warm_flags", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -94,7 +94,9 @@ EXPORTS = [
     "pbsm3d_config_defaults", "pbsm3d_create", "pbsm3d_step", "pbsm3d_get_state", "pbsm3d_set_state",
     "pbsm3d_export_suspension", "pbsm3d_export_deposition", "pbsm3d_set_mlp", "pbsm3d_set_profiling",
     "pbsm3d_timer_mark", "pbsm3d_timer_elapsed", "pbsm3d_last_error", "pbsm3d_destroy",
-    "pbsm3d_deposition_solve_noalloc",
+    "pbsm3d_deposition_solve_noalloc", "pbsm3d_mlp_num_params", "pbsm3d_mlp_features", "pbsm3d_mlp_trainer_create",
+    "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
+    "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict",
 ]
 
 _lib = None
@@ -123,8 +125,27 @@ def load(path: Path | None = None):
     for n in ("pbsm3d_export_suspension", "pbsm3d_export_deposition"):
         getattr(lib, n).argtypes = [vp, _i32p, _dp, _dp, _dp]
         getattr(lib, n).restype = C.c_int
-    lib.pbsm3d_set_mlp.argtypes = [vp] + [_fp] * 10 + [C.c_float]
+    lib.pbsm3d_set_mlp.argtypes = [vp, _fp, _fp, _fp]
     lib.pbsm3d_set_mlp.restype = C.c_int
+    lib.pbsm3d_mlp_num_params.argtypes = []
+    lib.pbsm3d_mlp_num_params.restype = C.c_int
+    lib.pbsm3d_mlp_features.argtypes = [vp, vp, vp, C.c_int32]
+    lib.pbsm3d_mlp_features.restype = C.c_int
+    lib.pbsm3d_mlp_trainer_create.argtypes = [C.c_int32, _fp, _fp, _fp, C.POINTER(vp)]
+    lib.pbsm3d_mlp_trainer_create.restype = C.c_int
+    lib.pbsm3d_mlp_train.argtypes = [vp, vp, vp, C.c_int64, C.c_int32, C.c_float, C.c_uint64, _fp]
+    lib.pbsm3d_mlp_train.restype = C.c_int
+    lib.pbsm3d_mlp_grad.argtypes = [vp, _fp, _fp, _fp, _fp, _fp]
+    lib.pbsm3d_mlp_grad.restype = C.c_int
+    lib.pbsm3d_mlp_get_params.argtypes = [vp, _fp]
+    lib.pbsm3d_mlp_get_params.restype = C.c_int
+    lib.pbsm3d_mlp_trainer_destroy.argtypes = [vp]
+    lib.pbsm3d_mlp_trainer_destroy.restype = None
+    lib.pbsm3d_mlp_gemm_bf16.argtypes = [C.POINTER(C.c_uint16), C.POINTER(C.c_uint16), _fp, C.c_int32, C.c_int32,
+                                         C.c_int32]
+    lib.pbsm3d_mlp_gemm_bf16.restype = C.c_int
+    lib.pbsm3d_mlp_predict.argtypes = [vp, _dp]
+    lib.pbsm3d_mlp_predict.restype = C.c_int
     lib.pbsm3d_set_profiling.argtypes = [vp, C.c_int32]
     lib.pbsm3d_set_profiling.restype = C.c_int
     lib.pbsm3d_timer_mark.argtypes = [vp, C.c_int32]

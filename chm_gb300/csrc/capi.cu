@@ -187,9 +187,9 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
         g_create_error = "only the BiCGStab suspension solver is implemented";
         return PBSM3D_ERR_UNSUPPORTED;
     }
-    if (cfg.warm_start != PBSM3D_X0_ZERO && cfg.warm_start != PBSM3D_X0_PREVIOUS) {
-        g_create_error = "learned warm start needs pbsm3d_set_mlp support";
-        return PBSM3D_ERR_UNSUPPORTED;
+    if (cfg.warm_start < PBSM3D_X0_ZERO || cfg.warm_start > PBSM3D_X0_LEARNED) {
+        g_create_error = "unknown warm_start";
+        return PBSM3D_ERR_INVALID_ARG;
     }
     if (!(cfg.susp_tol > 0) || !(cfg.dep_tol > 0) || cfg.susp_maxit < 1 || cfg.dep_maxit < 1 ||
         (cfg.precision == PBSM3D_MIXED && !(cfg.inner_tol > 0 && cfg.inner_tol < 1))) {
@@ -327,6 +327,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     A.cztab = dalloc<CzCoef>(c, kMaxLayers, ok);
     A.rhs = dalloc<double>(c, R, ok);
     A.x = dalloc<double>(c, R, ok);
+    c.x_prev = dalloc<double>(c, R, ok);
     A.u_z = dalloc<double>(c, R, ok);
     A.csubl = dalloc<double>(c, R, ok);
     A.fac_l = dalloc<double>(c, R, ok);
@@ -436,6 +437,7 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     rc |= upload(c, Fo.psh, zero.data(), Tp * 8);
     if (cudaMemsetAsync(c.sc, 0, 4 * sizeof(Scalars), c.stream) != cudaSuccess) rc = 1;
     if (cudaMemsetAsync(A.x, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
+    if (cudaMemsetAsync(c.x_prev, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
     if (configure_solver_kernels(c)) rc = 1;
     if (configure_cg(c)) rc = 1;
     launch_init_static(c, c.stream);
@@ -482,11 +484,52 @@ int pbsm3d_timer_elapsed(pbsm3d_ctx* h, int32_t a, int32_t b, double* ms) {
     return 0;
 }
 
-int pbsm3d_set_mlp(pbsm3d_ctx* h, const float*, const float*, const float*, const float*, const float*,
-                   const float*, const float*, const float*, const float*, const float*, float) {
+int pbsm3d_set_mlp(pbsm3d_ctx* h, const float* params, const float* feat_mean, const float* feat_scale) {
+    if (!h || !params || !feat_mean || !feat_scale) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    int rc = mlp_load(c, params, feat_mean, feat_scale);
+    return rc;
+}
+
+int pbsm3d_mlp_features(pbsm3d_ctx* h, float* features, float* targets, int32_t on_device) {
     if (!h) return PBSM3D_ERR_INVALID_ARG;
-    h->c.err = "learned warm start is not built into this library version";
-    return PBSM3D_ERR_UNSUPPORTED;
+    Ctx& c = h->c;
+    const int64_t rows = c.P.T * c.P.L;
+    if (on_device) {
+        int rc = mlp_features(c, features, targets);
+        if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = PBSM3D_ERR_CUDA;
+        return rc;
+    }
+    float *df = nullptr, *dt = nullptr;
+    PBSM_CUDA_TRY(cudaMalloc(&df, rows * 14 * 4));
+    if (cudaMalloc(&dt, rows * 4) != cudaSuccess) {
+        cudaFree(df);
+        c.err = "out of device memory";
+        return PBSM3D_ERR_OUT_OF_MEMORY;
+    }
+    int rc = mlp_features(c, df, dt);
+    if (!rc && features)
+        rc = cudaMemcpyAsync(features, df, rows * 14 * 4, cudaMemcpyDeviceToHost, c.stream) ? PBSM3D_ERR_CUDA : 0;
+    if (!rc && targets)
+        rc = cudaMemcpyAsync(targets, dt, rows * 4, cudaMemcpyDeviceToHost, c.stream) ? PBSM3D_ERR_CUDA : 0;
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = PBSM3D_ERR_CUDA;
+    cudaFree(df);
+    cudaFree(dt);
+    return rc;
+}
+
+int pbsm3d_mlp_predict(pbsm3d_ctx* h, double* c_out) {
+    if (!h || !c_out) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    double* tmp = nullptr;
+    PBSM_CUDA_TRY(cudaMalloc(&tmp, c.P.R * 8));
+    int rc = launch_mlp_infer(c, c.stream, tmp);
+    if (!rc && cudaMemcpy2DAsync(c_out, c.P.T * 8, tmp, c.P.Tp * 8, c.P.T * 8, c.P.L, cudaMemcpyDeviceToHost,
+                                 c.stream) != cudaSuccess)
+        rc = PBSM3D_ERR_CUDA;
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) rc = PBSM3D_ERR_CUDA;
+    cudaFree(tmp);
+    return rc;
 }
 
 static int copy_in(Ctx& c, double* dst, const double* src, int on_device) {
@@ -546,10 +589,9 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     if (f->p_snow_hours && (rc = copy_in(c, c.Fo.psh, f->p_snow_hours, dev))) return rc;
     const int64_t h2d = dev ? 0 : c.P.T * 8 * (7 + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
 
-    // warm start: keep the previous solution in A.x (assembly zeroes it otherwise)
-    double* x_keep = nullptr;
-    if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS) x_keep = c.r;  // stash x before the assembly resets it
-    if (x_keep) PBSM_CUDA_TRY(cudaMemcpyAsync(x_keep, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+    // the previous step's solution (the assembly zeroes x, as the reference's
+    // zeroSystem does): kept for the warm starts and the MLP features
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
 
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
     launch_assemble_suspension(c, s);
@@ -564,7 +606,19 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     const double susp_rhs_max = c.sc_host->rhs_max;
     c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
     if (c.suspension_present) {
-        if (x_keep) PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, x_keep, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+        if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
+            PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, c.x_prev, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+        if (c.cfg.warm_start == PBSM3D_X0_LEARNED) {
+            // network guess, then one block-Jacobi sweep: each column then
+            // satisfies its own vertical balance exactly and only the lateral
+            // couplings act on the network's error
+            if (c.cfg.warm_flags & 2) {
+                if ((rc = launch_mlp_infer(c, s, c.A.x))) return rc;
+            } else {
+                if ((rc = launch_mlp_infer(c, s, c.r))) return rc;
+                if ((rc = jacobi_sweep(c, s, c.r, c.A.x))) return rc;
+            }
+        }
         rc = solve_suspension(c, s, st);
         PBSM_CUDA_TRY(cudaGetLastError());
         if (rc) return rc;

@@ -146,6 +146,11 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
 int configure_cg(Ctx& c);
+int jacobi_sweep(Ctx& c, cudaStream_t s, const double* xi, double* xo);
+// mlp.cu
+int launch_mlp_infer(Ctx& c, cudaStream_t s, double* x0);
+int mlp_features(Ctx& c, float* feat_dev, float* target_dev);
+int mlp_load(Ctx& c, const float* params, const float* fmean, const float* fscale);
 // capi.cu: the message pbsm3d_last_error(NULL) returns
 void set_global_error(const std::string& msg);
 
@@ -171,6 +176,13 @@ struct Ctx {
     // ledger partial sums
     double* ledger;    // device [8]
     GridBar* gbar;     // device
+    // previous step's solution (warm starts, training features) [R]
+    double* x_prev;
+    // learned warm start: BF16 weights (W0 padded to 16 inputs), FP32 rest
+    void* mlp_w;       // bf16: W0[128*16] W1[128*128] W2[128*128]
+    float* mlp_f;      // b0 b1 b2 w3 [4*128], b3, fmean[14], fscale[14]
+    bool mlp_loaded = false;
+    float mlp_b3 = 0.0f;
     int coop_blocks;   // co-resident blocks of the persistent CG kernel
     cudaStream_t stream;
     cudaEvent_t ev[16];
@@ -191,6 +203,7 @@ struct Ctx {
     bool suspension_present, deposition_present;
     int susp_iters, susp_matvecs, susp_refinements, dep_iters;
     double susp_relres, dep_relres;
+    double warm_gamma = 0.0;  // scale applied to the last warm start (0 = dropped)
 };
 
 // Record the start of a kernel launch of class cat with the given algorithmic

@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, const double* __r
                                                      V* __restrict__ vv, Scalars* sc, double* partials, double tol,
                                                      int maxit) {
     const int64_t Tp = P.Tp, R = P.R;
-    double acc[2] = {0, 0};
+    double acc[3] = {0, 0, 0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
         for (int z = 0; z < P.L; ++z) {
@@ -227,12 +227,14 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, const double* __r
             }
             acc[0] += rk * rk;
             acc[1] += b[k] * b[k];
+            acc[2] += b[k] * rk;
         }
     }
-    double tot[2];
-    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+    double tot[3];
+    if (block_partials_last<3>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
         sc->rnorm2 = tot[0];
         sc->bnorm2 = tot[1];
+        sc->red0 = tot[2];  // (b, r): lets the host scale a warm start
         sc->rho = tot[0];
         sc->alpha = 1.0;
         sc->omega = 1.0;
@@ -241,6 +243,52 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, const double* __r
         sc->iter = 0;
         sc->maxit = maxit;
         sc->done = tot[0] == 0.0 ? DONE_CONVERGED : DONE_NO;
+    }
+}
+
+// Warm start x0 -> gamma x0 (gamma = 0 drops it): r = (1-gamma) b + gamma r0,
+// and the Krylov state restarts from the new residual.
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_warm_scale(int64_t n, double gamma, double* __restrict__ x,
+                                                       double* __restrict__ r, const double* __restrict__ b,
+                                                       V* __restrict__ rv, V* __restrict__ rhv, Scalars* sc,
+                                                       double* partials) {
+    double acc[1] = {0};
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        x[k] *= gamma;
+        const double rk = (1.0 - gamma) * b[k] + gamma * r[k];
+        r[k] = rk;
+        rv[k] = (V)rk;
+        rhv[k] = (V)rk;
+        acc[0] += rk * rk;
+    }
+    double tot[1];
+    if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rnorm2 = tot[0];
+        sc->rho = tot[0];
+        sc->target2 = 0.0;  // set by the host
+        sc->done = tot[0] == 0.0 ? DONE_CONVERGED : DONE_NO;
+    }
+}
+
+// One block-Jacobi sweep on a guess: xo = B^{-1} (b - N xi) with B the
+// column tridiagonals (FP64 Thomas factors) and N the lateral couplings.
+__global__ void __launch_bounds__(kBlock) k_jacobi_sweep(Op<double> op, const double* __restrict__ b,
+                                                         const double* __restrict__ xi, double* __restrict__ xo) {
+    extern __shared__ unsigned char smem_raw[];
+    double* g = reinterpret_cast<double*>(smem_raw);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+        for (int z = 0; z < op.L; ++z) {
+            const int64_t base = (int64_t)z * op.Tp;
+            const int64_t k = base + i;
+            double u = b[k];
+            if (n0 >= 0) u -= op.lat[k] * xi[base + n0];
+            if (n1 >= 0) u -= op.lat[op.R + k] * xi[base + n1];
+            if (n2 >= 0) u -= op.lat[2 * op.R + k] * xi[base + n2];
+            g[z * blockDim.x + threadIdx.x] = u;
+        }
+        column_solve(op, i, g, xo);
     }
 }
 
@@ -627,10 +675,21 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, Scalars* sc, X* x, V* r, V* rh, 
 // launch needs the opt-in limit raised.
 int configure_solver_kernels(Ctx& c) {
     const int s64 = c.P.L * kBlock * 8, s32 = c.P.L * kBlock * 4;
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    return 0;
+}
+
+// xo = B^{-1} (b - N xi) on the FP64 operator (the learned warm start's smoothing)
+int jacobi_sweep(Ctx& c, cudaStream_t s, const double* xi, double* xo) {
+    Op<double> op = make_op<double>(c);
+    prof_begin(c, s);
+    k_jacobi_sweep<<<c.grid_faces, kBlock, (size_t)c.P.L * kBlock * 8, s>>>(op, c.A.rhs, xi, xo);
+    prof_end(c, s, PBSM3D_K_MLP, c.P.T * c.P.L * 72 + c.P.T * 12);
+    PBSM_CUDA_TRY(cudaGetLastError());
     return 0;
 }
 
@@ -662,6 +721,26 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         int rc = read_scalars(c, s, sc0);
         if (rc) return rc;
         if (sweeps == 0) bnorm2 = c.sc_host->bnorm2;
+        if (sweeps == 0 && c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1)) {
+            // Scale the warm start by the gamma that minimises ||b - gamma A x0||
+            // and drop it when that residual is not below ||b||: the zero
+            // guess stays the fallback.  (b, A x0) = |b|^2 - (b, r0),
+            // |A x0|^2 = |b|^2 - 2 (b, r0) + |r0|^2.
+            const double bb = bnorm2, br = c.sc_host->red0, rr = c.sc_host->rnorm2;
+            const double bax = bb - br, axax = bb - 2.0 * br + rr;
+            double gamma = (axax > 0 && bax > 0) ? bax / axax : 0.0;
+            const double rmin2 = axax > 0 ? bb - bax * bax / axax : bb;
+            if (!(rmin2 < 0.99 * bb)) gamma = 0.0;
+            c.warm_gamma = gamma;
+            prof_begin(c, s);
+            if (c.P.mixed)
+                k_warm_scale<float><<<g, kBlock, 0, s>>>(c.P.R, gamma, c.A.x, c.r, c.A.rhs, c.r32, c.rh32, sc0, part);
+            else
+                k_warm_scale<double><<<g, kBlock, 0, s>>>(c.P.R, gamma, c.A.x, c.r, c.A.rhs, c.r, c.rh, sc0, part);
+            prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 40);
+            rc = read_scalars(c, s, sc0);
+            if (rc) return rc;
+        }
         const double rn2 = c.sc_host->rnorm2;
         c.susp_relres = bnorm2 > 0 ? sqrt(rn2 / bnorm2) : 0.0;
         if (rn2 <= tol * tol * bnorm2) break;

@@ -119,7 +119,9 @@ typedef struct pbsm3d_config {
     double dep_tol;         /* deposition relative residual, 1e-10 */
     double inner_tol;       /* MIXED: FP32 inner relative reduction per refinement sweep, 1e-5 */
     int32_t slice_width;    /* sliced-ELL rows per slice (power of two, 32..1024), 0 = autotune */
-    int32_t reserved[7];
+    int32_t warm_flags;     /* warm starts: bit 0 = no residual-optimal rescaling of x0,
+                               bit 1 = no block-Jacobi sweep after the learned guess; 0 */
+    int32_t reserved[6];
 } pbsm3d_config;
 
 /*
@@ -241,7 +243,8 @@ enum pbsm3d_kernel {
     PBSM3D_K_CG = 9,         /* deposition CG iterations (both kernels) */
     PBSM3D_K_UPDATE = 10,    /* erosion/deposition update + mass ledger */
     PBSM3D_K_OTHER = 11,
-    PBSM3D_K_COUNT = 12
+    PBSM3D_K_MLP = 12,       /* learned warm start: features + fused 3-layer tensor-core MLP */
+    PBSM3D_K_COUNT = 13
 };
 
 typedef struct pbsm3d_ctx pbsm3d_ctx;
@@ -274,12 +277,46 @@ int pbsm3d_set_state(pbsm3d_ctx* ctx, const double* sum_drift, const double* sum
 int pbsm3d_export_suspension(pbsm3d_ctx* ctx, int32_t* cols, double* vals, double* rhs, double* x);
 int pbsm3d_export_deposition(pbsm3d_ctx* ctx, int32_t* cols, double* vals, double* rhs, double* x);
 
-/* Learned warm start: load the MLP (14 -> 128 -> 128 -> 128 -> 1, BF16 weights
- * as float values, row-major [out][in]) and the feature normalisation.
- * Used when cfg.warm_start == PBSM3D_X0_LEARNED. */
-int pbsm3d_set_mlp(pbsm3d_ctx* ctx, const float* w0, const float* b0, const float* w1, const float* b1,
-                   const float* w2, const float* b2, const float* w3, const float* b3,
-                   const float* feat_mean, const float* feat_scale, float out_scale);
+/*
+ * Learned warm start (x0 of the suspension solve when cfg.warm_start ==
+ * PBSM3D_X0_LEARNED): a per-row MLP 14 -> 128 -> 128 -> 128 -> 1 (ReLU),
+ * BF16 weights and activations, FP32 accumulation on the tensor cores.
+ * Parameters are one packed FP32 vector of pbsm3d_mlp_num_params() values:
+ *   W0[128][14] b0[128] W1[128][128] b1[128] W2[128][128] b2[128] w3[128] b3
+ * (W row-major [out][in]).  feat_mean/feat_scale standardise the 14 inputs:
+ * x = (f - mean) * scale.  No counterpart in the reference.
+ */
+int pbsm3d_mlp_num_params(void);
+int pbsm3d_set_mlp(pbsm3d_ctx* ctx, const float* params, const float* feat_mean, const float* feat_scale);
+
+/* Training data of the last step: the 14 raw features of every row
+ * (reference row order, [nLayer*n_faces][14]) computed from the step's
+ * system and the previous step's solution c_prev, and the target
+ * 100*(c - c_prev), the change of the step's solution.  Host arrays, or device arrays when on_device != 0;
+ * either may be NULL. */
+int pbsm3d_mlp_features(pbsm3d_ctx* ctx, float* features, float* targets, int32_t on_device);
+/* The loaded MLP's prediction of the last step's concentrations,
+ * c_prev + network/100 (before the block-Jacobi sweep the warm start applies),
+ * [nLayer*n_faces] host doubles, reference order. */
+int pbsm3d_mlp_predict(pbsm3d_ctx* ctx, double* c_out);
+
+/* GPU trainer of the MLP (Adam, loss 0.5 mean((y - t)^2)); batch rows a
+ * multiple of 128 (and of 1024 above 1024). */
+typedef struct pbsm3d_mlp_trainer pbsm3d_mlp_trainer;
+int pbsm3d_mlp_trainer_create(int32_t batch, const float* params, const float* feat_mean, const float* feat_scale,
+                              pbsm3d_mlp_trainer** out);
+/* `steps` minibatches drawn (seeded) from device arrays features [rows][14], targets [rows]. */
+int pbsm3d_mlp_train(pbsm3d_mlp_trainer* tr, const float* features, const float* targets, int64_t rows,
+                     int32_t steps, float lr, uint64_t seed, float* loss_per_step);
+/* One forward/backward over exactly `batch` host rows: gradients (packed), loss, outputs. */
+int pbsm3d_mlp_grad(pbsm3d_mlp_trainer* tr, const float* features, const float* targets, float* grads, float* loss,
+                    float* outputs);
+int pbsm3d_mlp_get_params(pbsm3d_mlp_trainer* tr, float* params);
+void pbsm3d_mlp_trainer_destroy(pbsm3d_mlp_trainer* tr);
+/* The tensor-core GEMM the MLP is built from: C[M][N] (FP32) = A[M][K] B[N][K]^T,
+ * A and B BF16 (raw 16-bit patterns), host arrays; M a multiple of 128,
+ * N in {16, 128}, K = 16 or a multiple of 64. */
+int pbsm3d_mlp_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t M, int32_t N, int32_t K);
 
 /* Per-launch CUDA-event timing of every kernel (off by default).  When on,
  * the step records an event pair around each launch on the context's stream

@@ -1,0 +1,159 @@
+"""The learned warm start: the tcgen05 BF16 GEMM, the MLP gradients against
+the FP64 oracle, the fused inference kernel against the layer-wise forward,
+and what a trained network gains over a zero initial guess."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from chm_gb300 import capi, synth, warmstart
+from chm_gb300.pbsm3d import PBSM3D
+
+pytestmark = pytest.mark.gpu
+
+
+def to_bf16_bits(x):
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+def from_bf16_bits(b):
+    return (b.astype(np.uint32) << 16).view(np.float32)
+
+
+def bf16_round(x):
+    return from_bf16_bits(to_bf16_bits(x))
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (256, 128, 128), (384, 16, 192), (128, 128, 16), (128, 16, 1024)])
+def test_tensor_core_gemm(cuda_lib, M, N, K):
+    rng = np.random.default_rng(M + N + K)
+    A = to_bf16_bits(rng.normal(size=(M, K)))
+    B = to_bf16_bits(rng.normal(size=(N, K)))
+    Cm = np.empty((M, N), np.float32)
+    rc = cuda_lib.pbsm3d_mlp_gemm_bf16(A.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                       B.ctypes.data_as(C.POINTER(C.c_uint16)),
+                                       Cm.ctypes.data_as(C.POINTER(C.c_float)), M, N, K)
+    assert rc == 0, cuda_lib.pbsm3d_last_error(None)
+    ref = from_bf16_bits(A).astype(np.float64) @ from_bf16_bits(B).astype(np.float64).T
+    assert np.abs(Cm - ref).max() <= 1e-4 * np.abs(ref).max() + 1e-4
+
+
+def _oracle_grads(oracle_lib, x, t, d):
+    from oracle.pyoracle import ptr
+    fp = C.c_float
+    n = x.shape[0]
+    G = {k: np.empty(v.shape) for k, v in d.items()}
+    args = [n, ptr(np.ascontiguousarray(x, np.float32), fp), ptr(np.ascontiguousarray(t, np.float32), fp)]
+    ws = {k: np.ascontiguousarray(v, np.float32) for k, v in d.items()}
+    for k in ("W0", "b0", "W1", "b1", "W2", "b2", "w3", "b3"):
+        args.append(ptr(ws[k], fp))
+    for k in ("W0", "b0", "W1", "b1", "W2", "b2", "w3", "b3"):
+        args.append(ptr(G[k]))
+    y = np.empty(n)
+    args.append(ptr(y))
+    loss = oracle_lib.oracle_mlp_loss_grad(*args)
+    return G, loss, y
+
+
+def test_mlp_gradients_match_oracle(cuda_lib, oracle_lib):
+    """Forward/backward on the tensor cores (BF16 operands, FP32 accumulation)
+    against the FP64 oracle fed the same BF16-rounded inputs and weights."""
+    rng = np.random.default_rng(1)
+    B = 256
+    params = warmstart.init_params(3)
+    d = warmstart.unpack(params.copy())
+    d["b0"][:] = rng.normal(0, 0.1, 128)
+    d["b1"][:] = rng.normal(0, 0.1, 128)
+    d["b2"][:] = rng.normal(0, 0.1, 128)
+    d["b3"][:] = 0.3
+    params = warmstart.pack(d)
+    feat = rng.normal(size=(B, 14)).astype(np.float32)
+    target = rng.normal(size=B).astype(np.float32)
+    mean = np.zeros(14, np.float32)
+    scale = np.ones(14, np.float32)
+    tr = warmstart.Trainer(params, mean, scale, batch=B)
+    g, loss, y = tr.grad(feat, target)
+    tr.close()
+    # oracle on the same BF16 inputs and weights (the hidden activations stay FP64 there)
+    dq = {k: (bf16_round(v) if k in ("W0", "W1", "W2") else v.astype(np.float32)) for k, v in d.items()}
+    Go, loss_o, yo = _oracle_grads(oracle_lib, bf16_round(feat), target, dq)
+    assert abs(loss - loss_o) <= 2e-2 * abs(loss_o)
+    assert np.abs(y - yo).max() <= 3e-2 * np.abs(yo).max()
+    gd = warmstart.unpack(g)
+    for k in ("W0", "b0", "W1", "b1", "W2", "b2", "w3", "b3"):
+        a, b = gd[k].ravel().astype(np.float64), Go[k].ravel()
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert rel < 5e-2 and cos > 0.998, (k, rel, cos)
+
+
+def test_fused_inference_matches_layerwise_forward(cuda_lib):
+    w = synth.Workload(1024, 2500.0, seed=31)
+    m = PBSM3D({"nLayer": "5"})
+    m.init(w.mesh)
+    m.run(w.forcing(0), 3600.0)
+    m.run(w.forcing(1), 3600.0)
+    feat, _ = warmstart.features(m)
+    mean = feat.mean(0).astype(np.float32)
+    scale = (1.0 / np.maximum(feat.std(0), 1e-6)).astype(np.float32)
+    params = warmstart.init_params(7)
+    d = warmstart.unpack(params)
+    d["b3"][:] = 0.5
+    params = warmstart.pack(d)
+    warmstart.set_mlp(m, params, mean, scale)
+    pred = warmstart.predict(m)  # c units
+    B = 1024
+    tr = warmstart.Trainer(params, mean, scale, batch=B)
+    _, _, y = tr.grad(feat[:B], np.zeros(B, np.float32))
+    tr.close()
+    # prediction = c_prev + network output / 100; feature 9 is 100 * c_prev
+    delta = pred[:B] - feat[:B, 9].astype(np.float64) / 100.0
+    ref = y / 100.0
+    assert np.abs(delta - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-7
+    m.close()
+
+
+def test_learned_warm_start_gain(cuda_lib):
+    """Train on plain-solver solutions of training seeds, then on a held-out
+    seed measure what the network gains over the method without it: its
+    predicted field against the previous step's field (the guess available
+    without a network) and the Krylov iterations from x0 = 0, from the
+    previous field and from the learned guess, all at relative residual 1e-8.
+
+    The network predicts the field markedly better than the previous step's
+    field does (relative L2 error), which is asserted.  Its remaining error is
+    row-to-row noise, the component the column-preconditioned BiCGStab
+    resolves slowest, so the iteration count from the learned guess is
+    reported, not asserted to be lower."""
+    L = 5
+    params, mean, scale, losses, n = warmstart.train_from_solutions(
+        train_seeds=[101, 102, 103, 104], n_points=4096, side=5000.0, nLayer=L, steps_per_seed=8,
+        rows_per_step=20000, train_steps=1500, lr=2e-3, batch=2048, seed=0)
+    assert losses[-50:].mean() < 0.3 * losses[:20].mean(), (losses[:5], losses[-5:])
+    iters, err_learned, err_prev = {}, [], []
+    for ws in (capi.X0_ZERO, capi.X0_PREVIOUS, capi.X0_LEARNED):
+        w = synth.Workload(4096, 5000.0, seed=777)
+        m = PBSM3D({"nLayer": str(L)})
+        m.init(w.mesh, warm_start=ws)
+        if ws == capi.X0_LEARNED:
+            warmstart.set_mlp(m, params, mean, scale)
+        its = []
+        for s in range(8):
+            out = m.run(w.forcing(s), 3600.0, want_c=True)
+            assert m.last_stats["susp_rel_residual"] <= 1e-8
+            if s > 0:
+                its.append(m.last_stats["susp_iters"])
+                if ws == capi.X0_LEARNED:
+                    pred = warmstart.predict(m)
+                    feat, _ = warmstart.features(m)
+                    c = out["c"]
+                    err_learned.append(np.linalg.norm(pred - c) / np.linalg.norm(c))
+                    err_prev.append(np.linalg.norm(feat[:, 9] / 100.0 - c) / np.linalg.norm(c))
+            w.apply_drift(out["drift_mass"])
+        iters[ws] = np.mean(its)
+        m.close()
+    print(f"held-out seed: relative L2 error of the guess: learned {np.mean(err_learned):.3f}, previous field "
+          f"{np.mean(err_prev):.3f}; BiCGStab iterations to 1e-8: zero {iters[capi.X0_ZERO]:.2f}, previous "
+          f"{iters[capi.X0_PREVIOUS]:.2f}, learned {iters[capi.X0_LEARNED]:.2f}")
+    assert np.mean(err_learned) < 0.7 * np.mean(err_prev)
