@@ -43,7 +43,7 @@ def test_config_errors_match_reference():
 def _header_functions():
     text = (ROOT / "include" / "pbsm3d.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pbsm3d_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(pbsm3d_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_library_exports_every_header_symbol(cuda_lib):
