@@ -55,6 +55,10 @@ class MeshDesc(C.Structure):
     ]
 
 
+class Member(C.Structure):
+    _fields_ = [("ustar_th_scale", C.c_double), ("z0_snow", C.c_double), ("settling_scale", C.c_double)]
+
+
 class ForcingDesc(C.Structure):
     _fields_ = [(n, _dp) for n in ("U_R", "U_2m_above_srf", "vw_dir", "swe", "t", "rh", "snowdepthavg", "fetch",
                                    "p_snow_hours")] + [("on_device", C.c_int32)]
@@ -96,7 +100,7 @@ EXPORTS = [
     "pbsm3d_timer_mark", "pbsm3d_timer_elapsed", "pbsm3d_last_error", "pbsm3d_destroy",
     "pbsm3d_deposition_solve_noalloc", "pbsm3d_mlp_num_params", "pbsm3d_mlp_features", "pbsm3d_mlp_trainer_create",
     "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
-    "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict",
+    "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
 ]
 
 _lib = None
@@ -116,6 +120,11 @@ def load(path: Path | None = None):
     lib.pbsm3d_config_defaults.restype = None
     lib.pbsm3d_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(Config), C.POINTER(vp)]
     lib.pbsm3d_create.restype = C.c_int
+    lib.pbsm3d_ensemble_create.argtypes = [C.c_int32, C.POINTER(MeshDesc), C.POINTER(Member), C.POINTER(Config),
+                                           C.POINTER(vp)]
+    lib.pbsm3d_ensemble_create.restype = C.c_int
+    lib.pbsm3d_member_offsets.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.pbsm3d_member_offsets.restype = C.c_int
     lib.pbsm3d_step.argtypes = [vp, C.POINTER(ForcingDesc), C.c_double, C.POINTER(Outputs), C.POINTER(Stats)]
     lib.pbsm3d_step.restype = C.c_int
     lib.pbsm3d_get_state.argtypes = [vp, _dp, _dp, _dp, _dp]

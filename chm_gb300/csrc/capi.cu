@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <new>
 #include <string>
@@ -148,7 +149,8 @@ const char* pbsm3d_last_error(const pbsm3d_ctx* ctx) {
     return ctx ? ctx->c.err.c_str() : g_create_error.c_str();
 }
 
-int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbsm3d_ctx** out) {
+static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in,
+                       const std::vector<int64_t>& offsets, const std::vector<Member>& members, pbsm3d_ctx** out) {
     if (!out) return PBSM3D_ERR_INVALID_ARG;
     *out = nullptr;
     if (!mesh || !cfg_in) {
@@ -160,6 +162,12 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
         g_create_error = "config abi_version mismatch (use pbsm3d_config_defaults)";
         return PBSM3D_ERR_INVALID_ARG;
     }
+    for (const Member& m : members)
+        if (!(m.z0 > 0) || !std::isfinite(m.z0) || !(m.uth_scale > 0) || !std::isfinite(m.uth_scale) ||
+            !(m.settling_scale >= 0) || !std::isfinite(m.settling_scale)) {
+            g_create_error = "z0_snow and ustar_th_scale must be positive, settling_scale non-negative";
+            return PBSM3D_ERR_INVALID_ARG;
+        }
     if (mesh->n_faces <= 0 || mesh->n_faces > (int64_t)INT32_MAX / 2 || !mesh->neighbor || !mesh->edge_length ||
         !mesh->edge_normal || !mesh->area || !mesh->center) {
         g_create_error = "invalid mesh description";
@@ -247,17 +255,15 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     P.min_sd_trans = cfg.min_sd_trans;
     P.cutoff = cfg.cutoff;
     P.snow_diffusion_const = cfg.snow_diffusion_const;
-    P.uth_scale = cfg.ustar_th_scale;
-    P.z0_snow = cfg.z0_snow;
-    P.settling_scale = cfg.settling_scale;
     P.cos_pi_4 = cos(M_PI / 4.0);
     {
         const double fetch_ref = 300;
         P.Lc_tanh = 0.5 * tanh(0.1333333333e-1 * fetch_ref - 2.0) + 0.5;
     }
     P.log_2_0002 = log(2.0 / 0.0002);
-    P.log_zur_z0 = log(50.0 / cfg.z0_snow);
     P.mixed = cfg.precision == PBSM3D_MIXED;
+    c.member_offsets = offsets;
+    const int nm = (int)members.size();
 
     int sms = 0, dev = 0;
     cudaGetDevice(&dev);
@@ -324,7 +330,17 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     }
     Susp& A = c.A;
     A.band = dalloc<double>(c, 6 * R, ok);
-    A.cztab = dalloc<CzCoef>(c, kMaxLayers, ok);
+    A.cztab = dalloc<CzCoef>(c, (size_t)kMaxLayers * nm, ok);
+    int32_t* face_member = dalloc<int32_t>(c, Tp, ok);
+    Member* prm = dalloc<Member>(c, nm, ok);
+    c.Mb.n = nm;
+    c.Mb.face_member = face_member;
+    c.Mb.prm = prm;
+    c.Mb.rhs_max = dalloc<unsigned long long>(c, nm, ok);
+    c.Mb.dep_max = dalloc<unsigned long long>(c, nm, ok);
+    c.Mb.bb = dalloc<double>(c, nm, ok);
+    c.Mb.susp_present = dalloc<int>(c, nm, ok);
+    c.Mb.dep_present = dalloc<int>(c, nm, ok);
     A.rhs = dalloc<double>(c, R, ok);
     A.x = dalloc<double>(c, R, ok);
     c.x_prev = dalloc<double>(c, R, ok);
@@ -420,6 +436,16 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     if (mesh->is_water)
         for (int64_t i = 0; i < T; ++i) water[i] = mesh->is_water[i] ? 1 : 0;
     rc |= upload(c, F.water, water.data(), Tp);
+    {
+        std::vector<int32_t> fm(Tp, 0);
+        for (int m = 0; m < nm; ++m)
+            for (int64_t i = offsets[m]; i < offsets[m + 1]; ++i) fm[i] = m;
+        rc |= upload(c, face_member, fm.data(), Tp * 4);
+        rc |= upload(c, prm, members.data(), nm * sizeof(Member));
+        std::vector<int> ones(nm, 1);
+        rc |= upload(c, c.Mb.susp_present, ones.data(), nm * 4);
+        rc |= upload(c, c.Mb.dep_present, ones.data(), nm * 4);
+    }
     rc |= upload(c, c.dr, cx.data(), Tp * 8);
     rc |= upload(c, c.dz_, cy.data(), Tp * 8);
     // module state: CHM face variables start at -9999, sum_drift/sum_subl at 0
@@ -452,6 +478,103 @@ int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in, pbs
     c.bytes = 0;
     *out = h;
     return 0;
+}
+
+int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, pbsm3d_ctx** out) {
+    if (!mesh || !cfg) {
+        g_create_error = "null mesh or config";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    Member m{cfg->ustar_th_scale, cfg->z0_snow, cfg->settling_scale, log(50.0 / cfg->z0_snow)};
+    return create_core(mesh, cfg, {0, mesh->n_faces}, {m}, out);
+}
+
+int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, const pbsm3d_member* members,
+                           const pbsm3d_config* cfg, pbsm3d_ctx** out) {
+    if (!out || !meshes || !members || !cfg || n_members < 1 || n_members > kMaxMembers) {
+        g_create_error = "ensemble: 1..256 members with meshes, member parameters and a config";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    // the members' meshes as one disjoint union (faces in member order,
+    // neighbour ids shifted by each member's face offset)
+    std::vector<int64_t> off(n_members + 1, 0);
+    // vegetation is a per-domain switch in the reference (PBSM3D.cpp:283-325):
+    // the members must agree on it
+    bool veg = true, lai = false, sn = false, sd = false, water = false;
+    for (int m = 0; m < n_members; ++m) {
+        const pbsm3d_mesh_desc& d = meshes[m];
+        if (d.n_faces <= 0 || !d.neighbor || !d.edge_length || !d.edge_normal || !d.area || !d.center) {
+            g_create_error = "ensemble: invalid mesh of member " + std::to_string(m);
+            return PBSM3D_ERR_INVALID_ARG;
+        }
+        off[m + 1] = off[m] + d.n_faces;
+        bool mveg = d.canopy_height != nullptr;
+        if (mveg && d.has_vegetation)
+            for (int64_t i = 0; i < d.n_faces; ++i) mveg = mveg && d.has_vegetation[i];
+        if (m > 0 && mveg != veg) {
+            g_create_error = "ensemble: members must all have vegetation on every face, or none";
+            return PBSM3D_ERR_INVALID_ARG;
+        }
+        veg = mveg;
+        lai = lai || d.lai;
+        sn = sn || d.stalk_number;
+        sd = sd || d.stalk_diameter;
+        water = water || d.is_water;
+    }
+    const int64_t T = off[n_members];
+    std::vector<int32_t> nb(3 * T);
+    std::vector<double> E(3 * T), M(6 * T), area(T), C(3 * T), ch, la, sN, sD;
+    std::vector<uint8_t> wat;
+    if (veg) ch.resize(T);
+    if (veg && lai) la.assign(T, 0.0);
+    if (veg && sn) sN.assign(T, 1.0);
+    if (veg && sd) sD.assign(T, 0.8);
+    if (water) wat.assign(T, 0);
+    for (int m = 0; m < n_members; ++m) {
+        const pbsm3d_mesh_desc& d = meshes[m];
+        const int64_t o = off[m], n = d.n_faces;
+        for (int64_t k = 0; k < 3 * n; ++k) {
+            const int32_t v = d.neighbor[k];
+            if (v < -1 || v >= n) {
+                g_create_error = "ensemble: neighbour out of range in member " + std::to_string(m);
+                return PBSM3D_ERR_BAD_MESH;
+            }
+            nb[3 * o + k] = v >= 0 ? (int32_t)(v + o) : -1;
+        }
+        std::copy(d.edge_length, d.edge_length + 3 * n, E.begin() + 3 * o);
+        std::copy(d.edge_normal, d.edge_normal + 6 * n, M.begin() + 6 * o);
+        std::copy(d.area, d.area + n, area.begin() + o);
+        std::copy(d.center, d.center + 3 * n, C.begin() + 3 * o);
+        if (veg) std::copy(d.canopy_height, d.canopy_height + n, ch.begin() + o);
+        if (veg && lai && d.lai) std::copy(d.lai, d.lai + n, la.begin() + o);
+        if (veg && sn && d.stalk_number) std::copy(d.stalk_number, d.stalk_number + n, sN.begin() + o);
+        if (veg && sd && d.stalk_diameter) std::copy(d.stalk_diameter, d.stalk_diameter + n, sD.begin() + o);
+        if (water && d.is_water) std::copy(d.is_water, d.is_water + n, wat.begin() + o);
+    }
+    pbsm3d_mesh_desc u{};
+    u.n_faces = T;
+    u.neighbor = nb.data();
+    u.edge_length = E.data();
+    u.edge_normal = M.data();
+    u.area = area.data();
+    u.center = C.data();
+    u.canopy_height = veg ? ch.data() : nullptr;
+    u.lai = la.empty() ? nullptr : la.data();
+    u.stalk_number = sN.empty() ? nullptr : sN.data();
+    u.stalk_diameter = sD.empty() ? nullptr : sD.data();
+    u.has_vegetation = nullptr;
+    u.is_water = wat.empty() ? nullptr : wat.data();
+    std::vector<Member> mp(n_members);
+    for (int m = 0; m < n_members; ++m)
+        mp[m] = Member{members[m].ustar_th_scale, members[m].z0_snow, members[m].settling_scale,
+                       log(50.0 / members[m].z0_snow)};
+    return create_core(&u, cfg, off, mp, out);
+}
+
+int pbsm3d_member_offsets(const pbsm3d_ctx* h, int64_t* offsets) {
+    if (!h || !offsets) return PBSM3D_ERR_INVALID_ARG;
+    std::copy(h->c.member_offsets.begin(), h->c.member_offsets.end(), offsets);
+    return (int)h->c.member_offsets.size() - 1;
 }
 
 void pbsm3d_destroy(pbsm3d_ctx* h) {
@@ -532,6 +655,48 @@ int pbsm3d_mlp_predict(pbsm3d_ctx* h, double* c_out) {
     return rc;
 }
 
+// Ensembles (which 0: suspension, 1: deposition): each member's own
+// "present" test (||rhs_m||_inf > 1e-12, PBSM3D.cpp:1424-1427, 1661-1664);
+// absent members get a zero right-hand side (solution exactly 0, and no
+// update), and the joint Krylov target becomes tol * min_m ||rhs_m|| so every
+// present member reaches its own relative tolerance.
+static int member_presence(Ctx& c, cudaStream_t s, int which) {
+    const int n = c.Mb.n;
+    std::vector<unsigned long long> mx(n);
+    std::vector<int> present(n), susp(n);
+    PBSM_CUDA_TRY(cudaMemcpyAsync(mx.data(), which ? c.Mb.dep_max : c.Mb.rhs_max, n * 8, cudaMemcpyDeviceToHost, s));
+    if (which) PBSM_CUDA_TRY(cudaMemcpyAsync(susp.data(), c.Mb.susp_present, n * 4, cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    bool any = false;
+    for (int m = 0; m < n; ++m) {
+        double v;
+        memcpy(&v, &mx[m], 8);
+        present[m] = v > 1e-12 && (!which || susp[m]);
+        any = any || present[m];
+    }
+    PBSM_CUDA_TRY(cudaMemcpyAsync(which ? c.Mb.dep_present : c.Mb.susp_present, present.data(), n * 4,
+                                  cudaMemcpyHostToDevice, s));
+    launch_member_mask_norm(c, s, which);
+    std::vector<double> bb(n);
+    PBSM_CUDA_TRY(cudaMemcpyAsync(bb.data(), c.Mb.bb, n * 8, cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    double tot = 0, mn = -1;
+    for (int m = 0; m < n; ++m)
+        if (present[m]) {
+            tot += bb[m];
+            if (mn < 0 || bb[m] < mn) mn = bb[m];
+        }
+    const double scale2 = (any && tot > 0) ? mn / tot : 1.0;
+    if (which) {
+        c.deposition_present = any;
+        c.dep_target_scale2 = scale2;
+    } else {
+        c.suspension_present = any;
+        c.target_scale2 = scale2;
+    }
+    return 0;
+}
+
 static int copy_in(Ctx& c, double* dst, const double* src, int on_device) {
     PBSM_CUDA_TRY(cudaMemcpyAsync(dst, src, c.P.T * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                                   c.stream));
@@ -594,6 +759,10 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     PBSM_CUDA_TRY(cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
 
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
+    if (c.Mb.n > 1) {
+        PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.rhs_max, 0, c.Mb.n * 8, s));
+        PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s));
+    }
     launch_assemble_suspension(c, s);
     PBSM_CUDA_TRY(cudaGetLastError());
     PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
@@ -605,6 +774,8 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     }
     const double susp_rhs_max = c.sc_host->rhs_max;
     c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
+    c.target_scale2 = 1.0;
+    if (c.Mb.n > 1 && (rc = member_presence(c, s, 0))) return rc;
     if (c.suspension_present) {
         if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
             PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, c.x_prev, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
@@ -619,6 +790,7 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
                 if ((rc = jacobi_sweep(c, s, c.r, c.A.x))) return rc;
             }
         }
+        if (c.Mb.n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) launch_member_zero(c, s, c.A.x);
         rc = solve_suspension(c, s, st);
         PBSM_CUDA_TRY(cudaGetLastError());
         if (rc) return rc;
@@ -635,6 +807,8 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     }
     const double dep_rhs_max = c.sc_host->rhs_max;
     c.deposition_present = c.suspension_present && dep_rhs_max > 1e-12;  // PBSM3D.cpp:1661-1664
+    c.dep_target_scale2 = 1.0;
+    if (c.Mb.n > 1 && (rc = member_presence(c, s, 1))) return rc;
     if (c.deposition_present) {
         rc = solve_deposition(c, s, st);
         PBSM_CUDA_TRY(cudaGetLastError());

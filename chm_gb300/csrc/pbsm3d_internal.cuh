@@ -30,6 +30,7 @@ namespace pbsm {
 constexpr int kBlock = 256;
 constexpr int kMaxLayers = 64;
 constexpr int kMaxTerms = 4;
+constexpr int kMaxMembers = 256;
 
 // Configuration scalars every kernel sees (passed by value).
 struct Params {
@@ -39,11 +40,11 @@ struct Params {
     int use_exp_fetch, use_tanh_fetch, use_PomLi, use_R94_lambda, enable_veg;
     int do_fixed_settling, do_sublimation, do_lateral_diff, rouault;
     double settling_velocity, eps, min_sd_trans, cutoff, snow_diffusion_const;
-    double uth_scale, z0_snow, settling_scale;
     // constants computed once on the host with the C library, the way the
     // reference computes them (compile-time or libm): cos(pi/4), the tanh
-    // fetch factor, log(2/0.0002), log(50/z0).
-    double cos_pi_4, Lc_tanh, log_2_0002, log_zur_z0;
+    // fetch factor, log(2/0.0002).  The per-member constants (threshold
+    // scale, z0, settling scale, log(50/z0)) are in Member.
+    double cos_pi_4, Lc_tanh, log_2_0002;
     int mixed;
 };
 
@@ -85,9 +86,26 @@ struct CzCoef {
     double pad0;
 };
 
+// Parameters of one ensemble member (a plain context is one member).
+struct Member {
+    double uth_scale, z0, settling_scale, log_zur_z0;
+};
+
+// Per-member bookkeeping on the device.
+struct Members {
+    int n;
+    const int32_t* face_member;     // [Tp] member of each face (padding: 0)
+    const Member* prm;              // [n]
+    unsigned long long* rhs_max;    // [n] bit patterns of max |rhs| (suspension)
+    unsigned long long* dep_max;    // [n] bit patterns of max |rhs| (deposition)
+    double* bb;                     // [n] ||rhs_m||^2 (suspension), then deposition
+    int* susp_present;              // [n]
+    int* dep_present;               // [n]
+};
+
 // Suspension system.
 struct Susp {
-    CzCoef* cztab;    // [L] for faces with hs == 0
+    CzCoef* cztab;    // [n_members][L] for faces with hs == 0
     double* band;     // [6][R]
     double* rhs;      // [R]
     double* x;        // [R]
@@ -140,6 +158,8 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s);
 void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s);
 void launch_update(Ctx& c, cudaStream_t s);
 void launch_init_static(Ctx& c, cudaStream_t s);
+void launch_member_mask_norm(Ctx& c, cudaStream_t s, int which);
+void launch_member_zero(Ctx& c, cudaStream_t s, double* x);
 
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
@@ -162,6 +182,10 @@ struct Ctx {
     FaceState S;
     Susp A;
     Dep D;
+    Members Mb;
+    std::vector<int64_t> member_offsets;  // host, [n+1] face ranges
+    double target_scale2 = 1.0;           // min_m ||b_m||^2 / ||b||^2 over present members
+    double dep_target_scale2 = 1.0;
     // Krylov work vectors (FP64), [R] each
     double *r, *rh, *p, *v, *sv, *tv, *zp, *zs;
     // FP32 work vectors for MIXED, [R] each

@@ -83,7 +83,8 @@ __device__ __forceinline__ double dot2(double ax, double ay, double bx, double b
 // (PBSM3D.cpp:1003-1028, 1113-1120, 1157): mean particle radius and mass,
 // radius of the mean-mass particle, settling velocity, the log(cz) factor of
 // the undersaturation, the radiation term and the mixing length.
-__device__ __forceinline__ void cz_coeffs(double cz, double z0, const Params& P, CzCoef& o) {
+__device__ __forceinline__ void cz_coeffs(double cz, double z0, double settling_scale, const Params& P,
+                                          CzCoef& o) {
     const double lcz = log(cz);
     const double rm = 4.6e-5 * exp(-0.258 * lcz);                   // 4.6e-5 cz^-0.258
     const double mm_alpha = 4.08 + 12.6 * cz;
@@ -93,7 +94,7 @@ __device__ __forceinline__ void cz_coeffs(double cz, double z0, const Params& P,
     o.r_z = exp(lq);                                                // (3 mm / 4 pi rho)^0.3333333
     double omega = P.settling_velocity;
     if (!P.do_fixed_settling) omega = 1.1e7 * exp(1.8 * lq);       // 1.1e7 r_z^1.8
-    o.omega = omega * P.settling_scale;
+    o.omega = omega * settling_scale;
     o.Qr = 0.9 * M_PI * rm * rm * 120.0;
     o.sigfac = 1.019 + 0.027 * lcz;
     o.l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
@@ -106,26 +107,33 @@ __device__ __forceinline__ void cz_coeffs(double cz, double z0, const Params& P,
 
 // The same terms for every layer of a face with no saltation layer (hs = 0),
 // plus log((cz - z0)/z0) of the wind profile and its logarithm.
-__global__ void k_cz_table(Params P, CzCoef* tab) {
-    const int z = blockIdx.x * blockDim.x + threadIdx.x;
-    if (z >= P.L) return;
+__global__ void k_cz_table(Params P, Members Mb, CzCoef* tab) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Mb.n * P.L) return;
+    const int m = q / P.L, z = q % P.L;
     const double hs = 0.0;
     const double cz = z * P.dz + hs + P.dz / 2.;
-    const double z0 = P.z0_snow;
+    const double z0 = Mb.prm[m].z0;
     CzCoef o;
-    cz_coeffs(cz, z0, P, o);
+    cz_coeffs(cz, z0, Mb.prm[m].settling_scale, P, o);
     o.cz = cz;
     o.lwarg = log((cz - z0) * (1.0 / z0));
     o.llw = log(o.lwarg);
-    tab[z] = o;
+    tab[q] = o;
 }
 
 // One face: saltation (PBSM3D.cpp:417-925), layer coefficients (:927-1233),
 // suspension rows (:1236-1404) and the Thomas factorisation of its column.
 __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Faces G, Forcing F, FaceState S, Susp A,
-                                                               double* partials, Scalars* sc) {
+                                                               Members Mb, double* partials, Scalars* sc) {
     unsigned long long vmax_bits = 0;
     bool bad = false;
+    // per-member max |rhs| of this block (ensembles), folded into Mb.rhs_max at the end
+    __shared__ unsigned long long mb_max[kMaxMembers];
+    if (Mb.n > 1) {
+        for (int m = threadIdx.x; m < Mb.n; m += blockDim.x) mb_max[m] = 0ull;
+        __syncthreads();
+    }
     const int64_t Tp = P.Tp, R = P.R;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= P.T) {  // padding face: identity rows
@@ -148,6 +156,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             }
             continue;
         }
+        // ---- this face's ensemble member
+        const int mem = Mb.face_member[i];
+        const Member mp = Mb.prm[mem];
+        const CzCoef* tab = A.cztab + (int64_t)mem * P.L;
         // ---- saltation, PBSM3D.cpp:436-925
         double fetch = 1000;
         if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         const double z10 = 10. + snow_depth;
         double u10;
         if (z10 < kZUR)
-            u10 = log_scale_wind(uref, kZUR, z10, snow_depth, P.z0_snow);
+            u10 = log_scale_wind(uref, kZUR, z10, snow_depth, mp.z0);
         else
             u10 = uref;
         double swe = F.swe[i];
@@ -174,7 +186,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         // u*_th decides saltation (ustar >= u*_th) and enters the cancelling
         // c_salt bracket: evaluated without contraction, in the reference's order
         double uth = __dadd_rn(__dadd_rn(0.35, __dmul_rn(1.0 / 150.0, T_c)), __dmul_rn(__dmul_rn(1.0 / 8200.0, T_c), T_c));
-        uth = __dmul_rn(uth, P.uth_scale);
+        uth = __dmul_rn(uth, mp.uth_scale);
         const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
         if (height_diff <= P.cutoff && snow_depth >= min_sd_trans_avg && !G.water[i]) {
             if (P.use_R94_lambda)
@@ -184,14 +196,14 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             ustar = u2 * kKappa / P.log_2_0002;
             if (ustar >= uth) {
                 saltation = true;
-                z0 = P.z0_snow;
+                z0 = mp.z0;
             }
         }
         if (!saltation) {
-            z0 = P.z0_snow;
-            ustar = smax(0.01, kKappa * uref / P.log_zur_z0);
+            z0 = mp.z0;
+            ustar = smax(0.01, kKappa * uref / mp.log_zur_z0);
         }
-        z0 = smax(P.z0_snow, z0);
+        z0 = smax(mp.z0, z0);
         ustar = smax(0.01, ustar);
         double hs = 0;
         if (saltation) hs = 0.08436 * powpos(ustar, 1.27);
@@ -309,15 +321,16 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         const long long b001 = __double_as_longlong(0.01);
         const bool uref_pos = uref > 0.0;
         double prev_up = 0.0, prev_ib = 1.0;
+        unsigned long long face_max = 0;
         for (int z = 0; z < P.L; ++z) {
             CzCoef co;
             double cz;
             if (fast) {
-                co = A.cztab[z];
+                co = tab[z];
                 cz = co.cz;
             } else {
                 cz = z * P.dz + hs + P.dz / 2.;
-                cz_coeffs(cz, z0, P, co);
+                cz_coeffs(cz, z0, mp.settling_scale, P, co);
             }
             double u_z, xrz;
             if (in_canopy_possible && saltation && cz < height_diff) {
@@ -450,10 +463,17 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             prev_up = up;
             prev_ib = ib;
             vmax_bits = max(vmax_bits, abs_bits(b));
+            face_max = max(face_max, abs_bits(b));
             if (nonfinite(dg) | nonfinite(b) | nonfinite(lat[0]) | nonfinite(lat[1]) | nonfinite(lat[2]) |
                 nonfinite(lo) | nonfinite(up) | nonfinite(ib))
                 bad = true;
         }
+        if (Mb.n > 1) atomicMax(&mb_max[mem], face_max);
+    }
+    if (Mb.n > 1) {
+        __syncthreads();
+        for (int m = threadIdx.x; m < Mb.n; m += blockDim.x)
+            if (mb_max[m]) atomicMax(&Mb.rhs_max[m], mb_max[m]);
     }
     // ||rhs||_inf (as the bit pattern of a non-negative double, whose integer
     // order is its numeric order) and the NaN/Inf flag: last block finalises
@@ -515,9 +535,14 @@ __global__ void __launch_bounds__(kBlock) k_post(Params P, Susp A, FaceState S) 
 }
 
 __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces G, Forcing F, FaceState S, Dep D,
-                                                               double* partials, Scalars* sc) {
+                                                               Members Mb, double* partials, Scalars* sc) {
     const int64_t Tp = P.Tp;
     double vmax = 0, vnan = 0;
+    __shared__ unsigned long long mb_max[kMaxMembers];
+    if (Mb.n > 1) {
+        for (int m = threadIdx.x; m < Mb.n; m += blockDim.x) mb_max[m] = 0ull;
+        __syncthreads();
+    }
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= P.T) {
             D.diag[i] = 1.0;
@@ -563,7 +588,13 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
         D.rhs[i] = b;
         D.x[i] = 0.0;
         vmax = fmax(vmax, fabs(b));
+        if (Mb.n > 1) atomicMax(&mb_max[Mb.face_member[i]], abs_bits(b));
         if (isnan(dg) || isnan(b)) vnan = 1.0;
+    }
+    if (Mb.n > 1) {
+        __syncthreads();
+        for (int m = threadIdx.x; m < Mb.n; m += blockDim.x)
+            if (mb_max[m]) atomicMax(&Mb.dep_max[m], mb_max[m]);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     __shared__ double shm[2][kBlock / 32];
@@ -602,7 +633,7 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
 // PBSM3D.cpp:1710-1740 plus the FP64 mass ledger (deterministic partial sums).
 // rres holds b - A q from the solver's final residual.
 __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F, FaceState S, Dep D, const double* rres,
-                                                   int deposition_present, double* partials, Scalars* sc,
+                                                   int deposition_present, Members Mb, double* partials, Scalars* sc,
                                                    double* ledger) {
     double v[4] = {0, 0, 0, 0};  // divergence, deposited, clipped, residual
     double snow = 0;
@@ -612,6 +643,7 @@ __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F,
         const double area = G.area[i];
         snow += area * swe;
         if (!deposition_present) continue;
+        if (Mb.n > 1 && !Mb.dep_present[Mb.face_member[i]]) continue;  // this member had no deposition
         const double q = D.x[i];
         const double qdep = is_nan_chm(q) ? 0 : q;
         double mass = qdep * P.dt;
@@ -657,6 +689,37 @@ __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F,
     }
 }
 
+// Ensembles: zero the right-hand sides of members without suspension (or
+// deposition) so their solution is exactly 0, as the reference's skipped
+// solve leaves it; and ||rhs_m||^2 per member.
+__global__ void k_member_mask_norm(Params P, Members Mb, double* rhs, int layers, const int* present, double* bb) {
+    __shared__ double sbb[kMaxMembers];
+    for (int m = threadIdx.x; m < Mb.n; m += blockDim.x) sbb[m] = 0.0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = Mb.face_member[i];
+        double acc = 0.0;
+        for (int z = 0; z < layers; ++z) {
+            const int64_t r = (int64_t)z * P.Tp + i;
+            if (!present[m]) rhs[r] = 0.0;
+            acc += rhs[r] * rhs[r];
+        }
+        atomicAdd(&sbb[m], acc);
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < Mb.n; m += blockDim.x)
+        if (sbb[m] != 0.0) atomicAdd(&bb[m], sbb[m]);
+}
+
+// Ensembles: a warm start of a member without suspension is reset to 0 (its
+// right-hand side is 0, so the joint Krylov solve then keeps it exactly 0).
+__global__ void k_member_zero(Params P, Members Mb, double* x, const int* present) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
+        if (present[Mb.face_member[i]]) continue;
+        for (int z = 0; z < P.L; ++z) x[(int64_t)z * P.Tp + i] = 0.0;
+    }
+}
+
 // Centroid distances to neighbours (distance_UTM, coordinates.cpp:100-106).
 __global__ void k_init_static(Params P, Faces G, const double* cx, const double* cy) {
     const int64_t Tp = P.Tp;
@@ -676,10 +739,26 @@ __global__ void k_init_static(Params P, Faces G, const double* cx, const double*
 
 }  // namespace
 
+void launch_member_mask_norm(Ctx& c, cudaStream_t s, int which) {
+    cudaMemsetAsync(c.Mb.bb, 0, sizeof(double) * c.Mb.n, s);
+    prof_begin(c, s);
+    if (which == 0)
+        k_member_mask_norm<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Mb, c.A.rhs, c.P.L, c.Mb.susp_present, c.Mb.bb);
+    else
+        k_member_mask_norm<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Mb, c.D.rhs, 1, c.Mb.dep_present, c.Mb.bb);
+    prof_end(c, s, PBSM3D_K_OTHER, c.P.T * (which == 0 ? c.P.L : 1) * 16);
+}
+
+void launch_member_zero(Ctx& c, cudaStream_t s, double* x) {
+    prof_begin(c, s);
+    k_member_zero<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Mb, x, c.Mb.susp_present);
+    prof_end(c, s, PBSM3D_K_OTHER, c.P.T * 4);
+}
+
 void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     const int64_t T = c.P.T, rows = T * c.P.L;
     prof_begin(c, s);
-    k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.red.partials, c.sc);
+    k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
     // per face: 8 forcing + 133 B geometry in, Qsalt + flag out; per row 12 doubles out (+6 floats MIXED)
     prof_end(c, s, PBSM3D_K_ASSEMBLE, T * (64 + 133 + 9) + rows * (96 + (c.P.mixed ? 24 : 0)));
 }
@@ -690,20 +769,20 @@ void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {
     k_post<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.A, c.S);
     prof_end(c, s, PBSM3D_K_POST, rows * 24 + T * 40);
     prof_begin(c, s);
-    k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.red.partials, c.sc);
+    k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.Mb, c.red.partials, c.sc);
     prof_end(c, s, PBSM3D_K_DEP_ASSEMBLE, T * 196);
 }
 
 void launch_update(Ctx& c, cudaStream_t s) {
     prof_begin(c, s);
-    k_update<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.dr, c.deposition_present ? 1 : 0,
+    k_update<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.dr, c.deposition_present ? 1 : 0, c.Mb,
                                              c.red.partials, c.sc, c.ledger);
     prof_end(c, s, PBSM3D_K_UPDATE, c.P.T * 81);
 }
 
 // cx, cy: the centroid x/y staged in the CG work vectors by pbsm3d_create
 void launch_init_static(Ctx& c, cudaStream_t s) {
-    k_cz_table<<<1, 64, 0, s>>>(c.P, c.A.cztab);
+    k_cz_table<<<(c.Mb.n * c.P.L + 63) / 64, 64, 0, s>>>(c.P, c.Mb, c.A.cztab);
     k_init_static<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.dr, c.dz_);
 }
 

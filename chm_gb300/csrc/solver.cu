@@ -743,7 +743,9 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         }
         const double rn2 = c.sc_host->rnorm2;
         c.susp_relres = bnorm2 > 0 ? sqrt(rn2 / bnorm2) : 0.0;
-        if (rn2 <= tol * tol * bnorm2) break;
+        // ensembles: tol * min_m ||b_m|| bounds every member's residual (target_scale2 = 1 otherwise)
+        const double goal2 = tol * tol * bnorm2 * c.target_scale2;
+        if (rn2 <= goal2) break;
         if (total_iters >= maxit) {
             c.susp_iters = total_iters;
             c.err = "suspension solve failed to converge (relative residual " + std::to_string(c.susp_relres) + ")";
@@ -757,7 +759,7 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         if (c.P.mixed) {
             // inner: A32 d = r32, d0 = 0, to inner_tol relative -- or less when
             // the FP64 target is closer than that (no over-solving in the last sweep)
-            const double need = 0.5 * tol * sqrt(bnorm2 / rn2);
+            const double need = 0.5 * sqrt(goal2 / rn2);
             const double itol = std::min(0.5, std::max(c.cfg.inner_tol, need));
             Scalars init{};
             init.rho = rn2;
@@ -779,7 +781,7 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         } else {
             // target relative to ||b|| (the state's target2 is relative to ||r||)
             Scalars* h = c.sc_host;
-            h->target2 = tol * tol * bnorm2;
+            h->target2 = goal2;
             h->maxit = maxit - total_iters;
             PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->target2, &h->target2, sizeof(double), cudaMemcpyHostToDevice, s));
             PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->maxit, &h->maxit, sizeof(int), cudaMemcpyHostToDevice, s));
@@ -825,7 +827,7 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         return PBSM3D_ERR_CUDA;
     }
     PBSM_CUDA_TRY(cudaMemsetAsync(c.gbar, 0, sizeof(GridBar), s));
-    double tol = c.cfg.dep_tol;
+    double tol = c.cfg.dep_tol * sqrt(c.dep_target_scale2);  // ensembles: every member to dep_tol
     int maxit = c.cfg.dep_maxit;
     void* args[] = {&c.P, &c.D, &c.F.nbr, &c.dr, &c.dz_, &c.dp, &c.dq, &part, &c.gbar, &sc, &tol, &maxit};
     prof_begin(c, s);
@@ -849,7 +851,7 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     rc = read_scalars(c, s, sc);
     if (rc) return rc;
     c.dep_relres = bn2 > 0 ? sqrt(c.sc_host->tmp / bn2) : 0.0;
-    if (done != DONE_CONVERGED && !(c.sc_host->tmp <= c.cfg.dep_tol * c.cfg.dep_tol * bn2)) {
+    if (done != DONE_CONVERGED && !(c.sc_host->tmp <= tol * tol * bn2)) {
         c.err = "deposition solve failed to converge (relative residual " + std::to_string(c.dep_relres) + ")";
         return PBSM3D_ERR_NOT_CONVERGED;
     }

@@ -110,12 +110,26 @@ class PBSM3D:
 
     # PBSM3D::init (PBSM3D.cpp:221-398)
     def init(self, mesh, **solver):
+        lib = capi.load()
+        cfg = self.make_config(lib, **solver)
+        desc = capi.mesh_desc(mesh, self._keep)
+        ctx = C.c_void_p()
+        rc = lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx))
+        if rc != 0:
+            raise ModuleError(f"pbsm3d_create: {capi.STATUS_NAMES.get(rc, rc)}: "
+                              f"{lib.pbsm3d_last_error(None).decode()}")
+        self._lib = lib
+        self._ctx = ctx
+        self.n_faces = mesh.n_faces
+
+    def make_config(self, lib, **solver) -> capi.Config:
+        """The library's config struct from this module's keys (PBSM3D.cpp:221-280)
+        plus solver fields of the struct given by name."""
         g = lambda k, d: _get(self.cfg, k, d)  # noqa: E731
         self.nLayer = g("nLayer", 10)
         settling = g("settling_velocity", 0.5)
         if settling < 0:
             raise ModuleError("PBSM3D settling velocity must be positive")
-        lib = capi.load()
         cfg = capi.default_config(lib)
         cfg.nLayer = self.nLayer
         cfg.do_fixed_settling = int(g("do_fixed_settling", False))
@@ -138,17 +152,11 @@ class PBSM3D:
         cfg.use_R94_lambda = int(self.use_R94_lambda)
         cfg.debug_output = int(self.debug_output)
         for k, v in solver.items():
+            if not hasattr(cfg, k):
+                raise ModuleError(f"unknown solver setting {k}")
             setattr(cfg, k, v)
         self._cfg_struct = cfg
-        desc = capi.mesh_desc(mesh, self._keep)
-        ctx = C.c_void_p()
-        rc = lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx))
-        if rc != 0:
-            raise ModuleError(f"pbsm3d_create: {capi.STATUS_NAMES.get(rc, rc)}: "
-                              f"{lib.pbsm3d_last_error(None).decode()}")
-        self._lib = lib
-        self._ctx = ctx
-        self.n_faces = mesh.n_faces
+        return cfg
 
     def set_profiling(self, on: bool):
         self._lib.pbsm3d_set_profiling(self._ctx, int(on))

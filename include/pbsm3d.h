@@ -249,6 +249,13 @@ enum pbsm3d_kernel {
 
 typedef struct pbsm3d_ctx pbsm3d_ctx;
 
+/* Parameters of one ensemble member (the perturbed constants of config 4). */
+typedef struct pbsm3d_member {
+    double ustar_th_scale;  /* multiplies the threshold friction velocity */
+    double z0_snow;         /* aerodynamic roughness of snow (m) */
+    double settling_scale;  /* multiplies the settling velocity */
+} pbsm3d_member;
+
 /* Fill *cfg with the reference defaults. */
 void pbsm3d_config_defaults(pbsm3d_config* cfg);
 
@@ -256,6 +263,20 @@ void pbsm3d_config_defaults(pbsm3d_config* cfg);
  * mesh into device SoA, build the sliced-ELL pattern of both systems.
  * Replaces PBSM3D::PBSM3D + PBSM3D::init + the two NearestNeighborProblem ctors. */
 int pbsm3d_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, pbsm3d_ctx** out);
+
+/* A batched ensemble: n_members independent meshes of any sizes, each with
+ * its own parameters, in one context.  Every step advances all members with
+ * the same kernels: one joint system over the disjoint union of the meshes,
+ * each member with the reference's own "suspension/deposition present"
+ * tests and its own relative tolerance.  Forcing and output arrays of
+ * pbsm3d_step are the members' arrays concatenated in member order
+ * (pbsm3d_member_offsets gives the face ranges).  cfg.ustar_th_scale,
+ * z0_snow and settling_scale are ignored (members[] replaces them).
+ * No counterpart in the reference. */
+int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, const pbsm3d_member* members,
+                           const pbsm3d_config* cfg, pbsm3d_ctx** out);
+/* offsets[0..n_members] face ranges of the members; returns n_members. */
+int pbsm3d_member_offsets(const pbsm3d_ctx* ctx, int64_t* offsets);
 
 /* One timestep of dt seconds (global_param->dt(), integer seconds in CHM).
  * Replaces PBSM3D::run.  stats may be NULL. */

@@ -102,6 +102,61 @@ def test_create_rejects_bad_configs(cuda_lib):
     assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_BAD_MESH
 
 
+def test_ensemble_create_rejects_bad_members(cuda_lib):
+    """Argument checks of pbsm3d_ensemble_create run before any device call."""
+    from chm_gb300 import synth
+    meshes = [synth.make_mesh(64, 300.0, 0), synth.make_mesh(48, 250.0, 1)]
+    keep = []
+    descs = (capi.MeshDesc * 2)(*[capi.mesh_desc(m, keep) for m in meshes])
+    cfg = capi.default_config(cuda_lib)
+    ctx = C.c_void_p()
+    good = capi.Member(1.0, 0.01, 1.0)
+    for bad in (capi.Member(1.0, 0.0, 1.0), capi.Member(-1.0, 0.01, 1.0), capi.Member(1.0, 0.01, -0.5),
+                capi.Member(1.0, float("nan"), 1.0)):
+        mem = (capi.Member * 2)(good, bad)
+        assert cuda_lib.pbsm3d_ensemble_create(2, descs, mem, C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
+        assert b"positive" in cuda_lib.pbsm3d_last_error(None)
+    mem = (capi.Member * 2)(good, good)
+    assert cuda_lib.pbsm3d_ensemble_create(0, descs, mem, C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
+    assert cuda_lib.pbsm3d_ensemble_create(257, descs, mem, C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
+    # vegetation is a per-domain switch: members must agree on it
+    meshes[1].canopy_height = None
+    descs = (capi.MeshDesc * 2)(*[capi.mesh_desc(m, keep) for m in meshes])
+    assert cuda_lib.pbsm3d_ensemble_create(2, descs, mem, C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
+    assert b"vegetation" in cuda_lib.pbsm3d_last_error(None)
+    # a neighbour index outside its own member's mesh
+    meshes[1].canopy_height = np.zeros(meshes[1].n_faces)
+    nb = meshes[1].neighbor.copy()
+    nb[0, 0] = meshes[1].n_faces
+    meshes[1].neighbor = nb
+    descs = (capi.MeshDesc * 2)(*[capi.mesh_desc(m, keep) for m in meshes])
+    assert cuda_lib.pbsm3d_ensemble_create(2, descs, mem, C.byref(cfg), C.byref(ctx)) == capi.ERR_BAD_MESH
+
+
+def test_ensemble_forcing_split_and_members(cuda_lib):
+    """Host side of the ensemble wrapper: forcing concatenation and output split."""
+    from chm_gb300 import ensemble, synth
+    e = ensemble.Ensemble({"nLayer": "3"})
+    e.nLayer, e.n_members, e.offsets = 3, 2, np.array([0, 4, 7])
+    e.n_faces = 7
+    c = np.arange(21.0)
+    out = {"drift_mass": np.arange(7.0), "c": c}
+    parts = e.split(out)
+    np.testing.assert_array_equal(parts[1]["drift_mass"], [4, 5, 6])
+    np.testing.assert_array_equal(parts[0]["c"], [0, 1, 2, 3, 7, 8, 9, 10, 14, 15, 16, 17])
+    np.testing.assert_array_equal(parts[1]["c"], [4, 5, 6, 11, 12, 13, 18, 19, 20])
+    f = e.concat_forcing([{"t": np.zeros(4), "rh": np.ones(4)}, {"t": np.ones(3), "rh": np.ones(3)}])
+    assert f["t"].shape == (7,) and f["rh"].shape == (7,)
+    with pytest.raises(ModuleError):
+        e.concat_forcing([{"t": np.zeros(4)}, {"rh": np.ones(3)}])
+    ms = ensemble.perturbed_members(200, 0)
+    u = np.array([m.ustar_th_scale for m in ms])
+    z = np.array([m.z0_snow for m in ms])
+    s = np.array([m.settling_scale for m in ms])
+    assert u.min() >= 0.8 and u.max() <= 1.2 and z.min() >= 1e-4 and z.max() <= 1e-2
+    assert s.min() >= 0.85 and s.max() <= 1.15
+
+
 def _replica_worker(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
     import sys
