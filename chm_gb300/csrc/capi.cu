@@ -331,6 +331,12 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     Susp& A = c.A;
     A.band = dalloc<double>(c, 6 * R, ok);
     A.cztab = dalloc<CzCoef>(c, (size_t)kMaxLayers * nm, ok);
+    A.face_v = dalloc<double>(c, (size_t)FV_COUNT * Tp, ok);
+    A.slow_list = dalloc<int32_t>(c, Tp, ok);
+    A.n_slow = dalloc<int>(c, 1, ok);
+    A.slow_rows = dalloc<double>(c, (size_t)8 * R, ok);
+    MathTables* mt = dalloc<MathTables>(c, 1, ok);
+    P.mt = mt;
     int32_t* face_member = dalloc<int32_t>(c, Tp, ok);
     Member* prm = dalloc<Member>(c, nm, ok);
     c.Mb.n = nm;
@@ -445,6 +451,11 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         std::vector<int> ones(nm, 1);
         rc |= upload(c, c.Mb.susp_present, ones.data(), nm * 4);
         rc |= upload(c, c.Mb.dep_present, ones.data(), nm * 4);
+    }
+    {
+        MathTables h;
+        math_tables_fill(h);
+        rc |= upload(c, mt, &h, sizeof(h));
     }
     rc |= upload(c, c.dr, cx.data(), Tp * 8);
     rc |= upload(c, c.dz_, cy.data(), Tp * 8);

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/pbsm3d.h"
+#include "fp64_math.cuh"
 
 namespace pbsm {
 
@@ -46,6 +47,7 @@ struct Params {
     // scale, z0, settling scale, log(50/z0)) are in Member.
     double cos_pi_4, Lc_tanh, log_2_0002;
     int mixed;
+    const MathTables* mt;  // exp/log tables (device)
 };
 
 // Per-face static geometry (device pointers).
@@ -76,14 +78,20 @@ struct FaceState {
 };
 
 // Height-dependent coefficients of one layer (see cz_coeffs in physics.cu).
+// The first eight fields are also the per-row layout of Susp::slow_rows.
 struct CzCoef {
-    double inv_mm, r_z, omega, Qr, sigfac, l;
+    double inv_mm, omega, Qr, l;
     double rz2nu;  // 2 r_z / nu: Re = rz2nu * Vr
     double rsig;   // r_z * sigfac
-    double lwarg;  // table only: log((cz - z0) / z0), the wind-profile numerator
-    double llw;    // table only: log(lwarg)
+    double lwarg;  // log((cz - z0) / z0), the wind-profile numerator
+    double llw;    // log(lwarg)
     double cz;     // layer centre height above the snow surface
-    double pad0;
+    double pad[3];
+};
+
+// Per-face values the saltation pass hands to the row assembly, [FV_COUNT][Tp].
+enum FaceValue {
+    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QSUB, FV_C1R, FV_LR, FV_LU, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_COUNT
 };
 
 // Parameters of one ensemble member (a plain context is one member).
@@ -106,6 +114,10 @@ struct Members {
 // Suspension system.
 struct Susp {
     CzCoef* cztab;    // [n_members][L] for faces with hs == 0
+    double* face_v;   // [FV_COUNT][Tp] saltation pass results
+    int32_t* slow_list;  // [Tp] faces with a saltation layer (hs > 0)
+    int* n_slow;      // device count of slow_list
+    double* slow_rows;   // [8][R] layer terms of those faces' rows
     double* band;     // [6][R]
     double* rhs;      // [R]
     double* x;        // [R]

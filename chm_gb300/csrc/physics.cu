@@ -1,12 +1,18 @@
 // physics.cu -- per-face physics and system assembly of the PBSM3D step.
 //
 // The assembly is bound by the FP64 pipe (GB300 issues FP64 at a small
-// fraction of its FP32 rate), so it is written to spend as few FP64
+// fraction of its FP32 rate, and a warp instruction costs the same however
+// many of its lanes are active), so it is written to spend as few FP64 warp
 // instructions per row as the accuracy bar allows:
-//  * x^y for x > 0 is exp(y log x), and the particle-size terms share their
-//    logarithms (relative error a few 1e-16 against a correctly rounded pow);
-//  * terms that depend only on the layer height are tabulated per layer for
-//    the faces without a saltation layer;
+//  * three passes keep warps convergent: per-face saltation (pass 1), the
+//    height-dependent particle terms of the rows of saltating faces, one
+//    row per lane (pass 2), and the row assembly (pass 3), which reads those
+//    terms from pass 2 or, for faces without a saltation layer, from a
+//    per-layer table; saltating faces are spatially random, so a single
+//    per-face pass would run both paths in nearly every warp;
+//  * exp / log / 1/x are the table-driven routines of fp64_math.cuh, x^y for
+//    x > 0 is exp(y log x), and log(u_z) is assembled from per-face and
+//    per-layer logarithms so that u_z^1.36 is one exp per row;
 //  * NaN/Inf detection, the |rhs| maximum and sign tests run on the integer
 //    pipe (bit patterns);
 //  * multiply-adds contract to FMA, except in the saltation concentration
@@ -24,9 +30,6 @@ namespace {
 constexpr double kKappa = 0.4;    // PhysConst.h:31
 constexpr double kRhoIce = 917;   // PhysConst.h:39
 constexpr double kZUR = 50.0;     // Atmosphere.h:31
-
-// x^y for x > 0 (x = 0 gives 0 for y > 0): exp(y * log(x)).
-__device__ __forceinline__ double powpos(double x, double y) { return exp(y * log(x)); }
 
 // Bit-pattern tests that keep comparisons off the FP64 pipe.
 __device__ __forceinline__ bool nonfinite(double x) {
@@ -49,10 +52,10 @@ __device__ __forceinline__ double log_scale_wind(double u, double Z_in, double Z
 }
 
 // Atmosphere.cpp:62-80 (T in K against Tfreeze = 0: the water branch for any T > 0 K)
-__device__ __forceinline__ double saturated_vapour_pressure(double T) {
+__device__ __forceinline__ double saturated_vapour_pressure(double T, const MathTables& mt) {
     const double TA = T - 273.15;
-    if (T >= 0.) return 611.21 * exp((17.502 * TA) / (240.97 + TA));
-    return 611.15 * exp((22.452 * TA) / (272.55 + TA));
+    if (T >= 0.) return 611.21 * exp_t((17.502 * TA) * rcp_t(240.97 + TA), mt);
+    return 611.15 * exp_t((22.452 * TA) * rcp_t(272.55 + TA), mt);
 }
 
 // coordinates.cpp:112-131
@@ -64,10 +67,10 @@ __device__ __forceinline__ void bearing_to_cartesian(double bearing, double& x, 
 }
 
 // MeteoIO standard atmosphere (PBSM3D.cpp:785): p(z) / (R_dry T)
-__device__ __forceinline__ double std_dry_air_density(double altitude, double temperature) {
+__device__ __forceinline__ double std_dry_air_density(double altitude, double temperature, const MathTables& mt) {
     const double p0 = 101325., lapse = 0.0065, T0 = 288.15, Rd = 287.058, g = 9.80665, R0 = 6356766.0;
     const double expo = g / (lapse * Rd);
-    const double p = p0 * powpos(1. - ((lapse * R0 * altitude) / (T0 * (R0 + altitude))), expo);
+    const double p = p0 * pow_t(1. - ((lapse * R0 * altitude) / (T0 * (R0 + altitude))), expo, mt);
     return p / (287.058 * temperature);
 }
 
@@ -82,50 +85,247 @@ __device__ __forceinline__ double dot2(double ax, double ay, double bx, double b
 // Height-dependent terms of one suspension layer centred at cz
 // (PBSM3D.cpp:1003-1028, 1113-1120, 1157): mean particle radius and mass,
 // radius of the mean-mass particle, settling velocity, the log(cz) factor of
-// the undersaturation, the radiation term and the mixing length.
-__device__ __forceinline__ void cz_coeffs(double cz, double z0, double settling_scale, const Params& P,
-                                          CzCoef& o) {
-    const double lcz = log(cz);
-    const double rm = 4.6e-5 * exp(-0.258 * lcz);                   // 4.6e-5 cz^-0.258
-    const double mm_alpha = 4.08 + 12.6 * cz;
-    const double mm = 4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 / mm_alpha + 2. / (mm_alpha * mm_alpha));
-    o.inv_mm = 1.0 / mm;
-    const double lq = 0.3333333 * log((3.0 * mm) / (4 * M_PI * kRhoIce));
-    o.r_z = exp(lq);                                                // (3 mm / 4 pi rho)^0.3333333
+// the undersaturation, the radiation term and the mixing length; and the
+// wind-profile logarithm log((cz - z0)/z0) with its own logarithm.
+// hz_minus_d0 is the reference's Z_out - (snow depth + z0) of
+// log_scale_wind (Atmosphere.cpp:32-38).
+__device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double z0, double settling_scale,
+                                          const Params& P, const MathTables& t, CzCoef& o) {
+    const double lcz = log_t(cz, t);
+    const double rm = 4.6e-5 * exp_t(-0.258 * lcz, t);             // 4.6e-5 cz^-0.258
+    const double ia = rcp_t(4.08 + 12.6 * cz);                       // 1 / mm_alpha
+    const double mm = 4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 * ia + 2. * (ia * ia));
+    o.inv_mm = rcp_t(mm);
+    const double lq = 0.3333333 * log_t((3.0 * mm) * (1.0 / (4 * M_PI * kRhoIce)), t);
+    const double r_z = exp_t(lq, t);                                 // (3 mm / 4 pi rho)^0.3333333
     double omega = P.settling_velocity;
-    if (!P.do_fixed_settling) omega = 1.1e7 * exp(1.8 * lq);       // 1.1e7 r_z^1.8
+    if (!P.do_fixed_settling) omega = 1.1e7 * exp_t(1.8 * lq, t);   // 1.1e7 r_z^1.8
     o.omega = omega * settling_scale;
     o.Qr = 0.9 * M_PI * rm * rm * 120.0;
-    o.sigfac = 1.019 + 0.027 * lcz;
-    o.l = kKappa * (cz + z0) * 40.0 / (kKappa * (cz + z0) + 40.0);
-    o.rz2nu = 2.0 * o.r_z * (1.0 / 1.88e-5);                        // Re = rz2nu * Vr
-    o.rsig = o.r_z * o.sigfac;
-    o.lwarg = 0.0;
-    o.llw = 0.0;
+    const double sigfac = 1.019 + 0.027 * lcz;
+    const double kz = kKappa * (cz + z0);
+    o.l = kz * 40.0 * rcp_t(kz + 40.0);
+    o.rz2nu = 2.0 * r_z * (1.0 / 1.88e-5);                          // Re = rz2nu * Vr
+    o.rsig = r_z * sigfac;
+    o.lwarg = log_t(hz_minus_d0 * rcp_t(z0), t);
+    o.llw = log_t(o.lwarg, t);
     o.cz = cz;
 }
 
-// The same terms for every layer of a face with no saltation layer (hs = 0),
-// plus log((cz - z0)/z0) of the wind profile and its logarithm.
+// The same terms for every layer of a face with no saltation layer (hs = 0).
 __global__ void k_cz_table(Params P, Members Mb, CzCoef* tab) {
+    __shared__ MathTables mt;
+    math_tables_load(mt, P.mt);
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Mb.n * P.L) return;
     const int m = q / P.L, z = q % P.L;
-    const double hs = 0.0;
-    const double cz = z * P.dz + hs + P.dz / 2.;
+    const double cz = z * P.dz + P.dz / 2.;
     const double z0 = Mb.prm[m].z0;
     CzCoef o;
-    cz_coeffs(cz, z0, Mb.prm[m].settling_scale, P, o);
-    o.cz = cz;
-    o.lwarg = log((cz - z0) * (1.0 / z0));
-    o.llw = log(o.lwarg);
+    cz_coeffs(cz, cz - z0, z0, Mb.prm[m].settling_scale, P, mt, o);
     tab[q] = o;
 }
 
-// One face: saltation (PBSM3D.cpp:417-925), layer coefficients (:927-1233),
-// suspension rows (:1236-1404) and the Thomas factorisation of its column.
+// Pass 1 of the suspension assembly, one thread per face: saltation
+// (PBSM3D.cpp:436-925) and the per-face constants of the layer loop
+// (:927-1233).  Faces that carry a saltation layer (hs > 0: their layer
+// heights differ from the per-layer table) are appended to a list, so that
+// pass 2 computes their height-dependent terms with every lane busy.
+__global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcing F, FaceState S, Susp A, Members Mb) {
+    __shared__ MathTables mt;
+    math_tables_load(mt, P.mt);
+    const int64_t Tp = P.Tp;
+    const int lane = threadIdx.x & 31;
+    // Tp is a multiple of the block size: every lane of a warp runs the same iterations
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        bool slow = false;
+        if (i < P.T) {
+            const Member mp = Mb.prm[Mb.face_member[i]];
+            double fetch = 1000;
+            if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
+            const double uref = F.UR[i];
+            double snow_depth = F.sd[i];
+            snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
+            const double u2 = F.U2[i];
+            double swe = F.swe[i];
+            swe = is_nan_chm(swe) ? 0 : swe;
+            double height_diff = smax(0.0, G.canopy[i] - snow_depth);
+            if (!P.enable_veg) height_diff = 0;
+            double ustar = 1.3;
+            double lambda = 0;
+            bool saltation = false;
+            const double T_c = F.t[i];
+            // u*_th decides saltation (ustar >= u*_th) and enters the cancelling
+            // c_salt bracket: evaluated without contraction, in the reference's order
+            double uth =
+                __dadd_rn(__dadd_rn(0.35, __dmul_rn(1.0 / 150.0, T_c)), __dmul_rn(__dmul_rn(1.0 / 8200.0, T_c), T_c));
+            uth = __dmul_rn(uth, mp.uth_scale);
+            const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
+            if (height_diff <= P.cutoff && snow_depth >= P.min_sd_trans && !G.water[i]) {
+                if (P.use_R94_lambda)
+                    lambda = 0.5 * G.lai[i] * height_diff;
+                else
+                    lambda = stalkN * stalkD * height_diff;
+                ustar = u2 * kKappa / P.log_2_0002;
+                if (ustar >= uth) saltation = true;
+            }
+            // z0 is the member's snow roughness on both branches (:740-754)
+            const double z0 = mp.z0;
+            if (!saltation) ustar = smax(0.01, kKappa * uref / mp.log_zur_z0);
+            ustar = smax(0.01, ustar);
+            double hs = 0;
+            if (saltation) hs = 0.08436 * pow_t(ustar, 1.27, mt);
+            slow = saltation;  // hs > 0
+            double Qsalt = 0;
+            double c_salt = 0;
+            const double t = F.t[i] + 273.15;
+            double vx, vy;
+            bearing_to_cartesian(F.dir[i], vx, vy);
+            const double ux = -vx, uy = -vy;
+            double mx[3], my[3], Ej[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                mx[j] = G.mx[j * Tp + i];
+                my[j] = G.my[j * Tp + i];
+                Ej[j] = G.E[j * Tp + i];
+            }
+            if (saltation) {
+                const double rho_f = std_dry_air_density(G.zc[i], t, mt);
+                const double Beta = 202.0, mB = 0.16;
+                const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
+                const double tau_n_ratio = __ddiv_rn(mbl, __dadd_rn(1.0, mbl));
+                // the bracket cancels near the threshold: no contraction here
+                const double bracket =
+                    __dsub_rn(__dsub_rn(1.0, tau_n_ratio), __ddiv_rn(__dmul_rn(uth, uth), __dmul_rn(ustar, ustar)));
+                c_salt = __dmul_rn(__ddiv_rn(rho_f, __dmul_rn(3.29, ustar)), bracket);
+                if (c_salt < 0 || isnan(c_salt)) {
+                    c_salt = 0;
+                    saltation = false;
+                }
+                if (P.use_exp_fetch && fetch < 500) {
+                    const double fetch_ref = 500, mu = 3.0;
+                    c_salt *= 1.0 - exp(-mu * fetch / fetch_ref);
+                } else if (P.use_tanh_fetch && fetch <= 300.) {
+                    c_salt *= P.Lc_tanh;  // 0.5*tanh(0.01333*fetch_ref - 2)+0.5 with fetch_ref = 300
+                }
+                if (P.use_PomLi) {  // PBSM3D.cpp:848-865
+                    const double z10 = 10. + snow_depth;
+                    const double u10 = z10 < kZUR ? log_scale_wind(uref, kZUR, z10, snow_depth, z0) : uref;
+                    const double Ah = F.psh[i];
+                    const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
+                    const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
+                    const double z0v = (stalkN * stalkD * height_diff) / 2.0;
+                    const double us = u10 / sqrt((1 + 340.0 * z0v));
+                    const double Pu10 = 1.0 / (1.0 + exp((sqrt(M_PI) * (u_mean - us)) / delta));
+                    S.bsp[i] = Pu10;
+                    c_salt *= Pu10;
+                }
+                const double uhs = 2.8 * uth;
+                Qsalt = c_salt * uhs * hs;
+                double mass = 0;
+                for (int j = 0; j < 3; ++j) {
+                    const double udm = __dadd_rn(__dmul_rn(ux, mx[j]), __dmul_rn(uy, my[j]));
+                    mass = __dadd_rn(mass, __dmul_rn(__dmul_rn(-Ej[j], Qsalt), udm));
+                }
+                mass = __dmul_rn(__ddiv_rn(mass, G.area[i]), P.dt);
+                if (mass < 0 && fabs(mass) > swe) {
+                    c_salt = 0;
+                    Qsalt = c_salt * uhs * hs;
+                }
+            }
+            S.Qsalt[i] = Qsalt;
+            S.saltation[i] = saltation;
+
+            // per-face constants of the layer loop.  Division by a per-face or
+            // constant value becomes a product with its reciprocal and the
+            // sublimation rate is regrouped so that no division is left per
+            // row (each change moves a result by a few ulps).
+            const double rh = F.rh[i] / 100.;
+            const double es = saturated_vapour_pressure(t, mt);
+            const double D = 2.06e-5 * pow_t(t * (1.0 / 273.15), 1.75, mt);
+            const double lambda_t = 0.000063 * t + 0.00673;
+            const double Ls = 2.838e6, M = 18.01, Rg = 8313;
+            const double rho = (M * es) * rcp_t(Rg * t);
+            // dm/dt = Sh rho D (2 pi Nu R r sigma t^2 lt - L M Qr + Qr R t) /
+            //         (D L Sh (L M - R t) rho + lt t^2 Nu R),  Sh = Nu,
+            //       = q * ((c1 (rh-1)) Nu (r sigfac) - Qr (L M - R t))
+            const double Rgt = Rg * t;
+            const double c1r = 6.283185308 * Rg * (t * t * lambda_t) * (rh - 1.0);
+            const double q_sub = (rho * D) * rcp_t(D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
+            const double LR = Ls * M - Rgt;
+            const double sdz0 = snow_depth + z0;
+            const double logden = log_t((kZUR - sdz0) * rcp_t(z0), mt);
+            const double inv_logden = rcp_t(logden);
+            // log(u_z) = log(uref) - log(logden) + log(log((cz - z0)/z0)), so
+            // u_z^1.36 costs one exp per row
+            const double lu_face = uref > 0.0 ? log_t(uref, mt) - log_t(logden, mt) : 0.0;
+            double v1 = 0, v2 = 0;
+            v1 += ux * ux;
+            v2 += uy * uy;
+            const double inv_nrm = rcp_t(sqrt(v1 + v2));
+            double* fv = A.face_v;
+            fv[FV_HS * Tp + i] = hs;
+            fv[FV_USTAR * Tp + i] = ustar;
+            fv[FV_UTH * Tp + i] = uth;
+            fv[FV_CSALT * Tp + i] = c_salt;
+            fv[FV_QSUB * Tp + i] = q_sub;
+            fv[FV_C1R * Tp + i] = c1r;
+            fv[FV_LR * Tp + i] = LR;
+            fv[FV_LU * Tp + i] = lu_face;
+            fv[FV_INVLOGDEN * Tp + i] = inv_logden;
+            // lateral faces: udotm_f = u_z * k_f with k_f = (u_hat . m_f) / |u_hat|
+#pragma unroll
+            for (int f = 0; f < 3; ++f) fv[(FV_K0 + f) * Tp + i] = inv_nrm * dot2(ux, uy, mx[f], my[f]);
+        }
+        // append the faces with a saltation layer (one atomic per warp)
+        const unsigned ball = __ballot_sync(0xffffffffu, slow);
+        if (ball) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(A.n_slow, __popc(ball));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (slow) A.slow_list[base + __popc(ball & ((1u << lane) - 1u))] = (int32_t)i;
+        }
+    }
+}
+
+// Pass 2, one thread per row of a face on the list: the height-dependent
+// terms of its layer (cz = z dz + hs + dz/2), stored by row as pass 3
+// reads them.  Every lane of a warp does the same work.
+__global__ void __launch_bounds__(kBlock) k_salt_rows(Params P, Forcing F, Susp A, Members Mb) {
+    __shared__ MathTables mt;
+    math_tables_load(mt, P.mt);
+    const int64_t n = *A.n_slow;
+    const int64_t tasks = n * P.L, Tp = P.Tp, R = P.R;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < tasks; q += (int64_t)gridDim.x * blockDim.x) {
+        const int z = (int)(q / n);
+        const int64_t i = A.slow_list[q - (int64_t)z * n];
+        const Member mp = Mb.prm[Mb.face_member[i]];
+        double snow_depth = F.sd[i];
+        snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
+        const double hs = A.face_v[FV_HS * Tp + i];
+        const double cz = z * P.dz + hs + P.dz / 2.;
+        CzCoef o;
+        cz_coeffs(cz, cz + snow_depth - (snow_depth + mp.z0), mp.z0, mp.settling_scale, P, mt, o);
+        const int64_t r = (int64_t)z * Tp + i;
+        double* w = A.slow_rows + r;
+        w[0 * R] = o.inv_mm;
+        w[1 * R] = o.omega;
+        w[2 * R] = o.Qr;
+        w[3 * R] = o.l;
+        w[4 * R] = o.rz2nu;
+        w[5 * R] = o.rsig;
+        w[6 * R] = o.lwarg;
+        w[7 * R] = o.llw;
+    }
+}
+
+// Pass 3, one thread per face: the suspension rows (PBSM3D.cpp:1236-1404)
+// from the layer terms (table or pass 2) and the face constants (pass 1),
+// and the Thomas factorisation of the column.
 __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Faces G, Forcing F, FaceState S, Susp A,
                                                                Members Mb, double* partials, Scalars* sc) {
+    __shared__ MathTables mt;
+    math_tables_load(mt, P.mt);
     unsigned long long vmax_bits = 0;
     bool bad = false;
     // per-member max |rhs| of this block (ensembles), folded into Mb.rhs_max at the end
@@ -156,159 +356,39 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             }
             continue;
         }
-        // ---- this face's ensemble member
         const int mem = Mb.face_member[i];
         const Member mp = Mb.prm[mem];
         const CzCoef* tab = A.cztab + (int64_t)mem * P.L;
-        // ---- saltation, PBSM3D.cpp:436-925
-        double fetch = 1000;
-        if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
-        const double min_sd_trans_avg = P.min_sd_trans;
+        const double* fv = A.face_v;
+        const double hs = fv[FV_HS * Tp + i];
+        const double ustar = fv[FV_USTAR * Tp + i];
+        const double uth = fv[FV_UTH * Tp + i];
+        const double c_salt = fv[FV_CSALT * Tp + i];
+        const double q_sub = fv[FV_QSUB * Tp + i];
+        const double c1r = fv[FV_C1R * Tp + i];
+        const double LR = fv[FV_LR * Tp + i];
+        const double lu_face = fv[FV_LU * Tp + i];
+        const double inv_logden = fv[FV_INVLOGDEN * Tp + i];
+        const bool saltation = S.saltation[i];
         const double uref = F.UR[i];
         double snow_depth = F.sd[i];
         snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
-        const double u2 = F.U2[i];
-        const double z10 = 10. + snow_depth;
-        double u10;
-        if (z10 < kZUR)
-            u10 = log_scale_wind(uref, kZUR, z10, snow_depth, mp.z0);
-        else
-            u10 = uref;
-        double swe = F.swe[i];
-        swe = is_nan_chm(swe) ? 0 : swe;
         double height_diff = smax(0.0, G.canopy[i] - snow_depth);
         if (!P.enable_veg) height_diff = 0;
-        double ustar = 1.3;
-        double lambda = 0;
-        bool saltation = false;
-        double z0 = 0;
-        const double T_c = F.t[i];
-        // u*_th decides saltation (ustar >= u*_th) and enters the cancelling
-        // c_salt bracket: evaluated without contraction, in the reference's order
-        double uth = __dadd_rn(__dadd_rn(0.35, __dmul_rn(1.0 / 150.0, T_c)), __dmul_rn(__dmul_rn(1.0 / 8200.0, T_c), T_c));
-        uth = __dmul_rn(uth, mp.uth_scale);
-        const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
-        if (height_diff <= P.cutoff && snow_depth >= min_sd_trans_avg && !G.water[i]) {
-            if (P.use_R94_lambda)
-                lambda = 0.5 * G.lai[i] * height_diff;
-            else
-                lambda = stalkN * stalkD * height_diff;
-            ustar = u2 * kKappa / P.log_2_0002;
-            if (ustar >= uth) {
-                saltation = true;
-                z0 = mp.z0;
-            }
-        }
-        if (!saltation) {
-            z0 = mp.z0;
-            ustar = smax(0.01, kKappa * uref / mp.log_zur_z0);
-        }
-        z0 = smax(mp.z0, z0);
-        ustar = smax(0.01, ustar);
-        double hs = 0;
-        if (saltation) hs = 0.08436 * powpos(ustar, 1.27);
-        double Qsalt = 0;
-        double c_salt = 0;
-        const double t = F.t[i] + 273.15;
-        double vx, vy;
-        bearing_to_cartesian(F.dir[i], vx, vy);
-        const double ux = -vx, uy = -vy;
-        double mx[3], my[3], Ej[3], Af[3];
-        int32_t nb[3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            mx[j] = G.mx[j * Tp + i];
-            my[j] = G.my[j * Tp + i];
-            Ej[j] = G.E[j * Tp + i];
-            nb[j] = G.nbr[j * Tp + i];
-            Af[j] = Ej[j] * P.dz;
-        }
         const double area = G.area[i];
-        if (saltation) {
-            const double rho_f = std_dry_air_density(G.zc[i], t);
-            const double Beta = 202.0, mB = 0.16;
-            const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
-            const double tau_n_ratio = __ddiv_rn(mbl, __dadd_rn(1.0, mbl));
-            // the bracket cancels near the threshold: no contraction here
-            const double bracket =
-                __dsub_rn(__dsub_rn(1.0, tau_n_ratio), __ddiv_rn(__dmul_rn(uth, uth), __dmul_rn(ustar, ustar)));
-            c_salt = __dmul_rn(__ddiv_rn(rho_f, __dmul_rn(3.29, ustar)), bracket);
-            if (c_salt < 0 || isnan(c_salt)) {
-                c_salt = 0;
-                saltation = false;
-            }
-            if (P.use_exp_fetch && fetch < 500) {
-                const double fetch_ref = 500, mu = 3.0;
-                c_salt *= 1.0 - exp(-mu * fetch / fetch_ref);
-            } else if (P.use_tanh_fetch && fetch <= 300.) {
-                c_salt *= P.Lc_tanh;  // 0.5*tanh(0.01333*fetch_ref - 2)+0.5 with fetch_ref = 300
-            }
-            if (P.use_PomLi) {  // PBSM3D.cpp:848-865
-                const double Ah = F.psh[i];
-                const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
-                const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
-                const double z0v = (stalkN * stalkD * height_diff) / 2.0;
-                const double us = u10 / sqrt((1 + 340.0 * z0v));
-                const double Pu10 = 1.0 / (1.0 + exp((sqrt(M_PI) * (u_mean - us)) / delta));
-                S.bsp[i] = Pu10;
-                c_salt *= Pu10;
-            }
-            const double uhs = 2.8 * uth;
-            Qsalt = c_salt * uhs * hs;
-            double mass = 0;
-            for (int j = 0; j < 3; ++j) {
-                const double udm = __dadd_rn(__dmul_rn(ux, mx[j]), __dmul_rn(uy, my[j]));
-                mass = __dadd_rn(mass, __dmul_rn(__dmul_rn(-Ej[j], Qsalt), udm));
-            }
-            mass = __dmul_rn(__ddiv_rn(mass, area), P.dt);
-            if (mass < 0 && fabs(mass) > swe) {
-                c_salt = 0;
-                Qsalt = c_salt * uhs * hs;
-            }
-        }
-        S.Qsalt[i] = Qsalt;
-        S.saltation[i] = saltation;
-
-        // ---- layers, PBSM3D.cpp:927-1404
-        // Everything that does not change with the layer is computed once per
-        // face.  Division by a per-face or constant value becomes a product
-        // with its reciprocal and the sublimation rate is regrouped so that no
-        // division is left per row (each change moves a result by a few ulps).
-        const double rh = F.rh[i] / 100.;
-        const double es = saturated_vapour_pressure(t);
-        const double D = 2.06e-5 * powpos(t / 273.15, 1.75);
-        const double lambda_t = 0.000063 * t + 0.00673;
-        const double Ls = 2.838e6, M = 18.01, Rg = 8313;
-        const double rho = (M * es) / (Rg * t);
-        // dm/dt = Sh rho D (2 pi Nu R r sigma t^2 lt - L M Qr + Qr R t) /
-        //         (D L Sh (L M - R t) rho + lt t^2 Nu R),  Sh = Nu,
-        //       = q * ((c1 (rh-1)) Nu (r sigfac) - Qr (L M - R t))
-        const double Rgt = Rg * t;
-        const double c1r = 6.283185308 * Rg * (t * t * lambda_t) * (rh - 1.0);
-        const double q_sub = (rho * D) / (D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
-        const double LR = Ls * M - Rgt;
         const double V5 = area * P.dz / 5.0;
         const double areaK = area * P.inv_dz;
-        const double sdz0 = snow_depth + z0;
-        const double inv_z0 = 1.0 / z0;
-        const double logden = log((kZUR - sdz0) * inv_z0);
-        const double inv_logden = 1.0 / logden;
-        // log(u_z) = log(uref) - log(logden) + log(log((cz - z0)/z0)) on the
-        // fast path (hs == 0), so u_z^1.36 costs one exp per row there
-        const double lu_face = uref > 0.0 ? log(uref) - log(logden) : 0.0;
-        double v1 = 0, v2 = 0;
-        v1 += ux * ux;
-        v2 += uy * uy;
-        const double inv_nrm = 1.0 / sqrt(v1 + v2);
-        // lateral faces: udotm_f = u_z * k_f with k_f = (u_hat . m_f) / |u_hat|
         double Ak[3], al[3];
         bool out_f[3];
+        int32_t nb[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-            const double kf = inv_nrm * dot2(ux, uy, mx[f], my[f]);
-            Ak[f] = Af[f] * kf;
+            const double kf = fv[(FV_K0 + f) * Tp + i];
+            const double Af = G.E[f * Tp + i] * P.dz;
+            nb[f] = G.nbr[f * Tp + i];
+            Ak[f] = Af * kf;
             out_f[f] = gt0(kf);
-            al[f] = P.do_lateral_diff ? Af[f] * 0.00001 : 0.0;
+            al[f] = P.do_lateral_diff ? Af * 0.00001 : 0.0;
         }
         const double ust_dc = P.snow_diffusion_const * ustar;
         // Per-face versions of the per-row branch tests (no FP64 compare per
@@ -323,52 +403,46 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         double prev_up = 0.0, prev_ib = 1.0;
         unsigned long long face_max = 0;
         for (int z = 0; z < P.L; ++z) {
-            CzCoef co;
-            double cz;
-            if (fast) {
-                co = tab[z];
-                cz = co.cz;
-            } else {
-                cz = z * P.dz + hs + P.dz / 2.;
-                cz_coeffs(cz, z0, mp.settling_scale, P, co);
-            }
+            const int64_t r = (int64_t)z * Tp + i;
+            // layer terms: the member's table row, or this row of pass 2
+            const double* lp = fast ? &tab[z].inv_mm : A.slow_rows + r;
+            const int64_t ls = fast ? 1 : R;
+            const double inv_mm = lp[0], omega = lp[ls], Qr = lp[2 * ls], lmix = lp[3 * ls];
+            const double rz2nu = lp[4 * ls], rsig = lp[5 * ls], lwarg = lp[6 * ls], llw = lp[7 * ls];
+            const double cz = z * P.dz + hs + P.dz / 2.;
             double u_z, xrz;
             if (in_canopy_possible && saltation && cz < height_diff) {
                 u_z = 2.8 * uth;
-                xrz = 0.005 * powpos(u_z, 1.36);
+                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             } else if (in_canopy_possible && cz < height_diff) {
                 u_z = 0.01;
-                xrz = 0.005 * powpos(u_z, 1.36);
+                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             } else if (all_below_zur || cz + snow_depth < kZUR) {
                 // log_scale_wind(uref, 50, hz, snow_depth, z0), clamped at 0.01 m/s
-                const double larg = fast ? co.lwarg : log((cz + snow_depth - sdz0) * inv_z0);
-                const double u_raw = uref * larg * inv_logden;
+                const double u_raw = uref * lwarg * inv_logden;
                 const long long ub = __double_as_longlong(u_raw);
                 const bool above = ub > b001 && ub <= 0x7ff0000000000000ll;  // 0.01 < u_raw, not NaN
                 u_z = above ? u_raw : 0.01;
-                xrz = (fast && above && uref_pos) ? 0.005 * exp(1.36 * (lu_face + co.llw))
-                                                  : 0.005 * powpos(u_z, 1.36);
+                xrz = (above && uref_pos) ? 0.005 * exp_t(1.36 * (lu_face + llw), mt) : 0.005 * pow_t(u_z, 1.36, mt);
             } else {
                 u_z = fmax(0.01, uref);
-                xrz = 0.005 * powpos(u_z, 1.36);
+                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             }
-            const double omega = co.omega;
             const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
-            const double Nu = 1.79 + 0.606 * sqrt(co.rz2nu * Vr);
-            const double dmdtz = q_sub * (c1r * Nu * co.rsig - co.Qr * LR);
-            double csubl = dmdtz * co.inv_mm;
+            const double Nu = 1.79 + 0.606 * sqrt(rz2nu * Vr);
+            const double dmdtz = q_sub * (c1r * Nu * rsig - Qr * LR);
+            double csubl = dmdtz * inv_mm;
             const double w = omega;
             double K34;
             if (P.rouault)
-                K34 = (1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar))) * ustar * co.l;
+                K34 = (1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar))) * ustar * lmix;
             else
-                K34 = ust_dc * co.l;
+                K34 = ust_dc * lmix;
             double alpha[5] = {al[0], al[1], al[2], areaK * K34, 0.0};
             alpha[4] = alpha[3];
             double udm[5];
             udm[3] = -w;  // uvw . (0,0,1)
             udm[4] = w;   // uvw . (0,0,-1)
-            const int64_t r = (int64_t)z * Tp + i;
             if (!P.do_sublimation) csubl = 0.0;
             A.u_z[r] = u_z;
             A.csubl[r] = csubl;
@@ -449,7 +523,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             // Thomas factorisation of the column: beta_z = d_z - l_z * up_{z-1}
             const double lz = (z == 0) ? 0.0 : lo * prev_ib;
             const double beta = (z == 0) ? dg : dg - lz * prev_up;
-            const double ib = 1.0 / beta;
+            const double ib = rcp_t(beta);
             A.fac_l[r] = lz;
             A.fac_ib[r] = ib;
             if (P.mixed) {
@@ -757,10 +831,16 @@ void launch_member_zero(Ctx& c, cudaStream_t s, double* x) {
 
 void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     const int64_t T = c.P.T, rows = T * c.P.L;
+    // the three passes count as one assembly; the algorithmic bytes are those
+    // of the whole step: per face 8 forcing + 133 B geometry in, Qsalt + flag
+    // out; per row 12 doubles out (+6 floats MIXED)
     prof_begin(c, s);
+    cudaMemsetAsync(c.A.n_slow, 0, sizeof(int), s);
+    k_salt_faces<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
+    k_salt_rows<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Fo, c.A, c.Mb);
     k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
-    // per face: 8 forcing + 133 B geometry in, Qsalt + flag out; per row 12 doubles out (+6 floats MIXED)
     prof_end(c, s, PBSM3D_K_ASSEMBLE, T * (64 + 133 + 9) + rows * (96 + (c.P.mixed ? 24 : 0)));
+    c.launches += 2;
 }
 
 void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {
@@ -784,6 +864,15 @@ void launch_update(Ctx& c, cudaStream_t s) {
 void launch_init_static(Ctx& c, cudaStream_t s) {
     k_cz_table<<<(c.Mb.n * c.P.L + 63) / 64, 64, 0, s>>>(c.P, c.Mb, c.A.cztab);
     k_init_static<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.dr, c.dz_);
+}
+
+void math_tables_fill(MathTables& h) {
+    for (int j = 0; j < 256; ++j) {
+        h.exp2j[j] = (double)exp2l((long double)j / 256.0L);
+        const double c = 1.0 / (1.0 + (j + 0.5) / 256.0);
+        h.logc[j] = c;
+        h.logl[j] = (double)(-logl((long double)c));
+    }
 }
 
 }  // namespace pbsm
