@@ -304,6 +304,8 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
         return {"susp_iters_mean": float(np.mean([s["susp_iters"] for s in sts])),
                 "susp_refinements_mean": float(np.mean([s["susp_refinements"] for s in sts])),
                 "dep_iters_mean": float(np.mean([s["dep_iters"] for s in sts])),
+                "dep_refinements_mean": float(np.mean([s["dep_refinements"] for s in sts])),
+                "saltating_faces_mean": float(np.mean([s["n_slow_faces"] for s in sts])),
                 "susp_rel_residual_max": float(np.max([s["susp_rel_residual"] for s in sts])),
                 "ms_coefficients": float(np.mean([s["ms_coefficients"] for s in sts])),
                 "ms_susp_solve": float(np.mean([s["ms_susp_solve"] for s in sts])),

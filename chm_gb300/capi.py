@@ -81,7 +81,7 @@ class Stats(C.Structure):
         ("ledger_deposited", C.c_double), ("ledger_clipped", C.c_double), ("ledger_snow_mass", C.c_double),
         ("ledger_residual", C.c_double), ("bytes_moved", C.c_int64), ("gpu_launches", C.c_int32),
         ("profiled", C.c_int32), ("kern_ms", C.c_double * 16), ("kern_bytes", C.c_int64 * 16),
-        ("kern_launches", C.c_int32 * 16),
+        ("kern_launches", C.c_int32 * 16), ("dep_refinements", C.c_int32), ("n_slow_faces", C.c_int32),
     ]
 
     def as_dict(self) -> dict:

@@ -86,6 +86,8 @@ void free_all(Ctx& c) {
         if (e) cudaEventDestroy(e);
     if (c.sc_host) cudaFreeHost(c.sc_host);
     c.sc_host = nullptr;
+    if (c.n_slow_host) cudaFreeHost(c.n_slow_host);
+    c.n_slow_host = nullptr;
     if (c.stream) cudaStreamDestroy(c.stream);
     c.stream = nullptr;
 }
@@ -280,7 +282,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     }
     for (auto& e : c.ev) cudaEventCreate(&e);
     for (auto& e : c.user_ev) cudaEventCreate(&e);
-    if (cudaMallocHost(&c.sc_host, sizeof(Scalars)) != cudaSuccess) {
+    if (cudaMallocHost(&c.sc_host, sizeof(Scalars)) != cudaSuccess ||
+        cudaMallocHost(&c.n_slow_host, sizeof(int)) != cudaSuccess) {
         g_create_error = "cudaMallocHost failed";
         free_all(c);
         delete h;
@@ -388,6 +391,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     c.dz_ = dalloc<double>(c, Tp, ok);
     c.dp = dalloc<double>(c, Tp, ok);
     c.dq = dalloc<double>(c, Tp, ok);
+    if (P.mixed) c.dep32 = dalloc<float>(c, (size_t)11 * Tp, ok);
+    c.cg_flags = dalloc<unsigned>(c, (size_t)kMaxCgBlocks * 32, ok);
     c.sc = dalloc<Scalars>(c, 4, ok);
     c.red.partials = dalloc<double>(c, (size_t)8 * c.red.nblocks, ok);
     c.ledger = dalloc<double>(c, 8, ok);
@@ -777,12 +782,14 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     launch_assemble_suspension(c, s);
     PBSM_CUDA_TRY(cudaGetLastError());
     PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.n_slow_host, c.A.n_slow, sizeof(int), cudaMemcpyDeviceToHost, s));
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[2], s));
     PBSM_CUDA_TRY(cudaStreamSynchronize(s));
     if (c.sc_host->nan_flag != 0.0) {
         c.err = "NaN in the assembled suspension system (check the forcing)";
         return PBSM3D_ERR_NAN_INPUT;
     }
+    c.n_slow = *c.n_slow_host;
     const double susp_rhs_max = c.sc_host->rhs_max;
     c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
     c.target_scale2 = 1.0;
@@ -859,6 +866,8 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         st->susp_matvecs = c.susp_matvecs;
         st->susp_refinements = c.susp_refinements;
         st->dep_iters = c.dep_iters;
+        st->dep_refinements = c.dep_refinements;
+        st->n_slow_faces = c.n_slow;
         st->susp_rel_residual = c.susp_relres;
         st->dep_rel_residual = c.dep_relres;
         st->susp_rhs_max = susp_rhs_max;

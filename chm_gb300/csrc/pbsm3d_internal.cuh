@@ -32,6 +32,7 @@ constexpr int kBlock = 256;
 constexpr int kMaxLayers = 64;
 constexpr int kMaxTerms = 4;
 constexpr int kMaxMembers = 256;
+constexpr int kMaxCgBlocks = 1024;  // blocks of a cooperative CG launch
 
 // Configuration scalars every kernel sees (passed by value).
 struct Params {
@@ -207,8 +208,12 @@ struct Ctx {
     // reductions
     Scalars* sc;       // device
     Scalars* sc_host;  // pinned mirror
+    int* n_slow_host = nullptr;  // pinned: faces with a saltation layer in the last assembly
+    int n_slow = 0;
     ReduceWs red;
     int grid_rows, grid_faces;
+    int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
+    int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
     // ledger partial sums
     double* ledger;    // device [8]
     GridBar* gbar;     // device
@@ -220,6 +225,11 @@ struct Ctx {
     bool mlp_loaded = false;
     float mlp_b3 = 0.0f;
     int coop_blocks;   // co-resident blocks of the persistent CG kernel
+    int coop_blocks32 = 0;  // ... of its FP32 instance (MIXED)
+    unsigned* cg_flags;     // [kMaxCgBlocks][32] all-reduce flags of the persistent CG
+    // MIXED deposition: FP32 matrix (diag, off[3], dinv), right-hand side and
+    // the five CG vectors, [11][Tp]
+    float* dep32 = nullptr;
     cudaStream_t stream;
     cudaEvent_t ev[16];
     cudaEvent_t user_ev[16];
@@ -237,7 +247,7 @@ struct Ctx {
     int64_t kern_bytes[16];
     int kern_launches[16];
     bool suspension_present, deposition_present;
-    int susp_iters, susp_matvecs, susp_refinements, dep_iters;
+    int susp_iters, susp_matvecs, susp_refinements, dep_iters, dep_refinements = 1;
     double susp_relres, dep_relres;
     double warm_gamma = 0.0;  // scale applied to the last warm start (0 = dropped)
 };
@@ -304,6 +314,51 @@ __device__ __forceinline__ bool block_partials_last(double (&v)[NT], double* par
         for (int k = 0; k < NT; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
         __threadfence();
         unsigned prev = atomicAdd(counter, 1u);
+        is_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        double s = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(&partials[k * gridDim.x + b]);
+        tot[k] = s;
+    }
+    block_sum<NT>(tot);
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
+// Same for FP32 per-thread values: the warp-level sums stay in FP32 (off the
+// FP64 pipe); each warp's sum is widened to FP64 for the block and grid sums.
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <int NT>
+__device__ __forceinline__ bool block_partials_last(float (&vf)[NT], double* partials, unsigned* counter,
+                                                    double (&tot)[NT]) {
+    __shared__ double shf[NT][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const float w = warp_sum_f(vf[k]);
+        if (lane == 0) shf[k][wid] = (double)w;
+    }
+    __syncthreads();
+    __shared__ bool is_last;
+    if (threadIdx.x == 0) {
+        const int nw = (int)(blockDim.x >> 5);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            double s = 0;
+            for (int w = 0; w < nw; ++w) s += shf[k][w];
+            partials[k * gridDim.x + blockIdx.x] = s;
+        }
+        __threadfence();
+        const unsigned prev = atomicAdd(counter, 1u);
         is_last = (prev == gridDim.x - 1);
     }
     __syncthreads();

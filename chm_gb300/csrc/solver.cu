@@ -17,7 +17,8 @@
 // residuals, x and all norms stay FP64.
 //
 // Deposition (SPD: diag(area) + eps * weighted graph Laplacian):
-// Jacobi-preconditioned CG in FP64.
+// Jacobi-preconditioned CG in FP64 in one cooperative launch; MIXED runs
+// the same CG in FP32 inside FP64 iterative refinement.
 //
 // Every reduction is deterministic: fixed grid, per-block partials, the
 // last block sums them in block order.  Scalars live in device memory, so
@@ -124,13 +125,14 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, const V* __restri
 
 // v = p + N zp; rv = (rhat, v); alpha = rho / rv
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_v(Op<V> op, const V* __restrict__ p, const V* __restrict__ zp,
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, const V* __restrict__ p, const V* __restrict__ zp,
                                                    V* __restrict__ v, const V* __restrict__ rh, Scalars* sc,
                                                    double* partials) {
     if (sc->done) return;
     V acc[2] = {0, 0};
     lateral_apply<V, 1>(op, p, zp, v, rh, acc);
-    double d[1] = {(double)acc[0]}, tot[1];
+    V d[1] = {acc[0]};
+    double tot[1];
     if (block_partials_last<1>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
         const double rv = tot[0];
         sc->rv = rv;
@@ -144,13 +146,13 @@ __global__ void __launch_bounds__(kBlock) k_bicg_v(Op<V> op, const V* __restrict
 
 // t = s + N zs; ts = (t, s), tt = (t, t); omega = ts / tt
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_t(Op<V> op, const V* __restrict__ s, const V* __restrict__ zs,
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_t(Op<V> op, const V* __restrict__ s, const V* __restrict__ zs,
                                                    V* __restrict__ t, Scalars* sc, double* partials) {
     if (sc->done) return;
     V acc[2] = {0, 0};
     lateral_apply<V, 2>(op, s, zs, t, s, acc);
-    double d[2] = {(double)acc[0], (double)acc[1]}, tot[2];
-    if (block_partials_last<2>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+    double tot[2];
+    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
         sc->ts = tot[0];
         sc->tt = tot[1];
         sc->omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_t(Op<V> op, const V* __restrict
 
 // x += alpha zp + omega zs; r = s - omega t; rho' = (rhat, r), (r, r)
 template <typename V, typename X>
-__global__ void __launch_bounds__(kBlock) k_bicg_x(int64_t Tp, int L, X* __restrict__ x, const V* __restrict__ zp,
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, X* __restrict__ x, const V* __restrict__ zp,
                                                    const V* __restrict__ zs, const V* __restrict__ s,
                                                    const V* __restrict__ t, V* __restrict__ r,
                                                    const V* __restrict__ rh, Scalars* sc, double* partials) {
@@ -177,8 +179,8 @@ __global__ void __launch_bounds__(kBlock) k_bicg_x(int64_t Tp, int L, X* __restr
             acc[1] += rk * rk;
         }
     }
-    double d[2] = {(double)acc[0], (double)acc[1]}, tot[2];
-    if (block_partials_last<2>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+    double tot[2];
+    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
         const double rho_new = tot[0];
         sc->rnorm2 = tot[1];
         sc->iter += 1;
@@ -305,104 +307,7 @@ __global__ void k_zero(int64_t n, V* __restrict__ a) {
 }
 
 // ---------------------------------------------------------------- deposition CG
-// init: r = b, z = D^{-1} b, p = z, q = A z; (r,z), (p,q), (b,b)
-__global__ void __launch_bounds__(kBlock) k_cg_init(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
-                                                    double* zz, double* p, double* q, Scalars* sc, double* partials,
-                                                    double tol, int maxit) {
-    const int64_t Tp = P.Tp;
-    double acc[3] = {0, 0, 0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        const double bi = D.rhs[i];
-        const double zi = D.dinv[i] * bi;
-        double qi = D.diag[i] * zi;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const int32_t nb = nbr[j * Tp + i];
-            if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.rhs[nb]);
-        }
-        r[i] = bi;
-        zz[i] = zi;
-        p[i] = zi;
-        q[i] = qi;
-        D.x[i] = 0.0;
-        acc[0] += bi * zi;
-        acc[1] += zi * qi;
-        acc[2] += bi * bi;
-    }
-    double tot[3];
-    if (block_partials_last<3>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        sc->rho = tot[0];
-        sc->bnorm2 = tot[2];
-        sc->rnorm2 = tot[2];
-        sc->target2 = tol * tol * tot[2];
-        sc->iter = 0;
-        sc->maxit = maxit;
-        if (tot[2] == 0.0) {
-            sc->done = DONE_CONVERGED;
-        } else if (!(tot[1] > 0.0)) {
-            sc->done = DONE_BREAKDOWN;
-        } else {
-            sc->done = DONE_NO;
-            sc->alpha = tot[0] / tot[1];
-        }
-    }
-}
-
-// x += alpha p; r -= alpha q; z = D^{-1} r; (r,z), (r,r)
-__global__ void __launch_bounds__(kBlock) k_cg_x(Params P, Dep D, double* r, double* zz, const double* p,
-                                                 const double* q, Scalars* sc, double* partials) {
-    if (sc->done) return;
-    const double alpha = sc->alpha;
-    double acc[2] = {0, 0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        D.x[i] += alpha * p[i];
-        const double ri = r[i] - alpha * q[i];
-        r[i] = ri;
-        const double zi = D.dinv[i] * ri;
-        zz[i] = zi;
-        acc[0] += ri * zi;
-        acc[1] += ri * ri;
-    }
-    double tot[2];
-    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        sc->iter += 1;
-        sc->rnorm2 = tot[1];
-        sc->beta = tot[0] / sc->rho;
-        sc->rho = tot[0];
-        if (tot[1] <= sc->target2) sc->done = DONE_CONVERGED;
-        else if (!isfinite(tot[1])) sc->done = DONE_BREAKDOWN;
-        else if (sc->iter >= sc->maxit) sc->done = DONE_MAXIT;
-    }
-}
-
-// p = z + beta p; q = A z + beta q; (p,q) -> alpha = rho / (p,q)
-__global__ void __launch_bounds__(kBlock) k_cg_p(Params P, Dep D, const int32_t* __restrict__ nbr, const double* zz,
-                                                 double* p, double* q, Scalars* sc, double* partials) {
-    if (sc->done) return;
-    const double beta = sc->beta;
-    const int64_t Tp = P.Tp;
-    double acc[1] = {0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        double az = D.diag[i] * zz[i];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const int32_t nb = nbr[j * Tp + i];
-            if (nb >= 0) az += D.off[j * Tp + i] * zz[nb];
-        }
-        const double pi = zz[i] + beta * p[i];
-        const double qi = az + beta * q[i];
-        p[i] = pi;
-        q[i] = qi;
-        acc[0] += pi * qi;
-    }
-    double tot[1];
-    if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        if (!(tot[0] > 0.0)) sc->done = DONE_BREAKDOWN;
-        else sc->alpha = sc->rho / tot[0];
-    }
-}
-
-// r = b - A x (deposition), (r, r)
+// ||b - A x||^2 of the FP64 deposition system (final check, ledger residual)
 __global__ void __launch_bounds__(kBlock) k_cg_resid(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
                                                      Scalars* sc, double* partials) {
     const int64_t Tp = P.Tp;
@@ -423,10 +328,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_resid(Params P, Dep D, const int3
 }
 
 // ---------------------------------------------------------------- persistent deposition CG
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
     unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long global_timer_ns() {
     unsigned long long t;
@@ -435,103 +343,108 @@ __device__ __forceinline__ unsigned long long global_timer_ns() {
 }
 
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
-constexpr int kCgBlock = 512;  // one block per SM keeps barrier arrivals few
+constexpr int kCgBlock = 512;    // one block per SM keeps the all-reduce fan-in small
+constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 
-// Grid-wide barrier of a cooperative launch.  The wait is bounded: after
-// kBarrierLimitNs a block sets gb->err and every block leaves at its next
-// barrier, so a fault in the co-residency assumption ends in an error, never
-// in a hang.  Returns false when the kernel must exit.
-__device__ bool grid_barrier(GridBar* gb) {
+// All-reduce of NT per-thread values over a cooperative grid, identical in
+// every block, without atomics: block b writes its partials and then
+// releases flags[b] = epoch; thread t < gridDim of every block waits for
+// flags[t], reads block t's partials and the block sums them in block order
+// (deterministic).  Partials alternate between two buffers by epoch parity:
+// a block can only publish epoch e+2 after every block has published e+1,
+// i.e. after every block has finished reading epoch e.  The wait is bounded:
+// after kBarrierLimitNs a block sets *err and every block leaves at its next
+// all-reduce, so a broken co-residency assumption ends in an error, never a
+// hang.  Returns false when the kernel must exit.
+template <int NT>
+__device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, unsigned epoch, int* err,
+                            double (&tot)[NT]) {
+    __shared__ double bc[NT];
     __shared__ int ok;
-    __syncthreads();
+    block_sum<NT>(v);
+    const int G = gridDim.x;
+    double* pp = partials + (size_t)(epoch & 1u) * 4 * G;
     if (threadIdx.x == 0) {
-        const unsigned gen = ld_acquire_u32(&gb->gen);
-        __threadfence();
-        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        for (int k = 0; k < NT; ++k) pp[k * G + blockIdx.x] = v[k];
+        st_release_u32(&flags[blockIdx.x * kFlagStride], epoch);
         ok = 1;
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&gb->count, 0u);
-            __threadfence();
-            atomicAdd(&gb->gen, 1u);
-        } else {
-            const unsigned long long t0 = global_timer_ns();
-            while (ld_acquire_u32(&gb->gen) == gen) {
-                if (*(volatile int*)&gb->err) {
-                    ok = 0;
-                    break;
-                }
-                if (global_timer_ns() - t0 > kBarrierLimitNs) {
-                    atomicExch(&gb->err, 1);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(20);
-            }
-        }
-        __threadfence();
     }
     __syncthreads();
-    return ok != 0;
-}
-
-// Totals of NT per-thread values over the whole grid, identical in every
-// block (each block sums all partials in block order).  buf alternates
-// between two partial buffers so a fast block never overwrites partials a
-// slow block is still reading.
-template <int NT>
-__device__ bool grid_totals(double (&v)[NT], double* partials, GridBar* gb, double (&tot)[NT]) {
-    __shared__ double bc[NT];
-    block_sum<NT>(v);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < NT; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
-    if (!grid_barrier(gb)) return false;
     double t[NT];
-    for (int k = 0; k < NT; ++k) {
-        double acc = 0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) acc += __ldcg(&partials[k * gridDim.x + b]);
-        t[k] = acc;
+    for (int k = 0; k < NT; ++k) t[k] = 0.0;
+    for (int b = threadIdx.x; b < G; b += blockDim.x) {
+        const unsigned long long t0 = global_timer_ns();
+        while (ld_relaxed_u32(&flags[b * kFlagStride]) != epoch) {
+            if (*(volatile int*)err) {
+                ok = 0;
+                break;
+            }
+            if (global_timer_ns() - t0 > kBarrierLimitNs) {
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+        }
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        for (int k = 0; k < NT; ++k) t[k] += __ldcg(&pp[k * G + b]);
     }
     block_sum<NT>(t);
     if (threadIdx.x == 0)
         for (int k = 0; k < NT; ++k) bc[k] = t[k];
     __syncthreads();
     for (int k = 0; k < NT; ++k) tot[k] = bc[k];
+    const bool good = ok != 0;
     __syncthreads();
-    return true;
+    return good;
 }
 
-// Jacobi-preconditioned CG on the deposition system in one cooperative
-// launch; at 1M faces its vectors and matrix (~100 MB) stay in L2.
-__global__ void __launch_bounds__(kCgBlock) k_cg_persistent(Params P, Dep D, const int32_t* __restrict__ nbr, double* r,
-                                                          double* zz, double* p, double* q, double* partials,
-                                                          GridBar* gb, Scalars* sc, double tol, int maxit) {
-    const int64_t Tp = P.Tp;
+// The deposition system in one precision.
+template <typename V>
+struct DepSys {
+    const V* diag;      // [Tp]
+    const V* off;       // [3][Tp]
+    const V* dinv;      // [Tp] Jacobi preconditioner
+    const V* b;         // [Tp]
+    V* x;               // [Tp] solution (starts at 0)
+    V *r, *zz, *p, *q;  // [Tp] work
+};
+
+// Jacobi-preconditioned CG in one cooperative launch; at 1M faces its
+// vectors and matrix (~100 MB in FP64) stay in L2.  Two all-reduces per
+// iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
+// (q is updated from A z by the recurrence q = A z + beta q).
+template <typename V>
+__global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
+                                                          double* partials, unsigned* flags, int* err, Scalars* sc,
+                                                          double tol, int maxit) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    double* bufs[2] = {partials, partials + 4 * gridDim.x};
-    int nb_buf = 0;
+    unsigned epoch = 0;
     // init: r = b, z = D^-1 b, p = z, q = A z
-    double a3[3] = {0, 0, 0}, t3[3];
-    for (int64_t i = i0; i < Tp; i += stride) {
-        const double bi = D.rhs[i];
-        const double zi = D.dinv[i] * bi;
-        double qi = D.diag[i] * zi;
+    double a3[3], t3[3];
+    {
+        V acc[3] = {0, 0, 0};
+        for (int64_t i = i0; i < Tp; i += stride) {
+            const V bi = D.b[i];
+            const V zi = D.dinv[i] * bi;
+            V qi = D.diag[i] * zi;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const int32_t nb = nbr[j * Tp + i];
-            if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.rhs[nb]);
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.b[nb]);
+            }
+            D.r[i] = bi;
+            D.zz[i] = zi;
+            D.p[i] = zi;
+            D.q[i] = qi;
+            D.x[i] = 0;
+            acc[0] += bi * zi;
+            acc[1] += zi * qi;
+            acc[2] += bi * bi;
         }
-        r[i] = bi;
-        zz[i] = zi;
-        p[i] = zi;
-        q[i] = qi;
-        D.x[i] = 0.0;
-        a3[0] += bi * zi;
-        a3[1] += zi * qi;
-        a3[2] += bi * bi;
+        for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
     }
-    if (!grid_totals<3>(a3, bufs[nb_buf], gb, t3)) return;
-    nb_buf ^= 1;
+    if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
     double rho = t3[0];
     const double bb = t3[2];
     const double target2 = tol * tol * bb;
@@ -541,18 +454,23 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(Params P, Dep D, con
     else if (!(t3[1] > 0.0)) status = 2;
     double alpha = status ? 0.0 : rho / t3[1];
     while (status == 0) {
-        double a2[2] = {0, 0}, t2[2];
-        for (int64_t i = i0; i < Tp; i += stride) {
-            D.x[i] += alpha * p[i];
-            const double ri = r[i] - alpha * q[i];
-            r[i] = ri;
-            const double zi = D.dinv[i] * ri;
-            zz[i] = zi;
-            a2[0] += ri * zi;
-            a2[1] += ri * ri;
+        double a2[2], t2[2];
+        {
+            const V al = (V)alpha;
+            V acc[2] = {0, 0};
+            for (int64_t i = i0; i < Tp; i += stride) {
+                D.x[i] += al * D.p[i];
+                const V ri = D.r[i] - al * D.q[i];
+                D.r[i] = ri;
+                const V zi = D.dinv[i] * ri;
+                D.zz[i] = zi;
+                acc[0] += ri * zi;
+                acc[1] += ri * ri;
+            }
+            a2[0] = (double)acc[0];
+            a2[1] = (double)acc[1];
         }
-        if (!grid_totals<2>(a2, bufs[nb_buf], gb, t2)) return;
-        nb_buf ^= 1;
+        if (!grid_totals<2>(a2, partials, flags, ++epoch, err, t2)) return;
         ++it;
         rr = t2[1];
         if (rr <= target2) {
@@ -569,22 +487,26 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(Params P, Dep D, con
         }
         const double beta = t2[0] / rho;
         rho = t2[0];
-        double a1[1] = {0}, t1[1];
-        for (int64_t i = i0; i < Tp; i += stride) {
-            double az = D.diag[i] * zz[i];
+        double a1[1], t1[1];
+        {
+            const V be = (V)beta;
+            V acc = 0;
+            for (int64_t i = i0; i < Tp; i += stride) {
+                V az = D.diag[i] * D.zz[i];
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int32_t nb = nbr[j * Tp + i];
-                if (nb >= 0) az += D.off[j * Tp + i] * zz[nb];
+                for (int j = 0; j < 3; ++j) {
+                    const int32_t nb = nbr[j * Tp + i];
+                    if (nb >= 0) az += D.off[j * Tp + i] * D.zz[nb];
+                }
+                const V pi = D.zz[i] + be * D.p[i];
+                const V qi = az + be * D.q[i];
+                D.p[i] = pi;
+                D.q[i] = qi;
+                acc += pi * qi;
             }
-            const double pi = zz[i] + beta * p[i];
-            const double qi = az + beta * q[i];
-            p[i] = pi;
-            q[i] = qi;
-            a1[0] += pi * qi;
+            a1[0] = (double)acc;
         }
-        if (!grid_totals<1>(a1, bufs[nb_buf], gb, t1)) return;
-        nb_buf ^= 1;
+        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, t1)) return;
         if (!(t1[0] > 0.0)) {
             status = 2;
             break;
@@ -596,6 +518,47 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(Params P, Dep D, con
         sc->done = status;
         sc->rnorm2 = rr;
         sc->bnorm2 = bb;
+    }
+}
+
+// FP32 copies of the deposition matrix for the inner solves (MIXED).
+__global__ void __launch_bounds__(kBlock) k_dep_to_f32(Params P, Dep D, float* diag, float* off, float* dinv) {
+    const int64_t Tp = P.Tp;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        diag[i] = (float)D.diag[i];
+        dinv[i] = (float)D.dinv[i];
+        for (int j = 0; j < 3; ++j) off[j * Tp + i] = (float)D.off[j * Tp + i];
+    }
+}
+
+// x += d (FP64 accumulation of an FP32 correction)
+__global__ void __launch_bounds__(kBlock) k_dep_add(Params P, Dep D, const float* __restrict__ d) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.Tp; i += (int64_t)gridDim.x * blockDim.x)
+        D.x[i] += (double)d[i];
+}
+
+// r = b - A x in FP64, r32 = (float) r; (r, r) -> rnorm2, (b, b) -> bnorm2
+__global__ void __launch_bounds__(kBlock) k_dep_resid32(Params P, Dep D, const int32_t* __restrict__ nbr,
+                                                        float* __restrict__ r32, Scalars* sc, double* partials) {
+    const int64_t Tp = P.Tp;
+    double acc[2] = {0, 0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
+        double ax = D.diag[i] * D.x[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = nbr[j * Tp + i];
+            if (nb >= 0) ax += D.off[j * Tp + i] * D.x[nb];
+        }
+        const double bi = D.rhs[i];
+        const double ri = bi - ax;
+        r32[i] = (float)ri;
+        acc[0] += ri * ri;
+        acc[1] += bi * bi;
+    }
+    double tot[2];
+    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rnorm2 = tot[0];
+        sc->bnorm2 = tot[1];
     }
 }
 
@@ -638,21 +601,22 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, Scalars* sc, X* x, V* r, V* rh, 
         }
     }
     while (true) {
+        const int gc = c.grid_col[sizeof(V) == 4], gr = c.grid_red[sizeof(V) == 4];
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
-            k_bicg_p<V><<<g, kBlock, smem, s>>>(op, r, p, v, zp, sc);
+            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, r, p, v, zp, sc);
             prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
             prof_begin(c, s);
-            k_bicg_v<V><<<g, kBlock, 0, s>>>(op, p, zp, v, rh, sc, part);
+            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, p, zp, v, rh, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + T * 12);
             prof_begin(c, s);
-            k_bicg_s<V><<<g, kBlock, smem, s>>>(op, r, v, sv, zs, sc);
+            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, r, v, sv, zs, sc);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
             prof_begin(c, s);
-            k_bicg_t<V><<<g, kBlock, 0, s>>>(op, sv, zs, tv, sc, part);
+            k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, sv, zs, tv, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + T * 12);
             prof_begin(c, s);
-            k_bicg_x<V, X><<<g, kBlock, 0, s>>>(c.P.Tp, c.P.L, x, zp, zs, sv, tv, r, rh, sc, part);
+            k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, x, zp, zs, sv, tv, r, rh, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
         }
         int rc = read_scalars(c, s, sc);
@@ -680,6 +644,21 @@ int configure_solver_kernels(Ctx& c) {
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    // one full wave of co-resident blocks per kernel (grid-stride loops do the rest)
+    int dev = 0, sms = 0;
+    PBSM_CUDA_TRY(cudaGetDevice(&dev));
+    PBSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    auto wave = [&](const void* f, int smem, int& out) -> int {
+        int per = 0;
+        PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kBlock, smem));
+        out = std::max(1, std::min(c.grid_faces, sms * std::max(per, 1)));
+        return 0;
+    };
+    int rc;
+    if ((rc = wave((const void*)k_bicg_p<double>, s64, c.grid_col[0]))) return rc;
+    if ((rc = wave((const void*)k_bicg_p<float>, s32, c.grid_col[1]))) return rc;
+    if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
+    if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
     return 0;
 }
 
@@ -803,47 +782,121 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
 }
 
 int configure_cg(Ctx& c) {
-    int per_sm = 0, dev = 0, sms = 0;
+    int dev = 0, sms = 0, coop = 0;
     PBSM_CUDA_TRY(cudaGetDevice(&dev));
     PBSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int coop = 0;
     PBSM_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-    PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent, kCgBlock, 0));
     const int64_t need = (c.P.Tp + kCgBlock - 1) / kCgBlock;
-    // one co-resident block per SM (at most the partials workspace's 8 x grid_faces / 7 blocks)
-    int64_t blocks = std::min<int64_t>(need, per_sm >= 1 ? (int64_t)sms : 0);
-    blocks = std::min<int64_t>(blocks, (int64_t)c.red.nblocks);
-    c.coop_blocks = coop ? (int)blocks : 0;
+    // one co-resident block per SM, within the partials workspace and the flag lines
+    auto blocks_for = [&](const void* f, int& out) -> int {
+        int per_sm = 0;
+        PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kCgBlock, 0));
+        int64_t b = std::min<int64_t>(need, per_sm >= 1 ? (int64_t)sms : 0);
+        b = std::min<int64_t>(b, (int64_t)c.red.nblocks);
+        b = std::min<int64_t>(b, (int64_t)kMaxCgBlocks);
+        out = coop ? (int)b : 0;
+        return 0;
+    };
+    int rc;
+    if ((rc = blocks_for((const void*)k_cg_persistent<double>, c.coop_blocks))) return rc;
+    if ((rc = blocks_for((const void*)k_cg_persistent<float>, c.coop_blocks32))) return rc;
+    return 0;
+}
+
+// One cooperative CG launch on system D; returns the status and iterations in sc.
+template <typename V>
+static int launch_cg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* sc, double tol, int maxit) {
+    if (blocks <= 0) {
+        c.err = "the device does not support cooperative launches";
+        return PBSM3D_ERR_CUDA;
+    }
+    PBSM_CUDA_TRY(cudaMemsetAsync(c.cg_flags, 0, sizeof(unsigned) * kFlagStride * (size_t)blocks, s));
+    PBSM_CUDA_TRY(cudaMemsetAsync(&c.gbar->err, 0, sizeof(int), s));
+    int64_t Tp = c.P.Tp;
+    double* part = c.red.partials;
+    int* err = &c.gbar->err;
+    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit};
+    PBSM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_persistent<V>, dim3(blocks), dim3(kCgBlock), args,
+                                              0, s));
+    int rc = read_scalars(c, s, sc);
+    if (rc) return rc;
+    int e = 0;
+    PBSM_CUDA_TRY(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        c.err = "deposition solve: grid all-reduce timed out";
+        return PBSM3D_ERR_CUDA;
+    }
+    return 0;
+}
+
+// MIXED: FP64 iterative refinement around FP32 CG solves of A d = r;
+// x, the residual b - A x and its norm stay FP64.
+static int solve_deposition_mixed(Ctx& c, cudaStream_t s, double tol) {
+    double* part = c.red.partials;
+    Scalars* sc = c.sc + 2;
+    const int64_t T = c.P.T, Tp = c.P.Tp;
+    float* f = c.dep32;
+    float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
+    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    prof_begin(c, s);
+    k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
+    PBSM_CUDA_TRY(cudaMemsetAsync(c.D.x, 0, Tp * sizeof(double), s));
+    k_dep_resid32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, r32, sc, part);
+    prof_end(c, s, PBSM3D_K_CG, T * (56 + 20 + 8 + 64));
+    c.launches += 1;
+    int rc = read_scalars(c, s, sc);
+    if (rc) return rc;
+    const double bb = c.sc_host->bnorm2;
+    double rr = c.sc_host->rnorm2;
+    c.dep_iters = 0;
+    c.dep_refinements = 0;
+    for (int pass = 0; pass < 8 && !(rr <= tol * tol * bb); ++pass) {
+        // inner target relative to ||r||: what the outer target still needs,
+        // no tighter than FP32 reliably reaches
+        const double itol = std::max(1e-5, 0.3 * tol * sqrt(bb / rr));
+        prof_begin(c, s);
+        if ((rc = launch_cg<float>(c, s, D32, c.coop_blocks32, sc, itol, std::min(c.cfg.dep_maxit, 500)))) return rc;
+        const int inner = c.sc_host->iter;
+        prof_end(c, s, PBSM3D_K_CG, T * 48 + (int64_t)inner * T * 74);
+        c.dep_iters += inner;
+        c.dep_refinements += 1;
+        prof_begin(c, s);
+        k_dep_add<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, D32.x);
+        k_dep_resid32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, r32, sc, part);
+        prof_end(c, s, PBSM3D_K_CG, T * (20 + 56 + 20 + 8));
+        c.launches += 1;
+        rc = read_scalars(c, s, sc);
+        if (rc) return rc;
+        rr = c.sc_host->rnorm2;
+        if (!isfinite(rr)) break;
+    }
+    c.dep_relres = bb > 0 ? sqrt(rr / bb) : 0.0;
+    if (!(rr <= tol * tol * bb)) {
+        c.err = "deposition solve failed to converge (relative residual " + std::to_string(c.dep_relres) + ")";
+        return PBSM3D_ERR_NOT_CONVERGED;
+    }
+    // the final residual vector in FP64 for the mass ledger
+    prof_begin(c, s);
+    k_cg_resid<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);
+    prof_end(c, s, PBSM3D_K_CG, T * 76);
     return 0;
 }
 
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     (void)st;
+    const double tol = c.cfg.dep_tol * sqrt(c.dep_target_scale2);  // ensembles: every member to dep_tol
+    if (c.P.mixed) return solve_deposition_mixed(c, s, tol);
+    c.dep_refinements = 1;
     double* part = c.red.partials;
     Scalars* sc = c.sc + 2;
     const int64_t T = c.P.T;
-    if (c.coop_blocks <= 0) {
-        c.err = "the device does not support cooperative launches";
-        return PBSM3D_ERR_CUDA;
-    }
-    PBSM_CUDA_TRY(cudaMemsetAsync(c.gbar, 0, sizeof(GridBar), s));
-    double tol = c.cfg.dep_tol * sqrt(c.dep_target_scale2);  // ensembles: every member to dep_tol
-    int maxit = c.cfg.dep_maxit;
-    void* args[] = {&c.P, &c.D, &c.F.nbr, &c.dr, &c.dz_, &c.dp, &c.dq, &part, &c.gbar, &sc, &tol, &maxit};
+    DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
     prof_begin(c, s);
-    PBSM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_persistent, dim3(c.coop_blocks), dim3(kCgBlock),
-                                              args, 0, s));
-    int rc = read_scalars(c, s, sc);
+    int rc = launch_cg<double>(c, s, D, c.coop_blocks, sc, tol, c.cfg.dep_maxit);
     if (rc) return rc;
     const int done = c.sc_host->done;
     c.dep_iters = c.sc_host->iter;
     prof_end(c, s, PBSM3D_K_CG, T * 96 + (int64_t)c.dep_iters * T * 148);
-    GridBar gb;
-    PBSM_CUDA_TRY(cudaMemcpy(&gb, c.gbar, sizeof(GridBar), cudaMemcpyDeviceToHost));
-    if (gb.err) {
-        c.err = "deposition solve: grid barrier timed out";
-        return PBSM3D_ERR_CUDA;
-    }
     const double bn2 = c.sc_host->bnorm2;
     prof_begin(c, s);
     k_cg_resid<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);

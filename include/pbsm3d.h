@@ -227,6 +227,8 @@ typedef struct pbsm3d_stats {
     double kern_ms[16];
     int64_t kern_bytes[16];
     int32_t kern_launches[16];
+    int32_t dep_refinements;     /* MIXED: FP64 refinement sweeps of the deposition solve (1 otherwise) */
+    int32_t n_slow_faces;        /* faces with a saltation layer (per-row particle terms) */
 } pbsm3d_stats;
 
 /* Kernel classes reported in pbsm3d_stats.kern_*. */
