@@ -88,6 +88,8 @@ void free_all(Ctx& c) {
     c.sc_host = nullptr;
     if (c.n_slow_host) cudaFreeHost(c.n_slow_host);
     c.n_slow_host = nullptr;
+    if (c.ms_host) cudaFreeHost(c.ms_host);
+    c.ms_host = nullptr;
     if (c.stream) cudaStreamDestroy(c.stream);
     c.stream = nullptr;
 }
@@ -283,7 +285,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     for (auto& e : c.ev) cudaEventCreate(&e);
     for (auto& e : c.user_ev) cudaEventCreate(&e);
     if (cudaMallocHost(&c.sc_host, sizeof(Scalars)) != cudaSuccess ||
-        cudaMallocHost(&c.n_slow_host, sizeof(int)) != cudaSuccess) {
+        cudaMallocHost(&c.n_slow_host, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&c.ms_host, sizeof(MScal) * members.size()) != cudaSuccess) {
         g_create_error = "cudaMallocHost failed";
         free_all(c);
         delete h;
@@ -340,6 +343,31 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     A.slow_rows = dalloc<double>(c, (size_t)8 * R, ok);
     MathTables* mt = dalloc<MathTables>(c, 1, ok);
     P.mt = mt;
+    // batched-Krylov tiles: runs of at most kBlock faces within one member
+    std::vector<int32_t> t_start, t_member, m_tile(nm + 1, 0);
+    for (int m = 0; m < nm; ++m) {
+        m_tile[m] = (int32_t)t_start.size();
+        for (int64_t f = offsets[m]; f < offsets[m + 1]; f += kBlock) {
+            t_start.push_back((int32_t)f);
+            t_member.push_back(m);
+        }
+    }
+    m_tile[nm] = (int32_t)t_start.size();
+    const int ntiles = (int)t_start.size();
+    t_start.push_back((int32_t)T);
+    int32_t* tile_buf = dalloc<int32_t>(c, (size_t)2 * ntiles + 1 + nm + 1, ok);
+    c.tiles.start = tile_buf;
+    c.tiles.member = tile_buf + ntiles + 1;
+    c.tiles.mtile = tile_buf + 2 * ntiles + 1;
+    c.tiles.ntiles = ntiles;
+    c.tiles.n = nm;
+    c.act_buf = dalloc<int32_t>(c, ntiles, ok);
+    c.tiles.act = c.act_buf;
+    c.tiles.nact = 0;
+    c.tile_part = dalloc<double>(c, (size_t)4 * ntiles, ok);
+    c.msR = dalloc<MScal>(c, nm, ok);
+    c.ms0 = dalloc<MScal>(c, nm, ok);
+    c.ms1 = dalloc<MScal>(c, nm, ok);
     int32_t* face_member = dalloc<int32_t>(c, Tp, ok);
     Member* prm = dalloc<Member>(c, nm, ok);
     c.Mb.n = nm;
@@ -461,6 +489,9 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         MathTables h;
         math_tables_fill(h);
         rc |= upload(c, mt, &h, sizeof(h));
+        rc |= upload(c, tile_buf, t_start.data(), (ntiles + 1) * 4);
+        rc |= upload(c, tile_buf + ntiles + 1, t_member.data(), ntiles * 4);
+        rc |= upload(c, tile_buf + 2 * ntiles + 1, m_tile.data(), (nm + 1) * 4);
     }
     rc |= upload(c, c.dr, cx.data(), Tp * 8);
     rc |= upload(c, c.dz_, cy.data(), Tp * 8);

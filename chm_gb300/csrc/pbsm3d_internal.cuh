@@ -152,6 +152,28 @@ struct Scalars {
     unsigned counter[8];
 };
 
+// Krylov state of one ensemble member in a batched solve: each member runs
+// its own BiCGStab recurrences (its own alpha, omega, beta, rho) inside the
+// shared kernels, and stops on its own residual.  One 128-byte line each.
+struct MScal {
+    double rho, alpha, omega, beta;
+    double rnorm2, bnorm2, target2, red0;  // red0 = (b, r) of the residual pass
+    double gamma, pad0;                    // warm-start scale (set by the host)
+    int iter, done, maxit;
+    unsigned counter;                      // tiles reported to the current reduction
+    int pad1[4];
+};
+
+// Work tiles of the batched Krylov kernels: runs of at most kBlock faces
+// that never span two members, so a tile's block sum belongs to one member.
+struct Tiles {
+    const int32_t* start;   // [ntiles + 1] first face of each tile
+    const int32_t* member;  // [ntiles]
+    const int32_t* mtile;   // [n + 1] first tile of each member
+    const int32_t* act;     // [nact] tiles of the members still iterating, ascending
+    int ntiles, n, nact;
+};
+
 // Grid-wide barrier state of a persistent (cooperative) kernel.
 struct GridBar {
     unsigned count, gen;
@@ -212,6 +234,15 @@ struct Ctx {
     int n_slow = 0;
     ReduceWs red;
     int grid_rows, grid_faces;
+    // batched Krylov: tiles, per-member states (residual sums, FP64 plain /
+    // outer, FP32 inner), their pinned host mirror and the tile partials
+    Tiles tiles;
+    int32_t* act_buf = nullptr;      // device [ntiles]: the active-tile list
+    std::vector<int32_t> act_host;
+    MScal *msR = nullptr, *ms0 = nullptr, *ms1 = nullptr;
+    MScal* ms_host = nullptr;
+    double* tile_part = nullptr;  // [4][ntiles]
+    std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
     int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
     // ledger partial sums

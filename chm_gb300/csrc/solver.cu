@@ -65,15 +65,101 @@ __device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V
     }
 }
 
+// ---------------------------------------------------------------- batched BiCGStab
+// Every kernel walks the work tiles (grid-stride over tiles, one tile per
+// block at a time); a tile belongs to one member, whose scalars it reads
+// once.  Tiles of members that are done are skipped.
+
+__device__ __forceinline__ float wsum(float v) { return warp_sum_f(v); }
+__device__ __forceinline__ double wsum(double v) { return warp_sum(v); }
+
+// Block b owns the contiguous run [a0, a1) of the active-tile list (whole
+// members, ascending tiles); within it each run of one member's tiles is a
+// segment, flushed to the member's reduction once.
+struct TileRange {
+    int a0, a1;
+};
+__device__ __forceinline__ TileRange block_tiles(const Tiles& tl) {
+    const int64_t n = tl.nact, g = gridDim.x, b = blockIdx.x;
+    return TileRange{(int)(b * n / g), (int)((b + 1) * n / g)};
+}
+// End (exclusive, in active-list positions) of the segment that starts at
+// position a with tile t of member m.
+__device__ __forceinline__ int segment_end(const Tiles& tl, const TileRange& br, int a, int t, int m) {
+    return min(br.a1, a + (tl.mtile[m + 1] - t));
+}
+
+// A segment [ts, te) of member m adds NT per-thread values: the block sum
+// (warp sums in the vector precision, FP64 across warps) becomes tile ts's
+// partial (the segment's other tiles get 0); the block that completes
+// member m's tile count sums the member's partials in tile order
+// (deterministic) and returns true, with the totals in tot[] of thread 0.
+template <int NT, typename V>
+__device__ bool member_totals(V (&v)[NT], double* part, const Tiles& tl, int ts, int te, int m, MScal* ms,
+                              double (&tot)[NT]) {
+    __shared__ double shp[NT][32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        const V w = wsum(v[k]);
+        if (lane == 0) shp[k][wid] = (double)w;
+    }
+    __syncthreads();
+    if (te - ts > 1) {
+        for (int q = ts + 1 + (int)threadIdx.x; q < te; q += blockDim.x)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) part[(int64_t)k * tl.ntiles + q] = 0.0;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = (int)(blockDim.x >> 5);
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            double s = 0;
+            for (int w = 0; w < nw; ++w) s += shp[k][w];
+            part[(int64_t)k * tl.ntiles + ts] = s;
+        }
+        __threadfence();
+        const unsigned nt = (unsigned)(tl.mtile[m + 1] - tl.mtile[m]), mine = (unsigned)(te - ts);
+        last = atomicAdd(&ms[m].counter, mine) + mine == nt;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        double s = 0;
+        for (int q = tl.mtile[m] + threadIdx.x; q < tl.mtile[m + 1]; q += blockDim.x)
+            s += __ldcg(&part[(int64_t)k * tl.ntiles + q]);
+        tot[k] = s;
+    }
+    block_sum<NT>(tot);
+    if (threadIdx.x == 0) ms[m].counter = 0u;
+    return true;
+}
+
+// Member m has stopped (status st); the last member to stop ends the solve.
+__device__ __forceinline__ void member_stop(MScal* ms, int m, int st, Scalars* sc, int n) {
+    ms[m].done = st;
+    if (atomicAdd(&sc->counter[2], 1u) + 1u == (unsigned)n) sc->done = DONE_CONVERGED;
+}
+
 // p = r + beta (p - omega v); zp = B^{-1} p
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_p(Op<V> op, const V* __restrict__ r, V* __restrict__ p,
-                                                   const V* __restrict__ v, V* __restrict__ zp, const Scalars* sc) {
-    if (sc->done) return;
+__global__ void __launch_bounds__(kBlock) k_bicg_p(Op<V> op, Tiles tl, const V* __restrict__ r, V* __restrict__ p,
+                                                   const V* __restrict__ v, V* __restrict__ zp,
+                                                   const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
-    const V beta = (V)sc->beta, omega = (V)sc->omega;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1; ++a) {
+        const int t = tl.act[a], m = tl.member[t];
+        if (ms[m].done) continue;
+        const int64_t i = tl.start[t] + threadIdx.x;
+        if (i >= tl.start[t + 1]) continue;
+        const V beta = (V)ms[m].beta, omega = (V)ms[m].omega;
         for (int z = 0; z < op.L; ++z) {
             const int64_t k = (int64_t)z * op.Tp + i;
             const V pk = r[k] + beta * (p[k] - omega * v[k]);
@@ -86,13 +172,18 @@ __global__ void __launch_bounds__(kBlock) k_bicg_p(Op<V> op, const V* __restrict
 
 // s = r - alpha v; zs = B^{-1} s
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, const V* __restrict__ r, const V* __restrict__ v,
-                                                   V* __restrict__ s, V* __restrict__ zs, const Scalars* sc) {
-    if (sc->done) return;
+__global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* __restrict__ r,
+                                                   const V* __restrict__ v, V* __restrict__ s, V* __restrict__ zs,
+                                                   const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
-    const V alpha = (V)sc->alpha;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1; ++a) {
+        const int t = tl.act[a], m = tl.member[t];
+        if (ms[m].done) continue;
+        const int64_t i = tl.start[t] + threadIdx.x;
+        if (i >= tl.start[t + 1]) continue;
+        const V alpha = (V)ms[m].alpha;
         for (int z = 0; z < op.L; ++z) {
             const int64_t k = (int64_t)z * op.Tp + i;
             const V sk = r[k] - alpha * v[k];
@@ -103,173 +194,222 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, const V* __restrict
     }
 }
 
-// y = u + N z, with dot products (a, y) [and (y, y)]
+// y = u + N z for the column of face i, with (a, y) [and (y, y)]
 template <typename V, int NT>
-__device__ __forceinline__ void lateral_apply(const Op<V>& op, const V* __restrict__ u, const V* __restrict__ zz,
-                                              V* __restrict__ y, const V* __restrict__ a, V (&acc)[2]) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < op.Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
-        for (int z = 0; z < op.L; ++z) {
-            const int64_t base = (int64_t)z * op.Tp;
-            const int64_t k = base + i;
-            V yk = u[k];
-            if (n0 >= 0) yk += op.lat[k] * zz[base + n0];
-            if (n1 >= 0) yk += op.lat[op.R + k] * zz[base + n1];
-            if (n2 >= 0) yk += op.lat[2 * op.R + k] * zz[base + n2];
-            y[k] = yk;
-            acc[0] += a[k] * yk;
-            if (NT > 1) acc[1] += yk * yk;
-        }
+__device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const V* __restrict__ u,
+                                              const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
+                                              V (&acc)[2]) {
+    const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+    for (int z = 0; z < op.L; ++z) {
+        const int64_t base = (int64_t)z * op.Tp;
+        const int64_t k = base + i;
+        V yk = u[k];
+        if (n0 >= 0) yk += op.lat[k] * zz[base + n0];
+        if (n1 >= 0) yk += op.lat[op.R + k] * zz[base + n1];
+        if (n2 >= 0) yk += op.lat[2 * op.R + k] * zz[base + n2];
+        y[k] = yk;
+        acc[0] += a[k] * yk;
+        if (NT > 1) acc[1] += yk * yk;
     }
 }
 
 // v = p + N zp; rv = (rhat, v); alpha = rho / rv
 template <typename V>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, const V* __restrict__ p, const V* __restrict__ zp,
-                                                   V* __restrict__ v, const V* __restrict__ rh, Scalars* sc,
-                                                   double* partials) {
-    if (sc->done) return;
-    V acc[2] = {0, 0};
-    lateral_apply<V, 1>(op, p, zp, v, rh, acc);
-    V d[1] = {acc[0]};
-    double tot[1];
-    if (block_partials_last<1>(d, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        const double rv = tot[0];
-        sc->rv = rv;
-        if (rv == 0.0 || !isfinite(rv)) {
-            sc->done = DONE_BREAKDOWN;
-        } else {
-            sc->alpha = sc->rho / rv;
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
+                                                      const V* __restrict__ zp, V* __restrict__ v,
+                                                      const V* __restrict__ rh, MScal* ms, Scalars* sc,
+                                                      double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
         }
+        V acc[2] = {0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i < tl.start[t + 1]) lateral_apply<V, 1>(op, i, p, zp, v, rh, acc);
+        }
+        V a1[1] = {acc[0]};
+        double tot[1];
+        if (member_totals<1>(a1, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            const double rv = tot[0];
+            if (rv == 0.0 || !isfinite(rv))
+                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            else
+                ms[m].alpha = ms[m].rho / rv;
+        }
+        a = ae;
     }
 }
 
 // t = s + N zs; ts = (t, s), tt = (t, t); omega = ts / tt
 template <typename V>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_t(Op<V> op, const V* __restrict__ s, const V* __restrict__ zs,
-                                                   V* __restrict__ t, Scalars* sc, double* partials) {
-    if (sc->done) return;
-    V acc[2] = {0, 0};
-    lateral_apply<V, 2>(op, s, zs, t, s, acc);
-    double tot[2];
-    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        sc->ts = tot[0];
-        sc->tt = tot[1];
-        sc->omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_t(Op<V> op, Tiles tl, const V* __restrict__ s,
+                                                      const V* __restrict__ zs, V* __restrict__ tv, MScal* ms,
+                                                      double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        V acc[2] = {0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i < tl.start[t + 1]) lateral_apply<V, 2>(op, i, s, zs, tv, s, acc);
+        }
+        double tot[2];
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
+            ms[m].omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
+        a = ae;
     }
 }
 
 // x += alpha zp + omega zs; r = s - omega t; rho' = (rhat, r), (r, r)
 template <typename V, typename X>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, X* __restrict__ x, const V* __restrict__ zp,
-                                                   const V* __restrict__ zs, const V* __restrict__ s,
-                                                   const V* __restrict__ t, V* __restrict__ r,
-                                                   const V* __restrict__ rh, Scalars* sc, double* partials) {
-    if (sc->done) return;
-    const X alpha = (X)sc->alpha, omega = (X)sc->omega;
-    const V om = (V)sc->omega;
-    V acc[2] = {0, 0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        for (int z = 0; z < L; ++z) {
-            const int64_t k = (int64_t)z * Tp + i;
-            x[k] = x[k] + alpha * (X)zp[k] + omega * (X)zs[k];
-            const V rk = s[k] - om * t[k];
-            r[k] = rk;
-            acc[0] += rh[k] * rk;
-            acc[1] += rk * rk;
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, Tiles tl, X* __restrict__ x,
+                                                      const V* __restrict__ zp, const V* __restrict__ zs,
+                                                      const V* __restrict__ s, const V* __restrict__ tv,
+                                                      V* __restrict__ r, const V* __restrict__ rh, MScal* ms,
+                                                      Scalars* sc, double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
         }
-    }
-    double tot[2];
-    if (block_partials_last<2>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        const double rho_new = tot[0];
-        sc->rnorm2 = tot[1];
-        sc->iter += 1;
-        if (tot[1] <= sc->target2) {
-            sc->done = DONE_CONVERGED;
-        } else if (sc->omega == 0.0 || rho_new == 0.0 || !isfinite(rho_new) || !isfinite(tot[1])) {
-            sc->done = DONE_BREAKDOWN;
-        } else if (sc->iter >= sc->maxit) {
-            sc->done = DONE_MAXIT;
-        } else {
-            sc->beta = (rho_new / sc->rho) * (sc->alpha / sc->omega);
+        V acc[2] = {0, 0};
+        const X alpha = (X)ms[m].alpha, omega = (X)ms[m].omega;
+        const V om = (V)ms[m].omega;
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            for (int z = 0; z < L; ++z) {
+                const int64_t k = (int64_t)z * Tp + i;
+                x[k] = x[k] + alpha * (X)zp[k] + omega * (X)zs[k];
+                const V rk = s[k] - om * tv[k];
+                r[k] = rk;
+                acc[0] += rh[k] * rk;
+                acc[1] += rk * rk;
+            }
         }
-        sc->rho = rho_new;
+        double tot[2];
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            MScal& q = ms[m];
+            const double rho_new = tot[0];
+            q.rnorm2 = tot[1];
+            q.iter += 1;
+            atomicMax(&sc->iter, q.iter);
+            if (tot[1] <= q.target2)
+                member_stop(ms, m, DONE_CONVERGED, sc, tl.n);
+            else if (q.omega == 0.0 || rho_new == 0.0 || !isfinite(rho_new) || !isfinite(tot[1]))
+                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            else if (q.iter >= q.maxit)
+                member_stop(ms, m, DONE_MAXIT, sc, tl.n);
+            else
+                q.beta = (rho_new / q.rho) * (q.alpha / q.omega);
+            q.rho = rho_new;
+        }
+        a = ae;
     }
 }
 
-// r = b - A x with all six FP64 bands; optionally r32 = (float) r.
-// Also (r, r) and (b, b).  Resets the BiCGStab state: rhat = r, p = v = 0.
+// r = b - A x with all six FP64 bands; optionally r32 = (float) r.  Per
+// member (r, r), (b, b), (b, r) into ms[m].  Resets the Krylov vectors:
+// rhat = r, p = v = 0.  Members marked done in ms are skipped (their x is
+// final).
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_residual(Params P, const double* __restrict__ band,
+__global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const double* __restrict__ band,
                                                      const int32_t* __restrict__ nbr, const double* __restrict__ x,
                                                      const double* __restrict__ b, double* __restrict__ r,
                                                      V* __restrict__ rv, V* __restrict__ rhv, V* __restrict__ pv,
-                                                     V* __restrict__ vv, Scalars* sc, double* partials, double tol,
-                                                     int maxit) {
+                                                     V* __restrict__ vv, MScal* ms, double* part) {
     const int64_t Tp = P.Tp, R = P.R;
-    double acc[3] = {0, 0, 0};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
-        for (int z = 0; z < P.L; ++z) {
-            const int64_t base = (int64_t)z * Tp;
-            const int64_t k = base + i;
-            double ax = band[k] * x[k];
-#pragma unroll
-            for (int j = 0; j < 3; ++j)
-                if (nb[j] >= 0) ax += band[(j + 1) * R + k] * x[base + nb[j]];
-            if (z > 0) ax += band[4 * R + k] * x[k - Tp];
-            if (z < P.L - 1) ax += band[5 * R + k] * x[k + Tp];
-            const double rk = b[k] - ax;
-            r[k] = rk;
-            if (rv) {
-                rv[k] = (V)rk;
-                rhv[k] = (V)rk;
-                pv[k] = 0;
-                vv[k] = 0;
-            }
-            acc[0] += rk * rk;
-            acc[1] += b[k] * b[k];
-            acc[2] += b[k] * rk;
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
         }
-    }
-    double tot[3];
-    if (block_partials_last<3>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        sc->rnorm2 = tot[0];
-        sc->bnorm2 = tot[1];
-        sc->red0 = tot[2];  // (b, r): lets the host scale a warm start
-        sc->rho = tot[0];
-        sc->alpha = 1.0;
-        sc->omega = 1.0;
-        sc->beta = 0.0;
-        sc->target2 = tol * tol * tot[0];
-        sc->iter = 0;
-        sc->maxit = maxit;
-        sc->done = tot[0] == 0.0 ? DONE_CONVERGED : DONE_NO;
+        double acc[3] = {0, 0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
+            for (int z = 0; z < P.L; ++z) {
+                const int64_t base = (int64_t)z * Tp;
+                const int64_t k = base + i;
+                double ax = band[k] * x[k];
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    if (nb[j] >= 0) ax += band[(j + 1) * R + k] * x[base + nb[j]];
+                if (z > 0) ax += band[4 * R + k] * x[k - Tp];
+                if (z < P.L - 1) ax += band[5 * R + k] * x[k + Tp];
+                const double rk = b[k] - ax;
+                r[k] = rk;
+                if (rv) {
+                    rv[k] = (V)rk;
+                    rhv[k] = (V)rk;
+                    pv[k] = 0;
+                    vv[k] = 0;
+                }
+                acc[0] += rk * rk;
+                acc[1] += b[k] * b[k];
+                acc[2] += b[k] * rk;
+            }
+        }
+        double tot[3];
+        if (member_totals<3>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            ms[m].rnorm2 = tot[0];
+            ms[m].bnorm2 = tot[1];
+            ms[m].red0 = tot[2];
+        }
+        a = ae;
     }
 }
 
-// Warm start x0 -> gamma x0 (gamma = 0 drops it): r = (1-gamma) b + gamma r0,
-// and the Krylov state restarts from the new residual.
+// Warm start x0 -> gamma_m x0 per member (gamma = 0 drops it):
+// r = (1-gamma) b + gamma r0, rhat = r, and (r, r) per member.
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_warm_scale(int64_t n, double gamma, double* __restrict__ x,
+__global__ void __launch_bounds__(kBlock) k_warm_scale(Params P, Tiles tl, double* __restrict__ x,
                                                        double* __restrict__ r, const double* __restrict__ b,
-                                                       V* __restrict__ rv, V* __restrict__ rhv, Scalars* sc,
-                                                       double* partials) {
-    double acc[1] = {0};
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        x[k] *= gamma;
-        const double rk = (1.0 - gamma) * b[k] + gamma * r[k];
-        r[k] = rk;
-        rv[k] = (V)rk;
-        rhv[k] = (V)rk;
-        acc[0] += rk * rk;
-    }
-    double tot[1];
-    if (block_partials_last<1>(acc, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
-        sc->rnorm2 = tot[0];
-        sc->rho = tot[0];
-        sc->target2 = 0.0;  // set by the host
-        sc->done = tot[0] == 0.0 ? DONE_CONVERGED : DONE_NO;
+                                                       V* __restrict__ rv, V* __restrict__ rhv, MScal* ms,
+                                                       double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        double acc[1] = {0};
+        const double gamma = ms[m].gamma;
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            for (int z = 0; z < P.L; ++z) {
+                const int64_t k = (int64_t)z * P.Tp + i;
+                x[k] *= gamma;
+                const double rk = (1.0 - gamma) * b[k] + gamma * r[k];
+                r[k] = rk;
+                rv[k] = (V)rk;
+                rhv[k] = (V)rk;
+                acc[0] += rk * rk;
+            }
+        }
+        double tot[1];
+        if (member_totals<1>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) ms[m].rnorm2 = tot[0];
+        a = ae;
     }
 }
 
@@ -580,15 +720,68 @@ int read_scalars(Ctx& c, cudaStream_t s, Scalars* dev) {
 }
 
 // Run BiCGStab iterations on the state set up by k_residual until done.
+// Copy the n per-member states to the pinned host mirror.
+int read_members(Ctx& c, cudaStream_t s, const MScal* dev) {
+    PBSM_CUDA_TRY(
+        cudaMemcpyAsync(c.ms_host, dev, sizeof(MScal) * (size_t)c.tiles.n, cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    return 0;
+}
+
+// Faces of the members whose state is not done (host mirror).
+int64_t active_faces(const Ctx& c) {
+    int64_t f = 0;
+    for (int m = 0; m < c.tiles.n; ++m)
+        if (!c.ms_host[m].done) f += c.member_offsets[m + 1] - c.member_offsets[m];
+    return f;
+}
+
+// Active-tile list: every tile of the members with active[m] != 0.
+int set_active(Ctx& c, cudaStream_t s, const std::vector<char>& active) {
+    c.act_host.clear();
+    // the member tile ranges are regular: kBlock faces per tile within a member
+    int t = 0;
+    for (int m = 0; m < c.tiles.n; ++m) {
+        const int64_t f = c.member_offsets[m + 1] - c.member_offsets[m];
+        const int nt = (int)((f + kBlock - 1) / kBlock);
+        if (active[m])
+            for (int k = 0; k < nt; ++k) c.act_host.push_back(t + k);
+        t += nt;
+    }
+    c.tiles.nact = (int)c.act_host.size();
+    if (c.tiles.nact)
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.act_buf, c.act_host.data(), sizeof(int32_t) * c.act_host.size(),
+                                      cudaMemcpyHostToDevice, s));
+    return 0;
+}
+
+// Faces of the members not yet converged (conv[m] == 0).
+int64_t active_faces_of(const Ctx& c, const std::vector<char>& conv) {
+    int64_t f = 0;
+    for (int m = 0; m < c.tiles.n; ++m)
+        if (!conv[m]) f += c.member_offsets[m + 1] - c.member_offsets[m];
+    return f;
+}
+
+// Run BiCGStab iterations on the per-member states in ms (set up by the
+// host) until every member is done.  sc holds the batch totals: done, the
+// largest member iteration count and the count of stopped members.
 template <typename V, typename X>
-int bicgstab_iterations(Ctx& c, cudaStream_t s, Scalars* sc, X* x, V* r, V* rh, V* p, V* v, V* sv, V* tv, V* zp,
-                        V* zs, int& iters) {
+int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V* r, V* rh, V* p, V* v, V* sv,
+                        V* tv, V* zp, V* zs, int& iters) {
     Op<V> op = make_op<V>(c);
     const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
-    const int g = c.grid_faces;
-    double* part = c.red.partials;
-    const int64_t T = c.P.T, rows = T * c.P.L;
+    double* part = c.tile_part;
     const int64_t sv_ = sizeof(V), sx = sizeof(X);
+    std::vector<char> active(c.tiles.n);
+    for (int m = 0; m < c.tiles.n; ++m) active[m] = c.ms_host[m].done ? 0 : 1;
+    {
+        int rc = set_active(c, s, active);
+        if (rc) return rc;
+    }
+    Tiles tl = c.tiles;
+    int gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
+    int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
     int chunk = 4;
     int before = 0;
     {
@@ -600,33 +793,51 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, Scalars* sc, X* x, V* r, V* rh, 
             return 0;
         }
     }
+    int64_t act = active_faces(c);
     while (true) {
-        const int gc = c.grid_col[sizeof(V) == 4], gr = c.grid_red[sizeof(V) == 4];
+        const int64_t rows = act * c.P.L;
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
-            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, r, p, v, zp, sc);
+            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, zp, ms);
             prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
             prof_begin(c, s);
-            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, p, zp, v, rh, sc, part);
-            prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + T * 12);
+            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, p, zp, v, rh, ms, sc, part);
+            prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + act * 12);
             prof_begin(c, s);
-            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, r, v, sv, zs, sc);
+            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, zs, ms);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
             prof_begin(c, s);
-            k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, sv, zs, tv, sc, part);
-            prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + T * 12);
+            k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, tl, sv, zs, tv, ms, part);
+            prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + act * 12);
             prof_begin(c, s);
-            k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, x, zp, zs, sv, tv, r, rh, sc, part);
+            k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
         }
         int rc = read_scalars(c, s, sc);
         if (rc) return rc;
         const int ran = c.sc_host->iter - before;
         before = c.sc_host->iter;
-        // launches after the converging iteration returned at once: not counted
-        const int idle = chunk - ran - (c.sc_host->done == DONE_BREAKDOWN ? 1 : 0);
+        // launches after the last member stopped returned at once: not counted
+        const int idle = chunk - ran - (c.sc_host->done && ran < chunk ? 1 : 0);
         if (idle > 0) prof_drop(c, 5 * idle);
         if (c.sc_host->done) break;
+        if (tl.n > 1) {
+            // members that stopped leave the active-tile list
+            if ((rc = read_members(c, s, ms))) return rc;
+            bool changed = false;
+            for (int m = 0; m < tl.n; ++m)
+                if (active[m] && c.ms_host[m].done) {
+                    active[m] = 0;
+                    changed = true;
+                }
+            if (changed) {
+                if ((rc = set_active(c, s, active))) return rc;
+                tl = c.tiles;
+                gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
+                gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+            }
+            act = active_faces(c);
+        }
         chunk = std::min(16, chunk * 2);
     }
     iters = c.sc_host->iter;
@@ -673,101 +884,158 @@ int jacobi_sweep(Ctx& c, cudaStream_t s, const double* xi, double* xo) {
 }
 
 // Suspension solve: x0 = current contents of A.x.  Fills iteration stats.
+// Every ensemble member is its own BiCGStab (its own scalars and stopping
+// test on ||b_m - A_m x_m|| <= tol ||b_m||) inside the shared kernels; a
+// single mesh is the one-member case.
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     (void)st;
-    const int g = c.grid_faces;
-    double* part = c.red.partials;
-    Scalars* sc0 = c.sc;      // FP64 outer / plain
-    Scalars* sc1 = c.sc + 1;  // FP32 inner
+    const int n = c.tiles.n;
+    double* part = c.tile_part;
+    Scalars* sc0 = c.sc;      // FP64 plain: batch totals
+    Scalars* sc1 = c.sc + 1;  // FP32 inner: batch totals
     const double tol = c.cfg.susp_tol;
     int total_iters = 0, sweeps = 0;
-    double bnorm2 = 0;
     const int maxit = c.cfg.susp_maxit;
     c.susp_relres = 0;
+    c.member_bb.assign(n, 0.0);
+    std::vector<char> conv(n, 0);
+    std::vector<MScal> init(n);
+    double gamma_sum = 0;
+    // residual states: every member active at the first sweep
+    for (int m = 0; m < n; ++m) init[m] = MScal{};
+    PBSM_CUDA_TRY(cudaMemcpyAsync(c.msR, init.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
     while (true) {
-        // r = b - A x, in FP64; reset the Krylov state
-        if (c.P.mixed) {
-            prof_begin(c, s);
-            k_residual<float><<<g, kBlock, 0, s>>>(c.P, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
-                                                   c.p32, c.v32, sc0, part, tol, maxit);
-            prof_end(c, s, PBSM3D_K_RESIDUAL, c.P.T * c.P.L * 88 + c.P.T * 12);
-        } else {
-            prof_begin(c, s);
-            k_residual<double><<<g, kBlock, 0, s>>>(c.P, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
-                                                    c.v, sc0, part, tol, maxit);
-            prof_end(c, s, PBSM3D_K_RESIDUAL, c.P.T * c.P.L * 96 + c.P.T * 12);
+        // r = b - A x in FP64 per member (converged members are skipped); reset the Krylov vectors
+        const int64_t act = active_faces_of(c, conv);
+        {
+            std::vector<char> a(n);
+            for (int m = 0; m < n; ++m) a[m] = conv[m] ? 0 : 1;
+            int rc0 = set_active(c, s, a);
+            if (rc0) return rc0;
         }
-        int rc = read_scalars(c, s, sc0);
+        const Tiles tl = c.tiles;
+        const int gr = std::max(1, std::min(c.grid_red[0], tl.nact));
+        prof_begin(c, s);
+        if (c.P.mixed)
+            k_residual<float><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
+                                                    c.p32, c.v32, c.msR, part);
+        else
+            k_residual<double><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh,
+                                                     c.p, c.v, c.msR, part);
+        prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 88 : 96) + act * 12);
+        int rc = read_members(c, s, c.msR);
         if (rc) return rc;
-        if (sweeps == 0) bnorm2 = c.sc_host->bnorm2;
-        if (sweeps == 0 && c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1)) {
-            // Scale the warm start by the gamma that minimises ||b - gamma A x0||
-            // and drop it when that residual is not below ||b||: the zero
-            // guess stays the fallback.  (b, A x0) = |b|^2 - (b, r0),
-            // |A x0|^2 = |b|^2 - 2 (b, r0) + |r0|^2.
-            const double bb = bnorm2, br = c.sc_host->red0, rr = c.sc_host->rnorm2;
-            const double bax = bb - br, axax = bb - 2.0 * br + rr;
-            double gamma = (axax > 0 && bax > 0) ? bax / axax : 0.0;
-            const double rmin2 = axax > 0 ? bb - bax * bax / axax : bb;
-            if (!(rmin2 < 0.99 * bb)) gamma = 0.0;
-            c.warm_gamma = gamma;
-            prof_begin(c, s);
-            if (c.P.mixed)
-                k_warm_scale<float><<<g, kBlock, 0, s>>>(c.P.R, gamma, c.A.x, c.r, c.A.rhs, c.r32, c.rh32, sc0, part);
-            else
-                k_warm_scale<double><<<g, kBlock, 0, s>>>(c.P.R, gamma, c.A.x, c.r, c.A.rhs, c.r, c.rh, sc0, part);
-            prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 40);
-            rc = read_scalars(c, s, sc0);
-            if (rc) return rc;
+        if (sweeps == 0) {
+            for (int m = 0; m < n; ++m) c.member_bb[m] = c.ms_host[m].bnorm2;
+            if (c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1)) {
+                // Scale each member's warm start by the gamma that minimises
+                // ||b - gamma A x0|| and drop it when that residual is not
+                // below ||b||: the zero guess stays the fallback.
+                // (b, A x0) = |b|^2 - (b, r0), |A x0|^2 = |b|^2 - 2 (b, r0) + |r0|^2.
+                for (int m = 0; m < n; ++m) {
+                    const double bb = c.ms_host[m].bnorm2, br = c.ms_host[m].red0, rr = c.ms_host[m].rnorm2;
+                    const double bax = bb - br, axax = bb - 2.0 * br + rr;
+                    double gamma = (axax > 0 && bax > 0) ? bax / axax : 0.0;
+                    const double rmin2 = axax > 0 ? bb - bax * bax / axax : bb;
+                    if (!(rmin2 < 0.99 * bb)) gamma = 0.0;
+                    init[m] = MScal{};
+                    init[m].gamma = gamma;
+                    gamma_sum += gamma;
+                }
+                c.warm_gamma = gamma_sum / n;
+                PBSM_CUDA_TRY(cudaMemcpyAsync(c.msR, init.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
+                prof_begin(c, s);
+                if (c.P.mixed)
+                    k_warm_scale<float><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.x, c.r, c.A.rhs, c.r32, c.rh32, c.msR,
+                                                              part);
+                else
+                    k_warm_scale<double><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.x, c.r, c.A.rhs, c.r, c.rh, c.msR,
+                                                               part);
+                prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 40);
+                if ((rc = read_members(c, s, c.msR))) return rc;
+                for (int m = 0; m < n; ++m) c.ms_host[m].bnorm2 = c.member_bb[m];
+            }
         }
-        const double rn2 = c.sc_host->rnorm2;
-        c.susp_relres = bnorm2 > 0 ? sqrt(rn2 / bnorm2) : 0.0;
-        // ensembles: tol * min_m ||b_m|| bounds every member's residual (target_scale2 = 1 otherwise)
-        const double goal2 = tol * tol * bnorm2 * c.target_scale2;
-        if (rn2 <= goal2) break;
+        // per-member convergence on the true FP64 residual (members skipped
+        // by the residual pass keep the value they converged with)
+        bool all = true, finite = true;
+        double worst = 0;
+        for (int m = 0; m < n; ++m) {
+            const double rr = c.ms_host[m].rnorm2, bb = c.member_bb[m];
+            if (!isfinite(rr)) finite = false;
+            if (bb > 0) worst = std::max(worst, rr / bb);
+            if (conv[m]) continue;
+            if (rr <= tol * tol * bb)
+                conv[m] = 1;
+            else
+                all = false;
+        }
+        c.susp_relres = sqrt(worst);
+        if (!finite) {
+            c.err = "suspension solve produced a non-finite residual";
+            return PBSM3D_ERR_NOT_CONVERGED;
+        }
+        if (all) break;
         if (total_iters >= maxit) {
             c.susp_iters = total_iters;
             c.err = "suspension solve failed to converge (relative residual " + std::to_string(c.susp_relres) + ")";
             return PBSM3D_ERR_NOT_CONVERGED;
         }
-        if (!isfinite(rn2)) {
-            c.err = "suspension solve produced a non-finite residual";
-            return PBSM3D_ERR_NOT_CONVERGED;
+        // Krylov states: converged members are done from the start
+        int ndone = 0;
+        for (int m = 0; m < n; ++m) {
+            const double rr = c.ms_host[m].rnorm2, bb = c.member_bb[m];
+            MScal q{};
+            q.rho = rr;
+            q.alpha = q.omega = 1.0;
+            q.beta = 0.0;
+            q.maxit = std::max(1, maxit - total_iters);
+            if (c.P.mixed) {
+                // inner: A32 d = r32, d0 = 0, to inner_tol relative -- or less when
+                // the FP64 target is closer than that (no over-solving in the last sweep)
+                const double goal2 = tol * tol * bb;
+                const double need = rr > 0 ? 0.5 * sqrt(goal2 / rr) : 1.0;
+                const double itol = std::min(0.5, std::max(c.cfg.inner_tol, need));
+                q.target2 = itol * itol * rr;
+            } else {
+                q.target2 = tol * tol * bb;  // relative to ||b_m||
+            }
+            q.done = conv[m] || rr == 0.0 ? DONE_CONVERGED : DONE_NO;
+            ndone += q.done ? 1 : 0;
+            init[m] = q;
         }
+        // members whose x is final skip later residual passes
+        std::vector<MScal> rs(n);
+        for (int m = 0; m < n; ++m) {
+            rs[m] = MScal{};
+            rs[m].done = conv[m] ? 1 : 0;
+            rs[m].rnorm2 = c.ms_host[m].rnorm2;
+        }
+        MScal* ms = c.P.mixed ? c.ms1 : c.ms0;
+        Scalars* sc = c.P.mixed ? sc1 : sc0;
+        Scalars tot{};
+        tot.done = ndone == n ? DONE_CONVERGED : DONE_NO;
+        tot.counter[2] = (unsigned)ndone;
+        PBSM_CUDA_TRY(cudaMemcpyAsync(ms, init.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
+        PBSM_CUDA_TRY(cudaMemcpyAsync(sc, &tot, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+        for (int m = 0; m < n; ++m) c.ms_host[m] = init[m];
         int it = 0;
         if (c.P.mixed) {
-            // inner: A32 d = r32, d0 = 0, to inner_tol relative -- or less when
-            // the FP64 target is closer than that (no over-solving in the last sweep)
-            const double need = 0.5 * sqrt(goal2 / rn2);
-            const double itol = std::min(0.5, std::max(c.cfg.inner_tol, need));
-            Scalars init{};
-            init.rho = rn2;
-            init.alpha = init.omega = 1.0;
-            init.beta = 0.0;
-            init.bnorm2 = rn2;
-            init.target2 = itol * itol * rn2;
-            init.maxit = std::max(1, maxit - total_iters);
-            PBSM_CUDA_TRY(cudaMemcpyAsync(sc1, &init, sizeof(Scalars), cudaMemcpyHostToDevice, s));
             prof_begin(c, s);
-            k_zero<float><<<g, kBlock, 0, s>>>(c.P.R, c.x32);
+            k_zero<float><<<c.grid_faces, kBlock, 0, s>>>(c.P.R, c.x32);
             prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 4);
-            rc = bicgstab_iterations<float, float>(c, s, sc1, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32, c.t32,
+            rc = bicgstab_iterations<float, float>(c, s, ms, sc, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32, c.t32,
                                                    c.zp32, c.zs32, it);
             if (rc) return rc;
             prof_begin(c, s);
-            k_add_correction<<<g, kBlock, 0, s>>>(c.P.R, c.A.x, c.x32);
+            k_add_correction<<<c.grid_faces, kBlock, 0, s>>>(c.P.R, c.A.x, c.x32);
             prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 20);
         } else {
-            // target relative to ||b|| (the state's target2 is relative to ||r||)
-            Scalars* h = c.sc_host;
-            h->target2 = goal2;
-            h->maxit = maxit - total_iters;
-            PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->target2, &h->target2, sizeof(double), cudaMemcpyHostToDevice, s));
-            PBSM_CUDA_TRY(cudaMemcpyAsync(&sc0->maxit, &h->maxit, sizeof(int), cudaMemcpyHostToDevice, s));
-            rc = bicgstab_iterations<double, double>(c, s, sc0, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv, c.zp, c.zs,
-                                                     it);
+            rc = bicgstab_iterations<double, double>(c, s, ms, sc, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv, c.zp,
+                                                     c.zs, it);
             if (rc) return rc;
         }
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.msR, rs.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
         total_iters += it;
         sweeps++;
         if (sweeps > 64) {
