@@ -106,7 +106,10 @@ __device__ bool member_totals(V (&v)[NT], double* part, const Tiles& tl, int ts,
         if (lane == 0) shp[k][wid] = (double)w;
     }
     __syncthreads();
-    if (te - ts > 1) {
+    // one member: the finaliser reads only the segment heads (block starts),
+    // so the other tiles' partials need no zeros
+    const bool one = tl.n == 1;
+    if (!one && te - ts > 1) {
         for (int q = ts + 1 + (int)threadIdx.x; q < te; q += blockDim.x)
 #pragma unroll
             for (int k = 0; k < NT; ++k) part[(int64_t)k * tl.ntiles + q] = 0.0;
@@ -131,8 +134,17 @@ __device__ bool member_totals(V (&v)[NT], double* part, const Tiles& tl, int ts,
 #pragma unroll
     for (int k = 0; k < NT; ++k) {
         double s = 0;
-        for (int q = tl.mtile[m] + threadIdx.x; q < tl.mtile[m + 1]; q += blockDim.x)
-            s += __ldcg(&part[(int64_t)k * tl.ntiles + q]);
+        if (one) {
+            // the active list is every tile; block b's segment starts at b * nact / G
+            const int64_t na = tl.nact, g = gridDim.x;
+            for (int64_t b = threadIdx.x; b < g; b += blockDim.x) {
+                const int64_t a0 = b * na / g;
+                if (a0 < (b + 1) * na / g) s += __ldcg(&part[(int64_t)k * tl.ntiles + tl.act[a0]]);
+            }
+        } else {
+            for (int q = tl.mtile[m] + threadIdx.x; q < tl.mtile[m + 1]; q += blockDim.x)
+                s += __ldcg(&part[(int64_t)k * tl.ntiles + q]);
+        }
         tot[k] = s;
     }
     block_sum<NT>(tot);
@@ -661,6 +673,174 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V
     }
 }
 
+// ---------------------------------------------------------------- batched deposition CG (ensembles)
+// Jacobi-preconditioned CG per member inside shared tile kernels, like the
+// batched BiCGStab: each member its own alpha, beta, rho and stopping test
+// ||b_m - A_m x_m|| <= tol ||b_m||.  Two kernels per iteration.
+
+// r = b, z = D^-1 b, p = z, x = 0; (r, z) -> rho, (b, b) -> bnorm2
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_scg_start(Tiles tl, DepSys<V> D, MScal* ms, Scalars* sc,
+                                                      double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        V acc[2] = {0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            const V bi = D.b[i];
+            const V zi = D.dinv[i] * bi;
+            D.r[i] = bi;
+            D.zz[i] = zi;
+            D.p[i] = zi;
+            D.x[i] = 0;
+            acc[0] += bi * zi;
+            acc[1] += bi * bi;
+        }
+        double tot[2];
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            MScal& q = ms[m];
+            q.rho = tot[0];
+            q.bnorm2 = tot[1];
+            q.rnorm2 = tot[1];
+            q.beta = 0.0;
+            q.target2 *= tot[1];  // the host set tol^2: the target is relative to ||b_m||
+            if (tot[1] == 0.0) member_stop(ms, m, DONE_CONVERGED, sc, tl.n);
+            else if (!(tot[0] > 0.0) || !isfinite(tot[0])) member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+        }
+        a = ae;
+    }
+}
+
+// q = A z + beta q, p = z + beta p; alpha = rho / (p, q)
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_scg_q(Tiles tl, int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
+                                                  MScal* ms, Scalars* sc, double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        const V be = (V)ms[m].beta;
+        V acc[1] = {0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            V az = D.diag[i] * D.zz[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) az += D.off[j * Tp + i] * D.zz[nb];
+            }
+            const V pi = D.zz[i] + be * D.p[i];
+            const V qi = az + be * D.q[i];
+            D.p[i] = pi;
+            D.q[i] = qi;
+            acc[0] += pi * qi;
+        }
+        double tot[1];
+        if (member_totals<1>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            if (!(tot[0] > 0.0) || !isfinite(tot[0]))
+                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            else
+                ms[m].alpha = ms[m].rho / tot[0];
+        }
+        a = ae;
+    }
+}
+
+// x += alpha p, r -= alpha q, z = D^-1 r; (r, z), (r, r); beta, stopping test
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_scg_x(Tiles tl, DepSys<V> D, MScal* ms, Scalars* sc, double* part) {
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        const V al = (V)ms[m].alpha;
+        V acc[2] = {0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            D.x[i] += al * D.p[i];
+            const V ri = D.r[i] - al * D.q[i];
+            D.r[i] = ri;
+            const V zi = D.dinv[i] * ri;
+            D.zz[i] = zi;
+            acc[0] += ri * zi;
+            acc[1] += ri * ri;
+        }
+        double tot[2];
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            MScal& q = ms[m];
+            q.rnorm2 = tot[1];
+            q.iter += 1;
+            atomicMax(&sc->iter, q.iter);
+            if (tot[1] <= q.target2)
+                member_stop(ms, m, DONE_CONVERGED, sc, tl.n);
+            else if (!isfinite(tot[1]))
+                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            else if (q.iter >= q.maxit)
+                member_stop(ms, m, DONE_MAXIT, sc, tl.n);
+            else
+                q.beta = tot[0] / q.rho;
+            q.rho = tot[0];
+        }
+        a = ae;
+    }
+}
+
+// r = b - A x (FP64) per member: (r, r), (b, b) into ms; r32 = (float) r
+__global__ void __launch_bounds__(kBlock) k_sdep_resid(Tiles tl, Params P, Dep D, const int32_t* __restrict__ nbr,
+                                                       float* __restrict__ r32, double* __restrict__ r64, MScal* ms,
+                                                       double* part) {
+    const int64_t Tp = P.Tp;
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1;) {
+        const int ts = tl.act[a], m = tl.member[ts];
+        const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
+        if (ms[m].done) {
+            a = ae;
+            continue;
+        }
+        double acc[2] = {0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x;
+            if (i >= tl.start[t + 1]) continue;
+            double ax = D.diag[i] * D.x[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) ax += D.off[j * Tp + i] * D.x[nb];
+            }
+            const double bi = D.rhs[i];
+            const double ri = bi - ax;
+            if (r32) r32[i] = (float)ri;
+            if (r64) r64[i] = ri;
+            acc[0] += ri * ri;
+            acc[1] += bi * bi;
+        }
+        double tot[2];
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
+            ms[m].rnorm2 = tot[0];
+            ms[m].bnorm2 = tot[1];
+        }
+        a = ae;
+    }
+}
+
 // FP32 copies of the deposition matrix for the inner solves (MIXED).
 __global__ void __launch_bounds__(kBlock) k_dep_to_f32(Params P, Dep D, float* diag, float* off, float* dinv) {
     const int64_t Tp = P.Tp;
@@ -1150,9 +1330,175 @@ static int solve_deposition_mixed(Ctx& c, cudaStream_t s, double tol) {
     return 0;
 }
 
+// Per-member CG iterations on states set up by the host (target2 = tol^2
+// relative to ||b_m||, maxit, done for members not solved); returns the
+// largest member iteration count.
+template <typename V>
+static int scg_iterations(Ctx& c, cudaStream_t s, DepSys<V> D, MScal* ms, Scalars* sc, int& iters) {
+    double* part = c.tile_part;
+    const int n = c.tiles.n;
+    const int64_t sv_ = sizeof(V);
+    std::vector<char> active(n);
+    int ndone = 0;
+    for (int m = 0; m < n; ++m) {
+        active[m] = c.ms_host[m].done ? 0 : 1;
+        ndone += c.ms_host[m].done ? 1 : 0;
+    }
+    Scalars tot{};
+    tot.done = ndone == n ? DONE_CONVERGED : DONE_NO;
+    tot.counter[2] = (unsigned)ndone;
+    PBSM_CUDA_TRY(cudaMemcpyAsync(sc, &tot, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+    PBSM_CUDA_TRY(cudaMemcpyAsync(ms, c.ms_host, sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
+    int rc = set_active(c, s, active);
+    if (rc) return rc;
+    Tiles tl = c.tiles;
+    int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+    int64_t act = active_faces(c);
+    prof_begin(c, s);
+    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+    k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+    prof_end(c, s, PBSM3D_K_CG, act * sv_ * 17 + act * 12);
+    c.launches += 1;
+    int chunk = 8, before = 0;
+    while (true) {
+        for (int k = 0; k < chunk; ++k) {
+            prof_begin(c, s);
+            k_scg_x<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+            k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+            prof_end(c, s, PBSM3D_K_CG, act * sv_ * 18 + act * 12);
+            c.launches += 1;
+        }
+        if ((rc = read_scalars(c, s, sc))) return rc;
+        const int ran = c.sc_host->iter - before;
+        before = c.sc_host->iter;
+        const int idle = chunk - ran;
+        if (idle > 0) prof_drop(c, idle);
+        if (c.sc_host->done) break;
+        if ((rc = read_members(c, s, ms))) return rc;
+        bool changed = false;
+        for (int m = 0; m < n; ++m)
+            if (active[m] && c.ms_host[m].done) {
+                active[m] = 0;
+                changed = true;
+            }
+        if (changed) {
+            if ((rc = set_active(c, s, active))) return rc;
+            tl = c.tiles;
+            g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+            act = active_faces(c);
+        }
+        chunk = std::min(32, chunk * 2);
+    }
+    iters = c.sc_host->iter;
+    return 0;
+}
+
+// Ensembles: every member its own CG (FP64; MIXED: FP32 inner solves in
+// per-member FP64 refinement), each to ||b_m - A_m x_m|| <= tol ||b_m||.
+static int solve_deposition_members(Ctx& c, cudaStream_t s, double tol) {
+    const int n = c.tiles.n;
+    const int64_t Tp = c.P.Tp, T = c.P.T;
+    double* part = c.tile_part;
+    Scalars* sc = c.sc + 2;
+    std::vector<char> conv(n, 0), all_on(n, 1);
+    std::vector<double> bb(n, 0.0), rr(n, 0.0);
+    c.dep_iters = 0;
+    c.dep_refinements = 0;
+    auto residual = [&](float* r32) -> int {
+        std::vector<char> a(n);
+        for (int m = 0; m < n; ++m) a[m] = conv[m] ? 0 : 1;
+        int rc = set_active(c, s, a);
+        if (rc) return rc;
+        const Tiles tl = c.tiles;
+        std::vector<MScal> z(n);
+        for (int m = 0; m < n; ++m) z[m].done = conv[m] ? 1 : 0;
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.msR, z.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
+        const int g = std::max(1, std::min(c.grid_red[0], tl.nact));
+        prof_begin(c, s);
+        k_sdep_resid<<<g, kBlock, 0, s>>>(tl, c.P, c.D, c.F.nbr, r32, c.dr, c.msR, part);
+        prof_end(c, s, PBSM3D_K_CG, active_faces_of(c, conv) * (76 + (r32 ? 4 : 0)));
+        if ((rc = read_members(c, s, c.msR))) return rc;
+        for (int m = 0; m < n; ++m)
+            if (!conv[m]) {
+                rr[m] = c.ms_host[m].rnorm2;
+                bb[m] = c.ms_host[m].bnorm2;
+            }
+        return 0;
+    };
+    auto finish = [&]() -> int {
+        double worst = 0;
+        bool ok = true;
+        for (int m = 0; m < n; ++m) {
+            if (bb[m] > 0) worst = std::max(worst, rr[m] / bb[m]);
+            if (!(rr[m] <= tol * tol * bb[m])) ok = false;
+        }
+        c.dep_relres = sqrt(worst);
+        if (!ok) {
+            c.err = "deposition solve failed to converge (relative residual " + std::to_string(c.dep_relres) + ")";
+            return PBSM3D_ERR_NOT_CONVERGED;
+        }
+        return 0;
+    };
+    int rc;
+    if (!c.P.mixed) {
+        DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
+        for (int m = 0; m < n; ++m) {
+            c.ms_host[m] = MScal{};
+            c.ms_host[m].target2 = tol * tol;
+            c.ms_host[m].maxit = c.cfg.dep_maxit;
+        }
+        int it = 0;
+        if ((rc = scg_iterations<double>(c, s, D, c.ms0, sc, it))) return rc;
+        c.dep_iters = it;
+        c.dep_refinements = 1;
+        // the true residual (also the mass ledger's residual vector)
+        if ((rc = residual(nullptr))) return rc;
+        return finish();
+    }
+    float* f = c.dep32;
+    float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
+    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    prof_begin(c, s);
+    k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
+    prof_end(c, s, PBSM3D_K_CG, T * (56 + 20));
+    PBSM_CUDA_TRY(cudaMemsetAsync(c.D.x, 0, Tp * sizeof(double), s));
+    for (int pass = 0;; ++pass) {
+        if ((rc = residual(r32))) return rc;
+        bool all = true;
+        for (int m = 0; m < n; ++m) {
+            if (!conv[m] && rr[m] <= tol * tol * bb[m]) conv[m] = 1;
+            if (!conv[m]) all = false;
+        }
+        if (all || pass == 8) break;
+        for (int m = 0; m < n; ++m) {
+            c.ms_host[m] = MScal{};
+            if (conv[m]) {
+                c.ms_host[m].done = DONE_CONVERGED;
+                continue;
+            }
+            // inner target relative to ||r_m||: what the outer target still
+            // needs, no tighter than FP32 reliably reaches
+            const double itol = std::max(1e-5, 0.3 * tol * sqrt(bb[m] / rr[m]));
+            c.ms_host[m].target2 = itol * itol;
+            c.ms_host[m].maxit = std::min(c.cfg.dep_maxit, 500);
+        }
+        PBSM_CUDA_TRY(cudaMemsetAsync(D32.x, 0, Tp * sizeof(float), s));
+        int it = 0;
+        if ((rc = scg_iterations<float>(c, s, D32, c.ms1, sc, it))) return rc;
+        c.dep_iters += it;
+        c.dep_refinements += 1;
+        prof_begin(c, s);
+        k_dep_add<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, D32.x);
+        prof_end(c, s, PBSM3D_K_CG, T * 20);
+    }
+    // converged members kept the residual vector of their last pass
+    return finish();
+}
+
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     (void)st;
-    const double tol = c.cfg.dep_tol * sqrt(c.dep_target_scale2);  // ensembles: every member to dep_tol
+    if (c.tiles.n > 1) return solve_deposition_members(c, s, c.cfg.dep_tol);
+    const double tol = c.cfg.dep_tol;
     if (c.P.mixed) return solve_deposition_mixed(c, s, tol);
     c.dep_refinements = 1;
     double* part = c.red.partials;
