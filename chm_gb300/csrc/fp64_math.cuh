@@ -116,6 +116,21 @@ __device__ __forceinline__ double div_t(double a, double b) {
     return fma(fma(-b, q, a), y, q);
 }
 
+// (float) x, round to nearest even, on the integer pipe (an FP64->FP32
+// conversion instruction issues on the FP64 pipe).  Normal results only;
+// zero, subnormal, overflow, Inf and NaN take the conversion instruction.
+__device__ __forceinline__ float f32_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ff) - 1023 + 127;
+    if (e <= 0 || e >= 254) return (float)x;
+    const unsigned long long m = b & 0x000fffffffffffffull;
+    unsigned r = ((unsigned)e << 23) | (unsigned)(m >> 29);
+    const unsigned long long rem = m & 0x1fffffffull;  // the 29 dropped bits
+    r += (rem > 0x10000000ull || (rem == 0x10000000ull && (r & 1u))) ? 1u : 0u;
+    return __uint_as_float(r | (hi & 0x80000000u));
+}
+
 // x^y = exp(y log x) for x > 0
 __device__ __forceinline__ double pow_t(double x, double y, const MathTables& t) {
     return exp_t(y * log_t(x, t), t);

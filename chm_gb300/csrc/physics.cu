@@ -390,6 +390,23 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             out_f[f] = gt0(kf);
             al[f] = P.do_lateral_diff ? Af * 0.00001 : 0.0;
         }
+        // Lateral faces, PBSM3D.cpp:1248-1284: with the face's out/in and
+        // neighbour flags fixed, each face adds to the row
+        //   dg  += V5cs + ca_f alpha_f + cA_f (u_z A_f k_f)
+        //   lat_f = L0_f + u_z L1_f
+        // (out+nbr: ca -1, cA -1, lat alpha; out, no nbr: ca -0.01, cA -1;
+        //  in+nbr: ca -1, cA 0, lat alpha - Au; in, no nbr: ca -0.01, cA -0.99),
+        // so the three faces fold into per-face constants and a row costs
+        // four FMAs instead of lane-divergent branches.
+        double dg_a = 0.0, dg_u = 0.0, L0[3], L1[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const bool has = nb[f] >= 0;
+            dg_a += (has ? -1.0 : -0.01) * al[f];
+            dg_u += (out_f[f] ? -1.0 : (has ? 0.0 : -0.99)) * Ak[f];
+            L0[f] = has ? al[f] : 0.0;
+            L1[f] = (has && !out_f[f]) ? -Ak[f] : 0.0;
+        }
         const double ust_dc = P.snow_diffusion_const * ustar;
         // Per-face versions of the per-row branch tests (no FP64 compare per
         // row): the canopy test cz < height_diff can only hold when
@@ -409,7 +426,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             const int64_t ls = fast ? 1 : R;
             const double inv_mm = lp[0], omega = lp[ls], Qr = lp[2 * ls], lmix = lp[3 * ls];
             const double rz2nu = lp[4 * ls], rsig = lp[5 * ls], lwarg = lp[6 * ls], llw = lp[7 * ls];
-            const double cz = z * P.dz + hs + P.dz / 2.;
+            // the layer centre is only needed by the canopy and 50 m tests,
+            // which the per-face flags usually settle
+            const bool need_cz = in_canopy_possible || !all_below_zur;
+            const double cz = need_cz ? z * P.dz + hs + P.dz / 2. : 0.0;
             double u_z, xrz;
             if (in_canopy_possible && saltation && cz < height_diff) {
                 u_z = 2.8 * uth;
@@ -438,79 +458,33 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
                 K34 = (1.0 / (1.0 + (1.0 * w * w) / (1.56 * ustar * ustar))) * ustar * lmix;
             else
                 K34 = ust_dc * lmix;
-            double alpha[5] = {al[0], al[1], al[2], areaK * K34, 0.0};
-            alpha[4] = alpha[3];
-            double udm[5];
-            udm[3] = -w;  // uvw . (0,0,1)
-            udm[4] = w;   // uvw . (0,0,-1)
             if (!P.do_sublimation) csubl = 0.0;
             A.u_z[r] = u_z;
             A.csubl[r] = csubl;
             const double V5cs = V5 * csubl;
-            double dg = 0.0, lat[3] = {0, 0, 0}, lo = 0.0, up = 0.0, b = 0.0;
+            // Vertical faces (PBSM3D.cpp:1286-1404): udotm = -w on the top
+            // face, +w on the bottom one; alpha = area K / dz on both, except
+            // the bottom of layer 0, which couples to the saltation layer.
+            const double aw = area * w;    // area * |udotm| of a vertical face
+            const double aK = areaK * K34;  // alpha[3] = alpha[4]
+            const bool top_out = gt0(-w), bot_out = gt0(w);
+            double lat[3], lo = 0.0, up = 0.0, b = 0.0;
 #pragma unroll
-            for (int f = 0; f < 3; ++f) {
-                const bool has = nb[f] >= 0;
-                const double Au = u_z * Ak[f];  // A_f * udotm_f
-                if (out_f[f]) {
-                    if (has) {
-                        dg += (V5cs - Au - alpha[f]);
-                        lat[f] += alpha[f];
-                    } else {
-                        dg += (-0.1e-1 * alpha[f] - 1. * Au + V5cs);
-                    }
-                } else {
-                    if (has) {
-                        dg += V5cs - alpha[f];
-                        lat[f] += -Au + alpha[f];
-                    } else {
-                        dg += -0.1e-1 * alpha[f] - .99 * Au + V5cs;
-                    }
-                }
-            }
-            const bool top_out = gt0(udm[3]), bot_out = gt0(udm[4]);
+            for (int f = 0; f < 3; ++f) lat[f] = fma(u_z, L1[f], L0[f]);
+            // lateral faces plus the top face (every layer has one)
+            double dg = fma(u_z, dg_u, fma(4.0, V5cs, dg_a)) - aK;
+            if (top_out) dg += aw;
             if (z == 0) {
                 const double alpha4 = area * K34 / (hs / 2.0 + P.dz / 2.0);  // once per face
-                dg += V5cs - area * udm[4] - alpha4;
-                b += -alpha4 * c_salt;
-                if (top_out) {
-                    dg += V5cs - area * udm[3] - alpha[3];
-                    if (P.L > 1) up += alpha[3];
-                } else {
-                    dg += V5cs - alpha[3];
-                    if (P.L > 1) up += -area * udm[3] + alpha[3];
-                }
-            } else if (z == P.L - 1) {
-                const double cprecip = 0;
-                if (top_out) {
-                    dg += V5cs - area * udm[3] - alpha[3];
-                    b += -alpha[3] * cprecip;
-                } else {
-                    dg += V5cs - alpha[3];
-                    b += area * cprecip * udm[3] - alpha[3] * cprecip;
-                }
-                if (bot_out) {
-                    dg += V5cs - area * udm[4] - alpha[4];
-                    lo += alpha[4];
-                } else {
-                    dg += V5cs - alpha[4];
-                    lo += -area * udm[4] + alpha[4];
-                }
+                dg += V5cs - aw - alpha4;
+                b = -alpha4 * c_salt;
+                if (P.L > 1) up = top_out ? aK : aw + aK;
             } else {
-                if (top_out) {
-                    dg += V5cs - area * udm[3] - alpha[3];
-                    up += alpha[3];
-                } else {
-                    dg += V5cs - alpha[3];
-                    up += -area * udm[3] + alpha[3];
-                }
-                if (bot_out) {
-                    dg += V5cs - area * udm[4] - alpha[4];
-                    lo += alpha[4];
-                } else {
-                    dg += V5cs - alpha[4];
-                    lo += -area * udm[4] + alpha[4];
-                }
+                // bottom face; the top boundary of the last layer has no coupling
+                dg += V5cs - aK;
+                if (bot_out) dg -= aw;
+                lo = bot_out ? aK : aK - aw;
+                if (z < P.L - 1) up = top_out ? aK : aw + aK;
             }
             A.band[r] = dg;
             A.band[1 * R + r] = lat[0];
@@ -527,12 +501,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             A.fac_l[r] = lz;
             A.fac_ib[r] = ib;
             if (P.mixed) {
-                A.lat32[r] = (float)lat[0];
-                A.lat32[R + r] = (float)lat[1];
-                A.lat32[2 * R + r] = (float)lat[2];
-                A.l32[r] = (float)lz;
-                A.ib32[r] = (float)ib;
-                A.up32[r] = (float)up;
+                A.lat32[r] = f32_rn(lat[0]);
+                A.lat32[R + r] = f32_rn(lat[1]);
+                A.lat32[2 * R + r] = f32_rn(lat[2]);
+                A.l32[r] = f32_rn(lz);
+                A.ib32[r] = f32_rn(ib);
+                A.up32[r] = f32_rn(up);
             }
             prev_up = up;
             prev_ib = ib;
