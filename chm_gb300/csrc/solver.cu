@@ -212,6 +212,8 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const 
                                               const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
                                               V (&acc)[2]) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+    // layers are independent here: unrolled so their loads overlap
+#pragma unroll 4
     for (int z = 0; z < op.L; ++z) {
         const int64_t base = (int64_t)z * op.Tp;
         const int64_t k = base + i;
@@ -303,6 +305,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, Tiles t
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x;
             if (i >= tl.start[t + 1]) continue;
+#pragma unroll 4
             for (int z = 0; z < L; ++z) {
                 const int64_t k = (int64_t)z * Tp + i;
                 x[k] = x[k] + alpha * (X)zp[k] + omega * (X)zs[k];
