@@ -101,6 +101,7 @@ EXPORTS = [
     "pbsm3d_deposition_solve_noalloc", "pbsm3d_mlp_num_params", "pbsm3d_mlp_features", "pbsm3d_mlp_trainer_create",
     "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
+    "pbsm3d_set_snow", "pbsm3d_get_snow",
 ]
 
 _lib = None
@@ -125,6 +126,11 @@ def load(path: Path | None = None):
     lib.pbsm3d_ensemble_create.restype = C.c_int
     lib.pbsm3d_member_offsets.argtypes = [vp, C.POINTER(C.c_int64)]
     lib.pbsm3d_member_offsets.restype = C.c_int
+    dp = C.POINTER(C.c_double)
+    lib.pbsm3d_set_snow.argtypes = [vp, dp, dp, C.c_double, C.c_int]
+    lib.pbsm3d_set_snow.restype = C.c_int
+    lib.pbsm3d_get_snow.argtypes = [vp, dp, dp, C.c_int]
+    lib.pbsm3d_get_snow.restype = C.c_int
     lib.pbsm3d_step.argtypes = [vp, C.POINTER(ForcingDesc), C.c_double, C.POINTER(Outputs), C.POINTER(Stats)]
     lib.pbsm3d_step.restype = C.c_int
     lib.pbsm3d_get_state.argtypes = [vp, _dp, _dp, _dp, _dp]

@@ -766,8 +766,8 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     if (!h) return PBSM3D_ERR_INVALID_ARG;
     Ctx& c = h->c;
     c.err.clear();
-    if (!f || !f->U_R || !f->U_2m_above_srf || !f->vw_dir || !f->swe || !f->t || !f->rh || !f->snowdepthavg) {
-        c.err = "missing forcing array";
+    if (!f) {
+        c.err = "missing forcing";
         return PBSM3D_ERR_INVALID_ARG;
     }
     if ((c.cfg.use_exp_fetch || c.cfg.use_tanh_fetch) && !f->fetch) {
@@ -792,14 +792,29 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     int rc;
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[0], s));
     const int dev = f->on_device;
+    // swe and snow depth come from the context's snow state when the caller
+    // set one and leaves them NULL
+    const bool own_snow = c.snow_state && !f->swe && !f->snowdepthavg;
+    if (!own_snow && (!f->swe || !f->snowdepthavg)) {
+        c.err = "forcing swe and snowdepthavg are required (or pbsm3d_set_snow)";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (!f->U_R || !f->U_2m_above_srf || !f->vw_dir || !f->t || !f->rh) {
+        c.err = "forcing U_R, U_2m_above_srf, vw_dir, t and rh are required";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
     if ((rc = copy_in(c, c.Fo.UR, f->U_R, dev)) || (rc = copy_in(c, c.Fo.U2, f->U_2m_above_srf, dev)) ||
-        (rc = copy_in(c, c.Fo.dir, f->vw_dir, dev)) || (rc = copy_in(c, c.Fo.swe, f->swe, dev)) ||
-        (rc = copy_in(c, c.Fo.t, f->t, dev)) || (rc = copy_in(c, c.Fo.rh, f->rh, dev)) ||
-        (rc = copy_in(c, c.Fo.sd, f->snowdepthavg, dev)))
+        (rc = copy_in(c, c.Fo.dir, f->vw_dir, dev)) || (rc = copy_in(c, c.Fo.t, f->t, dev)) ||
+        (rc = copy_in(c, c.Fo.rh, f->rh, dev)))
         return rc;
+    if (!own_snow) {
+        if ((rc = copy_in(c, c.Fo.swe, f->swe, dev)) || (rc = copy_in(c, c.Fo.sd, f->snowdepthavg, dev))) return rc;
+        // a caller that passes its own snow state takes over from the context's
+        c.snow_state = false;
+    }
     if (f->fetch && (rc = copy_in(c, c.Fo.fetch, f->fetch, dev))) return rc;
     if (f->p_snow_hours && (rc = copy_in(c, c.Fo.psh, f->p_snow_hours, dev))) return rc;
-    const int64_t h2d = dev ? 0 : c.P.T * 8 * (7 + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
+    const int64_t h2d = dev ? 0 : c.P.T * 8 * ((own_snow ? 5 : 7) + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
 
     // the previous step's solution (the assembly zeroes x, as the reference's
     // zeroSystem does): kept for the warm starts and the MLP features
@@ -865,6 +880,7 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     }
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[5], s));
     launch_update(c, s);
+    if (own_snow) launch_consume_drift(c, s);
     PBSM_CUDA_TRY(cudaGetLastError());
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[6], s));
     int64_t d2h = 0;
@@ -953,6 +969,26 @@ int pbsm3d_set_state(pbsm3d_ctx* h, const double* sum_drift, const double* sum_s
         (drift_mass && (rc = copy_in(c, c.S.drift_mass, drift_mass, 0))) ||
         (more && (rc = copy_in(c, c.S.more, more, 0))))
         return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int pbsm3d_set_snow(pbsm3d_ctx* h, const double* swe, const double* depth, double drift_density, int on_device) {
+    if (!h || !swe || !depth || !(drift_density > 0) || !std::isfinite(drift_density)) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    int rc;
+    if ((rc = copy_in(c, c.Fo.swe, swe, on_device)) || (rc = copy_in(c, c.Fo.sd, depth, on_device))) return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    c.snow_state = true;
+    c.drift_density = drift_density;
+    return 0;
+}
+
+int pbsm3d_get_snow(pbsm3d_ctx* h, double* swe, double* depth, int on_device) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    int rc;
+    if ((rc = copy_out(c, swe, c.Fo.swe, on_device)) || (rc = copy_out(c, depth, c.Fo.sd, on_device))) return rc;
     PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return 0;
 }

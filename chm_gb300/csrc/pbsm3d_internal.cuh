@@ -195,6 +195,7 @@ void launch_update(Ctx& c, cudaStream_t s);
 void launch_init_static(Ctx& c, cudaStream_t s);
 void launch_member_mask_norm(Ctx& c, cudaStream_t s, int which);
 void launch_member_zero(Ctx& c, cudaStream_t s, double* x);
+void launch_consume_drift(Ctx& c, cudaStream_t s);
 
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
@@ -232,6 +233,9 @@ struct Ctx {
     Scalars* sc_host;  // pinned mirror
     int* n_slow_host = nullptr;  // pinned: faces with a saltation layer in the last assembly
     int n_slow = 0;
+    // device-resident snow state (pbsm3d_set_snow): swe and depth live in Fo.swe / Fo.sd
+    bool snow_state = false;
+    double drift_density = 300.0;
     ReduceWs red;
     int grid_rows, grid_faces;
     // batched Krylov: tiles, per-member states (residual sums, FP64 plain /

@@ -737,6 +737,29 @@ __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F,
     }
 }
 
+// The drift consumer of CHM's snow models on the device (snobal.cpp:363-387
+// and its _adj_snow): erosion removes depth at the pack's bulk density,
+// deposition adds it at drift_density; a pack whose depth or mass reaches 0
+// is removed.
+__global__ void __launch_bounds__(kBlock) k_consume_drift(Params P, FaceState S, Forcing F, double drift_density) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
+        double mass = S.drift_mass[i];
+        mass = is_nan_chm(mass) ? 0.0 : mass;
+        double swe = F.swe[i], depth = F.sd[i];
+        swe = is_nan_chm(swe) ? 0.0 : swe;
+        depth = is_nan_chm(depth) ? 0.0 : depth;
+        const double rho = (mass < 0.0 && depth > 0.0) ? swe / depth : drift_density;
+        depth += mass / rho;
+        swe += mass;
+        if (depth <= 0.0 || swe <= 0.0) {
+            depth = 0.0;
+            swe = 0.0;
+        }
+        F.swe[i] = swe;
+        F.sd[i] = depth;
+    }
+}
+
 // Ensembles: zero the right-hand sides of members without suspension (or
 // deposition) so their solution is exactly 0, as the reference's skipped
 // solve leaves it; and ||rhs_m||^2 per member.
@@ -825,6 +848,12 @@ void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {
     prof_begin(c, s);
     k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.Mb, c.red.partials, c.sc);
     prof_end(c, s, PBSM3D_K_DEP_ASSEMBLE, T * 196);
+}
+
+void launch_consume_drift(Ctx& c, cudaStream_t s) {
+    prof_begin(c, s);
+    k_consume_drift<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.S, c.Fo, c.drift_density);
+    prof_end(c, s, PBSM3D_K_UPDATE, c.P.T * 40);
 }
 
 void launch_update(Ctx& c, cudaStream_t s) {

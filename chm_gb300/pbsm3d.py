@@ -197,6 +197,26 @@ class PBSM3D:
         self.last_stats = st.as_dict()
         return out
 
+    def set_snow(self, swe, depth, drift_density: float = 300.0):
+        """Keep swe and snow depth on the device: later run() calls without
+        swe/snowdepthavg read them from the context, and each step applies
+        its drift_mass to them (include/pbsm3d.h, pbsm3d_set_snow)."""
+        swe = np.ascontiguousarray(swe, dtype=np.float64)
+        depth = np.ascontiguousarray(depth, dtype=np.float64)
+        if swe.shape != (self.n_faces,) or depth.shape != (self.n_faces,):
+            raise ModuleError("set_snow: swe and depth need one value per face")
+        rc = self._lib.pbsm3d_set_snow(self._ctx, capi.ptr(swe), capi.ptr(depth), float(drift_density), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_set_snow")
+
+    def get_snow(self):
+        swe = np.empty(self.n_faces)
+        depth = np.empty(self.n_faces)
+        rc = self._lib.pbsm3d_get_snow(self._ctx, capi.ptr(swe), capi.ptr(depth), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_get_snow")
+        return swe, depth
+
     def export_system(self, which: str):
         n, L = self.n_faces, self.nLayer
         rows = n * L if which == "suspension" else n

@@ -246,11 +246,25 @@ class Workload:
                        vw_dir=np.ascontiguousarray(vw_dir), swe=self.swe.copy(), t=t, rh=rh,
                        snowdepthavg=self.depth.copy(), fetch=np.full(nt, 1000.0))
 
-    def apply_drift(self, drift_mass: np.ndarray):
-        m = np.where(np.abs(drift_mass + 9999.0) < 1e-5, 0.0, drift_mass)
-        rho = np.where(m < 0, 250.0, 300.0)
-        self.swe = np.maximum(self.swe + m, 0.0)
-        self.depth = np.maximum(self.depth + m / rho, 0.0)
+    def apply_drift(self, drift_mass: np.ndarray, drift_density: float = 300.0):
+        self.swe, self.depth = consume_drift(self.swe, self.depth, drift_mass, drift_density)
+
+
+def consume_drift(swe, depth, drift_mass, drift_density: float = 300.0):
+    """How CHM's snobal consumes PBSM3D's drift_mass (snobal.cpp:363-387 and
+    its _adj_snow): mass 0 when NaN/-9999; the depth change is mass / rho,
+    rho the pack's bulk density swe/depth for erosion and drift_density for
+    deposition; a pack whose depth or mass reaches 0 is removed."""
+    m = np.asarray(drift_mass, dtype=np.float64)
+    m = np.where(np.isnan(m) | (np.abs(m + 9999.0) < 1e-5), 0.0, m)
+    swe = np.asarray(swe, dtype=np.float64)
+    depth = np.asarray(depth, dtype=np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rho = np.where((m < 0) & (depth > 0), swe / np.where(depth > 0, depth, 1.0), drift_density)
+    new_depth = depth + m / rho
+    new_swe = swe + m
+    gone = (new_depth <= 0) | (new_swe <= 0)
+    return np.where(gone, 0.0, new_swe), np.where(gone, 0.0, new_depth)
 
 
 # Named configurations of the measurement plan.

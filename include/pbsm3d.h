@@ -292,6 +292,23 @@ int pbsm3d_get_state(pbsm3d_ctx* ctx, double* sum_drift, double* sum_subl,
 int pbsm3d_set_state(pbsm3d_ctx* ctx, const double* sum_drift, const double* sum_subl,
                      const double* drift_mass, const double* pbsm_more_than_avail);
 
+/* Device-resident snow state: the drift consumer of CHM's snow models on the
+ * GPU, so multi-step runs keep swe and snow depth in HBM.  After
+ * pbsm3d_set_snow, a step whose forcing leaves swe and snowdepthavg NULL
+ * reads them from the context, and every step ends by applying its
+ * drift_mass to them as snobal does (snobal.cpp:363-387, _adj_snow):
+ *   mass = drift_mass (0 when NaN or -9999);
+ *   depth change = mass / rho, rho = the snowpack's bulk density swe/depth
+ *   for erosion (mass < 0), drift_density for deposition;
+ *   swe += mass, depth += depth change; the pack is removed (both 0) when
+ *   either reaches 0.
+ * swe (kg m^-2) and depth (m) are n_faces doubles (device pointers when
+ * on_device); drift_density > 0 (CHM default 300 kg m^-3).
+ * pbsm3d_get_snow copies the current state out.  No counterpart in the
+ * reference module itself: this is the caller side of its drift_mass output. */
+int pbsm3d_set_snow(pbsm3d_ctx* ctx, const double* swe, const double* depth, double drift_density, int on_device);
+int pbsm3d_get_snow(pbsm3d_ctx* ctx, double* swe, double* depth, int on_device);
+
 /* Sliced-ELL export of the last assembled systems in the reference row order
  * (row = z*n_faces + face) and the reference graph's slot order: self, lateral
  * neighbours in face order 0..2 (present ones only), below, above

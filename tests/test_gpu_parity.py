@@ -282,3 +282,36 @@ def test_full_size_properties(cuda_lib):
     assert abs(st["ledger_deposited"] - st["ledger_divergence"]) <= 1e-10 * st["ledger_snow_mass"]
     assert (out["Qsusp"] >= 0).all()
     m.close()
+
+
+def test_device_snow_state(cuda_lib, oracle_lib):
+    """The drift consumer on the device: swe and depth stay in the context
+    between steps and take each step's drift_mass exactly as the host rule
+    (chm_gb300.synth.consume_drift) does; the physics matches the oracle fed
+    the same snow state."""
+    L = 5
+    w = synth.Workload(1536, 3000.0, seed=5)
+    m = gpu_module(w.mesh, L)
+    o = oracle(w.mesh, L)
+    swe, depth = w.swe.copy(), w.depth.copy()
+    m.set_snow(swe, depth)
+    moved = 0.0
+    for s in range(3):
+        fa = w.forcing(s).arrays()
+        own = {k: v for k, v in fa.items() if k not in ("swe", "snowdepthavg")}
+        out = m.run(own, 3600.0, want_c=True)
+        ref, _ = o.step_exact({**fa, "swe": swe, "snowdepthavg": depth}, 3600.0)
+        for k in FIELDS:
+            assert relerr(out[k], ref[k]) < FIELD_TOL, (s, k, relerr(out[k], ref[k]))
+        swe, depth = synth.consume_drift(swe, depth, out["drift_mass"])
+        gswe, gdepth = m.get_snow()
+        np.testing.assert_array_equal(gswe, swe)
+        np.testing.assert_array_equal(gdepth, depth)
+        moved += np.abs(out["drift_mass"]).sum()
+    assert moved > 0
+    # without a snow state the step needs swe and snow depth from the caller
+    m2 = gpu_module(w.mesh, L)
+    with pytest.raises(ModuleError):
+        m2.run(own, 3600.0)
+    m.close()
+    m2.close()

@@ -200,3 +200,15 @@ def test_cpp_module_shim_selftest(cuda_lib):
     r = subprocess.run([str(exe), "--selftest"], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "selftest ok" in r.stdout
+
+
+def test_consume_drift_rule():
+    """snobal's use of drift_mass (snobal.cpp:363-387): erosion at the pack's
+    bulk density, deposition at drift_density, removal at zero, NaN/-9999 as 0."""
+    from chm_gb300.synth import consume_drift
+    swe = np.array([100.0, 100.0, 10.0, 50.0, 0.0, 80.0])
+    depth = np.array([0.5, 0.5, 0.05, 0.2, 0.0, 0.4])
+    dm = np.array([-20.0, 30.0, -10.0, -9999.0, 6.0, np.nan])
+    s, d = consume_drift(swe, depth, dm, 300.0)
+    np.testing.assert_allclose(s, [80.0, 130.0, 0.0, 50.0, 6.0, 80.0])
+    np.testing.assert_allclose(d, [0.5 - 20.0 / 200.0, 0.5 + 30.0 / 300.0, 0.0, 0.2, 6.0 / 300.0, 0.4])
