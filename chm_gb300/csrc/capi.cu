@@ -63,19 +63,8 @@ void prof_drop(Ctx& c, int n) {
 
 namespace {
 
-template <typename T>
-T* dalloc(Ctx& c, size_t n, bool& ok) {
-    void* p = nullptr;
-    if (n == 0) n = 1;
-    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
-        ok = false;
-        return nullptr;
-    }
-    c.allocations.push_back(p);
-    return static_cast<T*>(p);
-}
-
 void free_all(Ctx& c) {
+    graph_destroy(c);
     for (void* p : c.allocations) cudaFree(p);
     c.allocations.clear();
     for (auto& e : c.pev) cudaEventDestroy(e);
@@ -816,73 +805,83 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     if (f->p_snow_hours && (rc = copy_in(c, c.Fo.psh, f->p_snow_hours, dev))) return rc;
     const int64_t h2d = dev ? 0 : c.P.T * 8 * ((own_snow ? 5 : 7) + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
 
-    // the previous step's solution (the assembly zeroes x, as the reference's
-    // zeroSystem does): kept for the warm starts and the MLP features
-    PBSM_CUDA_TRY(cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+    double susp_rhs_max = 0.0, dep_rhs_max = 0.0;
+    if (c.cfg.graph) {
+        // the whole device part of the step as one CUDA-graph launch
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
+        if ((rc = graph_step(c, s, own_snow))) return rc;
+        for (int k = 2; k <= 6; ++k) PBSM_CUDA_TRY(cudaEventRecord(c.ev[k], s));
+        susp_rhs_max = c.graph_rhs_max[0];
+        dep_rhs_max = c.graph_rhs_max[1];
+    } else {
+        // the previous step's solution (the assembly zeroes x, as the reference's
+        // zeroSystem does): kept for the warm starts and the MLP features
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
 
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
-    if (c.Mb.n > 1) {
-        PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.rhs_max, 0, c.Mb.n * 8, s));
-        PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s));
-    }
-    launch_assemble_suspension(c, s);
-    PBSM_CUDA_TRY(cudaGetLastError());
-    PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-    PBSM_CUDA_TRY(cudaMemcpyAsync(c.n_slow_host, c.A.n_slow, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[2], s));
-    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
-    if (c.sc_host->nan_flag != 0.0) {
-        c.err = "NaN in the assembled suspension system (check the forcing)";
-        return PBSM3D_ERR_NAN_INPUT;
-    }
-    c.n_slow = *c.n_slow_host;
-    const double susp_rhs_max = c.sc_host->rhs_max;
-    c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
-    c.target_scale2 = 1.0;
-    if (c.Mb.n > 1 && (rc = member_presence(c, s, 0))) return rc;
-    if (c.suspension_present) {
-        if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
-            PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, c.x_prev, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
-        if (c.cfg.warm_start == PBSM3D_X0_LEARNED) {
-            // network guess, then one block-Jacobi sweep: each column then
-            // satisfies its own vertical balance exactly and only the lateral
-            // couplings act on the network's error
-            if (c.cfg.warm_flags & 2) {
-                if ((rc = launch_mlp_infer(c, s, c.A.x))) return rc;
-            } else {
-                if ((rc = launch_mlp_infer(c, s, c.r))) return rc;
-                if ((rc = jacobi_sweep(c, s, c.r, c.A.x))) return rc;
-            }
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
+        if (c.Mb.n > 1) {
+            PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.rhs_max, 0, c.Mb.n * 8, s));
+            PBSM_CUDA_TRY(cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s));
         }
-        if (c.Mb.n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) launch_member_zero(c, s, c.A.x);
-        rc = solve_suspension(c, s, st);
+        launch_assemble_suspension(c, s);
         PBSM_CUDA_TRY(cudaGetLastError());
-        if (rc) return rc;
-    }
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[3], s));
-    launch_post_and_assemble_deposition(c, s);
-    PBSM_CUDA_TRY(cudaGetLastError());
-    PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[4], s));
-    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
-    if (c.sc_host->nan_flag != 0.0) {
-        c.err = "NaN in the assembled deposition system";
-        return PBSM3D_ERR_NAN_INPUT;
-    }
-    const double dep_rhs_max = c.sc_host->rhs_max;
-    c.deposition_present = c.suspension_present && dep_rhs_max > 1e-12;  // PBSM3D.cpp:1661-1664
-    c.dep_target_scale2 = 1.0;
-    if (c.Mb.n > 1 && (rc = member_presence(c, s, 1))) return rc;
-    if (c.deposition_present) {
-        rc = solve_deposition(c, s, st);
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.n_slow_host, c.A.n_slow, sizeof(int), cudaMemcpyDeviceToHost, s));
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[2], s));
+        PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+        if (c.sc_host->nan_flag != 0.0) {
+            c.err = "NaN in the assembled suspension system (check the forcing)";
+            return PBSM3D_ERR_NAN_INPUT;
+        }
+        c.n_slow = *c.n_slow_host;
+        susp_rhs_max = c.sc_host->rhs_max;
+        c.suspension_present = susp_rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
+        c.target_scale2 = 1.0;
+        if (c.Mb.n > 1 && (rc = member_presence(c, s, 0))) return rc;
+        if (c.suspension_present) {
+            if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
+                PBSM_CUDA_TRY(cudaMemcpyAsync(c.A.x, c.x_prev, c.P.R * 8, cudaMemcpyDeviceToDevice, s));
+            if (c.cfg.warm_start == PBSM3D_X0_LEARNED) {
+                // network guess, then one block-Jacobi sweep: each column then
+                // satisfies its own vertical balance exactly and only the lateral
+                // couplings act on the network's error
+                if (c.cfg.warm_flags & 2) {
+                    if ((rc = launch_mlp_infer(c, s, c.A.x))) return rc;
+                } else {
+                    if ((rc = launch_mlp_infer(c, s, c.r))) return rc;
+                    if ((rc = jacobi_sweep(c, s, c.r, c.A.x))) return rc;
+                }
+            }
+            if (c.Mb.n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) launch_member_zero(c, s, c.A.x);
+            rc = solve_suspension(c, s, st);
+            PBSM_CUDA_TRY(cudaGetLastError());
+            if (rc) return rc;
+        }
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[3], s));
+        launch_post_and_assemble_deposition(c, s);
         PBSM_CUDA_TRY(cudaGetLastError());
-        if (rc) return rc;
+        PBSM_CUDA_TRY(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[4], s));
+        PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+        if (c.sc_host->nan_flag != 0.0) {
+            c.err = "NaN in the assembled deposition system";
+            return PBSM3D_ERR_NAN_INPUT;
+        }
+        dep_rhs_max = c.sc_host->rhs_max;
+        c.deposition_present = c.suspension_present && dep_rhs_max > 1e-12;  // PBSM3D.cpp:1661-1664
+        c.dep_target_scale2 = 1.0;
+        if (c.Mb.n > 1 && (rc = member_presence(c, s, 1))) return rc;
+        if (c.deposition_present) {
+            rc = solve_deposition(c, s, st);
+            PBSM_CUDA_TRY(cudaGetLastError());
+            if (rc) return rc;
+        }
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[5], s));
+        launch_update(c, s);
+        if (own_snow) launch_consume_drift(c, s);
+        PBSM_CUDA_TRY(cudaGetLastError());
+        PBSM_CUDA_TRY(cudaEventRecord(c.ev[6], s));
     }
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[5], s));
-    launch_update(c, s);
-    if (own_snow) launch_consume_drift(c, s);
-    PBSM_CUDA_TRY(cudaGetLastError());
-    PBSM_CUDA_TRY(cudaEventRecord(c.ev[6], s));
     int64_t d2h = 0;
     if (out) {
         const int od = out->on_device;
@@ -935,7 +934,7 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         st->ledger_snow_mass = ledger[4];
         st->bytes_moved = c.bytes + h2d + d2h;
         st->gpu_launches = c.launches;
-        if (c.prof) {
+        if (c.prof && !c.cfg.graph) {  // a graph replay records no per-launch events
             st->profiled = 1;
             for (int k = 0; k < c.pused; ++k) {
                 const int cat = c.pcat[k];

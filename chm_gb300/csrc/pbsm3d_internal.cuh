@@ -172,6 +172,7 @@ struct Tiles {
     const int32_t* mtile;   // [n + 1] first tile of each member
     const int32_t* act;     // [nact] tiles of the members still iterating, ascending
     int ntiles, n, nact;
+    const int* nact_dev;    // graph mode: nact lives in device memory (set by the controllers)
 };
 
 // Grid-wide barrier state of a persistent (cooperative) kernel.
@@ -199,6 +200,10 @@ void launch_consume_drift(Ctx& c, cudaStream_t s);
 
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
+// graph mode: the device part of a step as one CUDA-graph launch (built on
+// first use); fills the iteration/residual fields of c like the host path
+int graph_step(Ctx& c, cudaStream_t s, bool own_snow);
+void graph_destroy(Ctx& c);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
 int configure_cg(Ctx& c);
@@ -233,6 +238,10 @@ struct Ctx {
     Scalars* sc_host;  // pinned mirror
     int* n_slow_host = nullptr;  // pinned: faces with a saltation layer in the last assembly
     int n_slow = 0;
+    // graph mode (cfg.graph): the step as one CUDA graph, see solver.cu
+    const int* graph_dep_flag = nullptr;  // set only while the graph is captured
+    struct StepGraph* graph = nullptr;
+    double graph_rhs_max[2] = {0, 0};  // graph mode: ||rhs||_inf of the two systems
     // device-resident snow state (pbsm3d_set_snow): swe and depth live in Fo.swe / Fo.sd
     bool snow_state = false;
     double drift_density = 300.0;
@@ -286,6 +295,19 @@ struct Ctx {
     double susp_relres, dep_relres;
     double warm_gamma = 0.0;  // scale applied to the last warm start (0 = dropped)
 };
+
+// Device allocation owned by the context (freed with it); ok turns false on failure.
+template <typename T>
+T* dalloc(Ctx& c, size_t n, bool& ok) {
+    void* p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        ok = false;
+        return nullptr;
+    }
+    c.allocations.push_back(p);
+    return static_cast<T*>(p);
+}
 
 // Record the start of a kernel launch of class cat with the given algorithmic
 // bytes (profiling only).  Every launch also adds its bytes to c.bytes.

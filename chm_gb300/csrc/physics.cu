@@ -681,8 +681,9 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
 // PBSM3D.cpp:1710-1740 plus the FP64 mass ledger (deterministic partial sums).
 // rres holds b - A q from the solver's final residual.
 __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F, FaceState S, Dep D, const double* rres,
-                                                   int deposition_present, Members Mb, double* partials, Scalars* sc,
-                                                   double* ledger) {
+                                                   int deposition_present, const int* dep_flag, Members Mb,
+                                                   double* partials, Scalars* sc, double* ledger) {
+    if (dep_flag) deposition_present = *dep_flag;  // graph mode: decided on the device
     double v[4] = {0, 0, 0, 0};  // divergence, deposited, clipped, residual
     double snow = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.T; i += (int64_t)gridDim.x * blockDim.x) {
@@ -858,8 +859,8 @@ void launch_consume_drift(Ctx& c, cudaStream_t s) {
 
 void launch_update(Ctx& c, cudaStream_t s) {
     prof_begin(c, s);
-    k_update<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.dr, c.deposition_present ? 1 : 0, c.Mb,
-                                             c.red.partials, c.sc, c.ledger);
+    k_update<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.dr, c.deposition_present ? 1 : 0,
+                                             c.graph_dep_flag, c.Mb, c.red.partials, c.sc, c.ledger);
     prof_end(c, s, PBSM3D_K_UPDATE, c.P.T * 81);
 }
 

@@ -80,7 +80,7 @@ struct TileRange {
     int a0, a1;
 };
 __device__ __forceinline__ TileRange block_tiles(const Tiles& tl) {
-    const int64_t n = tl.nact, g = gridDim.x, b = blockIdx.x;
+    const int64_t n = tl.nact_dev ? *tl.nact_dev : tl.nact, g = gridDim.x, b = blockIdx.x;
     return TileRange{(int)(b * n / g), (int)((b + 1) * n / g)};
 }
 // End (exclusive, in active-list positions) of the segment that starts at
@@ -136,7 +136,7 @@ __device__ bool member_totals(V (&v)[NT], double* part, const Tiles& tl, int ts,
         double s = 0;
         if (one) {
             // the active list is every tile; block b's segment starts at b * nact / G
-            const int64_t na = tl.nact, g = gridDim.x;
+            const int64_t na = tl.nact_dev ? *tl.nact_dev : tl.nact, g = gridDim.x;
             for (int64_t b = threadIdx.x; b < g; b += blockDim.x) {
                 const int64_t a0 = b * na / g;
                 if (a0 < (b + 1) * na / g) s += __ldcg(&part[(int64_t)k * tl.ntiles + tl.act[a0]]);
@@ -1524,6 +1524,830 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     if (done != DONE_CONVERGED && !(c.sc_host->tmp <= tol * tol * bn2)) {
         c.err = "deposition solve failed to converge (relative residual " + std::to_string(c.dep_relres) + ")";
         return PBSM3D_ERR_NOT_CONVERGED;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------- graph mode
+// The device part of a step as one CUDA-graph launch.  The decisions the
+// host makes between launches in the default path (the "present" tests, the
+// per-member convergence and inner targets of the refinement sweeps, the
+// warm-start scale, the active-tile list, the end of each Krylov loop) are
+// made by one-block controller kernels, which steer conditional IF/WHILE
+// nodes with cudaGraphSetConditional.  Every loop has a device-side cap:
+// Krylov loops stop at their iteration limits, the refinement loops after
+// 64 (suspension) or 8 (deposition) sweeps, and a guard counter over all
+// loop bodies ends every loop and records an error past kGuardMax.  The
+// deposition solve runs as per-member tile CG (no cooperative launch inside
+// the graph).
+
+namespace {
+
+constexpr int kGuardMax = 200000;
+
+struct StepCtl {
+    int ok, err;  // err: PBSM3D_ERR_* of the failure, 0 while ok
+    int susp_present, dep_present;
+    int sweep, susp_iters, dep_iters, dep_sweeps;
+    int guard, n_active;
+    int kernels;  // kernels the graph executed this step (tallied by the controllers)
+    double susp_relres, dep_relres, susp_rhs_max, dep_rhs_max, gamma_sum;
+    int conv[kMaxMembers], dconv[kMaxMembers];
+    double bb[kMaxMembers], dbb[kMaxMembers];
+};
+
+// The conditional handles of the step graph.  A form without a warm start
+// or without the mixed deposition refinement has no node for those handles;
+// `valid` marks the ones that exist, and only those are ever set.
+enum HandleId { H_OK1, H_SUSP, H_OUTER, H_WARM, H_INNER, H_ILOOP, H_OK2, H_DEP, H_DOUTER, H_DINNER, H_DLOOP, H_OK3,
+                H_COUNT };
+struct Handles {
+    cudaGraphConditionalHandle h[H_COUNT];
+    unsigned valid;
+};
+
+__device__ __forceinline__ void hset(const Handles& h, int id, unsigned v) {
+    if (h.valid & (1u << id)) cudaGraphSetConditional(h.h[id], v);
+}
+
+__device__ __forceinline__ void stop_all(const Handles& h) {
+    for (int id : {H_OUTER, H_INNER, H_ILOOP, H_WARM, H_DOUTER, H_DINNER, H_DLOOP}) hset(h, id, 0u);
+}
+
+// One block: the active-tile list of the members with active[m] != 0 (in
+// shared memory, filled by the caller), in member order.
+__device__ void ctl_build_act(const Tiles& tl, int32_t* act, int* nact, const int* active) {
+    __shared__ int first[kMaxMembers + 1];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int m = 0; m < tl.n; ++m) {
+            first[m] = acc;
+            if (active[m]) acc += tl.mtile[m + 1] - tl.mtile[m];
+        }
+        first[tl.n] = acc;
+        *nact = acc;
+    }
+    __syncthreads();
+    const int total = first[tl.n];
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        // the last member whose first position is <= q; it holds position q
+        // (a member without tiles in the list shares its start with the next)
+        int lo = 0, hi = tl.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= q) lo = mid;
+            else hi = mid - 1;
+        }
+        act[q] = tl.mtile[lo] + (q - first[lo]);
+    }
+    __syncthreads();
+}
+
+// After the suspension assembly: NaN check, per-member "present" tests.
+__global__ void k_ctl_begin(StepCtl* ctl, const Scalars* sc0, Members Mb, int n, Handles h) {
+    if (threadIdx.x != 0) return;
+    const bool nan = sc0->nan_flag != 0.0;
+    bool any = false;
+    if (n == 1) {
+        any = sc0->rhs_max > 1e-12;  // PBSM3D.cpp:1424-1427
+    } else {
+        for (int m = 0; m < n; ++m) {
+            const double v = __longlong_as_double((long long)Mb.rhs_max[m]);
+            Mb.susp_present[m] = v > 1e-12;
+            any = any || Mb.susp_present[m];
+        }
+    }
+    ctl->ok = !nan;
+    ctl->err = nan ? PBSM3D_ERR_NAN_INPUT : 0;
+    ctl->susp_present = any;
+    ctl->dep_present = 0;
+    ctl->susp_rhs_max = sc0->rhs_max;
+    ctl->sweep = ctl->susp_iters = ctl->dep_iters = ctl->dep_sweeps = ctl->guard = 0;
+    ctl->kernels = 4 + (n > 1 ? 1 : 0);  // three assembly passes, this, the member mask
+    ctl->susp_relres = ctl->dep_relres = ctl->gamma_sum = 0.0;
+    hset(h, H_OK1, nan ? 0u : 1u);
+    hset(h, H_SUSP, (!nan && any) ? 1u : 0u);
+    hset(h, H_OK3, nan ? 0u : 1u);
+}
+
+// Start of the suspension solve: every member active, residual states clear.
+__global__ void k_ctl_solve_init(StepCtl* ctl, MScal* msR, Tiles tl, int32_t* act, int* nact, int warm, int start_kernels,
+                                 Handles h) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
+        msR[m] = MScal{};
+        active[m] = 1;
+        ctl->conv[m] = 0;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        ctl->kernels += 1 + start_kernels;
+        hset(h, H_OUTER, 1u);
+        hset(h, H_WARM, warm ? 1u : 0u);
+    }
+}
+
+// Sweep 0 with a warm start: the residual-optimal scale per member
+// (gamma = 0 keeps the zero guess), as the host path computes it.
+__global__ void k_ctl_gamma(StepCtl* ctl, MScal* msR, int n) {
+    if (threadIdx.x != 0) return;
+    double gs = 0.0;
+    for (int m = 0; m < n; ++m) {
+        const double bb = msR[m].bnorm2, br = msR[m].red0, rr = msR[m].rnorm2;
+        const double bax = bb - br, axax = bb - 2.0 * br + rr;
+        double gamma = (axax > 0 && bax > 0) ? bax / axax : 0.0;
+        const double rmin2 = axax > 0 ? bb - bax * bax / axax : bb;
+        if (!(rmin2 < 0.99 * bb)) gamma = 0.0;
+        msR[m].gamma = gamma;
+        ctl->bb[m] = bb;  // ||b_m||^2 before the scaling pass overwrites nothing else
+        gs += gamma;
+    }
+    ctl->gamma_sum = gs;
+    ctl->kernels += 2;  // this and the scaling pass
+}
+
+// After a residual pass: per-member convergence on the true FP64 residual,
+// then either the end of the solve or the next inner solve's states.
+__global__ void k_ctl_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Tiles tl, int32_t* act, int* nact,
+                            double tol, double inner_tol, int maxit, int mixed, Handles h) {
+    __shared__ int active[kMaxMembers];
+    __shared__ int s_all, s_finite, s_go;
+    __shared__ double s_worst;
+    const int n = tl.n;
+    if (threadIdx.x == 0) {
+        s_all = 1;
+        s_finite = 1;
+        s_worst = 0.0;
+    }
+    __syncthreads();
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        if (ctl->sweep == 0) ctl->bb[m] = msR[m].bnorm2;
+        const double rr = msR[m].rnorm2, bb = ctl->bb[m];
+        if (!isfinite(rr)) atomicExch(&s_finite, 0);
+        if (!ctl->conv[m] && rr <= tol * tol * bb) ctl->conv[m] = 1;
+        if (!ctl->conv[m]) atomicExch(&s_all, 0);
+        active[m] = !ctl->conv[m];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double worst = 0.0;
+        for (int m = 0; m < n; ++m)
+            if (ctl->bb[m] > 0) worst = fmax(worst, msR[m].rnorm2 / ctl->bb[m]);
+        ctl->susp_relres = sqrt(worst);
+        ctl->kernels += 2;  // the residual pass and this
+        hset(h, H_WARM, 0u);
+        int go = 0;
+        if (!s_finite || ++ctl->guard > kGuardMax) {
+            ctl->ok = 0;
+            ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+        } else if (!s_all) {
+            if (ctl->susp_iters >= maxit || ctl->sweep > 64) {
+                ctl->ok = 0;
+                ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+            } else {
+                go = 1;
+            }
+        }
+        s_go = go;
+        if (!go) {
+            hset(h, H_OUTER, 0u);
+            hset(h, H_INNER, 0u);
+            hset(h, H_ILOOP, 0u);
+            if (!ctl->ok) {
+                stop_all(h);
+                hset(h, H_OK3, 0u);
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_go) return;
+    __shared__ int s_ndone;
+    if (threadIdx.x == 0) s_ndone = 0;
+    __syncthreads();
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        const double rr = msR[m].rnorm2, bb = ctl->bb[m];
+        MScal q{};
+        q.rho = rr;
+        q.alpha = q.omega = 1.0;
+        q.beta = 0.0;
+        q.maxit = max(1, maxit - ctl->susp_iters);
+        if (mixed) {
+            const double goal2 = tol * tol * bb;
+            const double need = rr > 0 ? 0.5 * sqrt(goal2 / rr) : 1.0;
+            const double itol = fmin(0.5, fmax(inner_tol, need));
+            q.target2 = itol * itol * rr;
+        } else {
+            q.target2 = tol * tol * bb;
+        }
+        q.done = (ctl->conv[m] || rr == 0.0) ? 1 : 0;
+        if (q.done) {
+            atomicAdd(&s_ndone, 1);
+            active[m] = 0;
+        }
+        ms[m] = q;
+        msR[m].done = ctl->conv[m];
+        msR[m].counter = 0u;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        sc->done = s_ndone == n ? 1 : 0;
+        sc->counter[2] = (unsigned)s_ndone;
+        sc->iter = 0;
+        ctl->n_active = n - s_ndone;
+        hset(h, H_OUTER, 1u);
+        hset(h, H_INNER, 1u);
+        hset(h, H_ILOOP, s_ndone == n ? 0u : 1u);
+    }
+}
+
+// After each batched Krylov iteration: stop the loop when every member is
+// done; members that stopped leave the active-tile list.
+__global__ void k_ctl_inner(StepCtl* ctl, const MScal* ms, const Scalars* sc, Tiles tl, int32_t* act, int* nact,
+                            int loop, int body_kernels, Handles h) {
+    __shared__ int active[kMaxMembers];
+    __shared__ int s_rebuild;
+    if (threadIdx.x == 0) {
+        s_rebuild = 0;
+        ctl->kernels += body_kernels;
+        if (sc->done || ++ctl->guard > kGuardMax) {
+            hset(h, loop, 0u);
+            if (ctl->guard > kGuardMax) {
+                ctl->ok = 0;
+                ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+                stop_all(h);
+                hset(h, H_OK3, 0u);
+            }
+        } else if (tl.n > 1 && ctl->n_active != tl.n - (int)sc->counter[2]) {
+            s_rebuild = 1;
+            ctl->n_active = tl.n - (int)sc->counter[2];
+        }
+    }
+    __syncthreads();
+    if (!s_rebuild) return;
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) active[m] = ms[m].done ? 0 : 1;
+    ctl_build_act(tl, act, nact, active);
+}
+
+// End of a refinement sweep of the suspension solve: count the iterations;
+// the next residual pass covers the members not yet converged.
+__global__ void k_ctl_sweep_end(StepCtl* ctl, const Scalars* sc, Tiles tl, int32_t* act, int* nact, int extra) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) active[m] = !ctl->conv[m];
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        ctl->susp_iters += sc->iter;
+        ctl->sweep += 1;
+        ctl->kernels += 1 + extra;
+    }
+}
+
+// After the deposition assembly: NaN check and the "present" tests.
+__global__ void k_ctl_dep_begin(StepCtl* ctl, const Scalars* sc0, Members Mb, int n, int tail_kernels, Handles h) {
+    if (threadIdx.x != 0) return;
+    ctl->kernels += 3 + (n > 1 ? 1 : 0) + tail_kernels;  // post, deposition rows, this, mask; update
+    const bool nan = sc0->nan_flag != 0.0;
+    bool any = false;
+    if (n == 1) {
+        any = ctl->susp_present && sc0->rhs_max > 1e-12;  // PBSM3D.cpp:1661-1664
+    } else {
+        for (int m = 0; m < n; ++m) {
+            const double v = __longlong_as_double((long long)Mb.dep_max[m]);
+            Mb.dep_present[m] = v > 1e-12 && Mb.susp_present[m];
+            any = any || Mb.dep_present[m];
+        }
+    }
+    ctl->dep_rhs_max = sc0->rhs_max;
+    if (nan) {
+        ctl->ok = 0;
+        ctl->err = PBSM3D_ERR_NAN_INPUT;
+    }
+    ctl->dep_present = any && !nan;
+    hset(h, H_DEP, (!nan && any) ? 1u : 0u);
+    hset(h, H_OK3, ctl->ok ? 1u : 0u);
+}
+
+// After the suspension solve: a failed solve ends the step, as the host path
+// returns before the column post touches any state.
+__global__ void k_ctl_mid(StepCtl* ctl, Handles h) {
+    if (threadIdx.x != 0) return;
+    ctl->kernels += 1;
+    hset(h, H_OK2, ctl->ok ? 1u : 0u);
+}
+
+// Deposition CG states (plain: target tol relative to ||b_m||; mixed inner:
+// itol relative to ||r_m||), all members active unless converged.
+__global__ void k_ctl_dcg_init(StepCtl* ctl, MScal* ms, Scalars* sc, Tiles tl, int32_t* act, int* nact, double tol,
+                               int maxit, Handles h) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
+        MScal q{};
+        q.target2 = tol * tol;
+        q.maxit = maxit;
+        ms[m] = q;
+        active[m] = 1;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        sc->done = 0;
+        sc->counter[2] = 0u;
+        sc->iter = 0;
+        ctl->n_active = tl.n;
+        ctl->kernels += 3;  // this, the CG start and its first q
+        hset(h, H_DLOOP, 1u);
+    }
+}
+
+// The per-member CG's residual pass: every member (plain) or the members
+// not yet converged (mixed) get a fresh residual sum.
+__global__ void k_ctl_dres_init(StepCtl* ctl, MScal* msR, Tiles tl, int32_t* act, int* nact, int only_open) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
+        const int open = only_open ? !ctl->dconv[m] : 1;
+        MScal q{};
+        q.done = open ? 0 : 1;
+        q.rnorm2 = msR[m].rnorm2;
+        msR[m] = q;
+        active[m] = open;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) ctl->kernels += 2;  // this and the residual pass
+}
+
+// End of the plain deposition solve: every member's true residual.
+__global__ void k_ctl_dep_end(StepCtl* ctl, const MScal* msR, const Scalars* sc, int n, double tol, Handles h) {
+    if (threadIdx.x != 0) return;
+    double worst = 0.0;
+    bool ok = true;
+    for (int m = 0; m < n; ++m) {
+        const double rr = msR[m].rnorm2, bb = msR[m].bnorm2;
+        if (bb > 0) worst = fmax(worst, rr / bb);
+        if (!(rr <= tol * tol * bb)) ok = false;
+    }
+    ctl->dep_relres = sqrt(worst);
+    ctl->dep_iters = sc->iter;
+    ctl->dep_sweeps = 1;
+    ctl->kernels += 1;
+    if (!ok) {
+        ctl->ok = 0;
+        ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+        hset(h, H_OK3, 0u);
+    }
+}
+
+// Mixed deposition: start of the refinement (x = 0, nothing converged).
+__global__ void k_ctl_dmix_init(StepCtl* ctl, MScal* msR, Tiles tl, int32_t* act, int* nact, Handles h) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
+        ctl->dconv[m] = 0;
+        msR[m] = MScal{};
+        active[m] = 1;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        ctl->dep_sweeps = 0;
+        ctl->dep_iters = 0;
+        ctl->kernels += 2;  // the FP32 copy and this
+        hset(h, H_DOUTER, 1u);
+    }
+}
+
+// Mixed deposition, after a residual pass: convergence per member, then the
+// next FP32 inner solve's states or the end of the refinement.
+__global__ void k_ctl_dmix_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Tiles tl, int32_t* act,
+                                 int* nact, double tol, int maxit, Handles h) {
+    __shared__ int active[kMaxMembers];
+    __shared__ int s_all, s_go;
+    const int n = tl.n;
+    if (threadIdx.x == 0) s_all = 1;
+    __syncthreads();
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        if (ctl->dep_sweeps == 0) ctl->dbb[m] = msR[m].bnorm2;
+        const double rr = msR[m].rnorm2, bb = ctl->dbb[m];
+        if (!ctl->dconv[m] && rr <= tol * tol * bb) ctl->dconv[m] = 1;
+        if (!ctl->dconv[m]) atomicExch(&s_all, 0);
+        active[m] = !ctl->dconv[m];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double worst = 0.0;
+        for (int m = 0; m < n; ++m)
+            if (ctl->dbb[m] > 0) worst = fmax(worst, msR[m].rnorm2 / ctl->dbb[m]);
+        ctl->dep_relres = sqrt(worst);
+        ctl->kernels += 2;  // the residual pass and this
+        int go = !s_all;
+        if (go && (ctl->dep_sweeps >= 8 || ++ctl->guard > kGuardMax)) {
+            go = 0;
+            ctl->ok = 0;
+            ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+            stop_all(h);
+            hset(h, H_OK3, 0u);
+        }
+        s_go = go;
+        if (!go) {
+            hset(h, H_DOUTER, 0u);
+            hset(h, H_DINNER, 0u);
+            hset(h, H_DLOOP, 0u);
+        }
+    }
+    __syncthreads();
+    if (!s_go) return;
+    for (int m = threadIdx.x; m < n; m += blockDim.x) {
+        MScal q{};
+        if (ctl->dconv[m]) {
+            q.done = 1;
+        } else {
+            const double rr = msR[m].rnorm2, bb = ctl->dbb[m];
+            const double itol = fmax(1e-5, 0.3 * tol * sqrt(bb / rr));
+            q.target2 = itol * itol;
+            q.maxit = maxit;
+        }
+        ms[m] = q;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        int nd = 0;
+        for (int m = 0; m < n; ++m) nd += ctl->dconv[m] ? 1 : 0;
+        sc->done = 0;
+        sc->counter[2] = (unsigned)nd;
+        sc->iter = 0;
+        ctl->n_active = n - nd;
+        ctl->kernels += 3;  // zero, CG start, first q
+        hset(h, H_DOUTER, 1u);
+        hset(h, H_DINNER, 1u);
+        hset(h, H_DLOOP, 1u);
+    }
+}
+
+// Mixed deposition: end of an inner solve.
+__global__ void k_ctl_dmix_sweep_end(StepCtl* ctl, const Scalars* sc, MScal* msR, Tiles tl, int32_t* act, int* nact) {
+    __shared__ int active[kMaxMembers];
+    for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
+        active[m] = !ctl->dconv[m];
+        msR[m].done = ctl->dconv[m];
+        msR[m].counter = 0u;
+    }
+    ctl_build_act(tl, act, nact, active);
+    if (threadIdx.x == 0) {
+        ctl->dep_iters += sc->iter;
+        ctl->dep_sweeps += 1;
+        ctl->kernels += 2;  // the correction and this
+    }
+}
+
+}  // namespace
+
+struct StepGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    double dt = -1.0;
+    bool own_snow = false;
+    StepCtl* ctl = nullptr;      // device
+    StepCtl* ctl_host = nullptr;  // pinned
+    int* nact = nullptr;         // device
+    cudaStream_t cap[8] = {};
+};
+
+namespace {
+
+// Conditional node at the current capture point of stream s; its body graph
+// is captured on stream t until the returned guard ends it.
+struct CondBody {
+    cudaStream_t t = nullptr;
+    bool open = false;
+    int begin(cudaStream_t s, cudaStream_t t_, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type) {
+        t = t_;
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaGraph_t g;
+        if (cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return 1;
+        cudaGraphNodeParams p = {};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = type;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &p) != cudaSuccess) return 1;
+        if (cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+            return 1;
+        if (cudaStreamBeginCaptureToGraph(t, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed) != cudaSuccess)
+            return 1;
+        open = true;
+        return 0;
+    }
+    int end() {
+        if (!open) return 0;
+        open = false;
+        cudaGraph_t g;
+        return cudaStreamEndCapture(t, &g) != cudaSuccess;
+    }
+};
+
+// The batched BiCGStab iteration (the five kernels of bicgstab_iterations).
+template <typename V, typename X>
+void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, Scalars* sc, X* x, V* r, V* rh,
+                            V* p, V* v, V* sv, V* tv, V* zp, V* zs) {
+    Op<V> op = make_op<V>(c);
+    const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
+    const int gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.ntiles));
+    const int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
+    double* part = c.tile_part;
+    k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, zp, ms);
+    k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, p, zp, v, rh, ms, sc, part);
+    k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, zs, ms);
+    k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, tl, sv, zs, tv, ms, part);
+    k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
+}
+
+// The suspension solve (inside IF susp).
+template <typename V>
+int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& tl) {
+    cudaStream_t s = G.cap[depth];
+    const int n = tl.n;
+    const int gr = std::max(1, std::min(c.grid_red[0], tl.ntiles));
+    double* part = c.tile_part;
+    const bool mixed = c.P.mixed;
+    const int warm = c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1);
+    MScal* ms = mixed ? c.ms1 : c.ms0;
+    Scalars* sc = mixed ? c.sc + 1 : c.sc;
+    const int start_kernels = (c.cfg.warm_start == PBSM3D_X0_LEARNED ? ((c.cfg.warm_flags & 2) ? 1 : 2) : 0) +
+                              ((n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) ? 1 : 0);
+    k_ctl_solve_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, warm, start_kernels, h);
+    CondBody outer;
+    if (outer.begin(s, G.cap[depth + 1], h.h[H_OUTER], cudaGraphCondTypeWhile)) return 1;
+    {
+        cudaStream_t t = G.cap[depth + 1];
+        if (mixed)
+            k_residual<float><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
+                                                    c.p32, c.v32, c.msR, part);
+        else
+            k_residual<double><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
+                                                     c.v, c.msR, part);
+        if (warm) {
+            CondBody wb;
+            if (wb.begin(t, G.cap[depth + 2], h.h[H_WARM], cudaGraphCondTypeIf)) return 1;
+            cudaStream_t u = G.cap[depth + 2];
+            k_ctl_gamma<<<1, 32, 0, u>>>(G.ctl, c.msR, n);
+            if (mixed)
+                k_warm_scale<float><<<gr, kBlock, 0, u>>>(c.P, tl, c.A.x, c.r, c.A.rhs, c.r32, c.rh32, c.msR, part);
+            else
+                k_warm_scale<double><<<gr, kBlock, 0, u>>>(c.P, tl, c.A.x, c.r, c.A.rhs, c.r, c.rh, c.msR, part);
+            if (wb.end()) return 1;
+        }
+        k_ctl_outer<<<1, kBlock, 0, t>>>(G.ctl, c.msR, ms, sc, tl, c.act_buf, G.nact, c.cfg.susp_tol,
+                                         c.cfg.inner_tol, c.cfg.susp_maxit, mixed ? 1 : 0, h);
+        CondBody inner;
+        if (inner.begin(t, G.cap[depth + 2], h.h[H_INNER], cudaGraphCondTypeIf)) return 1;
+        {
+            cudaStream_t u = G.cap[depth + 2];
+            if (mixed) k_zero<float><<<c.grid_faces, kBlock, 0, u>>>(c.P.R, c.x32);
+            CondBody loop;
+            if (loop.begin(u, G.cap[depth + 3], h.h[H_ILOOP], cudaGraphCondTypeWhile)) return 1;
+            cudaStream_t w = G.cap[depth + 3];
+            if (mixed)
+                capture_bicg_iteration<float, float>(c, w, tl, ms, sc, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32,
+                                                     c.t32, c.zp32, c.zs32);
+            else
+                capture_bicg_iteration<double, double>(c, w, tl, ms, sc, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv,
+                                                       c.zp, c.zs);
+            k_ctl_inner<<<1, kBlock, 0, w>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_ILOOP, 6, h);
+            if (loop.end()) return 1;
+            if (mixed) k_add_correction<<<c.grid_faces, kBlock, 0, u>>>(c.P.R, c.A.x, c.x32);
+            k_ctl_sweep_end<<<1, kBlock, 0, u>>>(G.ctl, sc, tl, c.act_buf, G.nact, mixed ? 2 : 0);
+        }
+        if (inner.end()) return 1;
+    }
+    return outer.end();
+}
+
+// One per-member CG on system D (states set by a controller before).
+template <typename V>
+int capture_scg(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& tl, DepSys<V> D, MScal* ms,
+                Scalars* sc) {
+    cudaStream_t s = G.cap[depth];
+    const int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
+    double* part = c.tile_part;
+    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+    k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+    CondBody loop;
+    if (loop.begin(s, G.cap[depth + 1], h.h[H_DLOOP], cudaGraphCondTypeWhile)) return 1;
+    cudaStream_t t = G.cap[depth + 1];
+    k_scg_x<V><<<g, kBlock, 0, t>>>(tl, D, ms, sc, part);
+    k_scg_q<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+    k_ctl_inner<<<1, kBlock, 0, t>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_DLOOP, 3, h);
+    return loop.end();
+}
+
+// The deposition solve (inside IF dep).
+int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& tl) {
+    cudaStream_t s = G.cap[depth];
+    const int64_t Tp = c.P.Tp;
+    const double tol = c.cfg.dep_tol;
+    Scalars* sc = c.sc + 2;
+    const int gr = std::max(1, std::min(c.grid_red[0], tl.ntiles));
+    double* part = c.tile_part;
+    if (!c.P.mixed) {
+        DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
+        k_ctl_dcg_init<<<1, kBlock, 0, s>>>(G.ctl, c.ms0, sc, tl, c.act_buf, G.nact, tol, c.cfg.dep_maxit, h);
+        if (capture_scg<double>(c, G, h, depth, tl, D, c.ms0, sc)) return 1;
+        k_ctl_dres_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, 0);
+        k_sdep_resid<<<gr, kBlock, 0, s>>>(tl, c.P, c.D, c.F.nbr, nullptr, c.dr, c.msR, part);
+        k_ctl_dep_end<<<1, 32, 0, s>>>(G.ctl, c.msR, sc, tl.n, tol, h);
+        return 0;
+    }
+    float* f = c.dep32;
+    float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
+    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
+    if (cudaMemsetAsync(c.D.x, 0, Tp * sizeof(double), s) != cudaSuccess) return 1;
+    k_ctl_dmix_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, h);
+    CondBody outer;
+    if (outer.begin(s, G.cap[depth + 1], h.h[H_DOUTER], cudaGraphCondTypeWhile)) return 1;
+    {
+        cudaStream_t t = G.cap[depth + 1];
+        k_sdep_resid<<<gr, kBlock, 0, t>>>(tl, c.P, c.D, c.F.nbr, r32, c.dr, c.msR, part);
+        k_ctl_dmix_outer<<<1, kBlock, 0, t>>>(G.ctl, c.msR, c.ms1, sc, tl, c.act_buf, G.nact, tol,
+                                              std::min(c.cfg.dep_maxit, 500), h);
+        CondBody inner;
+        if (inner.begin(t, G.cap[depth + 2], h.h[H_DINNER], cudaGraphCondTypeIf)) return 1;
+        {
+            cudaStream_t u = G.cap[depth + 2];
+            k_zero<float><<<c.grid_faces, kBlock, 0, u>>>(Tp, D32.x);
+            if (capture_scg<float>(c, G, h, depth + 2, tl, D32, c.ms1, sc)) return 1;
+            k_dep_add<<<c.grid_faces, kBlock, 0, u>>>(c.P, c.D, D32.x);
+            k_ctl_dmix_sweep_end<<<1, kBlock, 0, u>>>(G.ctl, sc, c.msR, tl, c.act_buf, G.nact);
+        }
+        if (inner.end()) return 1;
+    }
+    return outer.end();
+}
+
+int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
+    cudaGraph_t g;
+    PBSM_CUDA_TRY(cudaGraphCreate(&g, 0));
+    Handles h{};
+    const bool warm = c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1);
+    h.valid = (1u << H_COUNT) - 1u;
+    if (!warm) h.valid &= ~(1u << H_WARM);
+    if (!c.P.mixed) h.valid &= ~((1u << H_DOUTER) | (1u << H_DINNER));
+    for (int id = 0; id < H_COUNT; ++id)
+        if (h.valid & (1u << id))
+            PBSM_CUDA_TRY(cudaGraphConditionalHandleCreate(&h.h[id], g, 0, cudaGraphCondAssignDefault));
+    const bool prof = c.prof;
+    c.prof = false;  // per-launch events are a host-path feature
+    Tiles tl = c.tiles;
+    tl.nact_dev = G.nact;
+    tl.nact = 0;
+    cudaStream_t s = G.cap[0];
+    int bad = 0;
+    PBSM_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    c.graph_dep_flag = &G.ctl->dep_present;
+    {
+        cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s);
+        if (c.Mb.n > 1) {
+            cudaMemsetAsync(c.Mb.rhs_max, 0, c.Mb.n * 8, s);
+            cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s);
+        }
+        launch_assemble_suspension(c, s);
+        k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, h);
+        if (c.Mb.n > 1) launch_member_mask_norm(c, s, 0);
+        CondBody ok1;
+        bad |= ok1.begin(s, G.cap[1], h.h[H_OK1], cudaGraphCondTypeIf);
+        if (!bad) {
+            cudaStream_t t = G.cap[1];
+            CondBody susp;
+            bad |= susp.begin(t, G.cap[2], h.h[H_SUSP], cudaGraphCondTypeIf);
+            if (!bad) {
+                cudaStream_t u = G.cap[2];
+                if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
+                    cudaMemcpyAsync(c.A.x, c.x_prev, c.P.R * 8, cudaMemcpyDeviceToDevice, u);
+                if (c.cfg.warm_start == PBSM3D_X0_LEARNED) {
+                    if (c.cfg.warm_flags & 2) {
+                        bad |= launch_mlp_infer(c, u, c.A.x);
+                    } else {
+                        bad |= launch_mlp_infer(c, u, c.r);
+                        bad |= jacobi_sweep(c, u, c.r, c.A.x);
+                    }
+                }
+                if (c.Mb.n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) launch_member_zero(c, u, c.A.x);
+                if (!bad) bad |= c.P.mixed ? capture_suspension<float>(c, G, h, 2, tl)
+                                           : capture_suspension<double>(c, G, h, 2, tl);
+                bad |= susp.end();
+            }
+            k_ctl_mid<<<1, 32, 0, t>>>(G.ctl, h);
+            CondBody ok2;
+            bad |= ok2.begin(t, G.cap[2], h.h[H_OK2], cudaGraphCondTypeIf);
+            if (!bad) {
+                cudaStream_t u = G.cap[2];
+                launch_post_and_assemble_deposition(c, u);
+                k_ctl_dep_begin<<<1, 32, 0, u>>>(G.ctl, c.sc, c.Mb, c.Mb.n, own_snow ? 2 : 1, h);
+                if (c.Mb.n > 1) launch_member_mask_norm(c, u, 1);
+                CondBody dep;
+                bad |= dep.begin(u, G.cap[3], h.h[H_DEP], cudaGraphCondTypeIf);
+                if (!bad) {
+                    bad |= capture_deposition(c, G, h, 3, tl);
+                    bad |= dep.end();
+                }
+                CondBody ok3;
+                bad |= ok3.begin(u, G.cap[3], h.h[H_OK3], cudaGraphCondTypeIf);
+                if (!bad) {
+                    launch_update(c, G.cap[3]);
+                    if (own_snow) launch_consume_drift(c, G.cap[3]);
+                    bad |= ok3.end();
+                }
+                bad |= ok2.end();
+            }
+            bad |= ok1.end();
+        }
+    }
+    c.graph_dep_flag = nullptr;
+    c.prof = prof;
+    cudaGraph_t out;
+    const cudaError_t e = cudaStreamEndCapture(s, &out);
+    if (bad || e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c.err = std::string("building the step graph failed: ") + cudaGetErrorString(e != cudaSuccess ? e
+                                                                                       : cudaGetLastError());
+        return PBSM3D_ERR_CUDA;
+    }
+    cudaGraphExec_t exec;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+    if (ei != cudaSuccess) {
+        cudaGraphDestroy(g);
+        c.err = std::string("instantiating the step graph failed: ") + cudaGetErrorString(ei);
+        return PBSM3D_ERR_CUDA;
+    }
+    G.graph = g;
+    G.exec = exec;
+    G.own_snow = own_snow;
+    G.dt = c.P.dt;
+    return 0;
+}
+
+}  // namespace
+
+void graph_destroy(Ctx& c) {
+    if (!c.graph) return;
+    StepGraph& G = *c.graph;
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    for (auto& st : G.cap)
+        if (st) cudaStreamDestroy(st);
+    if (G.ctl_host) cudaFreeHost(G.ctl_host);
+    delete c.graph;
+    c.graph = nullptr;
+}
+
+int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
+    if (!c.graph) {
+        c.graph = new StepGraph();
+        StepGraph& G = *c.graph;
+        for (auto& st : G.cap) PBSM_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        bool ok = true;
+        G.ctl = dalloc<StepCtl>(c, 1, ok);
+        G.nact = dalloc<int>(c, 1, ok);
+        if (!ok || cudaMallocHost(&G.ctl_host, sizeof(StepCtl)) != cudaSuccess) {
+            c.err = "out of memory for the step graph";
+            return PBSM3D_ERR_OUT_OF_MEMORY;
+        }
+    }
+    StepGraph& G = *c.graph;
+    if (!G.exec || G.dt != c.P.dt || G.own_snow != own_snow) {
+        if (G.exec) {
+            cudaGraphExecDestroy(G.exec);
+            cudaGraphDestroy(G.graph);
+            G.exec = nullptr;
+            G.graph = nullptr;
+        }
+        // the capture streams must follow s's earlier work
+        PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+        int rc = build_step_graph(c, G, own_snow);
+        if (rc) return rc;
+        c.bytes = 0;
+    }
+    PBSM_CUDA_TRY(cudaGraphLaunch(G.exec, s));
+    PBSM_CUDA_TRY(cudaMemcpyAsync(G.ctl_host, G.ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, s));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    const StepCtl& k = *G.ctl_host;
+    c.suspension_present = k.susp_present;
+    c.deposition_present = k.dep_present;
+    c.susp_iters = k.susp_iters;
+    c.susp_refinements = k.sweep;
+    c.susp_matvecs = 2 * k.susp_iters + k.sweep + 1;
+    c.susp_relres = k.susp_relres;
+    c.dep_iters = k.dep_iters;
+    c.dep_refinements = k.dep_sweeps;
+    c.dep_relres = k.dep_relres;
+    c.warm_gamma = c.tiles.n ? k.gamma_sum / c.tiles.n : 0.0;
+    c.launches = k.kernels;  // kernels the one graph launch executed
+    c.graph_rhs_max[0] = k.susp_rhs_max;
+    c.graph_rhs_max[1] = k.dep_rhs_max;
+    if (k.err) {
+        c.err = k.err == PBSM3D_ERR_NAN_INPUT ? "NaN in an assembled system (check the forcing)"
+                                              : "a Krylov solve failed to converge";
+        return k.err;
     }
     return 0;
 }

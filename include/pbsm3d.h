@@ -121,7 +121,9 @@ typedef struct pbsm3d_config {
     int32_t slice_width;    /* sliced-ELL rows per slice (power of two, 32..1024), 0 = autotune */
     int32_t warm_flags;     /* warm starts: bit 0 = no residual-optimal rescaling of x0,
                                bit 1 = no block-Jacobi sweep after the learned guess; 0 */
-    int32_t reserved[6];
+    int32_t graph;          /* 1: run each step as one CUDA-graph launch with device-side control
+                               (conditional nodes; no host round trip inside the step); 0 */
+    int32_t reserved[5];
 } pbsm3d_config;
 
 /*

@@ -44,8 +44,9 @@ def _check_member(out, ref, tag):
     np.testing.assert_array_equal(out["pbsm_more_than_avail"], ref["pbsm_more_than_avail"])
 
 
-@pytest.mark.parametrize("solver", [{}, {"precision": capi.MIXED}, {"warm_start": capi.X0_PREVIOUS}],
-                         ids=["fp64", "mixed", "warm"])
+@pytest.mark.parametrize("solver", [{}, {"precision": capi.MIXED}, {"warm_start": capi.X0_PREVIOUS},
+                                    {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1}],
+                         ids=["fp64", "mixed", "warm", "graph"])
 def test_members_match_oracle_over_steps(cuda_lib, oracle_lib, solver):
     from oracle import pyoracle
     ws = workloads()

@@ -315,3 +315,59 @@ def test_device_snow_state(cuda_lib, oracle_lib):
         m2.run(own, 3600.0)
     m.close()
     m2.close()
+
+
+@pytest.mark.parametrize("solver", [{}, {"precision": 1}, {"precision": 1, "warm_start": 1}],
+                         ids=["fp64", "mixed", "mixed_previous"])
+def test_graph_mode_matches_oracle(cuda_lib, oracle_lib, solver):
+    """The whole step as one CUDA-graph launch (device-side control of the
+    Krylov and refinement loops) against the exact oracle over coupled steps."""
+    L = 5
+    wg = synth.Workload(1536, 3000.0, seed=5)
+    wo = synth.Workload(1536, 3000.0, seed=5)
+    m = gpu_module(wg.mesh, L, graph=1, **solver)
+    o = oracle(wo.mesh, L)
+    for s in range(3):
+        fg, fo = wg.forcing(s), wo.forcing(s)
+        out = m.run(fg, 3600.0, want_c=True)
+        st = m.last_stats
+        # one graph launch; the count is the kernels it executed
+        assert st["susp_rel_residual"] <= 1e-8 and st["susp_iters"] > 0 and st["gpu_launches"] > 6 * st["susp_iters"]
+        ref, _ = o.step_exact(fo, 3600.0)
+        for k in FIELDS:
+            assert relerr(out[k], ref[k]) < FIELD_TOL, (s, k, relerr(out[k], ref[k]))
+        assert relerr(out["Qsalt"], ref["Qsalt"]) < 1e-12
+        wg.apply_drift(ref["drift_mass"])
+        wo.apply_drift(ref["drift_mass"])
+    m.close()
+
+
+def test_graph_mode_errors_and_state(cuda_lib, small):
+    """Graph mode reports the host path's errors and, like it, leaves the
+    module state untouched by a failed step; the device snow state works."""
+    f = small.forcing(0).arrays()
+    bad = dict(f)
+    bad["t"] = f["t"].copy()
+    bad["t"][10] = np.nan
+    m = gpu_module(small.mesh, 5, graph=1)
+    with pytest.raises(ModuleError, match="NAN_INPUT"):
+        m.run(bad, 3600.0)
+    assert np.all(m.state()["sum_subl"] == 0.0)
+    m.close()
+    m = gpu_module(small.mesh, 5, graph=1, susp_maxit=1)
+    with pytest.raises(ModuleError, match="NOT_CONVERGED"):
+        m.run(f, 3600.0)
+    assert np.all(m.state()["sum_subl"] == 0.0)
+    m.close()
+    # device snow state inside the graph, against the host path
+    outs = []
+    for graph in (0, 1):
+        m = gpu_module(small.mesh, 5, graph=graph)
+        m.set_snow(small.swe, small.depth)
+        own = {k: v for k, v in f.items() if k not in ("swe", "snowdepthavg")}
+        for s in range(2):
+            m.run(own, 3600.0)
+        outs.append(m.get_snow())
+        m.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert relerr(b, a) < 1e-6
