@@ -44,7 +44,7 @@ class Config(C.Structure):
         ("susp_maxit", C.c_int32), ("dep_maxit", C.c_int32),
         ("susp_tol", C.c_double), ("dep_tol", C.c_double), ("inner_tol", C.c_double),
         ("slice_width", C.c_int32), ("warm_flags", C.c_int32), ("graph", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 

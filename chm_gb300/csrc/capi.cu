@@ -806,7 +806,9 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     const int64_t h2d = dev ? 0 : c.P.T * 8 * ((own_snow ? 5 : 7) + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
 
     double susp_rhs_max = 0.0, dep_rhs_max = 0.0;
-    if (c.cfg.graph) {
+    // graph mode; with the autotuner on, the first step runs host-driven so
+    // that the geometry is tuned before the graph is built
+    if (c.cfg.graph && c.tuned) {
         // the whole device part of the step as one CUDA-graph launch
         PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
         if ((rc = graph_step(c, s, own_snow))) return rc;

@@ -206,6 +206,8 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow);
 void graph_destroy(Ctx& c);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
+int tuned_waves(Ctx& c);             // autotuner: the choice cached for this shape (0 = none)
+void apply_waves(Ctx& c, int mult);
 int configure_cg(Ctx& c);
 int jacobi_sweep(Ctx& c, cudaStream_t s, const double* xi, double* xo);
 // mlp.cu
@@ -258,6 +260,12 @@ struct Ctx {
     std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
     int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
+    // autotuner (cfg.autotune): one-wave grids, the candidate being timed,
+    // per-iteration times of the candidates; tuned = a choice is in force
+    int wave_col[2] = {1, 1}, wave_red[2] = {1, 1};
+    int tune_cand = 0;
+    float tune_ms[3] = {0, 0, 0};
+    bool tuned = false;
     // ledger partial sums
     double* ledger;    // device [8]
     GridBar* gbar;     // device

@@ -27,10 +27,48 @@
 #include <math.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "pbsm3d_internal.cuh"
 
 namespace pbsm {
+
+// ---------------------------------------------------------------- launch-geometry autotuner
+// The batched Krylov kernels walk their tiles with grid-stride loops, so the
+// grid is free: the tuner times 1, 2 and 4 waves of co-resident blocks on the
+// first suspension solve's own iterations (one polling chunk each) and keeps
+// the fastest.  The choice is remembered per problem shape for the process.
+constexpr int kTuneWaves[3] = {1, 2, 4};
+
+struct TuneKey {
+    int64_t Tp;
+    int L, n, mixed;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(Tp, L, n, mixed) < std::tie(o.Tp, o.L, o.n, o.mixed);
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, int> g_tune;
+
+static TuneKey tune_key(const Ctx& c) { return TuneKey{c.P.Tp, c.P.L, c.tiles.n, c.P.mixed}; }
+
+int tuned_waves(Ctx& c) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(c));
+    if (it == g_tune.end()) return 0;
+    return it->second;
+}
+
+void apply_waves(Ctx& c, int mult) {
+    for (int k = 0; k < 2; ++k) {
+        c.grid_col[k] = std::min(c.wave_col[k] * mult, std::max(1, c.tiles.ntiles));
+        c.grid_red[k] = std::min(c.wave_red[k] * mult, c.grid_faces);  // within the partials workspace
+    }
+    c.tuned = true;
+}
+
 namespace {
 
 template <typename V>
@@ -977,8 +1015,22 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         }
     }
     int64_t act = active_faces(c);
+    cudaEvent_t te[2] = {nullptr, nullptr};
     while (true) {
         const int64_t rows = act * c.P.L;
+        const bool timing = !c.tuned;
+        if (timing) {
+            // this chunk runs the candidate under test, at a fixed length
+            const int mult = kTuneWaves[c.tune_cand];
+            gc = std::max(1, std::min(c.wave_col[sizeof(V) == 4] * mult, tl.nact));
+            gr = std::max(1, std::min(std::min(c.wave_red[sizeof(V) == 4] * mult, c.grid_faces), tl.nact));
+            chunk = 4;
+            if (!te[0]) {
+                PBSM_CUDA_TRY(cudaEventCreate(&te[0]));
+                PBSM_CUDA_TRY(cudaEventCreate(&te[1]));
+            }
+            PBSM_CUDA_TRY(cudaEventRecord(te[0], s));
+        }
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
             k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, zp, ms);
@@ -996,10 +1048,31 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
         }
+        if (timing) PBSM_CUDA_TRY(cudaEventRecord(te[1], s));
         int rc = read_scalars(c, s, sc);
         if (rc) return rc;
         const int ran = c.sc_host->iter - before;
         before = c.sc_host->iter;
+        if (timing && ran == chunk) {
+            // a full chunk: its time per iteration decides
+            // per iteration and per active face: in an ensemble, later chunks
+            // carry fewer members
+            float ms = 0;
+            PBSM_CUDA_TRY(cudaEventElapsedTime(&ms, te[0], te[1]));
+            c.tune_ms[c.tune_cand] = ms / chunk / (float)std::max<int64_t>(1, act);
+            if (++c.tune_cand == 3) {
+                int best = 0;
+                for (int k = 1; k < 3; ++k)
+                    if (c.tune_ms[k] < c.tune_ms[best]) best = k;
+                apply_waves(c, kTuneWaves[best]);
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                g_tune[tune_key(c)] = kTuneWaves[best];
+            }
+        }
+        if (c.tuned) {
+            gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
+            gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+        }
         // launches after the last member stopped returned at once: not counted
         const int idle = chunk - ran - (c.sc_host->done && ran < chunk ? 1 : 0);
         if (idle > 0) prof_drop(c, 5 * idle);
@@ -1023,6 +1096,8 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         }
         chunk = std::min(16, chunk * 2);
     }
+    for (auto e : te)
+        if (e) cudaEventDestroy(e);
     iters = c.sc_host->iter;
     return 0;
 }
@@ -1053,6 +1128,16 @@ int configure_solver_kernels(Ctx& c) {
     if ((rc = wave((const void*)k_bicg_p<float>, s32, c.grid_col[1]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
+    for (int k = 0; k < 2; ++k) {
+        c.wave_col[k] = c.grid_col[k];
+        c.wave_red[k] = c.grid_red[k];
+    }
+    c.tuned = !c.cfg.autotune;
+    if (!c.tuned) {
+        // a choice made for this shape by an earlier context of the process
+        const int mult = tuned_waves(c);
+        if (mult > 0) apply_waves(c, mult);
+    }
     return 0;
 }
 

@@ -123,7 +123,10 @@ typedef struct pbsm3d_config {
                                bit 1 = no block-Jacobi sweep after the learned guess; 0 */
     int32_t graph;          /* 1: run each step as one CUDA-graph launch with device-side control
                                (conditional nodes; no host round trip inside the step); 0 */
-    int32_t reserved[5];
+    int32_t autotune;       /* 1: the first suspension solve times the batched Krylov kernels at 1, 2
+                               and 4 waves of blocks per SM on its own iterations and keeps the
+                               fastest (shared by later contexts of the same shape); 0 */
+    int32_t reserved[4];
 } pbsm3d_config;
 
 /*

@@ -317,8 +317,9 @@ def test_device_snow_state(cuda_lib, oracle_lib):
     m2.close()
 
 
-@pytest.mark.parametrize("solver", [{}, {"precision": 1}, {"precision": 1, "warm_start": 1}],
-                         ids=["fp64", "mixed", "mixed_previous"])
+@pytest.mark.parametrize("solver", [{}, {"precision": 1}, {"precision": 1, "warm_start": 1},
+                                    {"precision": 1, "warm_start": 1, "autotune": 1}],
+                         ids=["fp64", "mixed", "mixed_previous", "autotuned"])
 def test_graph_mode_matches_oracle(cuda_lib, oracle_lib, solver):
     """The whole step as one CUDA-graph launch (device-side control of the
     Krylov and refinement loops) against the exact oracle over coupled steps."""
@@ -331,8 +332,9 @@ def test_graph_mode_matches_oracle(cuda_lib, oracle_lib, solver):
         fg, fo = wg.forcing(s), wo.forcing(s)
         out = m.run(fg, 3600.0, want_c=True)
         st = m.last_stats
-        # one graph launch; the count is the kernels it executed
-        assert st["susp_rel_residual"] <= 1e-8 and st["susp_iters"] > 0 and st["gpu_launches"] > 6 * st["susp_iters"]
+        # one graph launch (after the autotuner's host-driven first steps);
+        # the count is the kernels it executed
+        assert st["susp_rel_residual"] <= 1e-8 and st["susp_iters"] > 0 and st["gpu_launches"] > 5 * st["susp_iters"]
         ref, _ = o.step_exact(fo, 3600.0)
         for k in FIELDS:
             assert relerr(out[k], ref[k]) < FIELD_TOL, (s, k, relerr(out[k], ref[k]))
