@@ -178,10 +178,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "nLayer must be in [1, 64]";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg.iterative_subl || cfg.z0_ustar_coupling || cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2 ||
-        cfg.debug_output) {
-        g_create_error =
-            "iterative_subl, z0_ustar_coupling, use_subgrid_topo(_V2) and debug_output are not implemented";
+    if (cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2 || cfg.debug_output) {
+        g_create_error = "use_subgrid_topo(_V2) and debug_output are not implemented";
         return PBSM3D_ERR_UNSUPPORTED;
     }
     if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {
@@ -255,6 +253,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     }
     P.log_2_0002 = log(2.0 / 0.0002);
     P.mixed = cfg.precision == PBSM3D_MIXED;
+    P.z0_ustar_coupling = cfg.z0_ustar_coupling != 0;
+    P.iterative_subl = cfg.iterative_subl != 0;
     c.member_offsets = offsets;
     const int nm = (int)members.size();
 

@@ -48,6 +48,7 @@ struct Params {
     // scale, z0, settling scale, log(50/z0)) are in Member.
     double cos_pi_4, Lc_tanh, log_2_0002;
     int mixed;
+    int z0_ustar_coupling, iterative_subl;  // the reference's non-default branches
     const MathTables* mt;  // exp/log tables (device)
 };
 
@@ -92,7 +93,8 @@ struct CzCoef {
 
 // Per-face values the saltation pass hands to the row assembly, [FV_COUNT][Tp].
 enum FaceValue {
-    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QSUB, FV_C1R, FV_LR, FV_LU, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_COUNT
+    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QSUB, FV_C1R, FV_LR, FV_LU, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0,
+    FV_COUNT
 };
 
 // Parameters of one ensemble member (a plain context is one member).

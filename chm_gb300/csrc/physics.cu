@@ -101,7 +101,9 @@ __device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double 
     double omega = P.settling_velocity;
     if (!P.do_fixed_settling) omega = 1.1e7 * exp_t(1.8 * lq, t);   // 1.1e7 r_z^1.8
     o.omega = omega * settling_scale;
-    o.Qr = 0.9 * M_PI * rm * rm * 120.0;
+    // the radiation term, or with iterative_subl, whose rate has no radiation
+    // term, the mean radius itself
+    o.Qr = P.iterative_subl ? rm : 0.9 * M_PI * rm * rm * 120.0;
     const double sigfac = 1.019 + 0.027 * lcz;
     const double kz = kKappa * (cz + z0);
     o.l = kz * 40.0 * rcp_t(kz + 40.0);
@@ -110,6 +112,118 @@ __device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double 
     o.lwarg = log_t(hz_minus_d0 * rcp_t(z0), t);
     o.llw = log_t(o.lwarg, t);
     o.cz = cz;
+}
+
+__device__ __forceinline__ int sgn(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
+
+// z0_ustar_coupling (PBSM3D.cpp:691-712): u* over snow with partly buried
+// vegetation, the root of Li and Pomeroy (2000) eqn 5
+//     g(u) = u2 kappa / log(2 / (c u^2 + lambda/2)) - u,  c = 0.6131702345e-2,
+// which falls with u.  The bracket comes from the walk of the reference's
+// bracket_and_solve_root(g, 1, factor 1, falling, 500 evaluations): from u = 1
+// up when g(1) >= 0 (or NaN), else down, by a factor that is 1 for the first
+// 31 moves (which stay at u = 1 and are skipped here), doubles at the 32nd
+// and then after 16, 8, 4, 2 more moves and at every move after that; a
+// downward walk that passes below DBL_MIN brackets the root 0.  The root is
+// then refined to full precision by Newton steps kept inside the bracket,
+// bisecting when a step leaves it (the reference stops its TOMS 748 at a
+// bracket narrower than 1e-8 and takes the midpoint).  At most 500
+// evaluations in the walk and 100 refinement steps.  false: no bracket.
+__device__ bool coupled_ustar(double u2, double lambda, const MathTables& mt, double& ustar) {
+    const double c = 0.6131702345e-2, A = u2 * kKappa, h = .5 * lambda;
+    auto g = [&](double u) { return div_t(A, log_t(div_t(2.0, c * u * u + h), mt)) - u; };
+    double a = 1.0, b = 1.0;
+    double fa = g(a), fb = fa;
+    const bool up = !(fa < 0);
+    double factor = 2.0;
+    int every = 16;
+    for (int s = 32; sgn(fa) == sgn(fb); ++s) {
+        if (!up && fabs(a) < 2.2250738585072014e-308) {
+            ustar = a / 2.0;
+            return true;
+        }
+        if (s >= 500) return false;
+        if (s > 32 && s % every == 0) {
+            factor *= 2;
+            if (every > 1) every /= 2;
+        }
+        if (up) {
+            a = b;
+            fa = fb;
+            b *= factor;
+            fb = g(b);
+        } else {
+            b = a;
+            fb = fa;
+            a /= factor;
+            fa = g(a);
+        }
+    }
+    if (fa == 0) { ustar = a; return true; }
+    if (fb == 0) { ustar = b; return true; }
+    double lo = a, flo = fa, hi = b;
+    double x = 0.5 * (lo + hi);
+    for (int it = 0; it < 100; ++it) {
+        const double q = c * x * x + h;
+        const double ell = log_t(div_t(2.0, q), mt);
+        const double fx = div_t(A, ell) - x;
+        if (fx == 0) break;
+        if (sgn(fx) == sgn(flo)) {
+            lo = x;
+            flo = fx;
+        } else {
+            hi = x;
+        }
+        const double d = div_t(A * (2.0 * c * x), q * ell * ell) - 1.0;
+        double xn = x - div_t(fx, d);
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const bool done = fabs(xn - x) <= 1e-15 * fabs(xn);
+        x = xn;
+        if (done) break;
+    }
+    ustar = x;
+    return true;
+}
+
+// iterative_subl (PBSM3D.cpp:1062-1096): the ice-bulb temperature Ti (C),
+// root of f(Ti) = T + D L (rho/1000 - .611 mw e(Ti) / (R (Ti+273.15) 1000)) / lambda_t - Ti,
+// e(Ti) = exp(17.3 Ti / (237.3 + Ti)), by the reference's
+// newton_raphson_iterate(f, T, -50, 0, 6 digits): Newton steps from T, the
+// result being the iterate after the first step no larger than |Ti| 2^-5.  A
+// step that would reach a bound goes half the way to it; the bound on the
+// side a step left from moves to the point it left.  At most 100 steps.
+__device__ double ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L,
+                                       const MathTables& mt) {
+    const double mw = 0.01801528 * 1000.0, R = 8.31441 / 1000.0;
+    const double rho = div_t(mw * ea, R * t);
+    const double k = div_t(D * L, lambda_t);
+    const double sat0 = .611 * mw * (1.0 / (R * 1000.0));
+    double lo = -50, hi = 0;
+    double x = T;
+    for (int it = 0; it < 100; ++it) {
+        const double iw = rcp_t(237.3 + x), ik = rcp_t(x + 273.15);
+        const double sat = sat0 * exp_t(17.3 * x * iw, mt) * ik;  // saturation vapour density (kg/m^3)
+        const double f = T + k * (rho * 1e-3 - sat) - x;
+        if (f == 0) break;
+        // d sat/dTi = sat (17.3 * 237.3 / (237.3 + Ti)^2 - 1 / (Ti + 273.15))
+        const double df = -k * sat * (17.3 * 237.3 * iw * iw - ik) - 1.0;
+        const double from = x;
+        double step = div_t(f, df);
+        x = from - step;
+        if (x <= lo) {
+            step = 0.5 * (from - lo);
+            x = from - step;
+        } else if (x >= hi) {
+            step = 0.5 * (from - hi);
+            x = from - step;
+        }
+        if (step > 0)
+            hi = from;
+        else
+            lo = from;
+        if (!(fabs(x * (1.0 / 32.0)) < fabs(step))) break;
+    }
+    return x;
 }
 
 // The same terms for every layer of a face with no saltation layer (hs = 0).
@@ -166,11 +280,20 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                     lambda = 0.5 * G.lai[i] * height_diff;
                 else
                     lambda = stalkN * stalkD * height_diff;
-                ustar = u2 * kKappa / P.log_2_0002;
+                if (P.z0_ustar_coupling) {
+                    double u;
+                    if (coupled_ustar(u2, lambda, mt, u)) ustar = u;  // no bracket: u* stays 1.3 (:710-713)
+                } else {
+                    ustar = u2 * kKappa / P.log_2_0002;
+                }
                 if (ustar >= uth) saltation = true;
             }
-            // z0 is the member's snow roughness on both branches (:740-754)
-            const double z0 = mp.z0;
+            // z0 is the member's snow roughness (:740-754), or with the
+            // coupling, Li and Pomeroy 2000 eqn 4 on saltating faces (:736),
+            // at least the snow roughness (:753)
+            double z0 = mp.z0;
+            if (P.z0_ustar_coupling && saltation)
+                z0 = smax(mp.z0, 0.6131702345e-2 * ustar * ustar + .5 * lambda);
             if (!saltation) ustar = smax(0.01, kKappa * uref / mp.log_zur_z0);
             ustar = smax(0.01, ustar);
             double hs = 0;
@@ -210,7 +333,7 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                 }
                 if (P.use_PomLi) {  // PBSM3D.cpp:848-865
                     const double z10 = 10. + snow_depth;
-                    const double u10 = z10 < kZUR ? log_scale_wind(uref, kZUR, z10, snow_depth, z0) : uref;
+                    const double u10 = z10 < kZUR ? log_scale_wind(uref, kZUR, z10, snow_depth, mp.z0) : uref;
                     const double Ah = F.psh[i];
                     const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
                     const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
@@ -251,7 +374,13 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             //       = q * ((c1 (rh-1)) Nu (r sigfac) - Qr (L M - R t))
             const double Rgt = Rg * t;
             const double c1r = 6.283185308 * Rg * (t * t * lambda_t) * (rh - 1.0);
-            const double q_sub = (rho * D) * rcp_t(D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
+            double q_sub = (rho * D) * rcp_t(D * Ls * (Ls * M - Rgt) * rho + lambda_t * t * t * Rg);
+            if (P.iterative_subl) {
+                // dm/dt = 2 pi rm lambda_t / L Nu (Ts - (t + 273.15)) (:1099, t already
+                // in K): q_sub carries everything but rm Nu
+                const double Ti = ice_bulb_temperature(T_c, t, rh * es / 1000., D, lambda_t, Ls, mt);
+                q_sub = 2.0 * M_PI * lambda_t * (1.0 / Ls) * ((Ti + 273.15) - (t + 273.15));
+            }
             const double LR = Ls * M - Rgt;
             const double sdz0 = snow_depth + z0;
             const double logden = log_t((kZUR - sdz0) * rcp_t(z0), mt);
@@ -273,6 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             fv[FV_LR * Tp + i] = LR;
             fv[FV_LU * Tp + i] = lu_face;
             fv[FV_INVLOGDEN * Tp + i] = inv_logden;
+            if (P.z0_ustar_coupling) fv[FV_Z0 * Tp + i] = z0;
             // lateral faces: udotm_f = u_z * k_f with k_f = (u_hat . m_f) / |u_hat|
 #pragma unroll
             for (int f = 0; f < 3; ++f) fv[(FV_K0 + f) * Tp + i] = inv_nrm * dot2(ux, uy, mx[f], my[f]);
@@ -303,9 +433,10 @@ __global__ void __launch_bounds__(kBlock) k_salt_rows(Params P, Forcing F, Susp 
         double snow_depth = F.sd[i];
         snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
         const double hs = A.face_v[FV_HS * Tp + i];
+        const double z0 = P.z0_ustar_coupling ? A.face_v[FV_Z0 * Tp + i] : mp.z0;
         const double cz = z * P.dz + hs + P.dz / 2.;
         CzCoef o;
-        cz_coeffs(cz, cz + snow_depth - (snow_depth + mp.z0), mp.z0, mp.settling_scale, P, mt, o);
+        cz_coeffs(cz, cz + snow_depth - (snow_depth + z0), z0, mp.settling_scale, P, mt, o);
         const int64_t r = (int64_t)z * Tp + i;
         double* w = A.slow_rows + r;
         w[0 * R] = o.inv_mm;
@@ -450,7 +581,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             }
             const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
             const double Nu = 1.79 + 0.606 * sqrt(rz2nu * Vr);
-            const double dmdtz = q_sub * (c1r * Nu * rsig - Qr * LR);
+            const double dmdtz = P.iterative_subl ? q_sub * (Qr * Nu) : q_sub * (c1r * Nu * rsig - Qr * LR);
             double csubl = dmdtz * inv_mm;
             const double w = omega;
             double K34;

@@ -88,11 +88,11 @@ typedef struct pbsm3d_config {
     int32_t do_lateral_diff;        /* "do_lateral_diff" true */
     int32_t rouault_diffusion_coef; /* "rouault_diffusion_coef" false */
     int32_t enable_veg;             /* "enable_veg" true */
-    int32_t iterative_subl;         /* "iterative_subl" false (true: UNSUPPORTED) */
+    int32_t iterative_subl;         /* "iterative_subl" false */
     int32_t use_exp_fetch;          /* "use_exp_fetch" false */
     int32_t use_tanh_fetch;         /* "use_tanh_fetch" true */
     int32_t use_PomLi_probability;  /* "use_PomLi_probability" false */
-    int32_t z0_ustar_coupling;      /* "z0_ustar_coupling" false (true: UNSUPPORTED) */
+    int32_t z0_ustar_coupling;      /* "z0_ustar_coupling" false */
     int32_t use_subgrid_topo;       /* "use_subgrid_topo" false (true: UNSUPPORTED) */
     int32_t use_subgrid_topo_V2;    /* "use_subgrid_topo_V2" false (true: UNSUPPORTED) */
     int32_t use_R94_lambda;         /* "use_R94_lambda" true */

@@ -91,6 +91,135 @@ double std_dry_air_density(double altitude, double temperature) {
     return std_air_pressure(altitude) / (287.058 * temperature);
 }
 
+inline int sgn(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
+
+// z0_ustar_coupling (PBSM3D.cpp:691-712): the friction velocity over snow
+// with partly buried vegetation is the root of Li and Pomeroy (2000) eqn 5,
+//     g(u) = u2 kappa / log(2 / (c u^2 + lambda/2)) - u,  c = 0.6131702345e-2,
+// which falls with u.  The reference calls Boost 1.85.0's (spack.yaml)
+// bracket_and_solve_root(g, guess 1, factor 1, falling, |a - b| < 1e-8,
+// 500 evaluations) and takes the midpoint of the final bracket; when no
+// bracket is found it throws and u* keeps its 1.3 placeholder.
+//
+// Restated: the same bracketing walk -- from u = 1 up when g(1) >= 0 (or
+// NaN), else down, multiplying or dividing by a factor that is 1 at first and
+// doubles at the 32nd move, then after 16, 8, 4, 2 more and at every move
+// after that; a downward walk that passes below DBL_MIN returns the bracket
+// (0, u) -- and the root of the bracket refined to full precision by
+// Newton-Raphson with a bisection fallback (rtsafe, Press et al., Numerical
+// Recipes, section 9.4) in place of TOMS 748.  The reference's midpoint lies
+// within 5e-9 of that root.  Returns false when the walk fails.
+//
+// Each call gets the full budget of 500 evaluations.  In the reference the
+// budget is an in/out argument shared by the faces of one OpenMP thread
+// (PBSM3D.cpp:422): Boost documents that it returns the evaluations used, so
+// later faces inherit a shrinking budget and its results depend on the thread
+// count.  That is not restated.
+bool coupled_ustar(double u2, double lambda, double& ustar) {
+    const double c = 0.6131702345e-2;
+    auto g = [&](double u) { return u2 * kKappa / std::log(2.0 / (c * u * u + .5 * lambda)) - u; };
+    const int budget = 500;
+    double a = 1.0, b = 1.0;
+    double fa = g(a), fb = fa;
+    const bool up = !(fa < 0);
+    double factor = 1.0;
+    int every = 32;
+    for (int s = 1; sgn(fa) == sgn(fb); ++s) {
+        if (!up && std::fabs(a) < 2.2250738585072014e-308) {
+            ustar = a / 2.0;
+            return true;
+        }
+        if (s >= budget) return false;
+        if (s % every == 0) {
+            factor *= 2;
+            if (every > 1) every /= 2;
+        }
+        if (up) {
+            a = b;
+            fa = fb;
+            b *= factor;
+            fb = g(b);
+        } else {
+            b = a;
+            fb = fa;
+            a /= factor;
+            fa = g(a);
+        }
+    }
+    if (fa == 0) { ustar = a; return true; }
+    if (fb == 0) { ustar = b; return true; }
+    double lo = a, flo = fa, hi = b;
+    double x = 0.5 * (lo + hi);
+    for (int it = 0; it < 100; ++it) {
+        const double q = c * x * x + .5 * lambda;
+        const double ell = std::log(2.0 / q);
+        const double fx = u2 * kKappa / ell - x;
+        if (fx == 0) break;
+        if (sgn(fx) == sgn(flo)) {
+            lo = x;
+            flo = fx;
+        } else {
+            hi = x;
+        }
+        const double d = u2 * kKappa * (2.0 * c * x) / (q * ell * ell) - 1.0;
+        double xn = x - fx / d;
+        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+        const bool done = std::fabs(xn - x) <= 1e-15 * std::fabs(xn);
+        x = xn;
+        if (done) break;
+    }
+    ustar = x;
+    return true;
+}
+
+// iterative_subl (PBSM3D.cpp:1062-1096): the ice-bulb temperature Ti (C) of
+// Pomeroy and Li (2000) / Harder (2013) A.5, the root of
+//     f(Ti) = T + D L (rho/1000 - .611 mw exp(17.3 Ti/(237.3+Ti)) / (R (Ti+273.15) 1000)) / lambda_t - Ti
+// by Boost's newton_raphson_iterate(f, guess T, min -50, max 0, 6 digits).
+// Restated as the Newton iteration that the call documents: start at T, stop
+// after the first step no larger than |Ti| 2^(1-6), return the iterate after
+// that step.  A step that would land on or beyond a bound is replaced by half
+// the way to that bound, and after each step the bound on the side the step
+// left from moves to the point it left.  f is concave with f' < -1, so every
+// iterate after the first lies at or above the root and they descend onto
+// it; a bound is met only when the root lies close to 0 C.
+double ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L) {
+    const double mw = 0.01801528 * 1000.0;
+    const double R = 8.31441 / 1000.0;
+    const double rho = (mw * ea) / (R * t);
+    const double tol = std::ldexp(1.0, 1 - 6);
+    double lo = -50, hi = 0;
+    double x = T;
+    for (int it = 0; it < 100; ++it) {
+        const double e = std::exp(17.3 * x / (237.3 + x));
+        const double f = T + D * L * (rho / 1000.0 - .611 * mw * e / (R * (x + 273.15) * 1000.0)) / lambda_t - x;
+        if (f == 0) break;
+        const double df =
+            D * L *
+                (-0.6110000000e-3 * mw * (17.3 / (237.3 + x) - 17.3 * x / ((237.3 + x) * (237.3 + x))) * e /
+                     (R * (x + 273.15)) +
+                 0.6110000000e-3 * mw * e / (R * (x + 273.15) * (x + 273.15))) /
+                lambda_t -
+            1;
+        const double from = x;
+        double step = f / df;
+        x = from - step;
+        if (x <= lo) {
+            step = 0.5 * (from - lo);
+            x = from - step;
+        } else if (x >= hi) {
+            step = 0.5 * (from - hi);
+            x = from - step;
+        }
+        if (step > 0)
+            hi = from;
+        else
+            lo = from;
+        if (!(std::fabs(x * tol) < std::fabs(step))) break;
+    }
+    return x;
+}
+
 // armadillo's direct dot of two 3-vectors: two accumulators (0,2) and (1).
 inline double dot3(const double* a, const double* b) {
     double v1 = 0, v2 = 0;
@@ -414,6 +543,10 @@ double oracle_log_scale_wind(double u, double z_in, double z_out, double sd, dou
 double oracle_saturated_vapour_pressure(double T) { return saturated_vapour_pressure(T); }
 void oracle_bearing_to_cartesian(double b, double* xy) { bearing_to_cartesian(b, xy[0], xy[1]); }
 double oracle_std_dry_air_density(double z, double T) { return std_dry_air_density(z, T); }
+int oracle_coupled_ustar(double u2, double lambda, double* ustar) { return coupled_ustar(u2, lambda, *ustar) ? 1 : 0; }
+double oracle_ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L) {
+    return ice_bulb_temperature(T, t, ea, D, lambda_t, L);
+}
 
 // triangulation.hpp:1466-1475 edge(i) = v[cw(i)] - v[ccw(i)], ccw(i)=(i+1)%3, cw(i)=(i+2)%3
 // triangulation.hpp:1443-1463 edge_unit_normal, :1493-1498 edge_length,
@@ -502,8 +635,7 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
         g_create_error = "PBSM3D settling velocity must be positive";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg->iterative_subl || cfg->z0_ustar_coupling || cfg->use_subgrid_topo || cfg->use_subgrid_topo_V2 ||
-        cfg->debug_output) {
+    if (cfg->use_subgrid_topo || cfg->use_subgrid_topo_V2 || cfg->debug_output) {
         g_create_error = "configuration branch not restated by the oracle";
         return PBSM3D_ERR_UNSUPPORTED;
     }
@@ -715,10 +847,18 @@ int oracle_stage_assemble_suspension(oracle_ctx* c, const pbsm3d_forcing* F, dou
                 lambda = 0.5 * c->lai[i] * height_diff;
             else
                 lambda = c->stalkN[i] * c->stalkD[i] * height_diff;
-            ustar = u2 * kKappa / std::log(2.0 / 0.0002);
+            if (cfg.z0_ustar_coupling) {
+                double u = 0;
+                if (coupled_ustar(u2, lambda, u)) ustar = u;  // no bracket: u* stays 1.3 (:710-713)
+            } else {
+                ustar = u2 * kKappa / std::log(2.0 / 0.0002);
+            }
             if (ustar >= u_star_saltation_threshold) {
                 saltation = true;
-                z0 = z0_snow;
+                if (cfg.z0_ustar_coupling)
+                    z0 = 0.6131702345e-2 * ustar * ustar + .5 * lambda;  // Li and Pomeroy 2000 eqn 4 (:736)
+                else
+                    z0 = z0_snow;
             }
         }
         if (!saltation) {
@@ -793,7 +933,14 @@ int oracle_stage_assemble_suspension(oracle_ctx* c, const pbsm3d_forcing* F, dou
         double rh = c->f_rh[i] / 100.;
         double es = saturated_vapour_pressure(t);
         double ea = rh * es / 1000.;
-        (void)ea;
+        // PBSM3D.cpp:1062-1096: with iterative_subl the ice-bulb temperature is
+        // a per-face value; the rate uses it below
+        double Ti = 0;
+        if (cfg.iterative_subl) {
+            double D = 2.06e-5 * std::pow(t / 273.15, 1.75);
+            double lambda_t = 0.000063 * t + 0.00673;
+            Ti = ice_bulb_temperature(T_c, t, ea, D, lambda_t, 2.838e6);
+        }
         double vwx, vwy;
         bearing_to_cartesian(c->f_dir[i], vwx, vwy);
         for (int z = 0; z < L; ++z) {
@@ -832,8 +979,16 @@ int oracle_stage_assemble_suspension(oracle_ctx* c, const pbsm3d_forcing* F, dou
             double sigma = (rh - 1.0) * (1.019 + 0.027 * std::log(cz));
             double rho = (M * es) / (R * t);
             double Qr = 0.9 * M_PI * rm * rm * 120.0;
-            double dmdtz = Sh * rho * D * (6.283185308 * Nu * R * r_z * sigma * t * t * lambda_t - Ls * M * Qr + Qr * R * t) /
-                           (D * Ls * Sh * (Ls * M - R * t) * rho + lambda_t * t * t * Nu * R);
+            double dmdtz;
+            if (cfg.iterative_subl) {
+                // eqn 13 of Pomeroy and Li 2000 as PBSM3D.cpp:1099 writes it: Ts in K
+                // against t + 273.15 with t already in K
+                double Ts = Ti + 273.15;
+                dmdtz = 2.0 * M_PI * rm * lambda_t / Ls * Nu * (Ts - (t + 273.15));
+            } else {
+                dmdtz = Sh * rho * D * (6.283185308 * Nu * R * r_z * sigma * t * t * lambda_t - Ls * M * Qr + Qr * R * t) /
+                        (D * Ls * Sh * (Ls * M - R * t) * rho + lambda_t * t * t * Nu * R);
+            }
             double csubl = dmdtz / mm;
             double K[5] = {0, 0, 0, 0, 0};
             double alpha[5] = {0, 0, 0, 0, 0};

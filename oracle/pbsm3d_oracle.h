@@ -83,6 +83,11 @@ double oracle_log_scale_wind(double u, double z_in, double z_out, double snowdep
 double oracle_saturated_vapour_pressure(double T);
 void oracle_bearing_to_cartesian(double bearing, double* xy);
 double oracle_std_dry_air_density(double altitude, double temperature);
+/* Li and Pomeroy (2000) eqn 5 friction velocity (z0_ustar_coupling); returns
+ * 0 when no bracket is found, 1 otherwise. */
+int oracle_coupled_ustar(double u2, double lambda, double* ustar);
+/* ice-bulb temperature (C) of iterative_subl: T in C, t in K, ea in kPa */
+double oracle_ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L);
 /* Face geometry of a triangle mesh (triangulation.hpp:1443-1498,1577-1589,1830-1856).
  * xyz [3*nv], tri [3*nt] vertex ids; outputs [3*nt], [6*nt], [nt], [3*nt]. */
 void oracle_face_geometry(int64_t nv, const double* xyz, int64_t nt, const int32_t* tri, double* edge_length,

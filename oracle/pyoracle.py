@@ -73,6 +73,10 @@ def load():
     lib.oracle_bearing_to_cartesian.restype = None
     lib.oracle_std_dry_air_density.argtypes = [C.c_double, C.c_double]
     lib.oracle_std_dry_air_density.restype = C.c_double
+    lib.oracle_coupled_ustar.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double)]
+    lib.oracle_coupled_ustar.restype = C.c_int
+    lib.oracle_ice_bulb_temperature.argtypes = [C.c_double] * 6
+    lib.oracle_ice_bulb_temperature.restype = C.c_double
     lib.oracle_face_geometry.argtypes = [C.c_int64, _dp, C.c_int64, _i32p, _dp, _dp, _dp, _dp]
     lib.oracle_face_geometry.restype = None
     lib.oracle_face_neighbors.argtypes = [C.c_int64, C.c_int64, _i32p, _i32p]

@@ -1,0 +1,131 @@
+"""Non-default configuration branches of PBSM3D: the CUDA step through the C
+ABI against the oracle's exact solve.
+
+z0_ustar_coupling (PBSM3D.cpp:691-737) and iterative_subl
+(PBSM3D.cpp:1062-1100) alone, together, and over steps with the snow state
+fed back, on a mesh whose vegetation ranges from buried to just above the
+snow (so the coupling's lambda is non-zero); and every other switch of the
+module's config block on that mesh.  Bars as in the default-branch parity
+tests: fields within relative 1e-6, Qsalt to rounding, the erosion flags
+bit-exact."""
+import numpy as np
+import pytest
+
+from chm_gb300 import capi, synth
+from chm_gb300.pbsm3d import PBSM3D
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-6
+FIELDS = ("c", "Qsalt", "Qsusp", "Qsubl", "Qsubl_mass", "drift_mass", "sum_drift", "sum_subl",
+          "blowingsnow_probability")
+L = 6
+
+
+def relerr(a, b):
+    scale = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / scale)
+
+
+def veg_workload(seed, wind=10.0):
+    w = synth.Workload(1536, 3000.0, seed=seed, wind_scale=wind)
+    n = w.mesh.n_faces
+    rng = np.random.default_rng(seed + 1000)
+    # canopy from 0.3 m below to 0.25 m above the snow surface (cutoff 0.3 m)
+    w.mesh.canopy_height = np.maximum(0.0, w.depth + rng.uniform(-0.3, 0.25, n))
+    w.mesh.lai = rng.uniform(0.5, 3.0, n)
+    return w
+
+
+def forcing(w, step, seed=0):
+    f = w.forcing(step).arrays()
+    rng = np.random.default_rng([seed, step])
+    f["fetch"] = rng.uniform(50.0, 1500.0, w.mesh.n_faces)
+    f["p_snow_hours"] = rng.uniform(1.0, 48.0, w.mesh.n_faces)
+    return f
+
+
+def module_cfg(cfg):
+    return {"nLayer": str(L), **{k: ("true" if v is True else "false" if v is False else str(v))
+                                 for k, v in cfg.items()}}
+
+
+def oracle_cfg(cfg):
+    return {k: (int(v) if isinstance(v, bool) else float(v)) for k, v in cfg.items()}
+
+
+def check(out, ref, tag):
+    for k in FIELDS:
+        assert relerr(out[k], ref[k]) < FIELD_TOL, (tag, k, relerr(out[k], ref[k]))
+    assert relerr(out["Qsalt"], ref["Qsalt"]) < 1e-12, tag
+    np.testing.assert_array_equal(out["pbsm_more_than_avail"], ref["pbsm_more_than_avail"])
+
+
+BRANCHES = {
+    "z0_ustar_coupling": {"z0_ustar_coupling": True},
+    "iterative_subl": {"iterative_subl": True},
+    "both": {"z0_ustar_coupling": True, "iterative_subl": True},
+    "coupling_pomeroy_lambda": {"z0_ustar_coupling": True, "use_R94_lambda": False},
+    "exp_fetch": {"use_exp_fetch": True, "use_tanh_fetch": False},
+    "no_fetch": {"use_tanh_fetch": False},
+    "pomli_probability": {"use_PomLi_probability": True, "use_tanh_fetch": False},
+    "rouault": {"rouault_diffusion_coef": True},
+    "no_lateral_diff": {"do_lateral_diff": False},
+    "no_sublimation": {"do_sublimation": False},
+    "fixed_settling": {"do_fixed_settling": True, "settling_velocity": 0.3},
+    "pomeroy_lambda": {"use_R94_lambda": False},
+    "no_veg": {"enable_veg": False},
+    "thresholds": {"cutoff": 0.15, "min_sd_trans": 0.3, "snow_diffusion_const": 0.5, "smooth_coeff": 2000.0},
+}
+
+
+@pytest.mark.parametrize("name", list(BRANCHES))
+def test_branch_matches_oracle(cuda_lib, oracle_lib, name):
+    from oracle import pyoracle
+    cfg = BRANCHES[name]
+    w = veg_workload(71)
+    f = forcing(w, 0)
+    m = PBSM3D(module_cfg(cfg))
+    m.init(w.mesh)
+    out = m.run(f, 3600.0, want_c=True)
+    assert m.last_stats["susp_rel_residual"] <= 1e-8
+    ref, _ = pyoracle.Oracle(w.mesh, nLayer=L, cfg=oracle_cfg(cfg)).step_exact(f, 3600.0)
+    check(out, ref, name)
+    m.close()
+
+
+def test_coupling_changes_the_answer(cuda_lib):
+    """The coupled branch is taken: with vegetation in the snow, u* and z0
+    from Li and Pomeroy eqns 4-5 move the saltation flux off the default's."""
+    w = veg_workload(72)
+    f = forcing(w, 0)
+    res = []
+    for cfg in ({}, {"z0_ustar_coupling": True}):
+        m = PBSM3D(module_cfg(cfg))
+        m.init(w.mesh)
+        res.append(m.run(f, 3600.0, want_c=True))
+        m.close()
+    assert relerr(res[1]["Qsalt"], res[0]["Qsalt"]) > 1e-3
+    assert relerr(res[1]["c"], res[0]["c"]) > 1e-3
+
+
+@pytest.mark.parametrize("solver", [{}, {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1}],
+                         ids=["host", "graph_mixed"])
+def test_branches_over_steps(cuda_lib, oracle_lib, solver):
+    """Both branches on, three hourly steps with drift_mass fed back into the
+    snow state and the module's sums carried."""
+    from oracle import pyoracle
+    cfg = {"z0_ustar_coupling": True, "iterative_subl": True}
+    wg, wo = veg_workload(73), veg_workload(73)
+    m = PBSM3D(module_cfg(cfg))
+    m.init(wg.mesh, **solver)
+    o = pyoracle.Oracle(wo.mesh, nLayer=L, cfg=oracle_cfg(cfg))
+    for s in range(3):
+        fg, fo = forcing(wg, s), forcing(wo, s)
+        out = m.run(fg, 3600.0, want_c=True)
+        ref, _ = o.step_exact(fo, 3600.0)
+        check(out, ref, s)
+        # both fed the oracle's drift, so that the inputs stay identical
+        wg.apply_drift(ref["drift_mass"])
+        wo.apply_drift(ref["drift_mass"])
+    m.close()

@@ -268,3 +268,95 @@ def test_mlp_oracle_gradients(oracle_lib):
         Wm[li][o_, k_] -= h
         fd = (loss(Wp, False) - loss(Wm, False)) / (2 * h)
         assert abs(fd - G[li][o_, k_]) <= 1e-3 * max(1.0, abs(fd)), (li, fd, G[li][o_, k_])
+
+
+def _ustar_g(u2, lam, u):
+    return u2 * 0.4 / math.log(2.0 / (0.6131702345e-2 * u * u + 0.5 * lam)) - u
+
+
+def test_coupled_ustar_root(oracle_lib):
+    """z0_ustar_coupling's u* (Li and Pomeroy 2000 eqn 5, PBSM3D.cpp:691-712)
+    against scipy's brentq on the physical root: the first sign change of the
+    falling g(u) = u2 kappa / log(2/(c u^2 + lambda/2)) - u above 0.  The
+    reference's TOMS 748 midpoint lies within 5e-9 of the same root."""
+    from scipy.optimize import brentq
+    out = C.c_double()
+    for u2 in (0.3, 1.0, 3.0, 7.5, 12.0, 20.0, 30.0):
+        for lam in (0.0, 0.01, 0.2, 1.0):
+            assert oracle_lib.oracle_coupled_ustar(u2, lam, C.byref(out)) == 1
+            # bracket the first sign change on a fine grid below the pole of g
+            grid = np.geomspace(1e-6, 50.0, 20000)
+            vals = np.array([_ustar_g(u2, lam, u) for u in grid])
+            k = int(np.argmax(vals < 0))
+            r = brentq(lambda u: _ustar_g(u2, lam, u), grid[k - 1], grid[k], xtol=1e-15, rtol=1e-15)
+            assert abs(out.value - r) <= 1e-13 * r, (u2, lam, out.value, r)
+
+
+def test_coupled_ustar_edges(oracle_lib):
+    out = C.c_double()
+    # no wind: g(u) = -u everywhere, the walk descends to the root 0
+    assert oracle_lib.oracle_coupled_ustar(0.0, 0.1, C.byref(out)) == 1
+    assert 0.0 <= out.value < 1e-300
+    # lambda/2 > 2: the logarithm is negative everywhere, g < 0, root 0
+    assert oracle_lib.oracle_coupled_ustar(5.0, 5.0, C.byref(out)) == 1
+    assert 0.0 <= out.value < 1e-300
+    # NaN wind: no sign change within the 500 evaluations, u* keeps its placeholder
+    assert oracle_lib.oracle_coupled_ustar(float("nan"), 0.1, C.byref(out)) == 0
+
+
+def _ice_bulb_newton(T, t, ea, D, lt, L):
+    """The Newton iteration of iterative_subl restated in Python: start at T,
+    stop after the first step no larger than |Ti| 2^-5."""
+    mw, R = 18.01528, 0.00831441
+    rho = mw * ea / (R * t)
+    x, lo, hi = T, -50.0, 0.0
+    for _ in range(100):
+        e = math.exp(17.3 * x / (237.3 + x))
+        sat = 0.611 * mw * e / (R * (x + 273.15) * 1000.0)
+        f = T + D * L * (rho / 1000.0 - sat) / lt - x
+        if f == 0:
+            break
+        df = -D * L * sat * (17.3 * 237.3 / (237.3 + x) ** 2 - 1.0 / (x + 273.15)) / lt - 1.0
+        frm = x
+        step = f / df
+        x = frm - step
+        if x <= lo:
+            step = 0.5 * (frm - lo)
+            x = frm - step
+        elif x >= hi:
+            step = 0.5 * (frm - hi)
+            x = frm - step
+        if step > 0:
+            hi = frm
+        else:
+            lo = frm
+        if not abs(x / 32.0) < abs(step):
+            break
+    return x
+
+
+def test_ice_bulb_temperature(oracle_lib):
+    """iterative_subl's Ti (PBSM3D.cpp:1062-1096): the oracle against the
+    Newton restatement above, and within |Ti|/32 of scipy's root (the loose
+    stopping rule of 6 binary digits)."""
+    from scipy.optimize import brentq
+    rng = np.random.default_rng(3)
+    for _ in range(300):
+        T = rng.uniform(-30, -0.5)
+        rh = rng.uniform(0.4, 1.0)
+        t = T + 273.15
+        es = oracle_lib.oracle_saturated_vapour_pressure(t)
+        ea = rh * es / 1000.0
+        D = 2.06e-5 * (t / 273.15) ** 1.75
+        lt = 0.000063 * t + 0.00673
+        L = 2.838e6
+        Ti = oracle_lib.oracle_ice_bulb_temperature(T, t, ea, D, lt, L)
+        ref = _ice_bulb_newton(T, t, ea, D, lt, L)
+        assert abs(Ti - ref) <= 1e-12 * abs(ref), (T, Ti, ref)
+        mw, R = 18.01528, 0.00831441
+
+        def f(x):
+            return T + D * L * (mw * ea / (R * t) / 1000.0
+                                - 0.611 * mw * math.exp(17.3 * x / (237.3 + x)) / (R * (x + 273.15) * 1000.0)) / lt - x
+        root = brentq(f, -60.0, 5.0)
+        assert abs(Ti - root) <= abs(Ti) / 32.0
