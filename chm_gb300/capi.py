@@ -12,7 +12,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libpbsm3d_cuda.so"
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 OK, ERR_INVALID_ARG, ERR_BAD_MESH, ERR_NAN_INPUT, ERR_NOT_CONVERGED, ERR_CUDA, ERR_UNSUPPORTED, ERR_OOM = (
     0, -1, -2, -3, -4, -5, -6, -7)
 STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "BAD_MESH", -3: "NAN_INPUT", -4: "NOT_CONVERGED", -5: "CUDA",
@@ -48,11 +48,16 @@ class Config(C.Structure):
     ]
 
 
+TPI_FIELDS = ("tpi_mean", "tpi_std", "tpi_neg_frac", "tpi_neg_mean", "tpi_neg_std")
+SUBGRID_OUTPUTS = ("frac_contrib", "frac_contrib_nosnw", "hold_topo", "tpi_lim", "test_int")
+
+
 class MeshDesc(C.Structure):
     _fields_ = [
         ("n_faces", C.c_int64), ("neighbor", _i32p), ("edge_length", _dp), ("edge_normal", _dp), ("area", _dp),
         ("center", _dp), ("has_vegetation", _u8p), ("canopy_height", _dp), ("lai", _dp), ("stalk_number", _dp),
-        ("stalk_diameter", _dp), ("is_water", _u8p),
+        ("stalk_diameter", _dp), ("is_water", _u8p), ("tpi_mean", _dp), ("tpi_std", _dp), ("tpi_neg_frac", _dp),
+        ("tpi_neg_mean", _dp), ("tpi_neg_std", _dp),
     ]
 
 
@@ -67,7 +72,8 @@ class ForcingDesc(C.Structure):
 
 class Outputs(C.Structure):
     _fields_ = [(n, _dp) for n in ("Qsalt", "Qsusp", "Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "sum_drift",
-                                   "pbsm_more_than_avail", "blowingsnow_probability", "c")] + [
+                                   "pbsm_more_than_avail", "blowingsnow_probability", "c", "frac_contrib",
+                                   "frac_contrib_nosnw", "hold_topo", "tpi_lim", "test_int")] + [
                    ("on_device", C.c_int32)]
 
 
@@ -217,4 +223,8 @@ def mesh_desc(mesh, keep: list) -> MeshDesc:
         d.canopy_height = ptr(c64(mesh.canopy_height))
     if mesh.lai is not None:
         d.lai = ptr(c64(mesh.lai))
+    for k in TPI_FIELDS:
+        a = getattr(mesh, k, None)
+        if a is not None:
+            setattr(d, k, ptr(c64(a)))
     return d

@@ -178,8 +178,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "nLayer must be in [1, 64]";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2 || cfg.debug_output) {
-        g_create_error = "use_subgrid_topo(_V2) and debug_output are not implemented";
+    if (cfg.debug_output) {
+        g_create_error = "debug_output is not implemented";
         return PBSM3D_ERR_UNSUPPORTED;
     }
     if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {
@@ -255,6 +255,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     P.mixed = cfg.precision == PBSM3D_MIXED;
     P.z0_ustar_coupling = cfg.z0_ustar_coupling != 0;
     P.iterative_subl = cfg.iterative_subl != 0;
+    P.subgrid = (cfg.use_subgrid_topo ? 1 : 0) | (cfg.use_subgrid_topo_V2 ? 2 : 0);
+    c.asm_kernels = P.subgrid ? 4 : 3;
     c.member_offsets = offsets;
     const int nm = (int)members.size();
 
@@ -322,6 +324,13 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         S.sum_drift = sbuf + 6 * Tp;
         S.more = sbuf + 7 * Tp;
         S.bsp = sbuf + 8 * Tp;
+    }
+    S.sub = nullptr;
+    c.sg = Subgrid{};
+    if (P.subgrid) {
+        S.sub = dalloc<double>(c, (size_t)SG_COUNT * Tp, ok);
+        c.sg.tpi = dalloc<double>(c, 5 * Tp, ok);
+        c.sg.I0 = dalloc<double>(c, Tp, ok);
     }
     Susp& A = c.A;
     A.band = dalloc<double>(c, 6 * R, ok);
@@ -497,6 +506,18 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     rc |= upload(c, S.bsp, nanv.data(), Tp * 8);
     rc |= upload(c, Fo.fetch, std::vector<double>(Tp, 1000.0).data(), Tp * 8);
     rc |= upload(c, Fo.psh, zero.data(), Tp * 8);
+    if (P.subgrid) {
+        // TPI statistics, NaN where the mesh has none; outputs start at -9999
+        std::vector<double> tpi(5 * Tp, NAN);
+        const double* src[5] = {mesh->tpi_mean, mesh->tpi_std, mesh->tpi_neg_frac, mesh->tpi_neg_mean,
+                                mesh->tpi_neg_std};
+        for (int k = 0; k < 5; ++k)
+            if (src[k]) std::copy(src[k], src[k] + T, tpi.begin() + k * Tp);
+        rc |= upload(c, c.sg.tpi, tpi.data(), 5 * Tp * 8);
+        std::vector<double> sub((size_t)SG_COUNT * Tp, -9999.0);
+        rc |= upload(c, S.sub, sub.data(), sub.size() * 8);
+        rc |= subgrid_init(c, c.stream);
+    }
     if (cudaMemsetAsync(c.sc, 0, 4 * sizeof(Scalars), c.stream) != cudaSuccess) rc = 1;
     if (cudaMemsetAsync(A.x, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
     if (cudaMemsetAsync(c.x_prev, 0, R * 8, c.stream) != cudaSuccess) rc = 1;
@@ -536,7 +557,7 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
     std::vector<int64_t> off(n_members + 1, 0);
     // vegetation is a per-domain switch in the reference (PBSM3D.cpp:283-325):
     // the members must agree on it
-    bool veg = true, lai = false, sn = false, sd = false, water = false;
+    bool veg = true, lai = false, sn = false, sd = false, water = false, tpi_any[5] = {false, false, false, false, false};
     for (int m = 0; m < n_members; ++m) {
         const pbsm3d_mesh_desc& d = meshes[m];
         if (d.n_faces <= 0 || !d.neighbor || !d.edge_length || !d.edge_normal || !d.area || !d.center) {
@@ -556,6 +577,8 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
         sn = sn || d.stalk_number;
         sd = sd || d.stalk_diameter;
         water = water || d.is_water;
+        const double* tp[5] = {d.tpi_mean, d.tpi_std, d.tpi_neg_frac, d.tpi_neg_mean, d.tpi_neg_std};
+        for (int k = 0; k < 5; ++k) tpi_any[k] = tpi_any[k] || tp[k];
     }
     const int64_t T = off[n_members];
     std::vector<int32_t> nb(3 * T);
@@ -566,6 +589,9 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
     if (veg && sn) sN.assign(T, 1.0);
     if (veg && sd) sD.assign(T, 0.8);
     if (water) wat.assign(T, 0);
+    std::vector<double> tpi[5];
+    for (int k = 0; k < 5; ++k)
+        if (tpi_any[k]) tpi[k].assign(T, NAN);
     for (int m = 0; m < n_members; ++m) {
         const pbsm3d_mesh_desc& d = meshes[m];
         const int64_t o = off[m], n = d.n_faces;
@@ -586,6 +612,9 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
         if (veg && sn && d.stalk_number) std::copy(d.stalk_number, d.stalk_number + n, sN.begin() + o);
         if (veg && sd && d.stalk_diameter) std::copy(d.stalk_diameter, d.stalk_diameter + n, sD.begin() + o);
         if (water && d.is_water) std::copy(d.is_water, d.is_water + n, wat.begin() + o);
+        const double* tp[5] = {d.tpi_mean, d.tpi_std, d.tpi_neg_frac, d.tpi_neg_mean, d.tpi_neg_std};
+        for (int k = 0; k < 5; ++k)
+            if (tp[k]) std::copy(tp[k], tp[k] + n, tpi[k].begin() + o);
     }
     pbsm3d_mesh_desc u{};
     u.n_faces = T;
@@ -600,6 +629,11 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
     u.stalk_diameter = sD.empty() ? nullptr : sD.data();
     u.has_vegetation = nullptr;
     u.is_water = wat.empty() ? nullptr : wat.data();
+    u.tpi_mean = tpi[0].empty() ? nullptr : tpi[0].data();
+    u.tpi_std = tpi[1].empty() ? nullptr : tpi[1].data();
+    u.tpi_neg_frac = tpi[2].empty() ? nullptr : tpi[2].data();
+    u.tpi_neg_mean = tpi[3].empty() ? nullptr : tpi[3].data();
+    u.tpi_neg_std = tpi[4].empty() ? nullptr : tpi[4].data();
     std::vector<Member> mp(n_members);
     for (int m = 0; m < n_members; ++m)
         mp[m] = Member{members[m].ustar_th_scale, members[m].z0_snow, members[m].settling_scale,
@@ -894,6 +928,14 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         for (int k = 0; k < 9; ++k) {
             if ((rc = copy_out(c, outs[k], srcs[k], od))) return rc;
             if (outs[k] && !od) d2h += c.P.T * 8;
+        }
+        if (c.S.sub) {
+            double* souts[5] = {out->hold_topo, out->frac_contrib, out->frac_contrib_nosnw, out->tpi_lim, out->test_int};
+            const int rows[5] = {SG_HOLD, SG_FRAC, SG_NOSNW, SG_TPILIM, SG_TESTINT};
+            for (int k = 0; k < 5; ++k) {
+                if ((rc = copy_out(c, souts[k], c.S.sub + (size_t)rows[k] * c.P.Tp, od))) return rc;
+                if (souts[k] && !od) d2h += c.P.T * 8;
+            }
         }
         if (out->c) {
             // layer-major with stride n_faces (the device stride is the padded Tp)

@@ -49,6 +49,7 @@ struct Params {
     double cos_pi_4, Lc_tanh, log_2_0002;
     int mixed;
     int z0_ustar_coupling, iterative_subl;  // the reference's non-default branches
+    int subgrid;  // bit 0: use_subgrid_topo, bit 1: use_subgrid_topo_V2
     const MathTables* mt;  // exp/log tables (device)
 };
 
@@ -77,6 +78,18 @@ struct Forcing {
 struct FaceState {
     uint8_t* saltation;
     double *Qsalt, *Qsusp, *Qsubl, *Qsubl_mass, *sum_subl, *drift_mass, *sum_drift, *more, *bsp;
+    double* sub;  // [SG_COUNT][Tp] subgrid results, NULL unless a subgrid branch is on
+};
+
+// Subgrid topography results per face, rows of FaceState::sub: the holding
+// capacity that gates saltation (min_sd_trans_avg, output "hold_topo"), the
+// contributing fraction that scales c_salt, and the other outputs.
+enum SubgridValue { SG_HOLD, SG_FRAC, SG_NOSNW, SG_TPILIM, SG_TESTINT, SG_COUNT };
+
+// Static inputs of the subgrid branches (device).
+struct Subgrid {
+    double* tpi;        // [5][Tp] TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean, TPI_neg_std (NaN = undefined)
+    double* I0;         // [Tp] normalisation integral of the filling function (use_subgrid_topo_V2)
 };
 
 // Height-dependent coefficients of one layer (see cz_coeffs in physics.cu).
@@ -200,6 +213,10 @@ void launch_member_mask_norm(Ctx& c, cudaStream_t s, int which);
 void launch_member_zero(Ctx& c, cudaStream_t s, double* x);
 void launch_consume_drift(Ctx& c, cudaStream_t s);
 
+// subgrid.cu
+void launch_subgrid(Ctx& c, cudaStream_t s);
+int subgrid_init(Ctx& c, cudaStream_t s);
+
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 // graph mode: the device part of a step as one CUDA-graph launch (built on
@@ -225,6 +242,8 @@ struct Ctx {
     Faces F;
     Forcing Fo;
     FaceState S;
+    Subgrid sg;
+    int asm_kernels = 3;  // kernels of one suspension assembly (4 with a subgrid branch)
     Susp A;
     Dep D;
     Members Mb;

@@ -23,6 +23,7 @@
 #include <math.h>
 
 #include "pbsm3d_internal.cuh"
+#include "roots.cuh"
 
 namespace pbsm {
 namespace {
@@ -114,75 +115,19 @@ __device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double 
     o.cz = cz;
 }
 
-__device__ __forceinline__ int sgn(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
-
 // z0_ustar_coupling (PBSM3D.cpp:691-712): u* over snow with partly buried
 // vegetation, the root of Li and Pomeroy (2000) eqn 5
 //     g(u) = u2 kappa / log(2 / (c u^2 + lambda/2)) - u,  c = 0.6131702345e-2,
-// which falls with u.  The bracket comes from the walk of the reference's
-// bracket_and_solve_root(g, 1, factor 1, falling, 500 evaluations): from u = 1
-// up when g(1) >= 0 (or NaN), else down, by a factor that is 1 for the first
-// 31 moves (which stay at u = 1 and are skipped here), doubles at the 32nd
-// and then after 16, 8, 4, 2 more moves and at every move after that; a
-// downward walk that passes below DBL_MIN brackets the root 0.  The root is
-// then refined to full precision by Newton steps kept inside the bracket,
-// bisecting when a step leaves it (the reference stops its TOMS 748 at a
-// bracket narrower than 1e-8 and takes the midpoint).  At most 500
-// evaluations in the walk and 100 refinement steps.  false: no bracket.
+// which falls with u, from guess 1 (roots.cuh).  false: no bracket.
 __device__ bool coupled_ustar(double u2, double lambda, const MathTables& mt, double& ustar) {
     const double c = 0.6131702345e-2, A = u2 * kKappa, h = .5 * lambda;
     auto g = [&](double u) { return div_t(A, log_t(div_t(2.0, c * u * u + h), mt)) - u; };
-    double a = 1.0, b = 1.0;
-    double fa = g(a), fb = fa;
-    const bool up = !(fa < 0);
-    double factor = 2.0;
-    int every = 16;
-    for (int s = 32; sgn(fa) == sgn(fb); ++s) {
-        if (!up && fabs(a) < 2.2250738585072014e-308) {
-            ustar = a / 2.0;
-            return true;
-        }
-        if (s >= 500) return false;
-        if (s > 32 && s % every == 0) {
-            factor *= 2;
-            if (every > 1) every /= 2;
-        }
-        if (up) {
-            a = b;
-            fa = fb;
-            b *= factor;
-            fb = g(b);
-        } else {
-            b = a;
-            fb = fa;
-            a /= factor;
-            fa = g(a);
-        }
-    }
-    if (fa == 0) { ustar = a; return true; }
-    if (fb == 0) { ustar = b; return true; }
-    double lo = a, flo = fa, hi = b;
-    double x = 0.5 * (lo + hi);
-    for (int it = 0; it < 100; ++it) {
-        const double q = c * x * x + h;
+    auto dg = [&](double u) {
+        const double q = c * u * u + h;
         const double ell = log_t(div_t(2.0, q), mt);
-        const double fx = div_t(A, ell) - x;
-        if (fx == 0) break;
-        if (sgn(fx) == sgn(flo)) {
-            lo = x;
-            flo = fx;
-        } else {
-            hi = x;
-        }
-        const double d = div_t(A * (2.0 * c * x), q * ell * ell) - 1.0;
-        double xn = x - div_t(fx, d);
-        if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
-        const bool done = fabs(xn - x) <= 1e-15 * fabs(xn);
-        x = xn;
-        if (done) break;
-    }
-    ustar = x;
-    return true;
+        return div_t(A * (2.0 * c * u), q * ell * ell) - 1.0;
+    };
+    return bracket_solve(g, dg, 1.0, false, ustar);
 }
 
 // iterative_subl (PBSM3D.cpp:1062-1096): the ice-bulb temperature Ti (C),
@@ -275,7 +220,9 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                 __dadd_rn(__dadd_rn(0.35, __dmul_rn(1.0 / 150.0, T_c)), __dmul_rn(__dmul_rn(1.0 / 8200.0, T_c), T_c));
             uth = __dmul_rn(uth, mp.uth_scale);
             const double stalkN = G.stalkN[i], stalkD = G.stalkD[i];
-            if (height_diff <= P.cutoff && snow_depth >= P.min_sd_trans && !G.water[i]) {
+            // PBSM3D.cpp:480-645: the subgrid holding capacity and contributing fraction
+            const double min_sd_trans_avg = P.subgrid ? S.sub[SG_HOLD * Tp + i] : P.min_sd_trans;
+            if (height_diff <= P.cutoff && snow_depth >= min_sd_trans_avg && !G.water[i]) {
                 if (P.use_R94_lambda)
                     lambda = 0.5 * G.lai[i] * height_diff;
                 else
@@ -343,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                     S.bsp[i] = Pu10;
                     c_salt *= Pu10;
                 }
+                if (P.subgrid) c_salt *= S.sub[SG_FRAC * Tp + i];  // :867-870
                 const double uhs = 2.8 * uth;
                 Qsalt = c_salt * uhs * hs;
                 double mass = 0;
@@ -965,11 +913,12 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     // out; per row 12 doubles out (+6 floats MIXED)
     prof_begin(c, s);
     cudaMemsetAsync(c.A.n_slow, 0, sizeof(int), s);
+    if (c.P.subgrid) launch_subgrid(c, s);
     k_salt_faces<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
     k_salt_rows<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Fo, c.A, c.Mb);
     k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
     prof_end(c, s, PBSM3D_K_ASSEMBLE, T * (64 + 133 + 9) + rows * (96 + (c.P.mixed ? 24 : 0)));
-    c.launches += 2;
+    c.launches += c.asm_kernels;
 }
 
 void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {

@@ -1690,7 +1690,7 @@ __device__ void ctl_build_act(const Tiles& tl, int32_t* act, int* nact, const in
 }
 
 // After the suspension assembly: NaN check, per-member "present" tests.
-__global__ void k_ctl_begin(StepCtl* ctl, const Scalars* sc0, Members Mb, int n, Handles h) {
+__global__ void k_ctl_begin(StepCtl* ctl, const Scalars* sc0, Members Mb, int n, int asm_kernels, Handles h) {
     if (threadIdx.x != 0) return;
     const bool nan = sc0->nan_flag != 0.0;
     bool any = false;
@@ -1709,7 +1709,7 @@ __global__ void k_ctl_begin(StepCtl* ctl, const Scalars* sc0, Members Mb, int n,
     ctl->dep_present = 0;
     ctl->susp_rhs_max = sc0->rhs_max;
     ctl->sweep = ctl->susp_iters = ctl->dep_iters = ctl->dep_sweeps = ctl->guard = 0;
-    ctl->kernels = 4 + (n > 1 ? 1 : 0);  // three assembly passes, this, the member mask
+    ctl->kernels = asm_kernels + 1 + (n > 1 ? 1 : 0);  // the assembly passes, this, the member mask
     ctl->susp_relres = ctl->dep_relres = ctl->gamma_sum = 0.0;
     hset(h, H_OK1, nan ? 0u : 1u);
     hset(h, H_SUSP, (!nan && any) ? 1u : 0u);
@@ -2296,7 +2296,7 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
             cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s);
         }
         launch_assemble_suspension(c, s);
-        k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, h);
+        k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, c.asm_kernels, h);
         if (c.Mb.n > 1) launch_member_mask_norm(c, s, 0);
         CondBody ok1;
         bad |= ok1.begin(s, G.cap[1], h.h[H_OK1], cudaGraphCondTypeIf);

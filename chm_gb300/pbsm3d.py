@@ -183,7 +183,7 @@ class PBSM3D:
             keep.append(a)
             setattr(f, k, capi.ptr(a))
         f.on_device = 0
-        out = outputs if outputs is not None else {k: np.empty(n) for k in OUTPUT_KEYS}
+        out = outputs if outputs is not None else {k: np.empty(n) for k in self.output_keys()}
         if want_c and "c" not in out:
             out["c"] = np.empty(self.nLayer * n)
         o = capi.Outputs()
@@ -196,6 +196,17 @@ class PBSM3D:
             self._error(rc, "pbsm3d_step")
         self.last_stats = st.as_dict()
         return out
+
+    def output_keys(self) -> tuple:
+        """The per-face outputs a step writes: the provides list of
+        PBSM3D.cpp:188-218 that carries values (test_err is provided but never
+        written by the reference)."""
+        keys = list(OUTPUT_KEYS)
+        if self.use_subgrid_topo:
+            keys += ["frac_contrib", "frac_contrib_nosnw", "hold_topo"]
+        if self.use_subgrid_topo_V2:
+            keys += [k for k in ("frac_contrib", "hold_topo", "tpi_lim", "test_int") if k not in keys]
+        return tuple(keys)
 
     def set_snow(self, swe, depth, drift_density: float = 300.0):
         """Keep swe and snow depth on the device: later run() calls without

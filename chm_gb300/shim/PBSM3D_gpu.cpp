@@ -36,6 +36,12 @@ PBSM3D::PBSM3D(config_file c) : module_base("PBSM3D", parallel::domain, c) {
         depends("p_snow_hours");
     provides("blowingsnow_probability");
     for (const char* v : {"Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "Qsusp", "Qsalt", "sum_drift"}) provides(v);
+    use_subgrid_topo = cfg.get("use_subgrid_topo", false);
+    use_subgrid_topo_V2 = cfg.get("use_subgrid_topo_V2", false);
+    if (use_subgrid_topo)  // PBSM3D.cpp:204-209
+        for (const char* v : {"frac_contrib", "frac_contrib_nosnw", "hold_topo"}) provides(v);
+    if (use_subgrid_topo_V2)  // :211-218
+        for (const char* v : {"frac_contrib", "hold_topo", "test_int", "test_err", "tpi_lim"}) provides(v);
     pbsm3d_config_defaults(&gpu_cfg);
 }
 
@@ -64,8 +70,8 @@ void PBSM3D::init(mesh& domain) {
     g.use_tanh_fetch = use_tanh_fetch;
     g.use_PomLi_probability = use_PomLi_probability;
     g.z0_ustar_coupling = cfg.get("z0_ustar_coupling", false);
-    g.use_subgrid_topo = cfg.get("use_subgrid_topo", false);
-    g.use_subgrid_topo_V2 = cfg.get("use_subgrid_topo_V2", false);
+    g.use_subgrid_topo = use_subgrid_topo;
+    g.use_subgrid_topo_V2 = use_subgrid_topo_V2;
     g.use_R94_lambda = cfg.get("use_R94_lambda", true);
     g.debug_output = cfg.get("debug_output", false);
     // this library's solver switch (not a reference key): "solver.mixed": "true"
@@ -84,6 +90,11 @@ void PBSM3D::init(mesh& domain) {
     d.stalk_number = m.stalk_number.empty() ? nullptr : m.stalk_number.data();
     d.stalk_diameter = m.stalk_diameter.empty() ? nullptr : m.stalk_diameter.data();
     d.is_water = m.is_water.empty() ? nullptr : m.is_water.data();
+    d.tpi_mean = m.tpi_mean.empty() ? nullptr : m.tpi_mean.data();
+    d.tpi_std = m.tpi_std.empty() ? nullptr : m.tpi_std.data();
+    d.tpi_neg_frac = m.tpi_neg_frac.empty() ? nullptr : m.tpi_neg_frac.data();
+    d.tpi_neg_mean = m.tpi_neg_mean.empty() ? nullptr : m.tpi_neg_mean.data();
+    d.tpi_neg_std = m.tpi_neg_std.empty() ? nullptr : m.tpi_neg_std.data();
     pbsm3d_destroy(ctx_);
     ctx_ = nullptr;
     check(pbsm3d_create(&d, &g, &ctx_), "PBSM3D init");
@@ -118,6 +129,15 @@ void PBSM3D::run(mesh& domain) {
     double** oslots[9] = {&o.Qsalt, &o.Qsusp, &o.Qsubl, &o.Qsubl_mass, &o.sum_subl, &o.drift_mass, &o.sum_drift,
                           &o.pbsm_more_than_avail, &o.blowingsnow_probability};
     for (int k = 0; k < 9; ++k) *oslots[k] = m.var(kOutputs[k]).data();
+    if (use_subgrid_topo || use_subgrid_topo_V2) {
+        o.frac_contrib = m.var("frac_contrib").data();
+        o.hold_topo = m.var("hold_topo").data();
+    }
+    if (use_subgrid_topo) o.frac_contrib_nosnw = m.var("frac_contrib_nosnw").data();
+    if (use_subgrid_topo_V2) {
+        o.tpi_lim = m.var("tpi_lim").data();
+        o.test_int = m.var("test_int").data();
+    }
     o.on_device = 0;
     check(pbsm3d_step(ctx_, &f, (double)dt, &o, &last_stats), "PBSM3D run");
 }

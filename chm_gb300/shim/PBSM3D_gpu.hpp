@@ -24,7 +24,7 @@ class PBSM3D : public module_base {
 
    private:
     void check(int rc, const char* what) const;
-    bool use_exp_fetch, use_tanh_fetch, use_PomLi_probability;
+    bool use_exp_fetch, use_tanh_fetch, use_PomLi_probability, use_subgrid_topo, use_subgrid_topo_V2;
     pbsm3d_ctx* ctx_ = nullptr;
     std::vector<double> f_[9], o_[9];
 };

@@ -70,6 +70,8 @@ class mesh_store {
     std::vector<double> area;             // [n]
     std::vector<double> center;           // [3n]
     std::vector<double> canopy_height, lai, stalk_number, stalk_diameter;  // vegetation parameters or empty
+    // subgrid parameters TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean, TPI_neg_std, or empty
+    std::vector<double> tpi_mean, tpi_std, tpi_neg_frac, tpi_neg_mean, tpi_neg_std;
     std::vector<uint8_t> is_water;
     // per-face variables ((*face)["name"_s]); created on first use at -9999
     std::vector<double>& var(const std::string& name) {

@@ -47,6 +47,13 @@ class Mesh:
     center: np.ndarray     # [nt, 3]
     canopy_height: np.ndarray | None = None
     lai: np.ndarray | None = None
+    # subgrid TPI statistics (mesh parameters TPI_mean, TPI_std, TPI_neg_frac,
+    # TPI_neg_mean, TPI_neg_std), None = undefined
+    tpi_mean: np.ndarray | None = None
+    tpi_std: np.ndarray | None = None
+    tpi_neg_frac: np.ndarray | None = None
+    tpi_neg_mean: np.ndarray | None = None
+    tpi_neg_std: np.ndarray | None = None
 
     @property
     def n_faces(self) -> int:

@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PBSM3D_ABI_VERSION 1
+#define PBSM3D_ABI_VERSION 2
 
 enum pbsm3d_status {
     PBSM3D_OK = 0,
@@ -93,8 +93,8 @@ typedef struct pbsm3d_config {
     int32_t use_tanh_fetch;         /* "use_tanh_fetch" true */
     int32_t use_PomLi_probability;  /* "use_PomLi_probability" false */
     int32_t z0_ustar_coupling;      /* "z0_ustar_coupling" false */
-    int32_t use_subgrid_topo;       /* "use_subgrid_topo" false (true: UNSUPPORTED) */
-    int32_t use_subgrid_topo_V2;    /* "use_subgrid_topo_V2" false (true: UNSUPPORTED) */
+    int32_t use_subgrid_topo;       /* "use_subgrid_topo" false */
+    int32_t use_subgrid_topo_V2;    /* "use_subgrid_topo_V2" false */
     int32_t use_R94_lambda;         /* "use_R94_lambda" true */
     int32_t debug_output;           /* "debug_output" false (true: UNSUPPORTED) */
     double settling_velocity;       /* "settling_velocity" 0.5 m/s, must be >= 0 */
@@ -152,6 +152,16 @@ typedef struct pbsm3d_mesh_desc {
     const double* stalk_number;    /* [n] "stalk_number" or NULL (default 1) */
     const double* stalk_diameter;  /* [n] "stalk_diameter" or NULL (default 0.8) */
     const uint8_t* is_water;       /* [n] landcover is_water flag or NULL */
+    /* Subgrid topographic-position-index statistics, the mesh parameters
+     * read by use_subgrid_topo_V2 (TPI_mean, TPI_std; PBSM3D.cpp:494-498) and
+     * use_subgrid_topo (TPI_neg_frac, TPI_neg_mean, TPI_neg_std; :607-613).
+     * NULL, NaN or -9999 on a face: the parameter is undefined there and the
+     * branch keeps its defaults for that face. */
+    const double* tpi_mean;        /* [n] "TPI_mean" or NULL */
+    const double* tpi_std;         /* [n] "TPI_std" or NULL */
+    const double* tpi_neg_frac;    /* [n] "TPI_neg_frac" or NULL */
+    const double* tpi_neg_mean;    /* [n] "TPI_neg_mean" or NULL */
+    const double* tpi_neg_std;     /* [n] "TPI_neg_std" or NULL */
 } pbsm3d_mesh_desc;
 
 /*
@@ -195,6 +205,16 @@ typedef struct pbsm3d_outputs {
     double* pbsm_more_than_avail;
     double* blowingsnow_probability;
     double* c;
+    /* provided with use_subgrid_topo / use_subgrid_topo_V2 (PBSM3D.cpp:204-218):
+     * frac_contrib and hold_topo with either, frac_contrib_nosnw with
+     * use_subgrid_topo, tpi_lim and test_int with use_subgrid_topo_V2.
+     * test_int keeps its previous value (from -9999) on faces where the
+     * normalisation integral is not evaluated. */
+    double* frac_contrib;
+    double* frac_contrib_nosnw;
+    double* hold_topo;
+    double* tpi_lim;
+    double* test_int;
     int32_t on_device;
 } pbsm3d_outputs;
 

@@ -93,40 +93,39 @@ double std_dry_air_density(double altitude, double temperature) {
 
 inline int sgn(double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); }
 
-// z0_ustar_coupling (PBSM3D.cpp:691-712): the friction velocity over snow
-// with partly buried vegetation is the root of Li and Pomeroy (2000) eqn 5,
-//     g(u) = u2 kappa / log(2 / (c u^2 + lambda/2)) - u,  c = 0.6131702345e-2,
-// which falls with u.  The reference calls Boost 1.85.0's (spack.yaml)
-// bracket_and_solve_root(g, guess 1, factor 1, falling, |a - b| < 1e-8,
-// 500 evaluations) and takes the midpoint of the final bracket; when no
-// bracket is found it throws and u* keeps its 1.3 placeholder.
+// The root finder of the reference's two bracket_and_solve_root calls
+// (PBSM3D.cpp:557, 708): Boost 1.85.0's (spack.yaml) bracket_and_solve_root(
+// f, guess, factor 1, rising, |a - b| < 1e-8, 500 evaluations), which walks
+// from the guess until f changes sign and then runs TOMS 748 on the bracket,
+// returning the bracket whose midpoint the reference takes; when no bracket
+// is found it throws and the caller keeps its default.
 //
-// Restated: the same bracketing walk -- from u = 1 up when g(1) >= 0 (or
-// NaN), else down, multiplying or dividing by a factor that is 1 at first and
-// doubles at the 32nd move, then after 16, 8, 4, 2 more and at every move
-// after that; a downward walk that passes below DBL_MIN returns the bracket
-// (0, u) -- and the root of the bracket refined to full precision by
+// Restated: the same walk -- away from zero (b *= factor) when f(guess) has
+// the sign that puts the root there ((f < 0) == (guess < 0 ? !rising :
+// rising)), else towards it (a /= factor), by a factor that is 1 at first and
+// doubles at the 32nd move, then after 16, 8, 4, 2 more moves and at every
+// move after that; a walk towards zero that passes below DBL_MIN returns the
+// bracket (a, 0) -- and the root of the bracket refined to full precision by
 // Newton-Raphson with a bisection fallback (rtsafe, Press et al., Numerical
-// Recipes, section 9.4) in place of TOMS 748.  The reference's midpoint lies
+// Recipes, section 9.4) in place of TOMS 748: the reference's midpoint lies
 // within 5e-9 of that root.  Returns false when the walk fails.
 //
 // Each call gets the full budget of 500 evaluations.  In the reference the
-// budget is an in/out argument shared by the faces of one OpenMP thread
+// budget is an in/out argument shared by all faces of one OpenMP thread
 // (PBSM3D.cpp:422): Boost documents that it returns the evaluations used, so
-// later faces inherit a shrinking budget and its results depend on the thread
+// later faces inherit a shrinking budget and the results depend on the thread
 // count.  That is not restated.
-bool coupled_ustar(double u2, double lambda, double& ustar) {
-    const double c = 0.6131702345e-2;
-    auto g = [&](double u) { return u2 * kKappa / std::log(2.0 / (c * u * u + .5 * lambda)) - u; };
+template <class F, class DF>
+bool bracket_solve(F f, DF df, double guess, bool rising, double& root) {
     const int budget = 500;
-    double a = 1.0, b = 1.0;
-    double fa = g(a), fb = fa;
-    const bool up = !(fa < 0);
+    double a = guess, b = guess;
+    double fa = f(a), fb = fa;
+    const bool away = (fa < 0) == (guess < 0 ? !rising : rising);
     double factor = 1.0;
     int every = 32;
     for (int s = 1; sgn(fa) == sgn(fb); ++s) {
-        if (!up && std::fabs(a) < 2.2250738585072014e-308) {
-            ustar = a / 2.0;
+        if (!away && std::fabs(a) < 2.2250738585072014e-308) {
+            root = a / 2.0;
             return true;
         }
         if (s >= budget) return false;
@@ -134,26 +133,25 @@ bool coupled_ustar(double u2, double lambda, double& ustar) {
             factor *= 2;
             if (every > 1) every /= 2;
         }
-        if (up) {
+        if (away) {
             a = b;
             fa = fb;
             b *= factor;
-            fb = g(b);
+            fb = f(b);
         } else {
             b = a;
             fb = fa;
             a /= factor;
-            fa = g(a);
+            fa = f(a);
         }
     }
-    if (fa == 0) { ustar = a; return true; }
-    if (fb == 0) { ustar = b; return true; }
-    double lo = a, flo = fa, hi = b;
+    if (fa == 0) { root = a; return true; }
+    if (fb == 0) { root = b; return true; }
+    double lo = std::min(a, b), hi = std::max(a, b);
+    double flo = lo == a ? fa : fb;
     double x = 0.5 * (lo + hi);
     for (int it = 0; it < 100; ++it) {
-        const double q = c * x * x + .5 * lambda;
-        const double ell = std::log(2.0 / q);
-        const double fx = u2 * kKappa / ell - x;
+        const double fx = f(x);
         if (fx == 0) break;
         if (sgn(fx) == sgn(flo)) {
             lo = x;
@@ -161,15 +159,236 @@ bool coupled_ustar(double u2, double lambda, double& ustar) {
         } else {
             hi = x;
         }
-        const double d = u2 * kKappa * (2.0 * c * x) / (q * ell * ell) - 1.0;
-        double xn = x - fx / d;
+        double xn = x - fx / df(x);
         if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
         const bool done = std::fabs(xn - x) <= 1e-15 * std::fabs(xn);
         x = xn;
         if (done) break;
     }
-    ustar = x;
+    root = x;
     return true;
+}
+
+// z0_ustar_coupling (PBSM3D.cpp:691-712): the friction velocity over snow
+// with partly buried vegetation is the root of Li and Pomeroy (2000) eqn 5,
+//     g(u) = u2 kappa / log(2 / (c u^2 + lambda/2)) - u,  c = 0.6131702345e-2,
+// which falls with u, found from guess 1.  false: no bracket (u* keeps its
+// 1.3 placeholder).
+bool coupled_ustar(double u2, double lambda, double& ustar) {
+    const double c = 0.6131702345e-2;
+    auto g = [&](double u) { return u2 * kKappa / std::log(2.0 / (c * u * u + .5 * lambda)) - u; };
+    auto dg = [&](double u) {
+        const double q = c * u * u + .5 * lambda;
+        const double ell = std::log(2.0 / q);
+        return u2 * kKappa * (2.0 * c * u) / (q * ell * ell) - 1.0;
+    };
+    return bracket_solve(g, dg, 1.0, false, ustar);
+}
+
+// ---------------------------------------------------- subgrid topography
+inline double smin(double a, double b) { return (b < a) ? b : a; }  // std::min
+
+// gsl_ran_gaussian_pdf(x, sigma) and gsl_cdf_gaussian_Q(x, sigma): the
+// normal density and upper tail.
+double gauss_pdf(double x, double sigma) {
+    const double u = x / sigma;
+    return std::exp(-u * u / 2.0) / (std::sqrt(2.0 * M_PI) * sigma);
+}
+double gauss_Q(double x, double sigma) { return 0.5 * std::erfc(x / (sigma * std::sqrt(2.0))); }
+
+// Regularised incomplete gamma functions P(a, x) and Q(a, x): the series for
+// x < a + 1 and the continued fraction (modified Lentz) otherwise (Press et
+// al., Numerical Recipes, section 6.2).
+void incomplete_gamma(double a, double x, double& P, double& Q) {
+    if (!(x > 0)) {
+        P = 0;
+        Q = 1;
+        return;
+    }
+    const double lpre = -x + a * std::log(x) - std::lgamma(a);
+    if (x < a + 1) {
+        double ap = a, del = 1.0 / a, sum = del;
+        for (int n = 0; n < 100000; ++n) {
+            ap += 1;
+            del *= x / ap;
+            sum += del;
+            if (std::fabs(del) < std::fabs(sum) * 1e-17) break;
+        }
+        P = sum * std::exp(lpre);
+        Q = 1.0 - P;
+    } else {
+        const double tiny = 1e-300;
+        double b = x + 1 - a, cc = 1 / tiny, d = 1 / b, h = d;
+        for (int i = 1; i < 100000; ++i) {
+            const double an = -i * (i - a);
+            b += 2;
+            d = an * d + b;
+            if (std::fabs(d) < tiny) d = tiny;
+            cc = b + an / cc;
+            if (std::fabs(cc) < tiny) cc = tiny;
+            d = 1 / d;
+            const double del = d * cc;
+            h *= del;
+            if (std::fabs(del - 1) < 1e-17) break;
+        }
+        Q = std::exp(lpre) * h;
+        P = 1.0 - Q;
+    }
+}
+// gsl_cdf_gamma_P / _Q (x, shape a, scale b) and gsl_ran_gamma_pdf
+double gamma_P(double x, double a, double b) {
+    double P, Q;
+    incomplete_gamma(a, x / b, P, Q);
+    return P;
+}
+double gamma_Q(double x, double a, double b) {
+    double P, Q;
+    incomplete_gamma(a, x / b, P, Q);
+    return Q;
+}
+double gamma_pdf(double x, double a, double b) {
+    if (x < 0) return 0;
+    if (x == 0) return a == 1 ? 1 / b : (a > 1 ? 0 : INFINITY);
+    return std::exp((a - 1) * std::log(x / b) - x / b - std::lgamma(a)) / b;
+}
+
+// Gauss-Legendre nodes and weights on [-1, 1] (Newton on P_n, Press et al.,
+// Numerical Recipes, section 4.5).
+struct GaussLegendre {
+    double x[20], w[20];
+    GaussLegendre() {
+        const int n = 20;
+        for (int i = 0; i < n; ++i) {
+            long double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0;
+            for (int it = 0; it < 100; ++it) {
+                long double p1 = 1, p2 = 0;
+                for (int j = 0; j < n; ++j) {
+                    const long double p3 = p2;
+                    p2 = p1;
+                    p1 = ((2 * j + 1) * z * p2 - j * p3) / (j + 1);
+                }
+                pp = n * (z * p1 - p2) / (z * z - 1);
+                const long double z1 = z;
+                z = z1 - p1 / pp;
+                if (std::fabs((double)(z - z1)) < 1e-19) break;
+            }
+            x[i] = (double)z;
+            w[i] = (double)(2 / ((1 - z * z) * pp * pp));
+        }
+    }
+};
+const GaussLegendre kGL20;
+
+template <class F>
+double gl20(F f, double a, double b) {
+    const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+    double s = 0;
+    for (int i = 0; i < 20; ++i) s += kGL20.w[i] * f(c + h * kGL20.x[i]);
+    return s * h;
+}
+template <class F>
+double adapt(F f, double a, double b, double whole, double floor, int depth) {
+    const double m = 0.5 * (a + b);
+    const double l = gl20(f, a, m), r = gl20(f, m, b);
+    if (depth >= 40 || std::fabs(l + r - whole) <= std::max(1e-14 * (std::fabs(l) + std::fabs(r)), floor))
+        return l + r;
+    return adapt(f, a, m, l, floor, depth + 1) + adapt(f, m, b, r, floor, depth + 1);
+}
+// The reference integrates with gsl_integration_qags (GSL, version unpinned in
+// spack.yaml; QUADPACK's QAGS) to relative 1e-7.  Here: 20-point
+// Gauss-Legendre on 64 panels, each bisected until its two halves agree with
+// it to relative 1e-14 (or absolute 1e-17 times the integrand's scale); the
+// panels keep a narrow Gaussian from falling between the nodes.  The QAGS
+// result lies within its tolerance of this.
+template <class F>
+double integrate(F f, double a, double b, double scale) {
+    const int panels = 64;
+    double s = 0;
+    for (int k = 0; k < panels; ++k) {
+        const double x0 = a + (b - a) * k / panels, x1 = a + (b - a) * (k + 1) / panels;
+        s += adapt(f, x0, x1, gl20(f, x0, x1), 1e-17 * scale, 0);
+    }
+    return s;
+}
+
+struct SubgridFace {
+    double min_sd_trans_avg, frac_contrib, frac_contrib_nosnw, tpi_lim, test_int;
+    bool have_test_int;
+};
+
+// PBSM3D.cpp:486-645: subgrid topographic holding capacity and contributing
+// fraction of one face.
+SubgridFace subgrid_face(const pbsm3d_config& cfg, double snow_depth, const double tpi[5]) {
+    SubgridFace o{cfg.min_sd_trans, 1.0, 1.0, 0.0, 0.0, false};
+    const double min_sd_trans = cfg.min_sd_trans;
+    if (cfg.use_subgrid_topo_V2) {  // :486-597
+        const double fac_fill = 0.8;
+        double tpi_lim = -min_sd_trans;
+        if (!is_nan(tpi[1])) {
+            const double moy_tpi = smax(-5.0, smin(5.0, tpi[0]));
+            const double std_tpi = smin(5.0, smax(0.1, tpi[1]));
+            if (snow_depth > min_sd_trans) {
+                // the depth-dependent coefficients of :509-537 are declared in
+                // inner scopes and never reach the integrals
+                const double a1 = 1.5, b1 = 0.3, a2 = 0.6, b2 = 0.55;
+                auto fill = [&](double x) {
+                    const double x2 = x + 0.25;
+                    if (x2 <= 0) return (1. - a1 * std::tanh(b1 * x2)) * gauss_pdf(x - moy_tpi, std_tpi);
+                    return (1. - a2 * std::tanh(b2 * x2)) * gauss_pdf(x - moy_tpi, std_tpi);
+                };
+                const double result = integrate(fill, -50, 50, 1.0);
+                o.test_int = result;
+                o.have_test_int = true;
+                auto froot = [&](double xx) {
+                    return (1 - a1 * std::tanh(b1 * (xx + 0.25))) * snow_depth / result + fac_fill * xx;
+                };
+                auto dfroot = [&](double xx) {
+                    const double th = std::tanh(b1 * (xx + 0.25));
+                    return -a1 * b1 * (1 - th * th) * snow_depth / result + fac_fill;
+                };
+                double r;
+                if (bracket_solve(froot, dfroot, -1.0, true, r)) tpi_lim = r;
+                auto fill2 = [&](double x) {
+                    const double x2 = x + 0.25;
+                    if (x2 <= 0) return (1. - a1 * std::tanh(b1 * x2)) * snow_depth / result * gauss_pdf(x - moy_tpi, std_tpi);
+                    return (1. - a2 * std::tanh(b2 * x2)) * snow_depth / result * gauss_pdf(x - moy_tpi, std_tpi);
+                };
+                const double h1 = integrate(fill2, -50, tpi_lim, snow_depth);
+                auto fill3 = [&](double x) { return -fac_fill * x * gauss_pdf(x - moy_tpi, std_tpi); };
+                const double h2 = integrate(fill3, tpi_lim, -min_sd_trans / fac_fill, 5.0);
+                const double h3 = min_sd_trans * gauss_Q(-min_sd_trans / fac_fill - moy_tpi, std_tpi);
+                o.min_sd_trans_avg = smin(h1 + h2 + h3, snow_depth);
+            }
+            o.frac_contrib = gauss_Q(tpi_lim - moy_tpi, std_tpi);
+        }
+        o.tpi_lim = tpi_lim;
+    }
+    if (cfg.use_subgrid_topo) {  // :604-645
+        if (!is_nan(tpi[2])) {
+            const double frac_neg = tpi[2];
+            if (frac_neg > 0.) {
+                const double moy_tpi_neg = smax(-10.0, smin(-0.05, tpi[3]));
+                const double std_tpi_neg = smin(5.0, smax(0.1, tpi[4]));
+                const double shape_gam = std::pow(moy_tpi_neg, 2.0) / std::pow(std_tpi_neg, 2.0);
+                const double scale_gam = -std::pow(std_tpi_neg, 2.0) / moy_tpi_neg;
+                o.frac_contrib = (1. - frac_neg) + frac_neg * gamma_P(snow_depth, shape_gam, scale_gam);
+                o.frac_contrib_nosnw = (1. - frac_neg);
+                if (snow_depth > min_sd_trans) {
+                    const double hint =
+                        shape_gam * scale_gam -
+                        scale_gam * (snow_depth * gamma_pdf(snow_depth, shape_gam, scale_gam) -
+                                     min_sd_trans * gamma_pdf(min_sd_trans, shape_gam, scale_gam) +
+                                     shape_gam * gamma_P(min_sd_trans, shape_gam, scale_gam) +
+                                     shape_gam * gamma_Q(snow_depth, shape_gam, scale_gam));
+                    o.min_sd_trans_avg =
+                        (1. - frac_neg) * min_sd_trans +
+                        frac_neg * (min_sd_trans * gamma_P(min_sd_trans, shape_gam, scale_gam) + hint +
+                                    snow_depth * gamma_Q(snow_depth, shape_gam, scale_gam));
+                }
+            }
+        }
+    }
+    return o;
 }
 
 // iterative_subl (PBSM3D.cpp:1062-1096): the ice-bulb temperature Ti (C) of
@@ -524,6 +743,8 @@ struct oracle_ctx {
     double dt = 0;
     // face variables
     std::vector<double> Qsalt, Qsusp, Qsubl, Qsubl_mass, sum_subl, drift_mass, sum_drift, more_than_avail, bsp;
+    // subgrid TPI parameters [5][T] (NaN = undefined) and the subgrid outputs
+    std::vector<double> tpi, frac_contrib, frac_contrib_nosnw, hold_topo, tpi_lim, test_int;
     System susp, dep;
     bool suspension_present = false, deposition_present = false;
     double susp_rhs_max = 0, dep_rhs_max = 0;
@@ -546,6 +767,16 @@ double oracle_std_dry_air_density(double z, double T) { return std_dry_air_densi
 int oracle_coupled_ustar(double u2, double lambda, double* ustar) { return coupled_ustar(u2, lambda, *ustar) ? 1 : 0; }
 double oracle_ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L) {
     return ice_bulb_temperature(T, t, ea, D, lambda_t, L);
+}
+void oracle_incomplete_gamma(double a, double x, double* P, double* Q) { incomplete_gamma(a, x, *P, *Q); }
+double oracle_gamma_pdf(double x, double a, double b) { return gamma_pdf(x, a, b); }
+void oracle_subgrid_face(const pbsm3d_config* cfg, double snow_depth, const double* tpi, double* out) {
+    const SubgridFace o = subgrid_face(*cfg, snow_depth, tpi);
+    out[0] = o.min_sd_trans_avg;
+    out[1] = o.frac_contrib;
+    out[2] = o.frac_contrib_nosnw;
+    out[3] = o.tpi_lim;
+    out[4] = o.have_test_int ? o.test_int : -9999.0;
 }
 
 // triangulation.hpp:1466-1475 edge(i) = v[cw(i)] - v[ccw(i)], ccw(i)=(i+1)%3, cw(i)=(i+2)%3
@@ -635,7 +866,7 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
         g_create_error = "PBSM3D settling velocity must be positive";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg->use_subgrid_topo || cfg->use_subgrid_topo_V2 || cfg->debug_output) {
+    if (cfg->debug_output) {
         g_create_error = "configuration branch not restated by the oracle";
         return PBSM3D_ERR_UNSUPPORTED;
     }
@@ -713,6 +944,18 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
     c->sum_drift.assign(T, 0);  // PBSM3D.cpp:392
     c->more_than_avail.assign(T, nanv);
     c->bsp.assign(T, nanv);
+    c->tpi.assign(5 * T, NAN);
+    {
+        const double* src[5] = {mesh->tpi_mean, mesh->tpi_std, mesh->tpi_neg_frac, mesh->tpi_neg_mean,
+                                mesh->tpi_neg_std};
+        for (int k = 0; k < 5; ++k)
+            if (src[k]) std::copy(src[k], src[k] + T, c->tpi.begin() + k * T);
+    }
+    c->frac_contrib.assign(T, nanv);
+    c->frac_contrib_nosnw.assign(T, nanv);
+    c->hold_topo.assign(T, nanv);
+    c->tpi_lim.assign(T, nanv);
+    c->test_int.assign(T, nanv);
     // Suspension graph: row z*T+i = self, lateral (same layer, face order),
     // below, above (LinearAlgebra.cpp:67-116).
     {
@@ -819,10 +1062,22 @@ int oracle_stage_assemble_suspension(oracle_ctx* c, const pbsm3d_forcing* F, dou
         if (cfg.use_exp_fetch || cfg.use_tanh_fetch) fetch = c->f_fetch[i];
         double frac_contrib = 1.;
         double min_sd_trans_avg = cfg.min_sd_trans;
-        (void)frac_contrib;
         double uref = c->f_UR[i];
         double snow_depth = c->f_sd[i];
         snow_depth = is_nan(snow_depth) ? 0 : snow_depth;
+        if (cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2) {  // PBSM3D.cpp:480-645
+            const double tpi[5] = {c->tpi[i], c->tpi[T + i], c->tpi[2 * T + i], c->tpi[3 * T + i], c->tpi[4 * T + i]};
+            const SubgridFace sg = subgrid_face(cfg, snow_depth, tpi);
+            frac_contrib = sg.frac_contrib;
+            min_sd_trans_avg = sg.min_sd_trans_avg;
+            c->frac_contrib[i] = sg.frac_contrib;
+            c->hold_topo[i] = sg.min_sd_trans_avg;
+            if (cfg.use_subgrid_topo) c->frac_contrib_nosnw[i] = sg.frac_contrib_nosnw;
+            if (cfg.use_subgrid_topo_V2) {
+                c->tpi_lim[i] = sg.tpi_lim;
+                if (sg.have_test_int) c->test_int[i] = sg.test_int;
+            }
+        }
         double u2 = c->f_U2[i];
         double z10 = 10. + snow_depth;
         double u10;
@@ -903,6 +1158,7 @@ int oracle_stage_assemble_suspension(oracle_ctx* c, const pbsm3d_forcing* F, dou
                 c->bsp[i] = Pu10;
                 c_salt *= Pu10;
             }
+            if (cfg.use_subgrid_topo || cfg.use_subgrid_topo_V2) c_salt *= frac_contrib;  // :867-870
             double uhs = 2.8 * u_star_saltation_threshold;
             Qsalt = c_salt * uhs * hs;
             double mass = 0;
@@ -1277,6 +1533,11 @@ int oracle_stage_update(oracle_ctx* c, const pbsm3d_outputs* out, pbsm3d_stats* 
         copy_out(out->sum_drift, c->sum_drift);
         copy_out(out->pbsm_more_than_avail, c->more_than_avail);
         copy_out(out->blowingsnow_probability, c->bsp);
+        copy_out(out->frac_contrib, c->frac_contrib);
+        copy_out(out->frac_contrib_nosnw, c->frac_contrib_nosnw);
+        copy_out(out->hold_topo, c->hold_topo);
+        copy_out(out->tpi_lim, c->tpi_lim);
+        copy_out(out->test_int, c->test_int);
         copy_out(out->c, c->susp.x);
     }
     if (st) {

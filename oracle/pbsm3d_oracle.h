@@ -88,6 +88,14 @@ double oracle_std_dry_air_density(double altitude, double temperature);
 int oracle_coupled_ustar(double u2, double lambda, double* ustar);
 /* ice-bulb temperature (C) of iterative_subl: T in C, t in K, ea in kPa */
 double oracle_ice_bulb_temperature(double T, double t, double ea, double D, double lambda_t, double L);
+/* regularised incomplete gamma P(a, x), Q(a, x) and the gamma density (shape a, scale b) */
+void oracle_incomplete_gamma(double a, double x, double* P, double* Q);
+double oracle_gamma_pdf(double x, double a, double b);
+/* subgrid topography of one face (use_subgrid_topo / _V2 per cfg): tpi[5] =
+ * TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean, TPI_neg_std; out[5] =
+ * hold_topo, frac_contrib, frac_contrib_nosnw, tpi_lim, test_int (-9999 when
+ * the normalisation integral is not evaluated) */
+void oracle_subgrid_face(const pbsm3d_config* cfg, double snow_depth, const double* tpi, double* out);
 /* Face geometry of a triangle mesh (triangulation.hpp:1443-1498,1577-1589,1830-1856).
  * xyz [3*nv], tri [3*nt] vertex ids; outputs [3*nt], [6*nt], [nt], [3*nt]. */
 void oracle_face_geometry(int64_t nv, const double* xyz, int64_t nt, const int32_t* tri, double* edge_length,

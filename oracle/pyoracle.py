@@ -77,6 +77,12 @@ def load():
     lib.oracle_coupled_ustar.restype = C.c_int
     lib.oracle_ice_bulb_temperature.argtypes = [C.c_double] * 6
     lib.oracle_ice_bulb_temperature.restype = C.c_double
+    lib.oracle_incomplete_gamma.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.oracle_incomplete_gamma.restype = None
+    lib.oracle_gamma_pdf.argtypes = [C.c_double] * 3
+    lib.oracle_gamma_pdf.restype = C.c_double
+    lib.oracle_subgrid_face.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.oracle_subgrid_face.restype = None
     lib.oracle_face_geometry.argtypes = [C.c_int64, _dp, C.c_int64, _i32p, _dp, _dp, _dp, _dp]
     lib.oracle_face_geometry.restype = None
     lib.oracle_face_neighbors.argtypes = [C.c_int64, C.c_int64, _i32p, _i32p]
@@ -134,6 +140,8 @@ class Oracle:
     def _outputs(self, want_c=True):
         from chm_gb300.pbsm3d import OUTPUT_KEYS
         out = {k: np.empty(self.n) for k in OUTPUT_KEYS}
+        if self.cfg.use_subgrid_topo or self.cfg.use_subgrid_topo_V2:
+            out.update({k: np.empty(self.n) for k in capi.SUBGRID_OUTPUTS})
         if want_c:
             out["c"] = np.empty(self.n * self.L)
         o = capi.Outputs()

@@ -34,6 +34,14 @@ def veg_workload(seed, wind=10.0):
     # canopy from 0.3 m below to 0.25 m above the snow surface (cutoff 0.3 m)
     w.mesh.canopy_height = np.maximum(0.0, w.depth + rng.uniform(-0.3, 0.25, n))
     w.mesh.lai = rng.uniform(0.5, 3.0, n)
+    # subgrid TPI statistics, a tenth of each undefined (-9999)
+    w.mesh.tpi_mean = rng.uniform(-3.0, 3.0, n)
+    w.mesh.tpi_std = 10 ** rng.uniform(-1.0, 0.5, n)
+    w.mesh.tpi_neg_frac = rng.uniform(0.0, 0.8, n)
+    w.mesh.tpi_neg_mean = rng.uniform(-3.0, -0.02, n)
+    w.mesh.tpi_neg_std = 10 ** rng.uniform(-1.2, 0.4, n)
+    for k in ("tpi_mean", "tpi_std", "tpi_neg_frac", "tpi_neg_mean", "tpi_neg_std"):
+        getattr(w.mesh, k)[rng.random(n) < 0.1] = -9999.0
     return w
 
 
@@ -59,6 +67,10 @@ def check(out, ref, tag):
         assert relerr(out[k], ref[k]) < FIELD_TOL, (tag, k, relerr(out[k], ref[k]))
     assert relerr(out["Qsalt"], ref["Qsalt"]) < 1e-12, tag
     np.testing.assert_array_equal(out["pbsm_more_than_avail"], ref["pbsm_more_than_avail"])
+    # subgrid diagnostics: quadrature, special functions and root to ~1e-13
+    for k in capi.SUBGRID_OUTPUTS:
+        if k in out:
+            assert relerr(out[k], ref[k]) < 1e-10, (tag, k, relerr(out[k], ref[k]))
 
 
 BRANCHES = {
@@ -76,6 +88,11 @@ BRANCHES = {
     "pomeroy_lambda": {"use_R94_lambda": False},
     "no_veg": {"enable_veg": False},
     "thresholds": {"cutoff": 0.15, "min_sd_trans": 0.3, "snow_diffusion_const": 0.5, "smooth_coeff": 2000.0},
+    "subgrid_topo": {"use_subgrid_topo": True},
+    "subgrid_topo_V2": {"use_subgrid_topo_V2": True},
+    "subgrid_both": {"use_subgrid_topo": True, "use_subgrid_topo_V2": True, "min_sd_trans": 0.25},
+    "everything": {"use_subgrid_topo": True, "use_subgrid_topo_V2": True, "z0_ustar_coupling": True,
+                   "iterative_subl": True, "use_PomLi_probability": True, "use_tanh_fetch": False},
 }
 
 
@@ -92,6 +109,48 @@ def test_branch_matches_oracle(cuda_lib, oracle_lib, name):
     ref, _ = pyoracle.Oracle(w.mesh, nLayer=L, cfg=oracle_cfg(cfg)).step_exact(f, 3600.0)
     check(out, ref, name)
     m.close()
+
+
+def test_subgrid_outputs_and_effect(cuda_lib):
+    """With the subgrid branches the module provides their variables, the
+    contributing fraction lies in [0, 1] and scales the saltation flux."""
+    w = veg_workload(74)
+    f = forcing(w, 0)
+    res = {}
+    for name, cfg in (("off", {}), ("on", {"use_subgrid_topo": True, "use_subgrid_topo_V2": True})):
+        m = PBSM3D(module_cfg(cfg))
+        m.init(w.mesh)
+        res[name] = m.run(f, 3600.0)
+        keys = m.output_keys()
+        m.close()
+    assert set(capi.SUBGRID_OUTPUTS) <= set(keys)
+    on = res["on"]
+    assert ((on["frac_contrib"] >= 0) & (on["frac_contrib"] <= 1)).all()
+    assert (on["Qsalt"] <= res["off"]["Qsalt"] + 1e-15).all()
+    assert relerr(on["Qsalt"], res["off"]["Qsalt"]) > 1e-3
+    # faces without TPI_std keep tpi_lim at -min_sd_trans and test_int at -9999
+    undefined = np.asarray(w.mesh.tpi_std) == -9999.0
+    assert (on["tpi_lim"][undefined] == -0.1).all() and (on["test_int"][undefined] == -9999.0).all()
+
+
+def test_subgrid_ensemble(cuda_lib, oracle_lib):
+    """Members' TPI parameters travel with their meshes into the batched context."""
+    from oracle import pyoracle
+    from chm_gb300.ensemble import Ensemble, MemberParams
+    cfg = {"use_subgrid_topo": True, "use_subgrid_topo_V2": True}
+    ws = [veg_workload(75), veg_workload(76, wind=12.0)]
+    members = [MemberParams(1.0, 0.01, 1.0), MemberParams(0.9, 0.005, 1.1)]
+    ens = Ensemble(module_cfg(cfg))
+    ens.init([w.mesh for w in ws], members)
+    fs = [forcing(w, 0) for w in ws]
+    outs = ens.run_members(fs, 3600.0, want_c=True)
+    for m, (w, p, f) in enumerate(zip(ws, members, fs)):
+        ocfg = {**oracle_cfg(cfg), "ustar_th_scale": p.ustar_th_scale, "z0_snow": p.z0_snow,
+                "settling_scale": p.settling_scale}
+        ref, _ = pyoracle.Oracle(w.mesh, nLayer=L, cfg=ocfg).step_exact(f, 3600.0)
+        for k in ("c", "Qsalt", "Qsusp", "Qsubl", "drift_mass"):
+            assert relerr(outs[m][k], ref[k]) < FIELD_TOL, (m, k)
+    ens.close()
 
 
 def test_coupling_changes_the_answer(cuda_lib):

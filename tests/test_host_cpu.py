@@ -92,9 +92,8 @@ def test_create_rejects_bad_configs(cuda_lib):
                 dict(abi_version=99)):
         cfg = capi.default_config(cuda_lib, **bad)
         assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
-    for unbuilt in (dict(use_subgrid_topo=1), dict(use_subgrid_topo_V2=1), dict(debug_output=1)):
-        cfg = capi.default_config(cuda_lib, **unbuilt)
-        assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_UNSUPPORTED
+    cfg = capi.default_config(cuda_lib, debug_output=1)
+    assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_UNSUPPORTED
     bad_nb = m.neighbor.copy()
     bad_nb[0, 0] = m.n_faces + 5
     m.neighbor = bad_nb

@@ -360,3 +360,119 @@ def test_ice_bulb_temperature(oracle_lib):
                                 - 0.611 * mw * math.exp(17.3 * x / (237.3 + x)) / (R * (x + 273.15) * 1000.0)) / lt - x
         root = brentq(f, -60.0, 5.0)
         assert abs(Ti - root) <= abs(Ti) / 32.0
+
+
+def test_incomplete_gamma_and_density(oracle_lib):
+    """use_subgrid_topo's gamma functions (gsl_cdf_gamma_P/Q,
+    gsl_ran_gamma_pdf; PBSM3D.cpp:615-639) against scipy.special over the
+    shapes the branch produces (TPI_neg_mean^2 / TPI_neg_std^2 in [1e-4, 1e4])."""
+    from scipy import special
+    rng = np.random.default_rng(5)
+    P, Q = C.c_double(), C.c_double()
+    for _ in range(3000):
+        a = 10 ** rng.uniform(-4, 4)
+        x = a * 10 ** rng.uniform(-2, 0.7) if rng.random() < 0.8 else 10 ** rng.uniform(-3, 3)
+        oracle_lib.oracle_incomplete_gamma(a, x, C.byref(P), C.byref(Q))
+        assert abs(P.value - special.gammainc(a, x)) < 5e-12, (a, x)
+        assert abs(Q.value - special.gammaincc(a, x)) < 5e-12, (a, x)
+    for _ in range(1000):
+        a, b, x = 10 ** rng.uniform(-4, 4), 10 ** rng.uniform(-3, 1), 10 ** rng.uniform(-3, 1)
+        ref = np.exp(special.xlogy(a - 1, x) - x / b - special.gammaln(a) - a * np.log(b))
+        if ref > 1e-250:
+            assert abs(oracle_lib.oracle_gamma_pdf(x, a, b) - ref) <= 1e-10 * ref
+
+
+def _v2_reference(sd, m, s, min_sd, epsrel):
+    """use_subgrid_topo_V2 (PBSM3D.cpp:486-597) with scipy's QUADPACK QAGS
+    (the algorithm gsl_integration_qags implements) and brentq."""
+    from scipy import integrate, optimize
+    a1, b1, a2, b2, fac = 1.5, 0.3, 0.6, 0.55, 0.8
+    m = max(-5.0, min(5.0, m))
+    s = min(5.0, max(0.1, s))
+
+    def pdf(x):
+        return math.exp(-((x - m) / s) ** 2 / 2) / (math.sqrt(2 * math.pi) * s)
+
+    def F(x):
+        return (1 - a1 * math.tanh(b1 * (x + 0.25))) if x + 0.25 <= 0 else (1 - a2 * math.tanh(b2 * (x + 0.25)))
+
+    q = dict(epsabs=0, epsrel=epsrel, limit=5000)
+    res = integrate.quad(lambda x: F(x) * pdf(x), -50, 50, points=[-0.25, m], **q)[0]
+
+    def fr(xx):
+        return (1 - a1 * math.tanh(b1 * (xx + 0.25))) * sd / res + fac * xx
+    lo = -1.0
+    while fr(lo) > 0:
+        lo *= 2
+    tl = optimize.brentq(fr, lo, 0.0, xtol=1e-15)
+    pts = [p for p in (-0.25, m) if -50 < p < tl]
+    h1 = integrate.quad(lambda x: F(x) * sd / res * pdf(x), -50, tl, points=pts or None, **q)[0]
+    h2 = integrate.quad(lambda x: -fac * x * pdf(x), tl, -min_sd / fac, **q)[0]
+    h3 = min_sd * 0.5 * math.erfc((-min_sd / fac - m) / (s * math.sqrt(2)))
+    return min(h1 + h2 + h3, sd), 0.5 * math.erfc((tl - m) / (s * math.sqrt(2))), tl, res
+
+
+def test_subgrid_v2_face(oracle_lib):
+    """The oracle's V2 holding capacity, contributing fraction, threshold and
+    normalisation integral against QUADPACK run tight; the reference's QAGS at
+    its relative 1e-7 stays within a few 1e-7 of them."""
+    from chm_gb300 import capi
+    lib = capi.load()
+    cfg = capi.default_config(lib, use_subgrid_topo_V2=1)
+    out, tpi = (C.c_double * 5)(), (C.c_double * 5)()
+    rng = np.random.default_rng(6)
+    for _ in range(150):
+        sd, m, s = rng.uniform(0.11, 3.0), rng.uniform(-6, 6), 10 ** rng.uniform(-1.2, 0.8)
+        tpi[0], tpi[1] = m, s
+        tpi[2] = tpi[3] = tpi[4] = float("nan")
+        oracle_lib.oracle_subgrid_face(C.byref(cfg), sd, tpi, out)
+        got = (out[0], out[1], out[3], out[4])
+        tight = _v2_reference(sd, m, s, 0.1, 2e-14)
+        for g, r in zip(got, tight):
+            assert abs(g - r) <= 1e-10 * max(abs(r), 1e-3), (sd, m, s, got, tight)
+        loose = _v2_reference(sd, m, s, 0.1, 1e-7)
+        for g, r in zip(got, loose):
+            assert abs(g - r) <= 5e-7 * max(abs(r), 1e-3)
+    # undefined TPI_std: defaults; snow at most min_sd_trans: no integrals
+    tpi[1] = -9999.0
+    oracle_lib.oracle_subgrid_face(C.byref(cfg), 1.0, tpi, out)
+    assert (out[0], out[1], out[3], out[4]) == (0.1, 1.0, -0.1, -9999.0)
+    tpi[0], tpi[1] = 0.5, 1.0
+    oracle_lib.oracle_subgrid_face(C.byref(cfg), 0.05, tpi, out)
+    assert out[0] == 0.1 and out[4] == -9999.0
+    assert abs(out[1] - 0.5 * math.erfc((-0.1 - 0.5) / math.sqrt(2))) < 1e-15
+
+
+def test_subgrid_v1_face(oracle_lib):
+    """use_subgrid_topo (PBSM3D.cpp:604-645) against the same closed forms
+    evaluated with scipy.special."""
+    from scipy import special
+    from chm_gb300 import capi
+    cfg = capi.default_config(capi.load(), use_subgrid_topo=1)
+    out, tpi = (C.c_double * 5)(), (C.c_double * 5)()
+    rng = np.random.default_rng(7)
+    msd = 0.1
+    for _ in range(500):
+        sd = rng.uniform(0, 3.0)
+        fn, mn, sn = rng.uniform(0, 1), rng.uniform(-12, 0), 10 ** rng.uniform(-1.3, 0.8)
+        tpi[0] = tpi[1] = float("nan")
+        tpi[2], tpi[3], tpi[4] = fn, mn, sn
+        oracle_lib.oracle_subgrid_face(C.byref(cfg), sd, tpi, out)
+        mn_c, sn_c = max(-10.0, min(-0.05, mn)), min(5.0, max(0.1, sn))
+        k, th = mn_c ** 2 / sn_c ** 2, -sn_c ** 2 / mn_c
+
+        def gP(x):
+            return special.gammainc(k, x / th)
+
+        def gQ(x):
+            return special.gammaincc(k, x / th)
+
+        def pdf(x):
+            return np.exp(special.xlogy(k - 1, x / th) - x / th - special.gammaln(k)) / th
+        frac = (1 - fn) + fn * gP(sd)
+        hold = msd
+        if sd > msd:
+            hint = k * th - th * (sd * pdf(sd) - msd * pdf(msd) + k * gP(msd) + k * gQ(sd))
+            hold = (1 - fn) * msd + fn * (msd * gP(msd) + hint + sd * gQ(sd))
+        assert abs(out[1] - frac) < 1e-11 and abs(out[2] - (1 - fn)) < 1e-15
+        assert abs(out[0] - hold) <= 1e-9 * max(1.0, abs(hold)), (sd, fn, mn, sn, out[0], hold)
