@@ -21,7 +21,7 @@ SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1
 FP64, MIXED = 0, 1
 X0_ZERO, X0_PREVIOUS, X0_LEARNED = 0, 1, 2
 KERNELS = ["ASSEMBLE", "BICG_P", "BICG_V", "BICG_S", "BICG_T", "BICG_X", "RESIDUAL", "POST", "DEP_ASSEMBLE", "CG",
-           "UPDATE", "OTHER", "MLP"]
+           "UPDATE", "OTHER", "MLP", "NEUMANN"]
 
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
@@ -44,7 +44,7 @@ class Config(C.Structure):
         ("susp_maxit", C.c_int32), ("dep_maxit", C.c_int32),
         ("susp_tol", C.c_double), ("dep_tol", C.c_double), ("inner_tol", C.c_double),
         ("slice_width", C.c_int32), ("warm_flags", C.c_int32), ("graph", C.c_int32),
-        ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("autotune", C.c_int32), ("neumann", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 

@@ -182,6 +182,10 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "debug_output is not implemented";
         return PBSM3D_ERR_UNSUPPORTED;
     }
+    if (cfg.neumann < 0 || cfg.neumann > 3) {
+        g_create_error = "neumann must be in [0, 3]";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
     if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {
         g_create_error = "only the BiCGStab suspension solver is implemented";
         return PBSM3D_ERR_UNSUPPORTED;
@@ -398,6 +402,10 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         c.zp32 = dalloc<float>(c, R, ok);
         c.zs32 = dalloc<float>(c, R, ok);
         c.x32 = dalloc<float>(c, R, ok);
+        if (cfg.neumann > 0) {
+            c.nw32 = dalloc<float>(c, R, ok);
+            c.nz32 = dalloc<float>(c, R, ok);
+        }
     } else {
         c.rh = dalloc<double>(c, R, ok);
         c.p = dalloc<double>(c, R, ok);
@@ -406,6 +414,10 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         c.tv = dalloc<double>(c, R, ok);
         c.zp = dalloc<double>(c, R, ok);
         c.zs = dalloc<double>(c, R, ok);
+        if (cfg.neumann > 0) {
+            c.nw = dalloc<double>(c, R, ok);
+            c.nz = dalloc<double>(c, R, ok);
+        }
     }
     Dep& D = c.D;
     D.diag = dalloc<double>(c, Tp, ok);

@@ -254,6 +254,9 @@ struct Ctx {
     double *r, *rh, *p, *v, *sv, *tv, *zp, *zs;
     // FP32 work vectors for MIXED, [R] each
     float *r32, *rh32, *p32, *v32, *s32, *t32, *zp32, *zs32, *x32;
+    // polynomial preconditioner (neumann > 0): the last u - N z and the other z, [R] each
+    double *nw = nullptr, *nz = nullptr;
+    float *nw32 = nullptr, *nz32 = nullptr;
     // deposition CG vectors [Tp]
     double *dr, *dz_, *dp, *dq;
     // reductions

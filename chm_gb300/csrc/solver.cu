@@ -244,6 +244,39 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* 
     }
 }
 
+// One step of the polynomial preconditioner M^-1 = B^-1 sum_{j<=K} (-C)^j,
+// C = N B^-1 (a truncated Neumann series; Saad, Iterative Methods for Sparse
+// Linear Systems, section 12.3): w = u - N zin, zout = B^{-1} w.  Starting
+// from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
+// so the lateral kernels that follow take w in place of u.
+template <typename V>
+__global__ void __launch_bounds__(kBlock) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
+                                                     const V* __restrict__ zin, V* __restrict__ w,
+                                                     V* __restrict__ zout, const MScal* __restrict__ ms) {
+    extern __shared__ unsigned char smem_raw[];
+    V* g = reinterpret_cast<V*>(smem_raw);
+    const TileRange br = block_tiles(tl);
+    for (int a = br.a0; a < br.a1; ++a) {
+        const int t = tl.act[a], m = tl.member[t];
+        if (ms[m].done) continue;
+        const int64_t i = tl.start[t] + threadIdx.x;
+        if (i >= tl.start[t + 1]) continue;
+        const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+#pragma unroll 4
+        for (int z = 0; z < op.L; ++z) {
+            const int64_t base = (int64_t)z * op.Tp;
+            const int64_t k = base + i;
+            V wk = u[k];
+            if (n0 >= 0) wk -= op.lat[k] * zin[base + n0];
+            if (n1 >= 0) wk -= op.lat[op.R + k] * zin[base + n1];
+            if (n2 >= 0) wk -= op.lat[2 * op.R + k] * zin[base + n2];
+            w[k] = wk;
+            g[z * blockDim.x + threadIdx.x] = wk;
+        }
+        column_solve(op, i, g, zout);
+    }
+}
+
 // y = u + N z for the column of face i, with (a, y) [and (y, y)]
 template <typename V, int NT>
 __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const V* __restrict__ u,
@@ -297,11 +330,12 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, Tiles tl, const 
     }
 }
 
-// t = s + N zs; ts = (t, s), tt = (t, t); omega = ts / tt
+// t = u + N zs (u = s, or the preconditioner's last s - N z); ts = (t, s),
+// tt = (t, t); omega = ts / tt
 template <typename V>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_t(Op<V> op, Tiles tl, const V* __restrict__ s,
-                                                      const V* __restrict__ zs, V* __restrict__ tv, MScal* ms,
-                                                      double* part) {
+__global__ void __launch_bounds__(kBlock, 5) k_bicg_t2(Op<V> op, Tiles tl, const V* __restrict__ u,
+                                                       const V* __restrict__ zs, V* __restrict__ tv,
+                                                       const V* __restrict__ s, MScal* ms, double* part) {
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
@@ -313,7 +347,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_t(Op<V> op, Tiles tl, const 
         V acc[2] = {0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x;
-            if (i < tl.start[t + 1]) lateral_apply<V, 2>(op, i, s, zs, tv, s, acc);
+            if (i < tl.start[t + 1]) lateral_apply<V, 2>(op, i, u, zs, tv, s, acc);
         }
         double tot[2];
         if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
@@ -987,9 +1021,29 @@ int64_t active_faces_of(const Ctx& c, const std::vector<char>& conv) {
 // Run BiCGStab iterations on the per-member states in ms (set up by the
 // host) until every member is done.  sc holds the batch totals: done, the
 // largest member iteration count and the count of stopped members.
+// K steps of the polynomial preconditioner on u, whose B^-1 u the column
+// kernel wrote to z0 (chosen so that the last step writes zfinal); returns
+// the vector the lateral kernel adds N zfinal to (u, or the last u - N z).
+template <typename V>
+const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gc, size_t smem, const V* u,
+                        V* zfinal, V* w, V* ztmp, const MScal* ms, int64_t rows, bool prof) {
+    const int K = c.cfg.neumann;
+    V* a = (K & 1) ? ztmp : zfinal;
+    V* b = (K & 1) ? zfinal : ztmp;
+    for (int j = 0; j < K; ++j) {
+        if (prof) prof_begin(c, s);
+        k_bicg_neu<V><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
+        if (prof) prof_end(c, s, PBSM3D_K_NEUMANN, rows * 10 * sizeof(V) + rows / c.P.L * 12);
+        std::swap(a, b);
+    }
+    return K > 0 ? w : u;
+}
+template <typename V>
+V* neumann_first(Ctx& c, V* zfinal, V* ztmp) { return (c.cfg.neumann & 1) ? ztmp : zfinal; }
+
 template <typename V, typename X>
 int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V* r, V* rh, V* p, V* v, V* sv,
-                        V* tv, V* zp, V* zs, int& iters) {
+                        V* tv, V* zp, V* zs, V* nw, V* nz, int& iters) {
     Op<V> op = make_op<V>(c);
     const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
     double* part = c.tile_part;
@@ -1033,16 +1087,18 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         }
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
-            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, zp, ms);
+            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, neumann_first(c, zp, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
+            const V* up = launch_neumann<V>(c, s, op, tl, gc, smem, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
-            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, p, zp, v, rh, ms, sc, part);
+            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + act * 12);
             prof_begin(c, s);
-            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, zs, ms);
+            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, neumann_first(c, zs, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
+            const V* us = launch_neumann<V>(c, s, op, tl, gc, smem, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
-            k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, tl, sv, zs, tv, ms, part);
+            k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
             prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + act * 12);
             prof_begin(c, s);
             k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
@@ -1113,6 +1169,8 @@ int configure_solver_kernels(Ctx& c) {
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     // one full wave of co-resident blocks per kernel (grid-stride loops do the rest)
     int dev = 0, sms = 0;
     PBSM_CUDA_TRY(cudaGetDevice(&dev));
@@ -1293,14 +1351,14 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
             k_zero<float><<<c.grid_faces, kBlock, 0, s>>>(c.P.R, c.x32);
             prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 4);
             rc = bicgstab_iterations<float, float>(c, s, ms, sc, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32, c.t32,
-                                                   c.zp32, c.zs32, it);
+                                                   c.zp32, c.zs32, c.nw32, c.nz32, it);
             if (rc) return rc;
             prof_begin(c, s);
             k_add_correction<<<c.grid_faces, kBlock, 0, s>>>(c.P.R, c.A.x, c.x32);
             prof_end(c, s, PBSM3D_K_OTHER, c.P.T * c.P.L * 20);
         } else {
             rc = bicgstab_iterations<double, double>(c, s, ms, sc, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv, c.zp,
-                                                     c.zs, it);
+                                                     c.zs, c.nw, c.nz, it);
             if (rc) return rc;
         }
         PBSM_CUDA_TRY(cudaMemcpyAsync(c.msR, rs.data(), sizeof(MScal) * n, cudaMemcpyHostToDevice, s));
@@ -1312,7 +1370,7 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         }
     }
     c.susp_iters = total_iters;
-    c.susp_matvecs = 2 * total_iters + sweeps + 1;
+    c.susp_matvecs = (2 + 2 * c.cfg.neumann) * total_iters + sweeps + 1;
     c.susp_refinements = sweeps;
     return 0;
 }
@@ -2133,16 +2191,18 @@ struct CondBody {
 // The batched BiCGStab iteration (the five kernels of bicgstab_iterations).
 template <typename V, typename X>
 void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, Scalars* sc, X* x, V* r, V* rh,
-                            V* p, V* v, V* sv, V* tv, V* zp, V* zs) {
+                            V* p, V* v, V* sv, V* tv, V* zp, V* zs, V* nw, V* nz) {
     Op<V> op = make_op<V>(c);
     const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
     const int gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.ntiles));
     const int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
     double* part = c.tile_part;
-    k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, zp, ms);
-    k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, p, zp, v, rh, ms, sc, part);
-    k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, zs, ms);
-    k_bicg_t<V><<<gr, kBlock, 0, s>>>(op, tl, sv, zs, tv, ms, part);
+    k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, neumann_first(c, zp, nz), ms);
+    const V* up = launch_neumann<V>(c, s, op, tl, gc, smem, p, zp, nw, nz, ms, 0, false);
+    k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
+    k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, neumann_first(c, zs, nz), ms);
+    const V* us = launch_neumann<V>(c, s, op, tl, gc, smem, sv, zs, nw, nz, ms, 0, false);
+    k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
     k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
 }
 
@@ -2193,11 +2253,12 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
             cudaStream_t w = G.cap[depth + 3];
             if (mixed)
                 capture_bicg_iteration<float, float>(c, w, tl, ms, sc, c.x32, c.r32, c.rh32, c.p32, c.v32, c.s32,
-                                                     c.t32, c.zp32, c.zs32);
+                                                     c.t32, c.zp32, c.zs32, c.nw32, c.nz32);
             else
                 capture_bicg_iteration<double, double>(c, w, tl, ms, sc, c.A.x, c.r, c.rh, c.p, c.v, c.sv, c.tv,
-                                                       c.zp, c.zs);
-            k_ctl_inner<<<1, kBlock, 0, w>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_ILOOP, 6, h);
+                                                       c.zp, c.zs, c.nw, c.nz);
+            k_ctl_inner<<<1, kBlock, 0, w>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_ILOOP,
+                                             6 + 2 * c.cfg.neumann, h);
             if (loop.end()) return 1;
             if (mixed) k_add_correction<<<c.grid_faces, kBlock, 0, u>>>(c.P.R, c.A.x, c.x32);
             k_ctl_sweep_end<<<1, kBlock, 0, u>>>(G.ctl, sc, tl, c.act_buf, G.nact, mixed ? 2 : 0);
@@ -2420,7 +2481,7 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
     c.deposition_present = k.dep_present;
     c.susp_iters = k.susp_iters;
     c.susp_refinements = k.sweep;
-    c.susp_matvecs = 2 * k.susp_iters + k.sweep + 1;
+    c.susp_matvecs = (2 + 2 * c.cfg.neumann) * k.susp_iters + k.sweep + 1;
     c.susp_relres = k.susp_relres;
     c.dep_iters = k.dep_iters;
     c.dep_refinements = k.dep_sweeps;

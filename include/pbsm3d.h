@@ -126,7 +126,10 @@ typedef struct pbsm3d_config {
     int32_t autotune;       /* 1: the first suspension solve times the batched Krylov kernels at 1, 2
                                and 4 waves of blocks per SM on its own iterations and keeps the
                                fastest (shared by later contexts of the same shape); 0 */
-    int32_t reserved[4];
+    int32_t neumann;        /* order K (0..3) of the polynomial preconditioner of the suspension
+                               Krylov solve: M^-1 = B^-1 sum_{j<=K} (-N B^-1)^j, B the column
+                               (tridiagonal) blocks, N the lateral couplings; 0 = B^-1 alone */
+    int32_t reserved[3];
 } pbsm3d_config;
 
 /*
@@ -271,7 +274,8 @@ enum pbsm3d_kernel {
     PBSM3D_K_UPDATE = 10,    /* erosion/deposition update + mass ledger */
     PBSM3D_K_OTHER = 11,
     PBSM3D_K_MLP = 12,       /* learned warm start: features + fused 3-layer tensor-core MLP */
-    PBSM3D_K_COUNT = 13
+    PBSM3D_K_NEUMANN = 13,   /* polynomial preconditioner steps: lateral gather + column solve */
+    PBSM3D_K_COUNT = 14
 };
 
 typedef struct pbsm3d_ctx pbsm3d_ctx;

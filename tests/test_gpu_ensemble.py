@@ -45,8 +45,10 @@ def _check_member(out, ref, tag):
 
 
 @pytest.mark.parametrize("solver", [{}, {"precision": capi.MIXED}, {"warm_start": capi.X0_PREVIOUS},
-                                    {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1}],
-                         ids=["fp64", "mixed", "warm", "graph"])
+                                    {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
+                                    {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                     "neumann": 2}],
+                         ids=["fp64", "mixed", "warm", "graph", "graph_neumann2"])
 def test_members_match_oracle_over_steps(cuda_lib, oracle_lib, solver):
     from oracle import pyoracle
     ws = workloads()

@@ -74,10 +74,11 @@ def test_assembled_systems_match_oracle(cuda_lib, oracle_lib, small):
     m.close()
 
 
-def test_step_matches_exact_oracle(cuda_lib, oracle_lib, small):
+@pytest.mark.parametrize("neumann", [0, 2])
+def test_step_matches_exact_oracle(cuda_lib, oracle_lib, small, neumann):
     L = 5
     f = small.forcing(0)
-    m = gpu_module(small.mesh, L)
+    m = gpu_module(small.mesh, L, neumann=neumann)
     out = m.run(f, 3600.0, want_c=True)
     st = m.last_stats
     assert st["suspension_present"] == 1 and st["deposition_present"] == 1
@@ -136,10 +137,11 @@ def test_mass_ledger_closes(cuda_lib, small):
     m.close()
 
 
-def test_mixed_precision_matches(cuda_lib, oracle_lib, small):
+@pytest.mark.parametrize("neumann", [0, 1, 2, 3])
+def test_mixed_precision_matches(cuda_lib, oracle_lib, small, neumann):
     L = 5
     f = small.forcing(0)
-    m = gpu_module(small.mesh, L, precision=1)
+    m = gpu_module(small.mesh, L, precision=1, neumann=neumann)
     out = m.run(f, 3600.0, want_c=True)
     st = m.last_stats
     assert st["susp_rel_residual"] <= 1e-8
@@ -151,11 +153,12 @@ def test_mixed_precision_matches(cuda_lib, oracle_lib, small):
 
 
 @pytest.mark.parametrize("wind", [4.0, 14.0])
-def test_wind_regimes(cuda_lib, oracle_lib, wind):
+@pytest.mark.parametrize("neumann", [0, 3])
+def test_wind_regimes(cuda_lib, oracle_lib, wind, neumann):
     L = 5
     w = synth.Workload(1024, 2500.0, seed=9, wind_scale=wind)
     f = w.forcing(0)
-    m = gpu_module(w.mesh, L)
+    m = gpu_module(w.mesh, L, neumann=neumann)
     out = m.run(f, 3600.0, want_c=True)
     ref, _ = oracle(w.mesh, L).step_exact(f, 3600.0)
     for k in FIELDS:
@@ -318,8 +321,10 @@ def test_device_snow_state(cuda_lib, oracle_lib):
 
 
 @pytest.mark.parametrize("solver", [{}, {"precision": 1}, {"precision": 1, "warm_start": 1},
-                                    {"precision": 1, "warm_start": 1, "autotune": 1}],
-                         ids=["fp64", "mixed", "mixed_previous", "autotuned"])
+                                    {"precision": 1, "warm_start": 1, "autotune": 1},
+                                    {"precision": 1, "warm_start": 1, "neumann": 2}, {"neumann": 1}],
+                         ids=["fp64", "mixed", "mixed_previous", "autotuned", "mixed_previous_neumann2",
+                              "fp64_neumann1"])
 def test_graph_mode_matches_oracle(cuda_lib, oracle_lib, solver):
     """The whole step as one CUDA-graph launch (device-side control of the
     Krylov and refinement loops) against the exact oracle over coupled steps."""
