@@ -168,10 +168,13 @@ VARIANTS = {
     "learned": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED},
     # the same step as one CUDA-graph launch with device-side control
     "graph_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
-    # with the polynomial (Neumann) preconditioner of order 3
-    "plain_fp64_neumann3": {"precision": capi.FP64, "neumann": 3},
-    "previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 3},
+    # with the polynomial (truncated Neumann) preconditioner of order 5
+    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5},
+    "previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5},
+    "graph_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 5},
+    "graph_learned_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED, "graph": 1, "neumann": 5},
     "graph_previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 3},
+    "graph_previous_neumann7": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 7},
 }
 
 
@@ -394,9 +397,9 @@ ENSEMBLE_VARIANTS = {
     "plain_fp64": {"precision": capi.FP64},
     "mixed_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS},
     "graph_mixed_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
-    "mixed_previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 3},
-    "graph_mixed_previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
-                                      "neumann": 3},
+    "mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5},
+    "graph_mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                      "neumann": 5},
 }
 
 
@@ -604,8 +607,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(synth.CONFIGS))
-    ap.add_argument("--variants", default="plain_fp64,mixed,previous,learned,graph_previous,plain_fp64_neumann3,"
-                                          "previous_neumann3,graph_previous_neumann3",
+    ap.add_argument("--variants", default="plain_fp64,mixed,previous,learned,graph_previous,plain_fp64_neumann5,"
+                                          "previous_neumann5,graph_previous_neumann5,graph_learned_neumann5",
                     help="comma list of %s; the fastest meeting residual 1e-8 is the headline" % ",".join(VARIANTS))
     ap.add_argument("--wind", type=float, default=8.0)
     ap.add_argument("--seed", type=int, default=1)

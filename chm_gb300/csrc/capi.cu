@@ -182,8 +182,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "debug_output is not implemented";
         return PBSM3D_ERR_UNSUPPORTED;
     }
-    if (cfg.neumann < 0 || cfg.neumann > 3) {
-        g_create_error = "neumann must be in [0, 3]";
+    if (cfg.neumann < 0 || cfg.neumann > 9) {
+        g_create_error = "neumann must be in [0, 9]";
         return PBSM3D_ERR_INVALID_ARG;
     }
     if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {

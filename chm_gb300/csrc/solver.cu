@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* 
 // Linear Systems, section 12.3): w = u - N zin, zout = B^{-1} w.  Starting
 // from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
 // so the lateral kernels that follow take w in place of u.
-template <typename V>
+template <typename V, bool WRITE_W>
 __global__ void __launch_bounds__(kBlock) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
                                                      const V* __restrict__ zin, V* __restrict__ w,
                                                      V* __restrict__ zout, const MScal* __restrict__ ms) {
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_neu(Op<V> op, Tiles tl, const V
             if (n0 >= 0) wk -= op.lat[k] * zin[base + n0];
             if (n1 >= 0) wk -= op.lat[op.R + k] * zin[base + n1];
             if (n2 >= 0) wk -= op.lat[2 * op.R + k] * zin[base + n2];
-            w[k] = wk;
+            if (WRITE_W) w[k] = wk;  // only the last step's w is read (by the lateral kernel)
             g[z * blockDim.x + threadIdx.x] = wk;
         }
         column_solve(op, i, g, zout);
@@ -1031,9 +1031,13 @@ const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl
     V* a = (K & 1) ? ztmp : zfinal;
     V* b = (K & 1) ? zfinal : ztmp;
     for (int j = 0; j < K; ++j) {
+        const bool last = j == K - 1;
         if (prof) prof_begin(c, s);
-        k_bicg_neu<V><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
-        if (prof) prof_end(c, s, PBSM3D_K_NEUMANN, rows * 10 * sizeof(V) + rows / c.P.L * 12);
+        if (last)
+            k_bicg_neu<V, true><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
+        else
+            k_bicg_neu<V, false><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
+        if (prof) prof_end(c, s, PBSM3D_K_NEUMANN, rows * (last ? 10 : 9) * sizeof(V) + rows / c.P.L * 12);
         std::swap(a, b);
     }
     return K > 0 ? w : u;
@@ -1169,8 +1173,10 @@ int configure_solver_kernels(Ctx& c) {
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
+    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
     // one full wave of co-resident blocks per kernel (grid-stride loops do the rest)
     int dev = 0, sms = 0;
     PBSM_CUDA_TRY(cudaGetDevice(&dev));

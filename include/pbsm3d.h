@@ -126,9 +126,11 @@ typedef struct pbsm3d_config {
     int32_t autotune;       /* 1: the first suspension solve times the batched Krylov kernels at 1, 2
                                and 4 waves of blocks per SM on its own iterations and keeps the
                                fastest (shared by later contexts of the same shape); 0 */
-    int32_t neumann;        /* order K (0..3) of the polynomial preconditioner of the suspension
+    int32_t neumann;        /* order K (0..9) of the polynomial preconditioner of the suspension
                                Krylov solve: M^-1 = B^-1 sum_{j<=K} (-N B^-1)^j, B the column
-                               (tridiagonal) blocks, N the lateral couplings; 0 = B^-1 alone */
+                               (tridiagonal) blocks, N the lateral couplings; 0 = B^-1 alone.
+                               Odd K make A M^-1 = I - (N B^-1)^(K+1), whose spectrum stays on one
+                               side of 1, and converge best */
     int32_t reserved[3];
 } pbsm3d_config;
 

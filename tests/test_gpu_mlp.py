@@ -125,17 +125,19 @@ def test_learned_warm_start_gain(cuda_lib):
     field does (relative L2 error), which is asserted.  Its remaining error is
     row-to-row noise, the component the column-preconditioned BiCGStab
     resolves slowest, so the iteration count from the learned guess is
-    reported, not asserted to be lower."""
+    reported, not asserted to be lower; it is reported with the column
+    preconditioner and with the order-5 polynomial one, which resolves
+    lateral error faster."""
     L = 5
     params, mean, scale, losses, n = warmstart.train_from_solutions(
         train_seeds=[101, 102, 103, 104], n_points=4096, side=5000.0, nLayer=L, steps_per_seed=8,
         rows_per_step=20000, train_steps=1500, lr=2e-3, batch=2048, seed=0)
     assert losses[-50:].mean() < 0.3 * losses[:20].mean(), (losses[:5], losses[-5:])
     iters, err_learned, err_prev = {}, [], []
-    for ws in (capi.X0_ZERO, capi.X0_PREVIOUS, capi.X0_LEARNED):
+    for ws, K in [(w_, k_) for k_ in (0, 5) for w_ in (capi.X0_ZERO, capi.X0_PREVIOUS, capi.X0_LEARNED)]:
         w = synth.Workload(4096, 5000.0, seed=777)
         m = PBSM3D({"nLayer": str(L)})
-        m.init(w.mesh, warm_start=ws)
+        m.init(w.mesh, warm_start=ws, neumann=K)
         if ws == capi.X0_LEARNED:
             warmstart.set_mlp(m, params, mean, scale)
         its = []
@@ -144,16 +146,18 @@ def test_learned_warm_start_gain(cuda_lib):
             assert m.last_stats["susp_rel_residual"] <= 1e-8
             if s > 0:
                 its.append(m.last_stats["susp_iters"])
-                if ws == capi.X0_LEARNED:
+                if ws == capi.X0_LEARNED and K == 0:
                     pred = warmstart.predict(m)
                     feat, _ = warmstart.features(m)
                     c = out["c"]
                     err_learned.append(np.linalg.norm(pred - c) / np.linalg.norm(c))
                     err_prev.append(np.linalg.norm(feat[:, 9] / 100.0 - c) / np.linalg.norm(c))
             w.apply_drift(out["drift_mass"])
-        iters[ws] = np.mean(its)
+        iters[ws, K] = np.mean(its)
         m.close()
-    print(f"held-out seed: relative L2 error of the guess: learned {np.mean(err_learned):.3f}, previous field "
-          f"{np.mean(err_prev):.3f}; BiCGStab iterations to 1e-8: zero {iters[capi.X0_ZERO]:.2f}, previous "
-          f"{iters[capi.X0_PREVIOUS]:.2f}, learned {iters[capi.X0_LEARNED]:.2f}")
+    for K in (0, 5):
+        print(f"held-out seed: relative L2 error of the guess: learned {np.mean(err_learned):.3f}, previous field "
+              f"{np.mean(err_prev):.3f}; BiCGStab iterations to 1e-8 with the order-{K} preconditioner: zero "
+              f"{iters[capi.X0_ZERO, K]:.2f}, previous {iters[capi.X0_PREVIOUS, K]:.2f}, learned "
+              f"{iters[capi.X0_LEARNED, K]:.2f}")
     assert np.mean(err_learned) < 0.7 * np.mean(err_prev)

@@ -74,7 +74,7 @@ def test_assembled_systems_match_oracle(cuda_lib, oracle_lib, small):
     m.close()
 
 
-@pytest.mark.parametrize("neumann", [0, 2])
+@pytest.mark.parametrize("neumann", [0, 5])
 def test_step_matches_exact_oracle(cuda_lib, oracle_lib, small, neumann):
     L = 5
     f = small.forcing(0)
@@ -137,7 +137,7 @@ def test_mass_ledger_closes(cuda_lib, small):
     m.close()
 
 
-@pytest.mark.parametrize("neumann", [0, 1, 2, 3])
+@pytest.mark.parametrize("neumann", [0, 1, 2, 3, 5, 9])
 def test_mixed_precision_matches(cuda_lib, oracle_lib, small, neumann):
     L = 5
     f = small.forcing(0)
@@ -153,7 +153,7 @@ def test_mixed_precision_matches(cuda_lib, oracle_lib, small, neumann):
 
 
 @pytest.mark.parametrize("wind", [4.0, 14.0])
-@pytest.mark.parametrize("neumann", [0, 3])
+@pytest.mark.parametrize("neumann", [0, 5])
 def test_wind_regimes(cuda_lib, oracle_lib, wind, neumann):
     L = 5
     w = synth.Workload(1024, 2500.0, seed=9, wind_scale=wind)
@@ -322,8 +322,8 @@ def test_device_snow_state(cuda_lib, oracle_lib):
 
 @pytest.mark.parametrize("solver", [{}, {"precision": 1}, {"precision": 1, "warm_start": 1},
                                     {"precision": 1, "warm_start": 1, "autotune": 1},
-                                    {"precision": 1, "warm_start": 1, "neumann": 2}, {"neumann": 1}],
-                         ids=["fp64", "mixed", "mixed_previous", "autotuned", "mixed_previous_neumann2",
+                                    {"precision": 1, "warm_start": 1, "neumann": 5}, {"neumann": 1}],
+                         ids=["fp64", "mixed", "mixed_previous", "autotuned", "mixed_previous_neumann5",
                               "fp64_neumann1"])
 def test_graph_mode_matches_oracle(cuda_lib, oracle_lib, solver):
     """The whole step as one CUDA-graph launch (device-side control of the
