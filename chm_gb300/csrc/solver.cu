@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* 
 // from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
 // so the lateral kernels that follow take w in place of u.
 template <typename V, bool WRITE_W>
-__global__ void __launch_bounds__(kBlock) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
+__global__ void __launch_bounds__(kBlock, (sizeof(V) == 4 && !WRITE_W) ? 8 : 6) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
                                                      const V* __restrict__ zin, V* __restrict__ w,
                                                      V* __restrict__ zout, const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
