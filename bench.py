@@ -308,7 +308,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     if prof_file.exists():
         try:
             tr = json.loads(prof_file.read_text())
-            key = f"{capi.KERNELS[top]}:{head}"
+            key = f"{capi.KERNELS[top]}:{args.config}"
             if key in tr:
                 traffic = tr[key]
         except Exception:
