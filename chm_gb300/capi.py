@@ -12,7 +12,7 @@ import numpy as np
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libpbsm3d_cuda.so"
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 OK, ERR_INVALID_ARG, ERR_BAD_MESH, ERR_NAN_INPUT, ERR_NOT_CONVERGED, ERR_CUDA, ERR_UNSUPPORTED, ERR_OOM = (
     0, -1, -2, -3, -4, -5, -6, -7)
 STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "BAD_MESH", -3: "NAN_INPUT", -4: "NOT_CONVERGED", -5: "CUDA",
@@ -44,7 +44,10 @@ class Config(C.Structure):
         ("susp_maxit", C.c_int32), ("dep_maxit", C.c_int32),
         ("susp_tol", C.c_double), ("dep_tol", C.c_double), ("inner_tol", C.c_double),
         ("slice_width", C.c_int32), ("warm_flags", C.c_int32), ("graph", C.c_int32),
-        ("autotune", C.c_int32), ("neumann", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("autotune", C.c_int32), ("neumann", C.c_int32), ("derive_wind", C.c_int32),
+        ("wind_ignore_canopy", C.c_int32), ("derive_fetch", C.c_int32), ("fetch_steps", C.c_int32),
+        ("fetch_incl_veg", C.c_int32), ("reserved", C.c_int32 * 3), ("fetch_max_distance", C.c_double),
+        ("fetch_I", C.c_double),
     ]
 
 
@@ -108,7 +111,7 @@ EXPORTS = [
     "pbsm3d_deposition_solve_noalloc", "pbsm3d_mlp_num_params", "pbsm3d_mlp_features", "pbsm3d_mlp_trainer_create",
     "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
-    "pbsm3d_set_snow", "pbsm3d_get_snow",
+    "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr",
 ]
 
 _lib = None
@@ -138,6 +141,10 @@ def load(path: Path | None = None):
     lib.pbsm3d_set_snow.restype = C.c_int
     lib.pbsm3d_get_snow.argtypes = [vp, dp, dp, C.c_int]
     lib.pbsm3d_get_snow.restype = C.c_int
+    lib.pbsm3d_scale_wind_vert.argtypes = [vp, dp, dp, dp, C.c_int]
+    lib.pbsm3d_scale_wind_vert.restype = C.c_int
+    lib.pbsm3d_fetchr.argtypes = [vp, dp, dp, C.c_int]
+    lib.pbsm3d_fetchr.restype = C.c_int
     lib.pbsm3d_step.argtypes = [vp, C.POINTER(ForcingDesc), C.c_double, C.POINTER(Outputs), C.POINTER(Stats)]
     lib.pbsm3d_step.restype = C.c_int
     lib.pbsm3d_get_state.argtypes = [vp, _dp, _dp, _dp, _dp]

@@ -133,6 +133,10 @@ void pbsm3d_config_defaults(pbsm3d_config* cfg) {
     cfg->susp_maxit = 1000;
     cfg->dep_maxit = 1000;
     cfg->susp_tol = 1e-8;
+    cfg->fetch_steps = 10;  // fetchr.cpp:34-45
+    cfg->fetch_incl_veg = 1;
+    cfg->fetch_max_distance = 1000.0;
+    cfg->fetch_I = 0.06;
     cfg->dep_tol = 1e-10;
     cfg->inner_tol = 1e-5;
     cfg->slice_width = 0;
@@ -181,6 +185,11 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     if (cfg.debug_output) {
         g_create_error = "debug_output is not implemented";
         return PBSM3D_ERR_UNSUPPORTED;
+    }
+    if (cfg.fetch_steps < 1 || cfg.fetch_steps > 100000 || !(cfg.fetch_max_distance > 0) ||
+        !std::isfinite(cfg.fetch_max_distance) || !std::isfinite(cfg.fetch_I)) {
+        g_create_error = "fetch_steps must be in [1, 100000], fetch_max_distance positive, fetch_I finite";
+        return PBSM3D_ERR_INVALID_ARG;
     }
     if (cfg.neumann < 0 || cfg.neumann > 9) {
         g_create_error = "neumann must be in [0, 9]";
@@ -260,7 +269,7 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     P.z0_ustar_coupling = cfg.z0_ustar_coupling != 0;
     P.iterative_subl = cfg.iterative_subl != 0;
     P.subgrid = (cfg.use_subgrid_topo ? 1 : 0) | (cfg.use_subgrid_topo_V2 ? 2 : 0);
-    c.asm_kernels = P.subgrid ? 4 : 3;
+    c.asm_kernels = 3 + (P.subgrid ? 1 : 0) + (cfg.derive_wind ? 2 : 0) + (cfg.derive_fetch ? 1 : 0);
     c.member_offsets = offsets;
     const int nm = (int)members.size();
 
@@ -329,6 +338,15 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         S.more = sbuf + 7 * Tp;
         S.bsp = sbuf + 8 * Tp;
     }
+    c.wnd = Wind{};
+    c.wnd.cx = dalloc<double>(c, Tp, ok);
+    c.wnd.cy = dalloc<double>(c, Tp, ok);
+    c.wnd.cz = F.zc;
+    c.wnd.canopy = dalloc<double>(c, Tp, ok);
+    c.wnd.lai = dalloc<double>(c, Tp, ok);
+    c.wnd.tmp = dalloc<double>(c, Tp, ok);
+    c.wnd.grid = dalloc<GridM>(c, nm, ok);
+    c.wnd.cell_face = dalloc<int32_t>(c, T, ok);
     S.sub = nullptr;
     c.sg = Subgrid{};
     if (P.subgrid) {
@@ -466,6 +484,63 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     }
     rc |= upload(c, F.area, area.data(), Tp * 8);
     rc |= upload(c, F.zc, zc.data(), Tp * 8);
+    rc |= upload(c, c.wnd.cx, cx.data(), Tp * 8);
+    rc |= upload(c, c.wnd.cy, cy.data(), Tp * 8);
+    {
+        // the wind modules read the raw vegetation (scale_wind_vert.cpp:66-69,
+        // fetchr.cpp:66-72): canopy height 0 where a face has none
+        std::vector<double> wc(Tp, 0.0), wl(Tp, 0.0);
+        if (mesh->canopy_height)
+            for (int64_t i = 0; i < T; ++i)
+                if (!mesh->has_vegetation || mesh->has_vegetation[i]) {
+                    wc[i] = mesh->canopy_height[i];
+                    wl[i] = mesh->lai ? mesh->lai[i] : 0.0;
+                }
+        rc |= upload(c, c.wnd.canopy, wc.data(), Tp * 8);
+        rc |= upload(c, c.wnd.lai, wl.data(), Tp * 8);
+        // fetchr's nearest-face grids: per member, about one face centre per cell
+        std::vector<GridM> grids(nm);
+        std::vector<int32_t> cell_start(1, 0), cell_face(T);
+        for (int m = 0; m < nm; ++m) {
+            const int64_t f0 = offsets[m], f1 = offsets[m + 1], n = f1 - f0;
+            double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+            for (int64_t i = f0; i < f1; ++i) {
+                x0 = std::min(x0, cx[i]);
+                x1 = std::max(x1, cx[i]);
+                y0 = std::min(y0, cy[i]);
+                y1 = std::max(y1, cy[i]);
+            }
+            const double w = x1 - x0, hgt = y1 - y0;
+            double h = std::sqrt(w * hgt / (double)n);
+            if (!(h > 0) || !std::isfinite(h)) h = std::max(std::max(w, hgt) / std::max(1.0, std::sqrt((double)n)), 1.0);
+            GridM g{};
+            g.x0 = x0;
+            g.y0 = y0;
+            g.h = h;
+            g.nx = (int)std::min<int64_t>(std::max<int64_t>(1, (int64_t)std::floor(w / h) + 1), 1 << 20);
+            g.ny = (int)std::min<int64_t>(std::max<int64_t>(1, (int64_t)std::floor(hgt / h) + 1), 1 << 20);
+            g.cell0 = (int)(cell_start.size() - 1);
+            const int64_t nc = (int64_t)g.nx * g.ny;
+            std::vector<int32_t> cnt(nc + 1, 0);
+            auto cell_of = [&](int64_t i) {
+                const int ci = std::min(std::max((int)std::floor((cx[i] - g.x0) / g.h), 0), g.nx - 1);
+                const int cj = std::min(std::max((int)std::floor((cy[i] - g.y0) / g.h), 0), g.ny - 1);
+                return (int64_t)cj * g.nx + ci;
+            };
+            for (int64_t i = f0; i < f1; ++i) cnt[cell_of(i) + 1]++;
+            for (int64_t k = 0; k < nc; ++k) cnt[k + 1] += cnt[k];
+            std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
+            const int32_t base = cell_start.back();
+            for (int64_t i = f0; i < f1; ++i) cell_face[base + pos[cell_of(i)]++] = (int32_t)i;
+            for (int64_t k = 1; k <= nc; ++k) cell_start.push_back(base + cnt[k]);
+            grids[m] = g;
+        }
+        c.wnd.cell_start = dalloc<int32_t>(c, cell_start.size(), ok);
+        if (!ok) rc = 1;
+        rc |= upload(c, c.wnd.grid, grids.data(), nm * sizeof(GridM));
+        if (ok) rc |= upload(c, c.wnd.cell_start, cell_start.data(), cell_start.size() * 4);
+        rc |= upload(c, c.wnd.cell_face, cell_face.data(), T * 4);
+    }
     std::vector<double> canopy(Tp, 0.0), lai(Tp, 0.0), sN(Tp, 0.0), sD(Tp, 0.0);
     if (P.enable_veg)
         for (int64_t i = 0; i < T; ++i) {
@@ -805,8 +880,8 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         c.err = "missing forcing";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if ((c.cfg.use_exp_fetch || c.cfg.use_tanh_fetch) && !f->fetch) {
-        c.err = "fetch forcing is required by use_exp_fetch/use_tanh_fetch";
+    if ((c.cfg.use_exp_fetch || c.cfg.use_tanh_fetch) && !f->fetch && !c.cfg.derive_fetch) {
+        c.err = "fetch forcing is required by use_exp_fetch/use_tanh_fetch (or derive_fetch)";
         return PBSM3D_ERR_INVALID_ARG;
     }
     if (c.cfg.use_PomLi_probability && !f->p_snow_hours) {
@@ -834,11 +909,13 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         c.err = "forcing swe and snowdepthavg are required (or pbsm3d_set_snow)";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (!f->U_R || !f->U_2m_above_srf || !f->vw_dir || !f->t || !f->rh) {
-        c.err = "forcing U_R, U_2m_above_srf, vw_dir, t and rh are required";
+    const bool derive_wind = c.cfg.derive_wind != 0, derive_fetch = c.cfg.derive_fetch != 0;
+    if (!f->U_R || (!f->U_2m_above_srf && !derive_wind) || !f->vw_dir || !f->t || !f->rh) {
+        c.err = "forcing U_R, U_2m_above_srf (unless derive_wind), vw_dir, t and rh are required";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if ((rc = copy_in(c, c.Fo.UR, f->U_R, dev)) || (rc = copy_in(c, c.Fo.U2, f->U_2m_above_srf, dev)) ||
+    if ((rc = copy_in(c, c.Fo.UR, f->U_R, dev)) ||
+        (!derive_wind && (rc = copy_in(c, c.Fo.U2, f->U_2m_above_srf, dev))) ||
         (rc = copy_in(c, c.Fo.dir, f->vw_dir, dev)) || (rc = copy_in(c, c.Fo.t, f->t, dev)) ||
         (rc = copy_in(c, c.Fo.rh, f->rh, dev)))
         return rc;
@@ -847,9 +924,12 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         // a caller that passes its own snow state takes over from the context's
         c.snow_state = false;
     }
-    if (f->fetch && (rc = copy_in(c, c.Fo.fetch, f->fetch, dev))) return rc;
+    if (f->fetch && !derive_fetch && (rc = copy_in(c, c.Fo.fetch, f->fetch, dev))) return rc;
     if (f->p_snow_hours && (rc = copy_in(c, c.Fo.psh, f->p_snow_hours, dev))) return rc;
-    const int64_t h2d = dev ? 0 : c.P.T * 8 * ((own_snow ? 5 : 7) + (f->fetch ? 1 : 0) + (f->p_snow_hours ? 1 : 0));
+    const int64_t h2d = dev ? 0
+                            : c.P.T * 8 *
+                                  ((own_snow ? 5 : 7) - (derive_wind ? 1 : 0) + (f->fetch && !derive_fetch ? 1 : 0) +
+                                   (f->p_snow_hours ? 1 : 0));
 
     double susp_rhs_max = 0.0, dep_rhs_max = 0.0;
     // graph mode; with the autotuner on, the first step runs host-driven so
@@ -1044,6 +1124,50 @@ int pbsm3d_get_snow(pbsm3d_ctx* h, double* swe, double* depth, int on_device) {
     Ctx& c = h->c;
     int rc;
     if ((rc = copy_out(c, swe, c.Fo.swe, on_device)) || (rc = copy_out(c, depth, c.Fo.sd, on_device))) return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// staging buffers of the stand-alone wind calls, allocated on first use
+static int wind_staging(Ctx& c) {
+    if (c.wnd.in0) return 0;
+    bool ok = true;
+    c.wnd.in0 = dalloc<double>(c, c.P.Tp, ok);
+    c.wnd.in1 = dalloc<double>(c, c.P.Tp, ok);
+    c.wnd.out = dalloc<double>(c, c.P.Tp, ok);
+    if (!ok) {
+        c.err = "out of device memory for the wind staging buffers";
+        return PBSM3D_ERR_OUT_OF_MEMORY;
+    }
+    return 0;
+}
+
+int pbsm3d_scale_wind_vert(pbsm3d_ctx* h, const double* U_R, const double* snowdepthavg, double* U_2m_above_srf,
+                           int on_device) {
+    if (!h || !U_R || !U_2m_above_srf) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    int rc;
+    if ((rc = wind_staging(c))) return rc;
+    if ((rc = copy_in(c, c.wnd.in0, U_R, on_device))) return rc;
+    if (snowdepthavg && (rc = copy_in(c, c.wnd.in1, snowdepthavg, on_device))) return rc;
+    launch_scale_wind_vert(c, c.stream, c.wnd.in0, snowdepthavg ? c.wnd.in1 : nullptr, c.wnd.out);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    if ((rc = copy_out(c, U_2m_above_srf, c.wnd.out, on_device))) return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+int pbsm3d_fetchr(pbsm3d_ctx* h, const double* vw_dir, double* fetch, int on_device) {
+    if (!h || !vw_dir || !fetch) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    int rc;
+    if ((rc = wind_staging(c))) return rc;
+    if ((rc = copy_in(c, c.wnd.in0, vw_dir, on_device))) return rc;
+    launch_fetchr(c, c.stream, c.wnd.in0, c.wnd.out);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    if ((rc = copy_out(c, fetch, c.wnd.out, on_device))) return rc;
     PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return 0;
 }

@@ -86,6 +86,25 @@ struct FaceState {
 // contributing fraction that scales c_salt, and the other outputs.
 enum SubgridValue { SG_HOLD, SG_FRAC, SG_NOSNW, SG_TPILIM, SG_TESTINT, SG_COUNT };
 
+// Per-member uniform grid of face centres for the nearest-face queries of fetchr.
+struct GridM {
+    double x0, y0, h;
+    int nx, ny, cell0;  // this member's cells are [cell0, cell0 + nx * ny) of the concatenated list
+    int pad;
+};
+
+// The wind-input modules (scale_wind_vert, fetchr) on the device.
+struct Wind {
+    double *cx = nullptr, *cy = nullptr, *cz = nullptr;  // [Tp] face centres
+    double* canopy = nullptr;  // [Tp] canopy height, 0 on faces without vegetation
+    double* lai = nullptr;     // [Tp]
+    GridM* grid = nullptr;     // [n_members]
+    int32_t* cell_start = nullptr;  // [ncells + 1]
+    int32_t* cell_face = nullptr;   // [T] faces by cell
+    double* tmp = nullptr;     // [Tp] scale_wind_vert's per-face pass
+    double *in0 = nullptr, *in1 = nullptr, *out = nullptr;  // [Tp] staging of the stand-alone calls
+};
+
 // Static inputs of the subgrid branches (device).
 struct Subgrid {
     double* tpi;        // [5][Tp] TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean, TPI_neg_std (NaN = undefined)
@@ -217,6 +236,10 @@ void launch_consume_drift(Ctx& c, cudaStream_t s);
 void launch_subgrid(Ctx& c, cudaStream_t s);
 int subgrid_init(Ctx& c, cudaStream_t s);
 
+// wind.cu
+void launch_scale_wind_vert(Ctx& c, cudaStream_t s, const double* U_R, const double* sd, double* u2m);
+void launch_fetchr(Ctx& c, cudaStream_t s, const double* dir, double* fetch);
+
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 // graph mode: the device part of a step as one CUDA-graph launch (built on
@@ -243,7 +266,8 @@ struct Ctx {
     Forcing Fo;
     FaceState S;
     Subgrid sg;
-    int asm_kernels = 3;  // kernels of one suspension assembly (4 with a subgrid branch)
+    Wind wnd;
+    int asm_kernels = 3;  // kernels of one suspension assembly (+1 subgrid, +2 derived wind, +1 derived fetch)
     Susp A;
     Dep D;
     Members Mb;

@@ -913,6 +913,9 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     // out; per row 12 doubles out (+6 floats MIXED)
     prof_begin(c, s);
     cudaMemsetAsync(c.A.n_slow, 0, sizeof(int), s);
+    // the wind inputs on the device (scale_wind_vert, fetchr), when asked for
+    if (c.cfg.derive_wind) launch_scale_wind_vert(c, s, c.Fo.UR, c.Fo.sd, c.Fo.U2);
+    if (c.cfg.derive_fetch) launch_fetchr(c, s, c.Fo.dir, c.Fo.fetch);
     if (c.P.subgrid) launch_subgrid(c, s);
     k_salt_faces<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
     k_salt_rows<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Fo, c.A, c.Mb);

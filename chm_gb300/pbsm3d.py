@@ -197,6 +197,28 @@ class PBSM3D:
         self.last_stats = st.as_dict()
         return out
 
+    def scale_wind_vert(self, U_R, snowdepthavg=None) -> np.ndarray:
+        """U_2m_above_srf from U_R on the device (scale_wind_vert.cpp:53-227),
+        with the context's wind_ignore_canopy."""
+        u = np.ascontiguousarray(U_R, dtype=np.float64)
+        sd = None if snowdepthavg is None else np.ascontiguousarray(snowdepthavg, dtype=np.float64)
+        out = np.empty(self.n_faces)
+        rc = self._lib.pbsm3d_scale_wind_vert(self._ctx, capi.ptr(u), capi.ptr(sd) if sd is not None else None,
+                                              capi.ptr(out), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_scale_wind_vert")
+        return out
+
+    def fetchr(self, vw_dir) -> np.ndarray:
+        """fetch from vw_dir on the device (fetchr.cpp:55-117), with the
+        context's fetch_* settings."""
+        d = np.ascontiguousarray(vw_dir, dtype=np.float64)
+        out = np.empty(self.n_faces)
+        rc = self._lib.pbsm3d_fetchr(self._ctx, capi.ptr(d), capi.ptr(out), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_fetchr")
+        return out
+
     def output_keys(self) -> tuple:
         """The per-face outputs a step writes: the provides list of
         PBSM3D.cpp:188-218 that carries values (test_err is provided but never

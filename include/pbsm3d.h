@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define PBSM3D_ABI_VERSION 2
+#define PBSM3D_ABI_VERSION 3
 
 enum pbsm3d_status {
     PBSM3D_OK = 0,
@@ -131,7 +131,17 @@ typedef struct pbsm3d_config {
                                (tridiagonal) blocks, N the lateral couplings; 0 = B^-1 alone.
                                Odd K make A M^-1 = I - (N B^-1)^(K+1), whose spectrum stays on one
                                side of 1, and converge best */
+    /* The wind inputs on the device (the upstream modules of PBSM3D in a CHM
+     * configuration), see pbsm3d_scale_wind_vert / pbsm3d_fetchr below. */
+    int32_t derive_wind;         /* 1: every step computes U_2m_above_srf from U_R and the snow depth
+                                    (scale_wind_vert) and ignores the forcing's; 0 */
+    int32_t wind_ignore_canopy;  /* scale_wind_vert "ignore_canopy", false */
+    int32_t derive_fetch;        /* 1: every step computes fetch from vw_dir (fetchr); 0 */
+    int32_t fetch_steps;         /* fetchr "steps", 10 */
+    int32_t fetch_incl_veg;      /* fetchr "incl_veg", true */
     int32_t reserved[3];
+    double fetch_max_distance;   /* fetchr "max_distance", 1000 m */
+    double fetch_I;              /* fetchr "I", 0.06 */
 } pbsm3d_config;
 
 /*
@@ -339,6 +349,27 @@ int pbsm3d_set_state(pbsm3d_ctx* ctx, const double* sum_drift, const double* sum
  * reference module itself: this is the caller side of its drift_mass output. */
 int pbsm3d_set_snow(pbsm3d_ctx* ctx, const double* swe, const double* depth, double drift_density, int on_device);
 int pbsm3d_get_snow(pbsm3d_ctx* ctx, double* swe, double* depth, int on_device);
+
+/*
+ * The modules that produce PBSM3D's wind inputs, on the context's mesh (all
+ * members of an ensemble), with the settings in its config:
+ *   pbsm3d_scale_wind_vert <- scale_wind_vert::run(mesh&)   scale_wind_vert.cpp:53-227
+ *     U_2m_above_srf from U_R through the canopy/snow log-exp profile
+ *     (Atmosphere.cpp:32-46), then the thin plate spline of the three
+ *     neighbours' values at the face centre (TPSpline.cpp:55-157), >= 0.1.
+ *     snowdepthavg may be NULL (the reference's optional variable; 0).
+ *   pbsm3d_fetchr          <- fetchr::run                    fetchr.cpp:55-117
+ *     fetch (m) from vw_dir: the upwind search in fetch_steps steps of
+ *     fetch_max_distance/fetch_steps, each taking the face whose centre is
+ *     nearest the search point (a kd-tree query in the reference,
+ *     triangulation.cpp:170-178; a uniform grid per member here, lowest index
+ *     on a tie), nearest within the face's own member mesh.
+ * on_device as for the forcing.  With derive_wind / derive_fetch the step
+ * runs them itself, before the assembly.
+ */
+int pbsm3d_scale_wind_vert(pbsm3d_ctx* ctx, const double* U_R, const double* snowdepthavg, double* U_2m_above_srf,
+                           int on_device);
+int pbsm3d_fetchr(pbsm3d_ctx* ctx, const double* vw_dir, double* fetch, int on_device);
 
 /* Sliced-ELL export of the last assembled systems in the reference row order
  * (row = z*n_faces + face) and the reference graph's slot order: self, lateral

@@ -185,6 +185,103 @@ bool coupled_ustar(double u2, double lambda, double& ustar) {
     return bracket_solve(g, dg, 1.0, false, ustar);
 }
 
+// ----------------------------------------------------------- wind inputs
+// Atmosphere.cpp:41-46
+double exp_scale_wind(double u, double Z_in, double Z_out, double alpha) { return u * std::exp(alpha * (Z_out / Z_in - 1)); }
+
+// Exponential integral E1(x), x > 0 (gsl_sf_expint_E1 in the reference; GSL
+// version unpinned): the power series for x <= 1, the continued fraction
+// (modified Lentz) above (Press et al., Numerical Recipes, section 6.3).
+double expint_e1(double x) {
+    const double euler = 0.57721566490153286061;
+    if (x <= 1.0) {
+        double sum = 0, term = 1;
+        for (int k = 1; k < 200; ++k) {
+            term *= -x / k;
+            const double d = -term / k;
+            sum += d;
+            if (std::fabs(d) < std::fabs(sum) * 1e-17) break;
+        }
+        return -euler - std::log(x) + sum;
+    }
+    const double tiny = 1e-300;
+    double b = x + 1.0, cc = 1.0 / tiny, d = 1.0 / b, h = d;
+    for (int i = 1; i < 10000; ++i) {
+        const double an = -(double)i * i;
+        b += 2.0;
+        d = 1.0 / (an * d + b);
+        cc = b + an / cc;
+        const double del = cc * d;
+        h *= del;
+        if (std::fabs(del - 1.0) < 1e-17) break;
+    }
+    return h * std::exp(-x);
+}
+
+// thin_plate_spline::operator() (interpolation/TPSpline.cpp:55-157) for n <= 3
+// samples: the (n+1)x(n+1) system [1, R(x_i, x_j)] / [0, 1 ... 1] with the
+// basis R(d) = -(log(q) + c + E1(q)), q = (d weight / 2)^2, weight 0.01 and
+// the reference's c = 0.577215; solved by Gaussian elimination with full
+// pivoting (Eigen::FullPivLU in the reference), evaluated at the query.
+double tps_interp(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+    const double weight = 0.01, c = 0.577215;
+    auto basis = [&](double dx, double dy) {
+        double d = std::sqrt(dx * dx + dy * dy);
+        d = (d * weight / 2.0) * (d * weight / 2.0);
+        return -(std::log(d) + c + expint_e1(d));
+    };
+    const int m = n + 1;
+    double A[4][4] = {}, b[4] = {}, x[4] = {};
+    for (int i = 0; i < n; ++i)
+        for (int j = i; j < n; ++j) {
+            const double xd = sx[i] - sx[j], yd = sy[i] - sy[j];
+            if (xd == 0. && yd == 0.) continue;
+            const double Rd = j == i ? 0.0 : basis(xd, yd);
+            A[i][j + 1] = Rd;
+            A[j][i + 1] = Rd;
+        }
+    for (int i = 0; i < m; ++i) {
+        A[i][0] = 1;
+        A[m - 1][i] = 1;
+    }
+    A[m - 1][0] = 0;
+    for (int i = 0; i < n; ++i) b[i] = sz[i];
+    b[m - 1] = 0.0;
+    // full-pivot elimination
+    int colp[4] = {0, 1, 2, 3};
+    for (int k = 0; k < m; ++k) {
+        int pr = k, pc = k;
+        double best = -1;
+        for (int i = k; i < m; ++i)
+            for (int j = k; j < m; ++j)
+                if (std::fabs(A[i][j]) > best) {
+                    best = std::fabs(A[i][j]);
+                    pr = i;
+                    pc = j;
+                }
+        if (best == 0) break;
+        for (int j = 0; j < m; ++j) std::swap(A[k][j], A[pr][j]);
+        std::swap(b[k], b[pr]);
+        for (int i = 0; i < m; ++i) std::swap(A[i][k], A[i][pc]);
+        std::swap(colp[k], colp[pc]);
+        for (int i = k + 1; i < m; ++i) {
+            const double f = A[i][k] / A[k][k];
+            for (int j = k; j < m; ++j) A[i][j] -= f * A[k][j];
+            b[i] -= f * b[k];
+        }
+    }
+    double y[4] = {};
+    for (int k = m - 1; k >= 0; --k) {
+        double v = b[k];
+        for (int j = k + 1; j < m; ++j) v -= A[k][j] * y[j];
+        y[k] = A[k][k] != 0 ? v / A[k][k] : 0.0;
+    }
+    for (int k = 0; k < m; ++k) x[colp[k]] = y[k];
+    double z0 = x[0];
+    for (int i = 1; i < m; ++i) z0 += x[i] * basis(sx[i - 1] - qx, sy[i - 1] - qy);
+    return z0;
+}
+
 // ---------------------------------------------------- subgrid topography
 inline double smin(double a, double b) { return (b < a) ? b : a; }  // std::min
 
@@ -743,6 +840,9 @@ struct oracle_ctx {
     double dt = 0;
     // face variables
     std::vector<double> Qsalt, Qsusp, Qsubl, Qsubl_mass, sum_subl, drift_mass, sum_drift, more_than_avail, bsp;
+    // raw vegetation (the wind modules read it whatever PBSM3D's enable_veg says)
+    std::vector<uint8_t> has_veg;
+    std::vector<double> canopy_raw, lai_raw;
     // subgrid TPI parameters [5][T] (NaN = undefined) and the subgrid outputs
     std::vector<double> tpi, frac_contrib, frac_contrib_nosnw, hold_topo, tpi_lim, test_int;
     System susp, dep;
@@ -916,6 +1016,15 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
             }
         }
     }
+    c->has_veg.assign(T, 0);
+    c->canopy_raw.assign(T, 0);
+    c->lai_raw.assign(T, 0);
+    if (mesh->canopy_height)
+        for (int64_t i = 0; i < T; ++i) {
+            c->has_veg[i] = mesh->has_vegetation ? mesh->has_vegetation[i] : 1;
+            c->canopy_raw[i] = mesh->canopy_height[i];
+            c->lai_raw[i] = mesh->lai ? mesh->lai[i] : 0.0;
+        }
     c->water.assign(T, 0);
     if (mesh->is_water) c->water.assign(mesh->is_water, mesh->is_water + T);
     // prism areas and neighbour flags (PBSM3D.cpp:362-392)
@@ -1589,6 +1698,116 @@ int oracle_get_system(const oracle_ctx* c, int32_t which, int64_t* rowptr, int32
     if (x) std::memcpy(x, S.x.data(), S.x.size() * sizeof(double));
     return 0;
 }
+// scale_wind_vert::run(mesh&) (scale_wind_vert.cpp:53-227): per face the
+// wind 2 m above the snow from U_R through the canopy profile (point_scale),
+// then the thin plate spline of the neighbours' values at the face centre,
+// clamped at 0.1 m/s.
+int oracle_scale_wind_vert(const oracle_ctx* c, int ignore_canopy, const double* U_R, const double* snowdepthavg,
+                           double* u2m) {
+    const int64_t T = c->T;
+    std::vector<double> pt(T);
+    for (int64_t i = 0; i < T; ++i) {
+        const double U = U_R[i];
+        const double Z_R = kZUR;
+        double Z_CanTop = 0;
+        if (!ignore_canopy && c->has_veg[i]) Z_CanTop = c->canopy_raw[i];
+        const double Z_CanBot = Z_CanTop / 2.0;
+        double sd = snowdepthavg ? snowdepthavg[i] : 0.0;
+        if (is_nan(sd)) sd = 0.0;
+        const double Z_2m = sd + 2.0;
+        if (Z_2m >= Z_R) {
+            pt[i] = U;
+            continue;
+        }
+        double u;
+        if (!ignore_canopy && (Z_CanTop > 0.0) && (Z_2m < Z_CanTop)) {
+            const double alpha = c->lai_raw[i];
+            if (sd < Z_CanTop) {
+                const double U_CanTop = log_scale_wind(U, Z_R, Z_CanTop, sd, kZ0Snow);
+                const double U_CanBot = exp_scale_wind(U_CanTop, Z_CanTop, Z_CanBot, alpha);
+                if (Z_2m < Z_CanBot)
+                    u = log_scale_wind(U_CanBot, Z_CanBot, Z_2m, sd, kZ0Snow);
+                else
+                    u = exp_scale_wind(U_CanTop, Z_CanTop, Z_2m, alpha);
+            } else {
+                u = log_scale_wind(U, Z_R, Z_2m, sd, kZ0Snow);
+            }
+        } else {
+            u = log_scale_wind(U, Z_R, Z_2m, sd, kZ0Snow);
+        }
+        pt[i] = smax(0.1, u);
+    }
+    for (int64_t i = 0; i < T; ++i) {
+        double sx[3], sy[3], sz[3];
+        int n = 0;
+        for (int j = 0; j < 3; ++j) {
+            const int32_t nb = c->nbr[3 * i + j];
+            if (nb < 0) continue;
+            sx[n] = c->center[3 * nb];
+            sy[n] = c->center[3 * nb + 1];
+            sz[n] = pt[nb];
+            ++n;
+        }
+        if (n > 0)
+            u2m[i] = smax(0.1, tps_interp(sx, sy, sz, n, c->center[3 * i], c->center[3 * i + 1]));
+        else
+            u2m[i] = smax(0.1, pt[i]);
+    }
+    return 0;
+}
+
+// fetchr::run (fetchr.cpp:55-117): upwind search along vw_dir in `steps`
+// steps of max_distance/steps; each step takes the face whose centre is
+// nearest the point at that distance (brute force here; a kd-tree of face
+// centres in the reference, triangulation.cpp:170-178; the lowest index wins
+// a tie) and stops at the first that is higher than the rising line of slope
+// I, or (incl_veg) within the internal-boundary-layer recovery length.
+int oracle_fetchr(const oracle_ctx* c, int steps, double max_distance, double I, int incl_veg, const double* vw_dir,
+                  double* fetch) {
+    const int64_t T = c->T;
+    const double size_of_step = max_distance / steps;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < T; ++i) {
+        fetch[i] = max_distance;
+        if (incl_veg && c->has_veg[i] && c->canopy_raw[i] > 1) {
+            fetch[i] = 0;
+            continue;
+        }
+        const double br = vw_dir[i] * (M_PI / 180.0);
+        const double cx = c->center[3 * i], cy = c->center[3 * i + 1], cz = c->center[3 * i + 2];
+        for (int j = 1; j <= steps; ++j) {
+            const double distance = j * size_of_step;
+            const double qx = cx + distance * std::sin(br), qy = cy + distance * std::cos(br);
+            int64_t f = 0;
+            double best = INFINITY;
+            for (int64_t k = 0; k < T; ++k) {
+                const double dx = c->center[3 * k] - qx, dy = c->center[3 * k + 1] - qy;
+                const double d2 = dx * dx + dy * dy;
+                if (d2 < best) {
+                    best = d2;
+                    f = k;
+                }
+            }
+            double Z_CanTop = 0;
+            if (incl_veg && c->has_veg[f]) Z_CanTop = c->canopy_raw[f];
+            const double Z_test = c->center[3 * f + 2] + Z_CanTop;
+            const double Z_core = cz + distance * I;
+            const double z0_1 = 0.12 * Z_CanTop, z0_2 = 0.001, n = 1.0 / 0.8, h = 5;
+            const double x_sss = std::pow(((33.33333333 * h - 25. * z0_2) / (std::log(z0_1 / z0_2) * z0_2)), n) * z0_2;
+            if (Z_test >= Z_core || (incl_veg && distance < x_sss)) {
+                fetch[i] = distance;
+                break;
+            }
+        }
+    }
+    return 0;
+}
+
+double oracle_expint_e1(double x) { return expint_e1(x); }
+double oracle_tps(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+    return tps_interp(sx, sy, sz, n, qx, qy);
+}
+
 int oracle_get_face_fields(const oracle_ctx* c, double* saltation, double* hs, double* z0, double* ustar,
                            double* c_salt, double* ustar_th, double* u_z, double* csubl) {
     if (saltation)

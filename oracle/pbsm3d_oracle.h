@@ -96,6 +96,14 @@ double oracle_gamma_pdf(double x, double a, double b);
  * hold_topo, frac_contrib, frac_contrib_nosnw, tpi_lim, test_int (-9999 when
  * the normalisation integral is not evaluated) */
 void oracle_subgrid_face(const pbsm3d_config* cfg, double snow_depth, const double* tpi, double* out);
+/* the wind-input modules: scale_wind_vert (U_2m_above_srf from U_R) and fetchr
+ * (fetch from vw_dir) over the context's mesh; snowdepthavg may be NULL */
+int oracle_scale_wind_vert(const oracle_ctx* c, int ignore_canopy, const double* U_R, const double* snowdepthavg,
+                           double* u2m);
+int oracle_fetchr(const oracle_ctx* c, int steps, double max_distance, double I, int incl_veg, const double* vw_dir,
+                  double* fetch);
+double oracle_expint_e1(double x);
+double oracle_tps(const double* sx, const double* sy, const double* sz, int n, double qx, double qy);
 /* Face geometry of a triangle mesh (triangulation.hpp:1443-1498,1577-1589,1830-1856).
  * xyz [3*nv], tri [3*nt] vertex ids; outputs [3*nt], [6*nt], [nt], [3*nt]. */
 void oracle_face_geometry(int64_t nv, const double* xyz, int64_t nt, const int32_t* tri, double* edge_length,

@@ -83,6 +83,14 @@ def load():
     lib.oracle_gamma_pdf.restype = C.c_double
     lib.oracle_subgrid_face.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.oracle_subgrid_face.restype = None
+    lib.oracle_scale_wind_vert.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double)]
+    lib.oracle_fetchr.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
+    lib.oracle_expint_e1.argtypes = [C.c_double]
+    lib.oracle_expint_e1.restype = C.c_double
+    lib.oracle_tps.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int, C.c_double, C.c_double]
+    lib.oracle_tps.restype = C.c_double
     lib.oracle_face_geometry.argtypes = [C.c_int64, _dp, C.c_int64, _i32p, _dp, _dp, _dp, _dp]
     lib.oracle_face_geometry.restype = None
     lib.oracle_face_neighbors.argtypes = [C.c_int64, C.c_int64, _i32p, _i32p]
@@ -223,6 +231,20 @@ class Oracle:
         self.lib.oracle_get_system(self.ctx, which, ptr(rp, C.c_int64), ptr(cols, C.c_int32), ptr(vals), ptr(rhs),
                                    ptr(x))
         return rp, cols, vals, rhs, x
+
+    def scale_wind_vert(self, U_R, snowdepthavg=None, ignore_canopy=False):
+        u = np.ascontiguousarray(U_R, dtype=np.float64)
+        sd = None if snowdepthavg is None else np.ascontiguousarray(snowdepthavg, dtype=np.float64)
+        out = np.empty(self.n)
+        self.lib.oracle_scale_wind_vert(self.ctx, int(ignore_canopy), ptr(u), ptr(sd) if sd is not None else None,
+                                        ptr(out))
+        return out
+
+    def fetchr(self, vw_dir, steps=10, max_distance=1000.0, I=0.06, incl_veg=True):
+        d = np.ascontiguousarray(vw_dir, dtype=np.float64)
+        out = np.empty(self.n)
+        self.lib.oracle_fetchr(self.ctx, int(steps), float(max_distance), float(I), int(incl_veg), ptr(d), ptr(out))
+        return out
 
     def face_fields(self):
         n, L = self.n, self.L

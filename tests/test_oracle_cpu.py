@@ -476,3 +476,85 @@ def test_subgrid_v1_face(oracle_lib):
             hold = (1 - fn) * msd + fn * (msd * gP(msd) + hint + sd * gQ(sd))
         assert abs(out[1] - frac) < 1e-11 and abs(out[2] - (1 - fn)) < 1e-15
         assert abs(out[0] - hold) <= 1e-9 * max(1.0, abs(hold)), (sd, fn, mn, sn, out[0], hold)
+
+
+def test_expint_e1(oracle_lib):
+    """The exponential integral of the thin-plate-spline basis against scipy."""
+    from scipy import special
+    for x in np.concatenate([np.geomspace(1e-8, 700, 400), [0.5, 1.0, 1.0000001, 2.0]]):
+        ref = special.exp1(x)
+        assert abs(oracle_lib.oracle_expint_e1(x) - ref) <= 1e-14 * ref + 1e-300, x
+
+
+def _tps_numpy(sx, sy, sz, qx, qy):
+    """interpolation/TPSpline.cpp:55-157 with numpy (dense solve)."""
+    from scipy import special
+    n = len(sx)
+
+    def basis(dx, dy):
+        d = math.hypot(dx, dy)
+        d = (d * 0.01 / 2.0) ** 2
+        return -(math.log(d) + 0.577215 + special.exp1(d))
+    A = np.zeros((n + 1, n + 1))
+    for i in range(n):
+        for j in range(i + 1, n):
+            A[i, j + 1] = A[j, i + 1] = basis(sx[i] - sx[j], sy[i] - sy[j])
+    A[:, 0] = 1
+    A[n, :] = 1
+    A[n, 0] = 0
+    b = np.append(np.asarray(sz, float), 0.0)
+    x = np.linalg.solve(A, b)
+    return x[0] + sum(x[i + 1] * basis(sx[i] - qx, sy[i] - qy) for i in range(n))
+
+
+def test_thin_plate_spline(oracle_lib):
+    rng = np.random.default_rng(8)
+    dp = C.POINTER(C.c_double)
+    for n in (1, 2, 3):
+        for _ in range(200):
+            sx, sy = rng.uniform(0, 300, n), rng.uniform(0, 300, n)
+            sz = rng.uniform(0.1, 15, n)
+            qx, qy = rng.uniform(0, 300), rng.uniform(0, 300)
+            a = [np.ascontiguousarray(v) for v in (sx, sy, sz)]
+            got = oracle_lib.oracle_tps(*[v.ctypes.data_as(dp) for v in a], n, qx, qy)
+            ref = _tps_numpy(sx, sy, sz, qx, qy)
+            assert abs(got - ref) <= 1e-9 * max(1.0, abs(ref)), (n, got, ref)
+    # interpolates its samples
+    sx, sy, sz = np.array([0., 100., 30.]), np.array([0., 10., 90.]), np.array([3., 5., 7.])
+    a = [np.ascontiguousarray(v) for v in (sx, sy, sz)]
+    for k in range(3):
+        got = oracle_lib.oracle_tps(*[v.ctypes.data_as(dp) for v in a], 3, sx[k] + 1e-9, sy[k])
+        assert abs(got - sz[k]) < 1e-5
+
+
+def test_wind_modules_oracle(oracle_lib):
+    """scale_wind_vert keeps U_2m within the neighbours' range and at least
+    0.1 m/s; fetchr is max_distance on flat open ground, 0 under tall canopy,
+    and shortens upwind of a ridge."""
+    from oracle import pyoracle
+    w = synth.Workload(600, 1500.0, seed=2)
+    o = pyoracle.Oracle(w.mesh, nLayer=3)
+    f = w.forcing(0)
+    u2 = o.scale_wind_vert(f.U_R, f.snowdepthavg)
+    assert (u2 >= 0.1).all() and np.isfinite(u2).all()
+    n = w.mesh.n_faces
+    flat = synth.Workload(600, 1500.0, seed=2)
+    flat.mesh.center = flat.mesh.center.copy()
+    flat.mesh.center[:, 2] = 0.0
+    of = pyoracle.Oracle(flat.mesh, nLayer=3)
+    fe = of.fetchr(np.full(n, 270.0), incl_veg=False)
+    assert (fe == 1000.0).all()
+    tall = synth.Workload(600, 1500.0, seed=2)
+    tall.mesh.canopy_height = np.full(n, 2.0)
+    ot = pyoracle.Oracle(tall.mesh, nLayer=3)
+    assert (ot.fetchr(np.full(n, 270.0)) == 0.0).all()
+    # a ridge to the west: faces east of it see a short fetch from 270 deg
+    ridge = synth.Workload(600, 1500.0, seed=2)
+    ridge.mesh.center = ridge.mesh.center.copy()
+    x = ridge.mesh.center[:, 0]
+    ridge.mesh.center[:, 2] = np.where(np.abs(x - 500.0) < 60.0, 100.0, 0.0)
+    orr = pyoracle.Oracle(ridge.mesh, nLayer=3)
+    fr = orr.fetchr(np.full(n, 270.0), incl_veg=False)
+    east = (x > 600) & (x < 900)
+    assert (fr[east] < 1000.0).mean() > 0.9
+    assert (fr[x < 400] == 1000.0).mean() > 0.9
