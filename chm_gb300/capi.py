@@ -55,6 +55,10 @@ TPI_FIELDS = ("tpi_mean", "tpi_std", "tpi_neg_frac", "tpi_neg_mean", "tpi_neg_st
 SUBGRID_OUTPUTS = ("frac_contrib", "frac_contrib_nosnw", "hold_topo", "tpi_lim", "test_int")
 
 
+class MeshError(RuntimeError):
+    """A mesh file the native reader refused."""
+
+
 class MeshDesc(C.Structure):
     _fields_ = [
         ("n_faces", C.c_int64), ("neighbor", _i32p), ("edge_length", _dp), ("edge_normal", _dp), ("area", _dp),
@@ -111,7 +115,8 @@ EXPORTS = [
     "pbsm3d_deposition_solve_noalloc", "pbsm3d_mlp_num_params", "pbsm3d_mlp_features", "pbsm3d_mlp_trainer_create",
     "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
-    "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr",
+    "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr", "pbsm3d_mesh_read",
+    "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error",
 ]
 
 _lib = None
@@ -145,6 +150,16 @@ def load(path: Path | None = None):
     lib.pbsm3d_scale_wind_vert.restype = C.c_int
     lib.pbsm3d_fetchr.argtypes = [vp, dp, dp, C.c_int]
     lib.pbsm3d_fetchr.restype = C.c_int
+    lib.pbsm3d_mesh_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
+    lib.pbsm3d_mesh_read.restype = C.c_int
+    lib.pbsm3d_mesh_describe.argtypes = [vp, C.POINTER(MeshDesc)]
+    lib.pbsm3d_mesh_describe.restype = C.c_int
+    lib.pbsm3d_mesh_arrays.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(dp), C.POINTER(C.POINTER(C.c_int32))]
+    lib.pbsm3d_mesh_arrays.restype = C.c_int
+    lib.pbsm3d_mesh_free.argtypes = [vp]
+    lib.pbsm3d_mesh_free.restype = None
+    lib.pbsm3d_mesh_last_error.argtypes = []
+    lib.pbsm3d_mesh_last_error.restype = C.c_char_p
     lib.pbsm3d_step.argtypes = [vp, C.POINTER(ForcingDesc), C.c_double, C.POINTER(Outputs), C.POINTER(Stats)]
     lib.pbsm3d_step.restype = C.c_int
     lib.pbsm3d_get_state.argtypes = [vp, _dp, _dp, _dp, _dp]

@@ -371,6 +371,26 @@ int pbsm3d_scale_wind_vert(pbsm3d_ctx* ctx, const double* U_R, const double* sno
                            int on_device);
 int pbsm3d_fetchr(pbsm3d_ctx* ctx, const double* vw_dir, double* fetch, int on_device);
 
+/*
+ * CHM's JSON mesh files (triangulation.cpp:206-356): a .mesh file
+ * {"mesh": {"vertex", "elem", "neigh", "nvertex", "nelem", "is_geographic", ...}}
+ * and an optional .param file of per-face parameters.  The geometry is
+ * computed as CHM's face class does; the neighbour lists are taken as given.
+ * Parameters read: area, TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean,
+ * TPI_neg_std, CanopyHeight, LAI (the last two stand in for CHM's landcover
+ * table).  Geographic meshes return PBSM3D_ERR_UNSUPPORTED; malformed files
+ * PBSM3D_ERR_BAD_MESH with the reason in pbsm3d_mesh_last_error().
+ * pbsm3d_mesh_describe fills a description whose arrays point into the mesh
+ * (valid until pbsm3d_mesh_free).  The HDF5 mesh and partition formats are not
+ * read.
+ */
+typedef struct pbsm3d_mesh pbsm3d_mesh;
+int pbsm3d_mesh_read(const char* mesh_path, const char* param_path, pbsm3d_mesh** out);
+int pbsm3d_mesh_describe(const pbsm3d_mesh* mesh, pbsm3d_mesh_desc* desc);
+int pbsm3d_mesh_arrays(const pbsm3d_mesh* mesh, int64_t* n_vertices, const double** vertex, const int32_t** elem);
+void pbsm3d_mesh_free(pbsm3d_mesh* mesh);
+const char* pbsm3d_mesh_last_error(void);
+
 /* Sliced-ELL export of the last assembled systems in the reference row order
  * (row = z*n_faces + face) and the reference graph's slot order: self, lateral
  * neighbours in face order 0..2 (present ones only), below, above

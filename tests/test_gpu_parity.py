@@ -378,3 +378,27 @@ def test_graph_mode_errors_and_state(cuda_lib, small):
         m.close()
     for a, b in zip(outs[0], outs[1]):
         assert relerr(b, a) < 1e-6
+
+
+def test_native_mesh_reader_end_to_end(cuda_lib, oracle_lib, tmp_path):
+    """The reference's slope mesh in CHM's JSON layout, read by the library's
+    native reader and stepped on the GPU, against the oracle on the same
+    mesh."""
+    from conftest import GOLDEN
+    from chm_gb300.meshio import ChmMesh, write_chm_mesh
+    d = np.load(GOLDEN / "slope_mesh.npz")
+    write_chm_mesh(tmp_path / "slope.mesh", d["vertex"], d["elem"], d["neigh"], {"area": d["area"]},
+                   tmp_path / "slope.param")
+    mesh = ChmMesh(tmp_path / "slope.mesh", tmp_path / "slope.param")
+    n = mesh.n_faces
+    rng = np.random.default_rng(3)
+    f = {"U_R": rng.uniform(8, 20, n), "U_2m_above_srf": rng.uniform(5, 12, n),
+         "vw_dir": np.full(n, 250.0) + rng.normal(0, 10, n), "swe": rng.uniform(20, 200, n),
+         "t": rng.uniform(-15, -2, n), "rh": rng.uniform(60, 95, n), "snowdepthavg": rng.uniform(0.2, 1.0, n),
+         "fetch": np.full(n, 1000.0)}
+    m = gpu_module(mesh, 6)
+    out = m.run(f, 3600.0, want_c=True)
+    ref, _ = oracle(mesh, 6).step_exact(f, 3600.0)
+    for k in FIELDS:
+        assert relerr(out[k], ref[k]) < FIELD_TOL, (k, relerr(out[k], ref[k]))
+    m.close()
