@@ -116,7 +116,7 @@ EXPORTS = [
     "pbsm3d_mlp_train", "pbsm3d_mlp_grad", "pbsm3d_mlp_get_params", "pbsm3d_mlp_trainer_destroy",
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
     "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr", "pbsm3d_mesh_read",
-    "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error",
+    "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error", "pbsm3d_get_debug",
 ]
 
 _lib = None
@@ -150,6 +150,8 @@ def load(path: Path | None = None):
     lib.pbsm3d_scale_wind_vert.restype = C.c_int
     lib.pbsm3d_fetchr.argtypes = [vp, dp, dp, C.c_int]
     lib.pbsm3d_fetchr.restype = C.c_int
+    lib.pbsm3d_get_debug.argtypes = [vp, C.c_char_p, dp, C.c_int]
+    lib.pbsm3d_get_debug.restype = C.c_int
     lib.pbsm3d_mesh_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
     lib.pbsm3d_mesh_read.restype = C.c_int
     lib.pbsm3d_mesh_describe.argtypes = [vp, C.POINTER(MeshDesc)]

@@ -182,10 +182,6 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "nLayer must be in [1, 64]";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg.debug_output) {
-        g_create_error = "debug_output is not implemented";
-        return PBSM3D_ERR_UNSUPPORTED;
-    }
     if (cfg.fetch_steps < 1 || cfg.fetch_steps > 100000 || !(cfg.fetch_max_distance > 0) ||
         !std::isfinite(cfg.fetch_max_distance) || !std::isfinite(cfg.fetch_I)) {
         g_create_error = "fetch_steps must be in [1, 100000], fetch_max_distance positive, fetch_I finite";
@@ -271,6 +267,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     P.subgrid = (cfg.use_subgrid_topo ? 1 : 0) | (cfg.use_subgrid_topo_V2 ? 2 : 0);
     c.asm_kernels = 3 + (P.subgrid ? 1 : 0) + (cfg.derive_wind ? 2 : 0) + (cfg.derive_fetch ? 1 : 0);
     c.member_offsets = offsets;
+    c.member_z0.resize(members.size());
+    for (size_t m = 0; m < members.size(); ++m) c.member_z0[m] = members[m].z0;
     const int nm = (int)members.size();
 
     int sms = 0, dev = 0;
@@ -1124,6 +1122,73 @@ int pbsm3d_get_snow(pbsm3d_ctx* h, double* swe, double* depth, int on_device) {
     Ctx& c = h->c;
     int rc;
     if ((rc = copy_out(c, swe, c.Fo.swe, on_device)) || (rc = copy_out(c, depth, c.Fo.sd, on_device))) return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// Diagnostics of the last step by the reference's debug_output names
+// (PBSM3D.cpp:141-186): per face "hs", "ustar", "u*_th", "csalt", "z0",
+// "is_drifting"; per layer z "c<z>", "csubl<z>", "u_z<z>", "cz<z>".
+int pbsm3d_get_debug(pbsm3d_ctx* h, const char* name, double* out, int on_device) {
+    if (!h || !name || !out) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    const int64_t T = c.P.T, Tp = c.P.Tp;
+    const std::string n(name);
+    auto face_row = [&](int fv) { return copy_out(c, out, c.A.face_v + (size_t)fv * Tp, on_device); };
+    auto layer_of = [&](const char* prefix, int& z) -> bool {
+        const size_t lp = strlen(prefix);
+        if (n.size() <= lp || n.compare(0, lp, prefix) != 0) return false;
+        const std::string rest = n.substr(lp);
+        if (rest.find_first_not_of("0123456789") != std::string::npos || rest.size() > 3) return false;
+        z = std::stoi(rest);
+        return z >= 0 && z < c.P.L;
+    };
+    // host-computed rows (copied to the device when asked for there)
+    auto put_host = [&](const std::vector<double>& v) -> int {
+        PBSM_CUDA_TRY(cudaMemcpy(out, v.data(), T * 8, on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost));
+        return 0;
+    };
+    int rc = 0, z = 0;
+    if (n == "hs")
+        rc = face_row(FV_HS);
+    else if (n == "ustar")
+        rc = face_row(FV_USTAR);
+    else if (n == "u*_th")
+        rc = face_row(FV_UTH);
+    else if (n == "csalt")
+        rc = face_row(FV_CSALT);
+    else if (n == "z0" && c.P.z0_ustar_coupling)
+        rc = face_row(FV_Z0);  // written for every face by the saltation pass with the coupling
+    else if (n == "z0") {
+        std::vector<double> z0v(T);
+        for (int m = 0; m < (int)c.member_offsets.size() - 1; ++m)
+            for (int64_t i = c.member_offsets[m]; i < c.member_offsets[m + 1]; ++i) z0v[i] = c.member_z0[m];
+        rc = put_host(z0v);
+    } else if (n == "is_drifting") {
+        std::vector<uint8_t> salt(T);
+        PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        PBSM_CUDA_TRY(cudaMemcpy(salt.data(), c.S.saltation, T, cudaMemcpyDeviceToHost));
+        std::vector<double> v(T);
+        for (int64_t i = 0; i < T; ++i) v[i] = salt[i] ? 1.0 : 0.0;
+        rc = put_host(v);
+    } else if (layer_of("csubl", z))
+        rc = copy_out(c, out, c.A.csubl + (size_t)z * Tp, on_device);
+    else if (layer_of("u_z", z))
+        rc = copy_out(c, out, c.A.u_z + (size_t)z * Tp, on_device);
+    else if (layer_of("cz", z)) {
+        std::vector<double> hs(T), v(T);
+        PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+        PBSM_CUDA_TRY(cudaMemcpy(hs.data(), c.A.face_v + (size_t)FV_HS * Tp, T * 8, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < T; ++i) v[i] = z * c.P.dz + hs[i] + c.P.dz / 2.;  // PBSM3D.cpp:941
+        rc = put_host(v);
+    } else if (layer_of("c", z))
+        rc = copy_out(c, out, c.A.x + (size_t)z * Tp, on_device);
+    else {
+        c.err = "unknown diagnostic " + n;
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (rc) return rc;
     PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
     return 0;
 }

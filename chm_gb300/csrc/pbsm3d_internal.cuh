@@ -272,6 +272,7 @@ struct Ctx {
     Dep D;
     Members Mb;
     std::vector<int64_t> member_offsets;  // host, [n+1] face ranges
+    std::vector<double> member_z0;        // host, [n] snow roughness of each member
     double target_scale2 = 1.0;           // min_m ||b_m||^2 / ||b||^2 over present members
     double dep_target_scale2 = 1.0;
     // Krylov work vectors (FP64), [R] each

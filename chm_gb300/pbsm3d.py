@@ -97,6 +97,9 @@ class PBSM3D:
         self.use_R94_lambda = g("use_R94_lambda", True)
         self.provides.append("blowingsnow_probability")
         self.debug_output = g("debug_output", False)
+        if self.debug_output:  # PBSM3D.cpp:141-186, the diagnostics this library keeps (debug())
+            self.provides += ["hs", "ustar", "u*_th", "csalt", "z0", "is_drifting"]
+            self.provides += [f"{v}{z}" for z in range(int(g("nLayer", 10))) for v in ("c", "csubl", "u_z", "cz")]
         self.provides += ["Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "Qsusp", "Qsalt", "sum_drift"]
         if self.use_subgrid_topo:
             self.provides += ["frac_contrib", "frac_contrib_nosnw", "hold_topo"]
@@ -217,6 +220,16 @@ class PBSM3D:
         rc = self._lib.pbsm3d_fetchr(self._ctx, capi.ptr(d), capi.ptr(out), 0)
         if rc != 0:
             self._error(rc, "pbsm3d_fetchr")
+        return out
+
+    def debug(self, name: str) -> np.ndarray:
+        """A diagnostic of the last step by its debug_output name ("hs",
+        "ustar", "u*_th", "csalt", "z0", "is_drifting", "c<z>", "csubl<z>",
+        "u_z<z>", "cz<z>")."""
+        out = np.empty(self.n_faces)
+        rc = self._lib.pbsm3d_get_debug(self._ctx, name.encode(), capi.ptr(out), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_get_debug")
         return out
 
     def output_keys(self) -> tuple:

@@ -42,6 +42,11 @@ PBSM3D::PBSM3D(config_file c) : module_base("PBSM3D", parallel::domain, c) {
         for (const char* v : {"frac_contrib", "frac_contrib_nosnw", "hold_topo"}) provides(v);
     if (use_subgrid_topo_V2)  // :211-218
         for (const char* v : {"frac_contrib", "hold_topo", "test_int", "test_err", "tpi_lim"}) provides(v);
+    if (cfg.get("debug_output", false)) {  // PBSM3D.cpp:141-186, the variables kept here
+        for (const char* v : {"hs", "ustar", "u*_th", "csalt", "z0", "is_drifting"}) provides(v);
+        for (int z = 0; z < cfg.get("nLayer", 10); ++z)
+            for (const char* v : {"c", "csubl", "u_z", "cz"}) provides(v + std::to_string(z));
+    }
     pbsm3d_config_defaults(&gpu_cfg);
 }
 
@@ -140,6 +145,16 @@ void PBSM3D::run(mesh& domain) {
     }
     o.on_device = 0;
     check(pbsm3d_step(ctx_, &f, (double)dt, &o, &last_stats), "PBSM3D run");
+    if (gpu_cfg.debug_output) {
+        // the diagnostics the library keeps, under the reference's names
+        for (const char* v : {"hs", "ustar", "u*_th", "csalt", "z0", "is_drifting"})
+            check(pbsm3d_get_debug(ctx_, v, m.var(v).data(), 0), "PBSM3D debug_output");
+        for (int z = 0; z < gpu_cfg.nLayer; ++z)
+            for (const char* v : {"c", "csubl", "u_z", "cz"}) {
+                const std::string name = v + std::to_string(z);
+                check(pbsm3d_get_debug(ctx_, name.c_str(), m.var(name).data(), 0), "PBSM3D debug_output");
+            }
+    }
 }
 
 void PBSM3D::checkpoint(mesh& domain, netcdf& chkpt) {

@@ -96,7 +96,7 @@ typedef struct pbsm3d_config {
     int32_t use_subgrid_topo;       /* "use_subgrid_topo" false */
     int32_t use_subgrid_topo_V2;    /* "use_subgrid_topo_V2" false */
     int32_t use_R94_lambda;         /* "use_R94_lambda" true */
-    int32_t debug_output;           /* "debug_output" false (true: UNSUPPORTED) */
+    int32_t debug_output;           /* "debug_output" false (diagnostics: pbsm3d_get_debug) */
     double settling_velocity;       /* "settling_velocity" 0.5 m/s, must be >= 0 */
     double smooth_coeff;            /* "smooth_coeff" 820 (Laplacian smoothing eps) */
     double min_sd_trans;            /* "min_sd_trans" 0.1 m */
@@ -384,6 +384,15 @@ int pbsm3d_fetchr(pbsm3d_ctx* ctx, const double* vw_dir, double* fetch, int on_d
  * (valid until pbsm3d_mesh_free).  The HDF5 mesh and partition formats are not
  * read.
  */
+/*
+ * Diagnostics of the last step by the names debug_output gives them in the
+ * reference (PBSM3D.cpp:141-186): per face "hs", "ustar", "u*_th", "csalt",
+ * "z0", "is_drifting"; per layer z (0-based) "c<z>", "csubl<z>", "u_z<z>",
+ * "cz<z>".  n_faces doubles.  Unknown names: PBSM3D_ERR_INVALID_ARG.  The
+ * reference's other debug variables (K, rm, mm, dm/dt, uvw, ...) are not kept.
+ */
+int pbsm3d_get_debug(pbsm3d_ctx* ctx, const char* name, double* out, int on_device);
+
 typedef struct pbsm3d_mesh pbsm3d_mesh;
 int pbsm3d_mesh_read(const char* mesh_path, const char* param_path, pbsm3d_mesh** out);
 int pbsm3d_mesh_describe(const pbsm3d_mesh* mesh, pbsm3d_mesh_desc* desc);

@@ -966,10 +966,6 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
         g_create_error = "PBSM3D settling velocity must be positive";
         return PBSM3D_ERR_INVALID_ARG;
     }
-    if (cfg->debug_output) {
-        g_create_error = "configuration branch not restated by the oracle";
-        return PBSM3D_ERR_UNSUPPORTED;
-    }
     if (cfg->nLayer < 1) {
         g_create_error = "nLayer must be >= 1";
         return PBSM3D_ERR_INVALID_ARG;

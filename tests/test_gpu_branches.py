@@ -188,3 +188,34 @@ def test_branches_over_steps(cuda_lib, oracle_lib, solver):
         wg.apply_drift(ref["drift_mass"])
         wo.apply_drift(ref["drift_mass"])
     m.close()
+
+
+@pytest.mark.parametrize("cfg", [{}, {"z0_ustar_coupling": True}], ids=["default", "coupling"])
+def test_debug_diagnostics(cuda_lib, oracle_lib, cfg):
+    """debug_output's variables kept by the library (pbsm3d_get_debug)
+    against the oracle's per-face and per-layer values of the same step."""
+    from oracle import pyoracle
+    w = veg_workload(77)
+    f = forcing(w, 0)
+    m = PBSM3D(module_cfg({**cfg, "debug_output": True}))
+    m.init(w.mesh)
+    assert "hs" in m.provides and f"c{L - 1}" in m.provides
+    out = m.run(f, 3600.0, want_c=True)
+    o = pyoracle.Oracle(w.mesh, nLayer=L, cfg=oracle_cfg(cfg))
+    ref, _ = o.step_exact(f, 3600.0)
+    ff = o.face_fields()
+    n = w.mesh.n_faces
+    for name, key in (("hs", "hs"), ("ustar", "ustar"), ("u*_th", "ustar_th"), ("csalt", "c_salt"), ("z0", "z0")):
+        assert relerr(m.debug(name), ff[key]) < 1e-12, name
+    np.testing.assert_array_equal(m.debug("is_drifting"), ff["saltation"])
+    dz = 5.0 / L
+    for z in (0, L - 1):
+        assert relerr(m.debug(f"c{z}"), out["c"][z * n:(z + 1) * n]) == 0.0
+        assert relerr(m.debug(f"c{z}"), ref["c"][z * n:(z + 1) * n]) < FIELD_TOL
+        assert relerr(m.debug(f"u_z{z}"), ff["u_z"][z * n:(z + 1) * n]) < 1e-12
+        assert relerr(m.debug(f"csubl{z}"), ff["csubl"][z * n:(z + 1) * n]) < 1e-12
+        assert relerr(m.debug(f"cz{z}"), z * dz + ff["hs"] + dz / 2.0) < 1e-14
+    from chm_gb300.pbsm3d import ModuleError
+    with pytest.raises(ModuleError, match="unknown diagnostic"):
+        m.debug(f"c{L}")
+    m.close()

@@ -92,8 +92,6 @@ def test_create_rejects_bad_configs(cuda_lib):
                 dict(abi_version=99), dict(neumann=10), dict(neumann=-1)):
         cfg = capi.default_config(cuda_lib, **bad)
         assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
-    cfg = capi.default_config(cuda_lib, debug_output=1)
-    assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_UNSUPPORTED
     bad_nb = m.neighbor.copy()
     bad_nb[0, 0] = m.n_faces + 5
     m.neighbor = bad_nb
