@@ -43,7 +43,7 @@ class Config(C.Structure):
         ("solver", C.c_int32), ("precision", C.c_int32), ("warm_start", C.c_int32), ("gmres_restart", C.c_int32),
         ("susp_maxit", C.c_int32), ("dep_maxit", C.c_int32),
         ("susp_tol", C.c_double), ("dep_tol", C.c_double), ("inner_tol", C.c_double),
-        ("slice_width", C.c_int32), ("warm_flags", C.c_int32), ("graph", C.c_int32),
+        ("warm_flags", C.c_int32), ("graph", C.c_int32),
         ("autotune", C.c_int32), ("neumann", C.c_int32), ("derive_wind", C.c_int32),
         ("wind_ignore_canopy", C.c_int32), ("derive_fetch", C.c_int32), ("fetch_steps", C.c_int32),
         ("fetch_incl_veg", C.c_int32), ("reserved", C.c_int32 * 3), ("fetch_max_distance", C.c_double),
