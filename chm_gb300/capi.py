@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "OK", -1: "INVALID_ARG", -2: "BAD_MESH", -3: "NAN_INPUT", -4:
                 -6: "UNSUPPORTED", -7: "OUT_OF_MEMORY"}
 SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1
 FP64, MIXED = 0, 1
+INTERP_SPLINE, INTERP_IDW, INTERP_NEAREST = 0, 1, 2
 X0_ZERO, X0_PREVIOUS, X0_LEARNED = 0, 1, 2
 KERNELS = ["ASSEMBLE", "BICG_P", "BICG_V", "BICG_S", "BICG_T", "BICG_X", "RESIDUAL", "POST", "DEP_ASSEMBLE", "CG",
            "UPDATE", "OTHER", "MLP", "NEUMANN"]
@@ -117,6 +118,7 @@ EXPORTS = [
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
     "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr", "pbsm3d_mesh_read",
     "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error", "pbsm3d_get_debug",
+    "pbsm3d_set_stations", "pbsm3d_uniform_wind",
 ]
 
 _lib = None
@@ -150,6 +152,10 @@ def load(path: Path | None = None):
     lib.pbsm3d_scale_wind_vert.restype = C.c_int
     lib.pbsm3d_fetchr.argtypes = [vp, dp, dp, C.c_int]
     lib.pbsm3d_fetchr.restype = C.c_int
+    lib.pbsm3d_set_stations.argtypes = [vp, C.c_int64, dp, dp, C.c_int32, C.c_double, C.c_int32]
+    lib.pbsm3d_set_stations.restype = C.c_int
+    lib.pbsm3d_uniform_wind.argtypes = [vp, dp, dp, dp, dp, C.c_int]
+    lib.pbsm3d_uniform_wind.restype = C.c_int
     lib.pbsm3d_get_debug.argtypes = [vp, C.c_char_p, dp, C.c_int]
     lib.pbsm3d_get_debug.restype = C.c_int
     lib.pbsm3d_mesh_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]

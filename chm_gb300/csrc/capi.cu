@@ -1236,6 +1236,120 @@ int pbsm3d_fetchr(pbsm3d_ctx* h, const double* vw_dir, double* fetch, int on_dev
     return 0;
 }
 
+int pbsm3d_set_stations(pbsm3d_ctx* h, int64_t ns, const double* x, const double* y, int32_t n_nearest,
+                        double radius, int32_t interp) {
+    if (!h || ns < 1 || !x || !y || n_nearest < 0 || !(radius >= 0) || interp < PBSM3D_INTERP_SPLINE ||
+        interp > PBSM3D_INTERP_NEAREST)
+        return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    if (n_nearest > 0 && radius > 0) {
+        c.err = "Cannot have both station_search_radius and station_N_nearest set.";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (n_nearest == 0 && radius == 0) n_nearest = interp == PBSM3D_INTERP_NEAREST ? 1 : 5;  // core.cpp:183-196
+    if (n_nearest > 0 && n_nearest < 2 && interp != PBSM3D_INTERP_NEAREST) {
+        c.err = "station_N_nearest must be >= 2 if spline or idw is used";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    if (n_nearest > 16) {
+        c.err = "at most 16 stations per face";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    const int64_t T = c.P.T;
+    std::vector<double> cx(T), cy(T);
+    PBSM_CUDA_TRY(cudaMemcpy(cx.data(), c.wnd.cx, T * 8, cudaMemcpyDeviceToHost));
+    PBSM_CUDA_TRY(cudaMemcpy(cy.data(), c.wnd.cy, T * 8, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> start(T + 1, 0), idx;
+    idx.reserve(T * (size_t)std::max(1, n_nearest));
+    std::vector<std::pair<double, int32_t>> d(ns);
+    for (int64_t i = 0; i < T; ++i) {
+        for (int64_t k = 0; k < ns; ++k) {
+            const double dx = x[k] - cx[i], dy = y[k] - cy[i];
+            d[k] = {dx * dx + dy * dy, (int32_t)k};
+        }
+        int n = 0;
+        if (n_nearest > 0) {
+            const int64_t take = std::min<int64_t>(n_nearest, ns);
+            std::partial_sort(d.begin(), d.begin() + take, d.end());
+            for (int64_t k = 0; k < take; ++k) idx.push_back(d[k].second);
+            n = (int)take;
+        } else {
+            for (int64_t k = 0; k < ns; ++k)
+                if (d[k].first <= radius * radius) {
+                    idx.push_back((int32_t)k);
+                    ++n;
+                }
+        }
+        if (n == 0 || n > 16 || (interp == PBSM3D_INTERP_NEAREST && n != 1)) {
+            c.err = "face " + std::to_string(i) + " has " + std::to_string(n) +
+                    " stations (NEAREST needs exactly 1, the others 1 to 16)";
+            return PBSM3D_ERR_INVALID_ARG;
+        }
+        start[i + 1] = (int32_t)idx.size();
+    }
+    // replace any earlier station set
+    Stations& st = c.st;
+    auto drop = [&](void* p) {
+        if (!p) return;
+        cudaFree(p);
+        c.allocations.erase(std::remove(c.allocations.begin(), c.allocations.end(), p), c.allocations.end());
+    };
+    for (void* p : {(void*)st.x, (void*)st.y, (void*)st.start, (void*)st.idx, (void*)st.u, (void*)st.dir,
+                    (void*)st.out_u, (void*)st.out_dir, (void*)st.bad})
+        drop(p);
+    st = Stations{};
+    bool ok = true;
+    st.n = ns;
+    st.interp = interp;
+    st.x = dalloc<double>(c, ns, ok);
+    st.y = dalloc<double>(c, ns, ok);
+    st.start = dalloc<int32_t>(c, T + 1, ok);
+    st.idx = dalloc<int32_t>(c, idx.size(), ok);
+    st.u = dalloc<double>(c, ns, ok);
+    st.dir = dalloc<double>(c, ns, ok);
+    st.out_u = dalloc<double>(c, c.P.Tp, ok);
+    st.out_dir = dalloc<double>(c, c.P.Tp, ok);
+    st.bad = dalloc<int>(c, 1, ok);
+    if (!ok) {
+        c.err = "out of device memory for the stations";
+        return PBSM3D_ERR_OUT_OF_MEMORY;
+    }
+    PBSM_CUDA_TRY(cudaMemcpy(st.x, x, ns * 8, cudaMemcpyHostToDevice));
+    PBSM_CUDA_TRY(cudaMemcpy(st.y, y, ns * 8, cudaMemcpyHostToDevice));
+    PBSM_CUDA_TRY(cudaMemcpy(st.start, start.data(), (T + 1) * 4, cudaMemcpyHostToDevice));
+    PBSM_CUDA_TRY(cudaMemcpy(st.idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int pbsm3d_uniform_wind(pbsm3d_ctx* h, const double* st_U, const double* st_dir, double* U_R, double* vw_dir,
+                        int on_device) {
+    if (!h || !st_U || !st_dir || !U_R || !vw_dir) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    c.err.clear();
+    Stations& st = c.st;
+    if (!st.x) {
+        c.err = "no stations (pbsm3d_set_stations)";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    const cudaMemcpyKind in = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    PBSM_CUDA_TRY(cudaMemcpyAsync(st.u, st_U, st.n * 8, in, c.stream));
+    PBSM_CUDA_TRY(cudaMemcpyAsync(st.dir, st_dir, st.n * 8, in, c.stream));
+    PBSM_CUDA_TRY(cudaMemsetAsync(st.bad, 0, sizeof(int), c.stream));
+    launch_uniform_wind(c, c.stream, st.out_u, st.out_dir);
+    PBSM_CUDA_TRY(cudaGetLastError());
+    int bad = 0, rc;
+    PBSM_CUDA_TRY(cudaMemcpyAsync(&bad, st.bad, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    if (bad) {
+        c.err = "uniform_wind: a face has no station with a valid U_R and vw_dir";
+        return PBSM3D_ERR_NAN_INPUT;
+    }
+    if ((rc = copy_out(c, U_R, st.out_u, on_device)) || (rc = copy_out(c, vw_dir, st.out_dir, on_device))) return rc;
+    PBSM_CUDA_TRY(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
 static int export_system(Ctx& c, int which, int32_t* cols, double* vals, double* rhs, double* x) {
     const int64_t T = c.P.T, Tp = c.P.Tp;
     const int L = which == 0 ? c.P.L : 1;

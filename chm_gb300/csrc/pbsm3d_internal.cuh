@@ -105,6 +105,18 @@ struct Wind {
     double *in0 = nullptr, *in1 = nullptr, *out = nullptr;  // [Tp] staging of the stand-alone calls
 };
 
+// Met stations of the station-driven modules (uniform_wind) and each face's
+// station list, [start[i], start[i+1]) of idx.
+struct Stations {
+    int64_t n = 0;
+    int interp = 0;                 // PBSM3D_INTERP_*
+    double *x = nullptr, *y = nullptr;
+    int32_t *start = nullptr, *idx = nullptr;
+    double *u = nullptr, *dir = nullptr;  // [n] this call's station values
+    double *out_u = nullptr, *out_dir = nullptr;  // [Tp] staging
+    int* bad = nullptr;             // set when a face has no valid station
+};
+
 // Static inputs of the subgrid branches (device).
 struct Subgrid {
     double* tpi;        // [5][Tp] TPI_mean, TPI_std, TPI_neg_frac, TPI_neg_mean, TPI_neg_std (NaN = undefined)
@@ -239,6 +251,7 @@ int subgrid_init(Ctx& c, cudaStream_t s);
 // wind.cu
 void launch_scale_wind_vert(Ctx& c, cudaStream_t s, const double* U_R, const double* sd, double* u2m);
 void launch_fetchr(Ctx& c, cudaStream_t s, const double* dir, double* fetch);
+void launch_uniform_wind(Ctx& c, cudaStream_t s, double* U_R, double* vw_dir);
 
 // solver.cu
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
@@ -267,6 +280,7 @@ struct Ctx {
     FaceState S;
     Subgrid sg;
     Wind wnd;
+    Stations st;
     int asm_kernels = 3;  // kernels of one suspension assembly (+1 subgrid, +2 derived wind, +1 derived fetch)
     Susp A;
     Dep D;

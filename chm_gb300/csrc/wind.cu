@@ -14,6 +14,10 @@
 //    nearer centre.  Distances are computed with explicitly rounded
 //    operations, and the lowest face index wins a tie, as in the oracle's
 //    brute-force search.
+//  * uniform_wind (interp_met/uniform_wind.cpp:58-127): each face
+//    interpolates its stations' wind components (thin plate spline, inverse
+//    distance or nearest, interpolation/*.cpp) from the station lists that
+//    pbsm3d_set_stations builds the way CHM's core does.
 #include <math.h>
 
 #include "pbsm3d_internal.cuh"
@@ -283,7 +287,155 @@ __global__ void k_fetchr(int64_t T, Wind w, const int32_t* __restrict__ face_mem
     }
 }
 
+// The thin plate spline of n <= 16 samples carrying two fields at once (the
+// system does not depend on the field), full pivoting; local-memory arrays.
+__device__ void tps_interp2(const double* sx, const double* sy, const double* z0v, const double* z1v, int n,
+                            double qx, double qy, double& o0, double& o1) {
+    const int m = n + 1;
+    double A[17][17], b[2][17];
+    int colp[17];
+    for (int i = 0; i < m; ++i) {
+        colp[i] = i;
+        b[0][i] = b[1][i] = 0.0;
+        for (int j = 0; j < m; ++j) A[i][j] = 0.0;
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = i; j < n; ++j) {
+            const double xd = sx[i] - sx[j], yd = sy[i] - sy[j];
+            if (xd == 0. && yd == 0.) continue;
+            const double Rd = j == i ? 0.0 : tps_basis(xd, yd);
+            A[i][j + 1] = Rd;
+            A[j][i + 1] = Rd;
+        }
+    for (int i = 0; i < m; ++i) {
+        A[i][0] = 1;
+        A[m - 1][i] = 1;
+    }
+    A[m - 1][0] = 0;
+    for (int i = 0; i < n; ++i) {
+        b[0][i] = z0v[i];
+        b[1][i] = z1v[i];
+    }
+    for (int k = 0; k < m; ++k) {
+        int pr = k, pc = k;
+        double best = -1;
+        for (int i = k; i < m; ++i)
+            for (int j = k; j < m; ++j)
+                if (fabs(A[i][j]) > best) {
+                    best = fabs(A[i][j]);
+                    pr = i;
+                    pc = j;
+                }
+        if (best == 0) break;
+        for (int j = 0; j < m; ++j) {
+            const double t = A[k][j];
+            A[k][j] = A[pr][j];
+            A[pr][j] = t;
+        }
+        for (int f = 0; f < 2; ++f) {
+            const double t = b[f][k];
+            b[f][k] = b[f][pr];
+            b[f][pr] = t;
+        }
+        for (int i = 0; i < m; ++i) {
+            const double t = A[i][k];
+            A[i][k] = A[i][pc];
+            A[i][pc] = t;
+        }
+        {
+            const int t = colp[k];
+            colp[k] = colp[pc];
+            colp[pc] = t;
+        }
+        for (int i = k + 1; i < m; ++i) {
+            const double g = A[i][k] / A[k][k];
+            for (int j = k; j < m; ++j) A[i][j] -= g * A[k][j];
+            b[0][i] -= g * b[0][k];
+            b[1][i] -= g * b[1][k];
+        }
+    }
+    double out[2];
+    for (int f = 0; f < 2; ++f) {
+        double y[17], x[17];
+        for (int k = m - 1; k >= 0; --k) {
+            double v = b[f][k];
+            for (int j = k + 1; j < m; ++j) v -= A[k][j] * y[j];
+            y[k] = A[k][k] != 0 ? v / A[k][k] : 0.0;
+        }
+        for (int k = 0; k < m; ++k) x[colp[k]] = y[k];
+        double z = x[0];
+        for (int i = 1; i < m; ++i) z += x[i] * tps_basis(sx[i - 1] - qx, sy[i - 1] - qy);
+        out[f] = z;
+    }
+    o0 = out[0];
+    o1 = out[1];
+}
+
+// inv_dist::operator() (interpolation/inv_dist.cpp:36-78): weights 1/d^2; a
+// sample at the query resets the sums to it and later samples still add.
+__device__ double idw_interp(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+    double numerator = 0.0, denominator = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double xdiff = sx[i] - qx, ydiff = sy[i] - qy;
+        const double di = pow(sqrt(pow(xdiff, 2.0) + pow(ydiff, 2.0)), 2.0);
+        if (di == 0) {
+            numerator = sz[i];
+            denominator = 1.0;
+        } else {
+            numerator += sz[i] / di;
+            denominator += 1 / di;
+        }
+    }
+    return numerator / denominator;
+}
+
+// uniform_wind::run (interp_met/uniform_wind.cpp:58-127)
+__global__ void k_uniform_wind(int64_t T, Wind w, Stations st, double* __restrict__ U_R,
+                               double* __restrict__ vw_dir) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T; i += (int64_t)gridDim.x * blockDim.x) {
+        double px[16], py[16], pu[16], pv[16];
+        int m = 0;
+        for (int k = st.start[i]; k < st.start[i + 1] && m < 16; ++k) {
+            const int s = st.idx[k];
+            const double su = st.u[s], sd = st.dir[s];
+            if (is_nan_chm(su) || is_nan_chm(sd)) continue;
+            const double W = smax(su, 0.1);
+            const double theta = sd * M_PI / 180.;
+            double sn, cs;
+            sincos(theta, &sn, &cs);
+            px[m] = st.x[s];
+            py[m] = st.y[s];
+            pu[m] = -W * sn;
+            pv[m] = -W * cs;
+            ++m;
+        }
+        if (m == 0) {
+            atomicExch(st.bad, 1);
+            continue;
+        }
+        const double qx = w.cx[i], qy = w.cy[i];
+        double zu, zv;
+        if (st.interp == PBSM3D_INTERP_SPLINE) {
+            tps_interp2(px, py, pu, pv, m, qx, qy, zu, zv);
+        } else if (st.interp == PBSM3D_INTERP_IDW) {
+            zu = idw_interp(px, py, pu, m, qx, qy);
+            zv = idw_interp(px, py, pv, m, qx, qy);
+        } else {
+            zu = pu[0];
+            zv = pv[0];
+        }
+        double theta = 3.0 * M_PI * 0.5 - atan2(zv, zu);
+        if (theta > 2 * M_PI) theta = theta - 2 * M_PI;
+        U_R[i] = smax(sqrt(zu * zu + zv * zv), 0.1);
+        vw_dir[i] = theta * 180.0 / M_PI;
+    }
+}
+
 }  // namespace
+
+void launch_uniform_wind(Ctx& c, cudaStream_t s, double* U_R, double* vw_dir) {
+    k_uniform_wind<<<c.grid_faces, kBlock, 0, s>>>(c.P.T, c.wnd, c.st, U_R, vw_dir);
+}
 
 void launch_scale_wind_vert(Ctx& c, cudaStream_t s, const double* U_R, const double* sd, double* u2m) {
     k_wind_point<<<c.grid_faces, kBlock, 0, s>>>(c.P.T, c.wnd, c.cfg.wind_ignore_canopy, U_R, sd, c.wnd.tmp);

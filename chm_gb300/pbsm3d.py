@@ -222,6 +222,26 @@ class PBSM3D:
             self._error(rc, "pbsm3d_fetchr")
         return out
 
+    def set_stations(self, x, y, n_nearest: int = 0, radius: float = 0.0, interp: int = capi.INTERP_SPLINE):
+        """Met stations and each face's station list (core.cpp:168-205)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        rc = self._lib.pbsm3d_set_stations(self._ctx, x.size, capi.ptr(x), capi.ptr(y), int(n_nearest),
+                                           float(radius), int(interp))
+        if rc != 0:
+            self._error(rc, "pbsm3d_set_stations")
+
+    def uniform_wind(self, station_U_R, station_vw_dir):
+        """Per-face U_R and vw_dir interpolated from one time step of the
+        stations (interp_met/uniform_wind.cpp:58-127)."""
+        u = np.ascontiguousarray(station_U_R, dtype=np.float64)
+        d = np.ascontiguousarray(station_vw_dir, dtype=np.float64)
+        U, D = np.empty(self.n_faces), np.empty(self.n_faces)
+        rc = self._lib.pbsm3d_uniform_wind(self._ctx, capi.ptr(u), capi.ptr(d), capi.ptr(U), capi.ptr(D), 0)
+        if rc != 0:
+            self._error(rc, "pbsm3d_uniform_wind")
+        return U, D
+
     def debug(self, name: str) -> np.ndarray:
         """A diagnostic of the last step by its debug_output name ("hs",
         "ustar", "u*_th", "csalt", "z0", "is_drifting", "c<z>", "csubl<z>",

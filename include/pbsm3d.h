@@ -371,6 +371,27 @@ int pbsm3d_scale_wind_vert(pbsm3d_ctx* ctx, const double* U_R, const double* sno
 int pbsm3d_fetchr(pbsm3d_ctx* ctx, const double* vw_dir, double* fetch, int on_device);
 
 /*
+ * Met stations and the station-driven wind provider uniform_wind
+ * (interp_met/uniform_wind.cpp:28-127).  pbsm3d_set_stations takes the
+ * stations' x, y (host arrays, the mesh's projection) and builds each face's
+ * station list as CHM's core does (core.cpp:168-205, metdata.cpp:591-622):
+ * the n_nearest nearest (station_N_nearest; nearest first, the lower index on
+ * a tie) or, with n_nearest = 0 and radius > 0, every station within radius
+ * (station_search_radius; ascending index).  n_nearest = 0 and radius = 0 take
+ * the core's defaults: 1 for NEAREST, 5 otherwise.  SPLINE and IDW need at
+ * least 2 stations per list, NEAREST exactly 1 (the reference throws
+ * otherwise); at most 16 per face.  pbsm3d_uniform_wind interpolates one
+ * time step of the stations' U_R and vw_dir (n_stations each; a station with
+ * -9999/NaN in either is skipped) to every face: U_R (>= 0.1 m/s) and vw_dir
+ * (degrees).  PBSM3D_ERR_NAN_INPUT when a face is left without a station.
+ */
+enum pbsm3d_interp { PBSM3D_INTERP_SPLINE = 0, PBSM3D_INTERP_IDW = 1, PBSM3D_INTERP_NEAREST = 2 };
+int pbsm3d_set_stations(pbsm3d_ctx* ctx, int64_t n_stations, const double* x, const double* y, int32_t n_nearest,
+                        double radius, int32_t interp);
+int pbsm3d_uniform_wind(pbsm3d_ctx* ctx, const double* station_U_R, const double* station_vw_dir, double* U_R,
+                        double* vw_dir, int on_device);
+
+/*
  * CHM's JSON mesh files (triangulation.cpp:206-356): a .mesh file
  * {"mesh": {"vertex", "elem", "neigh", "nvertex", "nelem", "is_geographic", ...}}
  * and an optional .param file of per-face parameters.  The geometry is

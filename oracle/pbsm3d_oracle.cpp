@@ -218,12 +218,14 @@ double expint_e1(double x) {
     return h * std::exp(-x);
 }
 
-// thin_plate_spline::operator() (interpolation/TPSpline.cpp:55-157) for n <= 3
+// thin_plate_spline::operator() (interpolation/TPSpline.cpp:55-157) for n <= 16
 // samples: the (n+1)x(n+1) system [1, R(x_i, x_j)] / [0, 1 ... 1] with the
 // basis R(d) = -(log(q) + c + E1(q)), q = (d weight / 2)^2, weight 0.01 and
 // the reference's c = 0.577215; solved by Gaussian elimination with full
-// pivoting (Eigen::FullPivLU in the reference), evaluated at the query.
-double tps_interp(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+// pivoting (Eigen::FullPivLU in the reference) for nz right-hand sides (the
+// same samples carry several fields), evaluated at the query.
+void tps_interp_multi(const double* sx, const double* sy, const double* const* sz, int nz, int n, double qx,
+                      double qy, double* out) {
     const double weight = 0.01, c = 0.577215;
     auto basis = [&](double dx, double dy) {
         double d = std::sqrt(dx * dx + dy * dy);
@@ -231,7 +233,7 @@ double tps_interp(const double* sx, const double* sy, const double* sz, int n, d
         return -(std::log(d) + c + expint_e1(d));
     };
     const int m = n + 1;
-    double A[4][4] = {}, b[4] = {}, x[4] = {};
+    double A[17][17] = {}, b[2][17] = {}, y[17] = {}, x[17] = {};
     for (int i = 0; i < n; ++i)
         for (int j = i; j < n; ++j) {
             const double xd = sx[i] - sx[j], yd = sy[i] - sy[j];
@@ -245,10 +247,12 @@ double tps_interp(const double* sx, const double* sy, const double* sz, int n, d
         A[m - 1][i] = 1;
     }
     A[m - 1][0] = 0;
-    for (int i = 0; i < n; ++i) b[i] = sz[i];
-    b[m - 1] = 0.0;
-    // full-pivot elimination
-    int colp[4] = {0, 1, 2, 3};
+    for (int f = 0; f < nz; ++f) {
+        for (int i = 0; i < n; ++i) b[f][i] = sz[f][i];
+        b[f][m - 1] = 0.0;
+    }
+    int colp[17];
+    for (int k = 0; k < m; ++k) colp[k] = k;
     for (int k = 0; k < m; ++k) {
         int pr = k, pc = k;
         double best = -1;
@@ -261,25 +265,50 @@ double tps_interp(const double* sx, const double* sy, const double* sz, int n, d
                 }
         if (best == 0) break;
         for (int j = 0; j < m; ++j) std::swap(A[k][j], A[pr][j]);
-        std::swap(b[k], b[pr]);
+        for (int f = 0; f < nz; ++f) std::swap(b[f][k], b[f][pr]);
         for (int i = 0; i < m; ++i) std::swap(A[i][k], A[i][pc]);
         std::swap(colp[k], colp[pc]);
         for (int i = k + 1; i < m; ++i) {
-            const double f = A[i][k] / A[k][k];
-            for (int j = k; j < m; ++j) A[i][j] -= f * A[k][j];
-            b[i] -= f * b[k];
+            const double g = A[i][k] / A[k][k];
+            for (int j = k; j < m; ++j) A[i][j] -= g * A[k][j];
+            for (int f = 0; f < nz; ++f) b[f][i] -= g * b[f][k];
         }
     }
-    double y[4] = {};
-    for (int k = m - 1; k >= 0; --k) {
-        double v = b[k];
-        for (int j = k + 1; j < m; ++j) v -= A[k][j] * y[j];
-        y[k] = A[k][k] != 0 ? v / A[k][k] : 0.0;
+    for (int f = 0; f < nz; ++f) {
+        for (int k = m - 1; k >= 0; --k) {
+            double v = b[f][k];
+            for (int j = k + 1; j < m; ++j) v -= A[k][j] * y[j];
+            y[k] = A[k][k] != 0 ? v / A[k][k] : 0.0;
+        }
+        for (int k = 0; k < m; ++k) x[colp[k]] = y[k];
+        double z0 = x[0];
+        for (int i = 1; i < m; ++i) z0 += x[i] * basis(sx[i - 1] - qx, sy[i - 1] - qy);
+        out[f] = z0;
     }
-    for (int k = 0; k < m; ++k) x[colp[k]] = y[k];
-    double z0 = x[0];
-    for (int i = 1; i < m; ++i) z0 += x[i] * basis(sx[i - 1] - qx, sy[i - 1] - qy);
-    return z0;
+}
+double tps_interp(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+    double out;
+    const double* z[1] = {sz};
+    tps_interp_multi(sx, sy, z, 1, n, qx, qy, &out);
+    return out;
+}
+
+// inv_dist::operator() (interpolation/inv_dist.cpp:36-78): weights 1/d^2; a
+// sample at the query resets the sums to it and the later samples still add.
+double idw_interp(const double* sx, const double* sy, const double* sz, int n, double qx, double qy) {
+    double numerator = 0.0, denominator = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double xdiff = sx[i] - qx, ydiff = sy[i] - qy;
+        const double di = std::pow(std::sqrt(std::pow(xdiff, 2.0) + std::pow(ydiff, 2.0)), 2.0);
+        if (di == 0) {
+            numerator = sz[i];
+            denominator = 1.0;
+        } else {
+            numerator += sz[i] / di;
+            denominator += 1 / di;
+        }
+    }
+    return numerator / denominator;
 }
 
 // ---------------------------------------------------- subgrid topography
@@ -1797,6 +1826,85 @@ int oracle_fetchr(const oracle_ctx* c, int steps, double max_distance, double I,
         }
     }
     return 0;
+}
+
+// The face -> station lists of CHM's core (core.cpp:168-205, metdata.cpp:
+// 591-622): the n_nearest nearest stations (nearest first, the lower index on a
+// tie), or every station within radius (ascending index).  Returns the count.
+int oracle_select_stations(const oracle_ctx* c, int64_t face, int64_t ns, const double* sx, const double* sy,
+                           int n_nearest, double radius, int32_t* out) {
+    const double qx = c->center[3 * face], qy = c->center[3 * face + 1];
+    std::vector<std::pair<double, int>> d(ns);
+    for (int64_t k = 0; k < ns; ++k) {
+        const double dx = sx[k] - qx, dy = sy[k] - qy;
+        d[k] = {dx * dx + dy * dy, (int)k};
+    }
+    int n = 0;
+    if (n_nearest > 0) {
+        std::sort(d.begin(), d.end());
+        for (int k = 0; k < n_nearest && k < (int)ns; ++k) out[n++] = d[k].second;
+    } else {
+        for (int64_t k = 0; k < ns; ++k)
+            if (d[k].first <= radius * radius) out[n++] = (int)k;
+    }
+    return n;
+}
+
+// uniform_wind::run (interp_met/uniform_wind.cpp:58-127): per face, the
+// stations' winds as zonal components (speed at least 0.1 m/s; stations
+// with a missing speed or direction are skipped), interpolated to the face
+// centre (interp 0 = thin plate spline, 1 = IDW, 2 = nearest), back to
+// speed (at least 0.1) and bearing.  Returns -1 when a face has no valid
+// station.
+int oracle_uniform_wind(const oracle_ctx* c, int64_t ns, const double* sx, const double* sy, int n_nearest,
+                        double radius, int interp, const double* st_U, const double* st_dir, double* U_R,
+                        double* vw_dir) {
+    const int64_t T = c->T;
+    int bad = 0;
+    std::vector<int32_t> sel(ns);
+    for (int64_t i = 0; i < T; ++i) {
+        const int n = oracle_select_stations(c, i, ns, sx, sy, n_nearest, radius, sel.data());
+        double px[16], py[16], pu[16], pv[16];
+        int m = 0;
+        for (int k = 0; k < n && m < 16; ++k) {
+            const int s = sel[k];
+            if (is_nan(st_U[s]) || is_nan(st_dir[s])) continue;
+            double W = st_U[s];
+            W = smax(W, 0.1);
+            const double theta = st_dir[s] * M_PI / 180.;
+            px[m] = sx[s];
+            py[m] = sy[s];
+            pu[m] = -W * std::sin(theta);
+            pv[m] = -W * std::cos(theta);
+            ++m;
+        }
+        if (m == 0) {
+            bad = 1;
+            continue;
+        }
+        const double qx = c->center[3 * i], qy = c->center[3 * i + 1];
+        double zu, zv;
+        if (interp == 0) {
+            const double* z[2] = {pu, pv};
+            double o[2];
+            tps_interp_multi(px, py, z, 2, m, qx, qy, o);
+            zu = o[0];
+            zv = o[1];
+        } else if (interp == 1) {
+            zu = idw_interp(px, py, pu, m, qx, qy);
+            zv = idw_interp(px, py, pv, m, qx, qy);
+        } else {
+            zu = pu[0];
+            zv = pv[0];
+        }
+        double theta = 3.0 * M_PI * 0.5 - std::atan2(zv, zu);
+        if (theta > 2 * M_PI) theta = theta - 2 * M_PI;
+        double W = std::sqrt(zu * zu + zv * zv);
+        W = smax(W, 0.1);
+        U_R[i] = W;
+        vw_dir[i] = theta * 180.0 / M_PI;
+    }
+    return bad ? -1 : 0;
 }
 
 double oracle_expint_e1(double x) { return expint_e1(x); }

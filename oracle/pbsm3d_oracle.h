@@ -102,6 +102,11 @@ int oracle_scale_wind_vert(const oracle_ctx* c, int ignore_canopy, const double*
                            double* u2m);
 int oracle_fetchr(const oracle_ctx* c, int steps, double max_distance, double I, int incl_veg, const double* vw_dir,
                   double* fetch);
+/* uniform_wind from stations (interp 0 spline, 1 IDW, 2 nearest) and the face's
+ * station list (n_nearest > 0, or radius); -1 when a face has no valid station */
+int oracle_uniform_wind(const oracle_ctx* c, int64_t ns, const double* sx, const double* sy, int n_nearest,
+                        double radius, int interp, const double* st_U, const double* st_dir, double* U_R,
+                        double* vw_dir);
 double oracle_expint_e1(double x);
 double oracle_tps(const double* sx, const double* sy, const double* sz, int n, double qx, double qy);
 /* Face geometry of a triangle mesh (triangulation.hpp:1443-1498,1577-1589,1830-1856).

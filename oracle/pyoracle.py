@@ -87,6 +87,9 @@ def load():
                                            C.POINTER(C.c_double)]
     lib.oracle_fetchr.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)]
+    lib.oracle_uniform_wind.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int,
+                                        C.c_double, C.c_int] + [C.POINTER(C.c_double)] * 4
+    lib.oracle_uniform_wind.restype = C.c_int
     lib.oracle_expint_e1.argtypes = [C.c_double]
     lib.oracle_expint_e1.restype = C.c_double
     lib.oracle_tps.argtypes = [C.POINTER(C.c_double)] * 3 + [C.c_int, C.c_double, C.c_double]
@@ -245,6 +248,15 @@ class Oracle:
         out = np.empty(self.n)
         self.lib.oracle_fetchr(self.ctx, int(steps), float(max_distance), float(I), int(incl_veg), ptr(d), ptr(out))
         return out
+
+    def uniform_wind(self, sx, sy, st_U, st_dir, n_nearest=5, radius=0.0, interp=0):
+        a = [np.ascontiguousarray(v, dtype=np.float64) for v in (sx, sy, st_U, st_dir)]
+        U, D = np.empty(self.n), np.empty(self.n)
+        rc = self.lib.oracle_uniform_wind(self.ctx, a[0].size, ptr(a[0]), ptr(a[1]), int(n_nearest), float(radius),
+                                          int(interp), ptr(a[2]), ptr(a[3]), ptr(U), ptr(D))
+        if rc != 0:
+            raise RuntimeError("oracle_uniform_wind: a face has no valid station")
+        return U, D
 
     def face_fields(self):
         n, L = self.n, self.L

@@ -143,3 +143,61 @@ def test_step_derives_its_wind_inputs(cuda_lib, oracle_lib, solver):
         wg.apply_drift(ref["drift_mass"])
         m.set_snow(wo.swe, wo.depth)
     m.close()
+
+
+def _stations(seed, n, side):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-0.1 * side, 1.1 * side, n), rng.uniform(-0.1 * side, 1.1 * side, n)
+
+
+@pytest.mark.parametrize("interp,n_nearest,radius", [(capi.INTERP_SPLINE, 5, 0.0), (capi.INTERP_SPLINE, 2, 0.0),
+                                                     (capi.INTERP_IDW, 4, 0.0), (capi.INTERP_NEAREST, 1, 0.0),
+                                                     (capi.INTERP_SPLINE, 0, 0.0), (capi.INTERP_IDW, 0, 1400.0)],
+                         ids=["spline5", "spline2", "idw4", "nearest", "spline_default", "idw_radius"])
+def test_uniform_wind(cuda_lib, oracle_lib, interp, n_nearest, radius):
+    """uniform_wind (interp_met/uniform_wind.cpp:58-127) from 12 stations, the
+    station lists built as CHM's core does, against the oracle; one station
+    missing its data this step (except with the nearest station alone, where
+    that leaves faces without a station: an error, as in the reference)."""
+    from oracle import pyoracle
+    w = terrain_workload(37, veg=False)
+    sx, sy = _stations(5, 12, 2500.0)
+    rng = np.random.default_rng(6)
+    su, sd = rng.uniform(2, 15, 12), rng.uniform(0, 360, 12)
+    if interp != capi.INTERP_NEAREST:
+        su[3] = -9999.0  # the faces whose only station it is would be left without one
+    m = PBSM3D({"nLayer": "3"})
+    m.init(w.mesh)
+    o = pyoracle.Oracle(w.mesh, nLayer=3)
+    m.set_stations(sx, sy, n_nearest, radius, interp)
+    eff_n = n_nearest or (1 if interp == capi.INTERP_NEAREST else 5)
+    U, D = m.uniform_wind(su, sd)
+    Ur, Dr = o.uniform_wind(sx, sy, su, sd, eff_n if not radius else 0, radius, interp)
+    assert relerr(U, Ur) < 1e-12, relerr(U, Ur)
+    # bearings: compare on the circle
+    dd = np.abs((D - Dr + 180.0) % 360.0 - 180.0)
+    assert dd.max() < 1e-9
+    assert (U >= 0.1).all() and ((D >= 0) & (D <= 360)).all()
+    m.close()
+
+
+def test_uniform_wind_errors(cuda_lib):
+    from chm_gb300.pbsm3d import ModuleError
+    w = terrain_workload(38, veg=False, n_points=300, side=800.0)
+    sx, sy = _stations(7, 4, 800.0)
+    m = PBSM3D({"nLayer": "3"})
+    m.init(w.mesh)
+    with pytest.raises(ModuleError, match="both"):
+        m.set_stations(sx, sy, 3, 100.0)
+    with pytest.raises(ModuleError, match=">= 2"):
+        m.set_stations(sx, sy, 1, 0.0, capi.INTERP_IDW)
+    with pytest.raises(ModuleError, match="exactly 1"):
+        m.set_stations(sx, sy, 2, 0.0, capi.INTERP_NEAREST)
+    with pytest.raises(ModuleError, match="no stations"):
+        m.uniform_wind(np.ones(4), np.ones(4))
+    m.set_stations(sx, sy, 2, 0.0, capi.INTERP_IDW)
+    with pytest.raises(ModuleError, match="NAN_INPUT"):
+        m.uniform_wind(np.full(4, np.nan), np.ones(4))
+    U, D = m.uniform_wind(np.full(4, 5.0), np.full(4, 90.0))
+    assert np.allclose(U, 5.0) and np.allclose(D, 90.0)
+    m.close()
