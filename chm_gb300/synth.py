@@ -283,4 +283,7 @@ CONFIGS = {
     # the same point density at a quarter of the size (~262k faces), for
     # profiler captures that must stay small
     "cfg2q": dict(n_points=131072, side=35000.0, nLayer=10),
+    # the learned-warm-start configuration's size: ~4.2M faces at the same
+    # point density, 10 layers
+    "cfg5": dict(n_points=2097152, side=140000.0, nLayer=10),
 }
