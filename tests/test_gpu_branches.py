@@ -219,3 +219,47 @@ def test_debug_diagnostics(cuda_lib, oracle_lib, cfg):
     with pytest.raises(ModuleError, match="unknown diagnostic"):
         m.debug(f"c{L}")
     m.close()
+
+
+def test_everything_in_one_graph_ensemble(cuda_lib, oracle_lib):
+    """A two-member ensemble with every switch on: one CUDA-graph launch per
+    step, FP32-inner/FP64-refined order-5 polynomial-preconditioned solve,
+    previous-step start, the coupled u* and iterative sublimation, both
+    subgrid branches, the PomLi probability, the exp fetch, U_2m and fetch
+    derived on the device, and the snow state kept there.  Each member
+    against the oracle given that member's constants and the oracle's wind
+    modules' outputs, over two steps."""
+    from oracle import pyoracle
+    from chm_gb300.ensemble import Ensemble, MemberParams
+    keys = {"z0_ustar_coupling": True, "iterative_subl": True, "use_subgrid_topo": True, "use_subgrid_topo_V2": True,
+            "use_PomLi_probability": True, "use_tanh_fetch": False, "use_exp_fetch": True}
+    ws = [veg_workload(81), veg_workload(82, wind=12.0)]
+    members = [MemberParams(1.05, 0.01, 1.0), MemberParams(0.9, 0.003, 1.1)]
+    ens = Ensemble(module_cfg(keys))
+    ens.init([w.mesh for w in ws], members, precision=capi.MIXED, warm_start=capi.X0_PREVIOUS, graph=1, neumann=5,
+             derive_wind=1, derive_fetch=1)
+    ens.set_snow(np.concatenate([w.swe for w in ws]), np.concatenate([w.depth for w in ws]))
+    orcs = [pyoracle.Oracle(w.mesh, nLayer=L, cfg={**oracle_cfg(keys), "ustar_th_scale": p.ustar_th_scale,
+                                                  "z0_snow": p.z0_snow, "settling_scale": p.settling_scale})
+            for w, p in zip(ws, members)]
+    off = ens.offsets
+    for s in range(2):
+        fs = [forcing(w, s) for w in ws]
+        fg = ens.concat_forcing(fs)
+        for k in ("U_2m_above_srf", "fetch", "swe", "snowdepthavg"):
+            fg.pop(k)
+        out = ens.run(fg, 3600.0, want_c=True)
+        assert ens.last_stats["susp_rel_residual"] <= 1e-8
+        for m, (o, f, w) in enumerate(zip(orcs, fs, ws)):
+            fo = dict(f)
+            fo["U_2m_above_srf"] = o.scale_wind_vert(fo["U_R"], fo["snowdepthavg"])
+            fo["fetch"] = o.fetchr(fo["vw_dir"])
+            ref, _ = o.step_exact(fo, 3600.0)
+            n = w.mesh.n_faces
+            for k in ("Qsalt", "Qsusp", "Qsubl", "drift_mass", "frac_contrib", "hold_topo"):
+                assert relerr(out[k][off[m]:off[m + 1]], ref[k]) < FIELD_TOL, (s, m, k)
+            c = out["c"].reshape(L, -1)[:, off[m]:off[m + 1]].ravel()
+            assert relerr(c, ref["c"]) < FIELD_TOL, (s, m, "c")
+            w.apply_drift(ref["drift_mass"])
+        ens.set_snow(np.concatenate([w.swe for w in ws]), np.concatenate([w.depth for w in ws]))
+    ens.close()
