@@ -1,8 +1,9 @@
 // capi.cu -- the extern "C" boundary of libpbsm3d_cuda (declared in
 // include/pbsm3d.h): context creation (PBSM3D::PBSM3D + init + the two
 // NearestNeighborProblem constructors), the step (PBSM3D::run) and the
-// checkpoint state.  The step never falls back to the CPU: a missing or
-// failing GPU is an error returned to the caller.
+// checkpoint state; the ensemble constructor, the device snow state, the
+// stand-alone wind modules and the diagnostics.  The step never falls back
+// to the CPU: a missing or failing GPU is an error returned to the caller.
 #include <math.h>
 #include <string.h>
 

@@ -18,6 +18,10 @@
  *                                                    src/modules/PBSM3D.cpp:1753-1773
  *   error codes     <- CHM_THROW_EXCEPTION(module_error, ...)
  *                                                    src/modules/PBSM3D.cpp:1447,1704
+ * and, around the step: the upstream wind modules (pbsm3d_scale_wind_vert,
+ * pbsm3d_fetchr, pbsm3d_uniform_wind), the snow models' consumption of
+ * drift_mass (pbsm3d_set_snow), CHM's JSON mesh reader (pbsm3d_mesh_read),
+ * and batched parameter ensembles (pbsm3d_ensemble_create).
  *
  * Conventions
  *   - Plain C structs, POD arrays, no exceptions across the ABI.
