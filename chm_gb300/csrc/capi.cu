@@ -139,7 +139,7 @@ void pbsm3d_config_defaults(pbsm3d_config* cfg) {
     cfg->fetch_max_distance = 1000.0;
     cfg->fetch_I = 0.06;
     cfg->dep_tol = 1e-10;
-    cfg->inner_tol = 1e-5;
+    cfg->inner_tol = 1e-4;
 }
 
 const char* pbsm3d_last_error(const pbsm3d_ctx* ctx) {

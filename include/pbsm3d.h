@@ -121,7 +121,7 @@ typedef struct pbsm3d_config {
     int32_t dep_maxit;      /* 1000 */
     double susp_tol;        /* relative residual ||b-Ax||/||b||, 1e-8 (LinearAlgebra.cpp:168) */
     double dep_tol;         /* deposition relative residual, 1e-10 */
-    double inner_tol;       /* MIXED: FP32 inner relative reduction per refinement sweep, 1e-5 */
+    double inner_tol;       /* MIXED: FP32 inner relative reduction per refinement sweep, 1e-4 */
     int32_t warm_flags;     /* warm starts: bit 0 = no residual-optimal rescaling of x0,
                                bit 1 = no block-Jacobi sweep after the learned guess; 0 */
     int32_t graph;          /* 1: run each step as one CUDA-graph launch with device-side control

@@ -315,7 +315,7 @@ def _fill_defaults(c):
     c.dep_maxit = 1000
     c.susp_tol = 1e-8
     c.dep_tol = 1e-10
-    c.inner_tol = 1e-5
+    c.inner_tol = 1e-4
 
 
 def ref_atmosphere():
