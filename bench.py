@@ -168,13 +168,18 @@ VARIANTS = {
     "learned": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED},
     # the same step as one CUDA-graph launch with device-side control
     "graph_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
-    # with the polynomial (truncated Neumann) preconditioner of order 5
-    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5},
-    "previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5},
-    "graph_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 5},
-    "graph_learned_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED, "graph": 1, "neumann": 5},
-    "graph_previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 3},
-    "graph_previous_neumann7": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1, "neumann": 7},
+    # with the polynomial (truncated Neumann) preconditioners: order 5 (or K) in the
+    # suspension solve, order 1 in the deposition CG
+    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
+    "previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5, "dep_neumann": 1},
+    "graph_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                "neumann": 5, "dep_neumann": 1},
+    "graph_learned_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED, "graph": 1,
+                               "neumann": 5, "dep_neumann": 1},
+    "graph_previous_neumann3": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                "neumann": 3, "dep_neumann": 1},
+    "graph_previous_neumann7": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                "neumann": 7, "dep_neumann": 1},
 }
 
 
@@ -397,9 +402,10 @@ ENSEMBLE_VARIANTS = {
     "plain_fp64": {"precision": capi.FP64},
     "mixed_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS},
     "graph_mixed_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
-    "mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5},
+    "mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS,
+                                "neumann": 5, "dep_neumann": 1},
     "graph_mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
-                                      "neumann": 5},
+                                      "neumann": 5, "dep_neumann": 1},
 }
 
 

@@ -47,7 +47,8 @@ class Config(C.Structure):
         ("warm_flags", C.c_int32), ("graph", C.c_int32),
         ("autotune", C.c_int32), ("neumann", C.c_int32), ("derive_wind", C.c_int32),
         ("wind_ignore_canopy", C.c_int32), ("derive_fetch", C.c_int32), ("fetch_steps", C.c_int32),
-        ("fetch_incl_veg", C.c_int32), ("reserved", C.c_int32 * 3), ("fetch_max_distance", C.c_double),
+        ("fetch_incl_veg", C.c_int32), ("dep_neumann", C.c_int32),
+        ("reserved", C.c_int32 * 2), ("fetch_max_distance", C.c_double),
         ("fetch_I", C.c_double),
     ]
 

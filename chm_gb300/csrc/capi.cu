@@ -191,6 +191,10 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
         g_create_error = "neumann must be in [0, 9]";
         return PBSM3D_ERR_INVALID_ARG;
     }
+    if (cfg.dep_neumann != 0 && cfg.dep_neumann != 1) {
+        g_create_error = "dep_neumann must be 0 or 1";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
     if (cfg.solver != PBSM3D_SOLVER_BICGSTAB) {
         g_create_error = "only the BiCGStab suspension solver is implemented";
         return PBSM3D_ERR_UNSUPPORTED;
@@ -445,7 +449,10 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     c.dz_ = dalloc<double>(c, Tp, ok);
     c.dp = dalloc<double>(c, Tp, ok);
     c.dq = dalloc<double>(c, Tp, ok);
-    if (P.mixed) c.dep32 = dalloc<float>(c, (size_t)11 * Tp, ok);
+    // the polynomial deposition preconditioner reads the previous residual
+    // of its neighbours while the new one is written: a second buffer
+    if (cfg.dep_neumann && !P.mixed) c.dr2 = dalloc<double>(c, Tp, ok);
+    if (P.mixed) c.dep32 = dalloc<float>(c, (size_t)(cfg.dep_neumann ? 12 : 11) * Tp, ok);
     c.cg_flags = dalloc<unsigned>(c, (size_t)kMaxCgBlocks * 32, ok);
     c.sc = dalloc<Scalars>(c, 4, ok);
     c.red.partials = dalloc<double>(c, (size_t)8 * c.red.nblocks, ok);

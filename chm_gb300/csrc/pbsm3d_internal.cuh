@@ -298,6 +298,7 @@ struct Ctx {
     float *nw32 = nullptr, *nz32 = nullptr;
     // deposition CG vectors [Tp]
     double *dr, *dz_, *dp, *dq;
+    double* dr2 = nullptr;  // second residual buffer of the polynomial deposition CG (FP64)
     // reductions
     Scalars* sc;       // device
     Scalars* sc_host;  // pinned mirror

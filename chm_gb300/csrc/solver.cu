@@ -634,11 +634,35 @@ struct DepSys {
     const V* b;         // [Tp]
     V* x;               // [Tp] solution (starts at 0)
     V *r, *zz, *p, *q;  // [Tp] work
+    V* r2;              // [Tp] second residual buffer; non-null selects the polynomial preconditioner
 };
 
-// Jacobi-preconditioned CG in one cooperative launch; at 1M faces its
-// vectors and matrix (~100 MB in FP64) stay in L2.  Two all-reduces per
-// iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
+// The preconditioner z = M^-1 r at row i.  Jacobi: z_i = r_i / d_i.  With
+// D.r2 set, the order-1 truncated Neumann series of the Jacobi splitting
+// A = D - R (Saad, Iterative Methods for Sparse Linear Systems, 2nd ed.,
+// sec. 12.3.1): M^-1 = D^-1 + D^-1 R D^-1, symmetric, and positive definite
+// because the spectral radius of D^-1 R is below 1 for this strictly
+// diagonally dominant matrix with non-positive off-diagonals; about half the
+// iterations of Jacobi.  The neighbours' residuals are recomputed from the
+// previous iteration's r and q (rn = r - alpha q), so z needs no grid-wide
+// wait between the residual update and the dot products; the new residual
+// goes to the other buffer, since neighbours still read the old one.
+template <typename V>
+__device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __restrict__ nbr, int64_t Tp, int64_t i,
+                                         V rn, const V* __restrict__ rin, const V* __restrict__ q, V al) {
+    if (!D.r2) return D.dinv[i] * rn;
+    V acc = rn;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int32_t nb = nbr[j * Tp + i];
+        if (nb >= 0) acc -= D.off[j * Tp + i] * (D.dinv[nb] * (q ? rin[nb] - al * q[nb] : rin[nb]));
+    }
+    return D.dinv[i] * acc;
+}
+
+// CG in one cooperative launch, Jacobi or polynomial preconditioner; at 1M
+// faces its vectors and matrix (~100 MB in FP64) stay in L2.  Two all-reduces
+// per iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
 // (q is updated from A z by the recurrence q = A z + beta q).
 template <typename V>
 __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
@@ -649,7 +673,37 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V
     unsigned epoch = 0;
     // init: r = b, z = D^-1 b, p = z, q = A z
     double a3[3], t3[3];
-    {
+    if (D.r2) {
+        // polynomial preconditioner: z = M^-1 b needs the neighbours' b
+        // only, but A z needs their z, hence a second phase
+        V acc[3] = {0, 0, 0};
+        for (int64_t i = i0; i < Tp; i += stride) {
+            const V bi = D.b[i];
+            const V zi = dep_precond<V>(D, nbr, Tp, i, bi, D.b, nullptr, V(0));
+            D.r[i] = bi;
+            D.zz[i] = zi;
+            D.p[i] = zi;
+            D.x[i] = 0;
+            acc[0] += bi * zi;
+            acc[2] += bi * bi;
+        }
+        for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
+        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
+        V zq = 0;
+        for (int64_t i = i0; i < Tp; i += stride) {
+            V qi = D.diag[i] * D.zz[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) qi += D.off[j * Tp + i] * D.zz[nb];
+            }
+            D.q[i] = qi;
+            zq += D.zz[i] * qi;
+        }
+        double a1[1] = {(double)zq}, t1[1];
+        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, t1)) return;
+        t3[1] = t1[0];
+    } else {
         V acc[3] = {0, 0, 0};
         for (int64_t i = i0; i < Tp; i += stride) {
             const V bi = D.b[i];
@@ -670,8 +724,8 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V
             acc[2] += bi * bi;
         }
         for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
+        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
     }
-    if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
     double rho = t3[0];
     const double bb = t3[2];
     const double target2 = tol * tol * bb;
@@ -685,11 +739,15 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V
         {
             const V al = (V)alpha;
             V acc[2] = {0, 0};
+            // polynomial preconditioner: the residual alternates between
+            // two buffers (read the old, write the new)
+            const V* rin = (D.r2 && (it & 1)) ? D.r2 : D.r;
+            V* rout = D.r2 ? ((it & 1) ? D.r : D.r2) : D.r;
             for (int64_t i = i0; i < Tp; i += stride) {
                 D.x[i] += al * D.p[i];
-                const V ri = D.r[i] - al * D.q[i];
-                D.r[i] = ri;
-                const V zi = D.dinv[i] * ri;
+                const V ri = rin[i] - al * D.q[i];
+                rout[i] = ri;
+                const V zi = dep_precond<V>(D, nbr, Tp, i, ri, rin, D.q, al);
                 D.zz[i] = zi;
                 acc[0] += ri * zi;
                 acc[1] += ri * ri;
@@ -753,9 +811,10 @@ __global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V
 // batched BiCGStab: each member its own alpha, beta, rho and stopping test
 // ||b_m - A_m x_m|| <= tol ||b_m||.  Two kernels per iteration.
 
-// r = b, z = D^-1 b, p = z, x = 0; (r, z) -> rho, (b, b) -> bnorm2
+// r = b, z = M^-1 b, p = z, x = 0; (r, z) -> rho, (b, b) -> bnorm2
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_scg_start(Tiles tl, DepSys<V> D, MScal* ms, Scalars* sc,
+__global__ void __launch_bounds__(kBlock) k_scg_start(Tiles tl, int64_t Tp, DepSys<V> D,
+                                                      const int32_t* __restrict__ nbr, MScal* ms, Scalars* sc,
                                                       double* part) {
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
@@ -770,7 +829,7 @@ __global__ void __launch_bounds__(kBlock) k_scg_start(Tiles tl, DepSys<V> D, MSc
             const int64_t i = tl.start[t] + threadIdx.x;
             if (i >= tl.start[t + 1]) continue;
             const V bi = D.b[i];
-            const V zi = D.dinv[i] * bi;
+            const V zi = dep_precond<V>(D, nbr, Tp, i, bi, D.b, nullptr, V(0));
             D.r[i] = bi;
             D.zz[i] = zi;
             D.p[i] = zi;
@@ -833,9 +892,12 @@ __global__ void __launch_bounds__(kBlock) k_scg_q(Tiles tl, int64_t Tp, DepSys<V
     }
 }
 
-// x += alpha p, r -= alpha q, z = D^-1 r; (r, z), (r, r); beta, stopping test
+// x += alpha p, r -= alpha q, z = M^-1 r; (r, z), (r, r); beta, stopping test.
+// With the polynomial preconditioner the residual alternates between D.r and
+// D.r2 by the member's iteration parity (k_scg_start wrote D.r).
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_scg_x(Tiles tl, DepSys<V> D, MScal* ms, Scalars* sc, double* part) {
+__global__ void __launch_bounds__(kBlock) k_scg_x(Tiles tl, int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
+                                                  MScal* ms, Scalars* sc, double* part) {
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
@@ -845,14 +907,17 @@ __global__ void __launch_bounds__(kBlock) k_scg_x(Tiles tl, DepSys<V> D, MScal* 
             continue;
         }
         const V al = (V)ms[m].alpha;
+        const bool odd = D.r2 && (ms[m].iter & 1);
+        const V* rin = odd ? D.r2 : D.r;
+        V* rout = D.r2 ? (odd ? D.r : D.r2) : D.r;
         V acc[2] = {0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x;
             if (i >= tl.start[t + 1]) continue;
             D.x[i] += al * D.p[i];
-            const V ri = D.r[i] - al * D.q[i];
-            D.r[i] = ri;
-            const V zi = D.dinv[i] * ri;
+            const V ri = rin[i] - al * D.q[i];
+            rout[i] = ri;
+            const V zi = dep_precond<V>(D, nbr, Tp, i, ri, rin, D.q, al);
             D.zz[i] = zi;
             acc[0] += ri * zi;
             acc[1] += ri * ri;
@@ -1403,6 +1468,19 @@ int configure_cg(Ctx& c) {
     return 0;
 }
 
+// The deposition CG's system and work vectors, FP64 and (MIXED) FP32; the
+// second residual buffer exists with dep_neumann only.
+static DepSys<double> dep_sys64(Ctx& c) {
+    return DepSys<double>{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq, c.dr2};
+}
+
+static DepSys<float> dep_sys32(Ctx& c) {
+    const int64_t Tp = c.P.Tp;
+    float* f = c.dep32;
+    return DepSys<float>{f,          f + Tp,     f + 4 * Tp, f + 5 * Tp, f + 6 * Tp,
+                         f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp, c.cfg.dep_neumann ? f + 11 * Tp : nullptr};
+}
+
 // One cooperative CG launch on system D; returns the status and iterations in sc.
 template <typename V>
 static int launch_cg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* sc, double tol, int maxit) {
@@ -1437,7 +1515,7 @@ static int solve_deposition_mixed(Ctx& c, cudaStream_t s, double tol) {
     const int64_t T = c.P.T, Tp = c.P.Tp;
     float* f = c.dep32;
     float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
-    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    DepSys<float> D32 = dep_sys32(c);
     prof_begin(c, s);
     k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
     PBSM_CUDA_TRY(cudaMemsetAsync(c.D.x, 0, Tp * sizeof(double), s));
@@ -1507,7 +1585,7 @@ static int scg_iterations(Ctx& c, cudaStream_t s, DepSys<V> D, MScal* ms, Scalar
     int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
     int64_t act = active_faces(c);
     prof_begin(c, s);
-    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     prof_end(c, s, PBSM3D_K_CG, act * sv_ * 17 + act * 12);
     c.launches += 1;
@@ -1515,7 +1593,7 @@ static int scg_iterations(Ctx& c, cudaStream_t s, DepSys<V> D, MScal* ms, Scalar
     while (true) {
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
-            k_scg_x<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+            k_scg_x<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
             k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
             prof_end(c, s, PBSM3D_K_CG, act * sv_ * 18 + act * 12);
             c.launches += 1;
@@ -1593,7 +1671,7 @@ static int solve_deposition_members(Ctx& c, cudaStream_t s, double tol) {
     };
     int rc;
     if (!c.P.mixed) {
-        DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
+        DepSys<double> D = dep_sys64(c);
         for (int m = 0; m < n; ++m) {
             c.ms_host[m] = MScal{};
             c.ms_host[m].target2 = tol * tol;
@@ -1609,7 +1687,7 @@ static int solve_deposition_members(Ctx& c, cudaStream_t s, double tol) {
     }
     float* f = c.dep32;
     float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
-    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    DepSys<float> D32 = dep_sys32(c);
     prof_begin(c, s);
     k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
     prof_end(c, s, PBSM3D_K_CG, T * (56 + 20));
@@ -1656,7 +1734,7 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     double* part = c.red.partials;
     Scalars* sc = c.sc + 2;
     const int64_t T = c.P.T;
-    DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
+    DepSys<double> D = dep_sys64(c);
     prof_begin(c, s);
     int rc = launch_cg<double>(c, s, D, c.coop_blocks, sc, tol, c.cfg.dep_maxit);
     if (rc) return rc;
@@ -2281,12 +2359,12 @@ int capture_scg(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& 
     cudaStream_t s = G.cap[depth];
     const int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
     double* part = c.tile_part;
-    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, D, ms, sc, part);
+    k_scg_start<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     CondBody loop;
     if (loop.begin(s, G.cap[depth + 1], h.h[H_DLOOP], cudaGraphCondTypeWhile)) return 1;
     cudaStream_t t = G.cap[depth + 1];
-    k_scg_x<V><<<g, kBlock, 0, t>>>(tl, D, ms, sc, part);
+    k_scg_x<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     k_scg_q<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     k_ctl_inner<<<1, kBlock, 0, t>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_DLOOP, 3, h);
     return loop.end();
@@ -2301,7 +2379,7 @@ int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     const int gr = std::max(1, std::min(c.grid_red[0], tl.ntiles));
     double* part = c.tile_part;
     if (!c.P.mixed) {
-        DepSys<double> D{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq};
+        DepSys<double> D = dep_sys64(c);
         k_ctl_dcg_init<<<1, kBlock, 0, s>>>(G.ctl, c.ms0, sc, tl, c.act_buf, G.nact, tol, c.cfg.dep_maxit, h);
         if (capture_scg<double>(c, G, h, depth, tl, D, c.ms0, sc)) return 1;
         k_ctl_dres_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, 0);
@@ -2311,7 +2389,7 @@ int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     }
     float* f = c.dep32;
     float *diag32 = f, *off32 = f + Tp, *dinv32 = f + 4 * Tp, *r32 = f + 5 * Tp;
-    DepSys<float> D32{diag32, off32, dinv32, r32, f + 6 * Tp, f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp};
+    DepSys<float> D32 = dep_sys32(c);
     k_dep_to_f32<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, diag32, off32, dinv32);
     if (cudaMemsetAsync(c.D.x, 0, Tp * sizeof(double), s) != cudaSuccess) return 1;
     k_ctl_dmix_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, h);

@@ -48,6 +48,19 @@ PBSM3D::PBSM3D(config_file c) : module_base("PBSM3D", parallel::domain, c) {
             for (const char* v : {"c", "csubl", "u_z", "cz"}) provides(v + std::to_string(z));
     }
     pbsm3d_config_defaults(&gpu_cfg);
+    // this library's solver switches (not reference keys); the plain FP64
+    // form without them
+    pbsm3d_config& g = gpu_cfg;
+    if (cfg.get("solver.mixed", false)) g.precision = PBSM3D_MIXED;
+    const std::string x0 = cfg.get<std::string>("solver.warm_start", "zero");
+    if (x0 == "previous")
+        g.warm_start = PBSM3D_X0_PREVIOUS;
+    else if (x0 != "zero")  // the learned start needs weights: the C ABI's pbsm3d_set_mlp
+        throw module_error("solver.warm_start must be zero or previous, not '" + x0 + "'");
+    g.graph = cfg.get("solver.graph", false) ? 1 : 0;
+    g.neumann = cfg.get("solver.neumann", 0);
+    if (g.neumann < 0 || g.neumann > 9) throw module_error("solver.neumann must be in [0, 9]");
+    g.dep_neumann = cfg.get("solver.dep_neumann", false) ? 1 : 0;
 }
 
 PBSM3D::~PBSM3D() { pbsm3d_destroy(ctx_); }
@@ -79,8 +92,6 @@ void PBSM3D::init(mesh& domain) {
     g.use_subgrid_topo_V2 = use_subgrid_topo_V2;
     g.use_R94_lambda = cfg.get("use_R94_lambda", true);
     g.debug_output = cfg.get("debug_output", false);
-    // this library's solver switch (not a reference key): "solver.mixed": "true"
-    if (cfg.get("solver.mixed", false)) g.precision = PBSM3D_MIXED;
     mesh_store& m = *domain;
     const int64_t n = m.size_faces();
     pbsm3d_mesh_desc d{};

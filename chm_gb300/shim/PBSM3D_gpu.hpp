@@ -19,7 +19,8 @@ class PBSM3D : public module_base {
     void load_checkpoint(mesh& domain, netcdf& chkpt) override;
 
     pbsm3d_stats last_stats{};
-    // solver settings beyond the reference keys ("solver.precision": "mixed")
+    // solver settings beyond the reference keys ("solver.mixed", "solver.warm_start",
+    // "solver.graph", "solver.neumann", "solver.dep_neumann")
     pbsm3d_config gpu_cfg{};
 
    private:

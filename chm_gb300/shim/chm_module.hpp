@@ -56,6 +56,8 @@ template <>
 inline int config_file::parse<int>(const std::string&, const std::string& v) { return (int)std::stod(v); }
 template <>
 inline double config_file::parse<double>(const std::string&, const std::string& v) { return std::stod(v); }
+template <>
+inline std::string config_file::parse<std::string>(const std::string&, const std::string& v) { return v; }
 
 // A triangle mesh with CHM's per-face variable store.
 class mesh_store {

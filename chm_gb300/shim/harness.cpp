@@ -74,6 +74,32 @@ static int selftest() {
     ph.put("use_tanh_fetch", "false");
     auto m2 = module_factory::create("PBSM3D", ph);
     expect(has(m2->depends(), "p_snow_hours") && !has(m2->depends(), "fetch"), "p_snow_hours dependency");
+    config_file fast;
+    fast.put("solver.mixed", "true");
+    fast.put("solver.warm_start", "previous");
+    fast.put("solver.graph", "true");
+    fast.put("solver.neumann", "5");
+    fast.put("solver.dep_neumann", "true");
+    auto m3 = module_factory::create("PBSM3D", fast);
+    const pbsm3d_config& g = dynamic_cast<PBSM3D&>(*m3).gpu_cfg;
+    expect(g.precision == PBSM3D_MIXED && g.warm_start == PBSM3D_X0_PREVIOUS && g.graph == 1 && g.neumann == 5 &&
+               g.dep_neumann == 1,
+           "solver keys");
+    const pbsm3d_config& g0 = dynamic_cast<PBSM3D&>(*m).gpu_cfg;
+    expect(g0.precision == PBSM3D_FP64 && g0.warm_start == PBSM3D_X0_ZERO && g0.graph == 0 && g0.neumann == 0 &&
+               g0.dep_neumann == 0,
+           "plain form by default");
+    for (auto kv : {std::pair<const char*, const char*>{"solver.warm_start", "learned"}, {"solver.neumann", "10"}}) {
+        config_file b2;
+        b2.put(kv.first, kv.second);
+        threw = false;
+        try {
+            module_factory::create("PBSM3D", b2);
+        } catch (module_error&) {
+            threw = true;
+        }
+        expect(threw, kv.first);
+    }
     std::cout << (fails ? "selftest FAILED\n" : "selftest ok\n");
     return fails ? 1 : 0;
 }

@@ -142,7 +142,11 @@ typedef struct pbsm3d_config {
     int32_t derive_fetch;        /* 1: every step computes fetch from vw_dir (fetchr); 0 */
     int32_t fetch_steps;         /* fetchr "steps", 10 */
     int32_t fetch_incl_veg;      /* fetchr "incl_veg", true */
-    int32_t reserved[3];
+    int32_t dep_neumann;         /* 1: the deposition CG preconditioned by the order-1 truncated Neumann
+                                    series of its Jacobi splitting, M^-1 = D^-1 + D^-1 R D^-1
+                                    (A = D - R; SPD for the diagonally dominant deposition matrix),
+                                    about half the iterations of Jacobi; 0 = D^-1 alone */
+    int32_t reserved[2];
     double fetch_max_distance;   /* fetchr "max_distance", 1000 m */
     double fetch_I;              /* fetchr "I", 0.06 */
 } pbsm3d_config;

@@ -47,8 +47,12 @@ def _check_member(out, ref, tag):
 @pytest.mark.parametrize("solver", [{}, {"precision": capi.MIXED}, {"warm_start": capi.X0_PREVIOUS},
                                     {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
                                     {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
-                                     "neumann": 5}],
-                         ids=["fp64", "mixed", "warm", "graph", "graph_neumann5"])
+                                     "neumann": 5},
+                                    {"dep_neumann": 1}, {"precision": capi.MIXED, "dep_neumann": 1},
+                                    {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                     "neumann": 5, "dep_neumann": 1}],
+                         ids=["fp64", "mixed", "warm", "graph", "graph_neumann5", "fp64_dep_neumann",
+                              "mixed_dep_neumann", "graph_neumann5_dep_neumann"])
 def test_members_match_oracle_over_steps(cuda_lib, oracle_lib, solver):
     from oracle import pyoracle
     ws = workloads()

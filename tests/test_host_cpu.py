@@ -89,7 +89,7 @@ def test_create_rejects_bad_configs(cuda_lib):
     desc = capi.mesh_desc(m, keep)
     ctx = C.c_void_p()
     for bad in (dict(use_exp_fetch=1, use_tanh_fetch=1), dict(settling_velocity=-0.1), dict(nLayer=0),
-                dict(abi_version=99), dict(neumann=10), dict(neumann=-1)):
+                dict(abi_version=99), dict(neumann=10), dict(neumann=-1), dict(dep_neumann=2)):
         cfg = capi.default_config(cuda_lib, **bad)
         assert cuda_lib.pbsm3d_create(C.byref(desc), C.byref(cfg), C.byref(ctx)) == capi.ERR_INVALID_ARG
     bad_nb = m.neighbor.copy()
