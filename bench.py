@@ -299,9 +299,13 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
 
     # ---- roofline of the dominant kernel class (events around each launch);
     # a graph-mode step has no per-launch events: use the fastest profiled form
-    prof_name = head if all(s["profiled"] for s in stats) else min(
-        (n for n in names if all(s["profiled"] for s in results[n]["stats"])), key=lambda n: results[n]["t_max"])
-    stats_p = results[prof_name]["stats"]
+    profiled = [n for n in names if all(s["profiled"] for s in results[n]["stats"])]
+    if not profiled:  # only graph forms asked for: no per-kernel figures
+        prof_name = None
+        profiled = [head]
+    else:
+        prof_name = head if head in profiled else min(profiled, key=lambda n: results[n]["t_max"])
+    stats_p = results[prof_name or head]["stats"]
     kern_ms = np.sum([s["kern_ms"] for s in stats_p], axis=0)
     kern_bytes = np.sum([s["kern_bytes"] for s in stats_p], axis=0)
     kern_n = np.sum([s["kern_launches"] for s in stats_p], axis=0)
@@ -325,7 +329,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                                  "share": round(float(kern_ms[k]) / total_ms, 4) if total_ms > 0 else None}
                for k in range(len(capi.KERNELS)) if kern_n[k] > 0}
     alg_bytes = float(np.sum([s["bytes_moved"] for s in stats_p]))
-    t_prof = results[prof_name]["t_dev"]
+    t_prof = results[prof_name or head]["t_dev"]
 
     def solver_summary(sts):
         return {"susp_iters_mean": float(np.mean([s["susp_iters"] for s in sts])),
@@ -360,6 +364,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                           "frac": round(alg_bytes / t_prof / 1e9 / peak, 4), "variant": prof_name},
         "kernels": kernels,
         "solver": solver_summary(stats),
+        **({} if prof_name else {"roofline": None, "step_roofline": None, "kernels": None}),
         "variants": {n: {"value": faces_total / results[n]["t_max"],
                          "ms_per_step": results[n]["t_max"] / args.steps * 1e3,
                          "speedup_vs_plain_fp64": (results["plain_fp64"]["t_max"] / results[n]["t_max"]

@@ -570,7 +570,12 @@ __device__ __forceinline__ unsigned long long global_timer_ns() {
 }
 
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s
-constexpr int kCgBlock = 512;    // one block per SM keeps the all-reduce fan-in small
+// Two 512-thread blocks per SM (64 registers a thread): each thread's chain
+// of dependent loads (neighbour index, then the gathered values) over its
+// grid-stride rows is half as long as with one block per SM, which is what
+// bounds an iteration whose vectors sit in L2.
+constexpr int kCgBlock = 512;
+constexpr int kCgBlocksPerSm = 2;
 constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 
 // All-reduce of NT per-thread values over a cooperative grid, identical in
@@ -665,7 +670,7 @@ __device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __re
 // per iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
 // (q is updated from A z by the recurrence q = A z + beta q).
 template <typename V>
-__global__ void __launch_bounds__(kCgBlock) k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
+__global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
                                                           double* partials, unsigned* flags, int* err, Scalars* sc,
                                                           double tol, int maxit) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -1452,11 +1457,12 @@ int configure_cg(Ctx& c) {
     PBSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PBSM_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     const int64_t need = (c.P.Tp + kCgBlock - 1) / kCgBlock;
-    // one co-resident block per SM, within the partials workspace and the flag lines
+    // up to kCgBlocksPerSm co-resident blocks per SM, within the partials
+    // workspace and the flag lines
     auto blocks_for = [&](const void* f, int& out) -> int {
         int per_sm = 0;
         PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kCgBlock, 0));
-        int64_t b = std::min<int64_t>(need, per_sm >= 1 ? (int64_t)sms : 0);
+        int64_t b = std::min<int64_t>(need, (int64_t)std::min(per_sm, kCgBlocksPerSm) * sms);
         b = std::min<int64_t>(b, (int64_t)c.red.nblocks);
         b = std::min<int64_t>(b, (int64_t)kMaxCgBlocks);
         out = coop ? (int)b : 0;
