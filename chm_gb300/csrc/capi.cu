@@ -266,6 +266,7 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     }
     P.log_2_0002 = log(2.0 / 0.0002);
     P.mixed = cfg.precision == PBSM3D_MIXED;
+    P.fac64 = !P.mixed || cfg.warm_start == PBSM3D_X0_LEARNED;
     P.z0_ustar_coupling = cfg.z0_ustar_coupling != 0;
     P.iterative_subl = cfg.iterative_subl != 0;
     P.subgrid = (cfg.use_subgrid_topo ? 1 : 0) | (cfg.use_subgrid_topo_V2 ? 2 : 0);
@@ -362,7 +363,7 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     A.face_v = dalloc<double>(c, (size_t)FV_COUNT * Tp, ok);
     A.slow_list = dalloc<int32_t>(c, Tp, ok);
     A.n_slow = dalloc<int>(c, 1, ok);
-    A.slow_rows = dalloc<double>(c, (size_t)8 * R, ok);
+    A.slow_rows = dalloc<double>(c, (size_t)kRowTerms * R, ok);
     MathTables* mt = dalloc<MathTables>(c, 1, ok);
     P.mt = mt;
     // batched-Krylov tiles: runs of at most kBlock faces within one member

@@ -48,6 +48,7 @@ struct Params {
     // scale, z0, settling scale, log(50/z0)) are in Member.
     double cos_pi_4, Lc_tanh, log_2_0002;
     int mixed;
+    int fac64;  // FP64 Thomas factors needed (FP64 solves, or the learned start's sweep)
     int z0_ustar_coupling, iterative_subl;  // the reference's non-default branches
     int subgrid;  // bit 0: use_subgrid_topo, bit 1: use_subgrid_topo_V2
     const MathTables* mt;  // exp/log tables (device)
@@ -124,20 +125,26 @@ struct Subgrid {
 };
 
 // Height-dependent coefficients of one layer (see cz_coeffs in physics.cu).
-// The first eight fields are also the per-row layout of Susp::slow_rows.
+// The first kRowTerms fields are also the per-row layout of Susp::slow_rows.
+// The particle mass mm divides the sublimation rate, so it is folded into the
+// two terms the rate combines (one multiply a row fewer).
 struct CzCoef {
-    double inv_mm, omega, Qr, l;
-    double rz2nu;  // 2 r_z / nu: Re = rz2nu * Vr
-    double rsig;   // r_z * sigfac
-    double lwarg;  // log((cz - z0) / z0), the wind-profile numerator
-    double llw;    // log(lwarg)
-    double cz;     // layer centre height above the snow surface
-    double pad[3];
+    double omega;   // settling velocity
+    double qr_m;    // Qr / mm: the radiation term (iterative_subl: the mean radius) over the mass
+    double l;       // mixing length
+    double rz2nu;   // 2 r_z / nu: Re = rz2nu * Vr
+    double rsig_m;  // r_z sigfac / mm
+    double lwarg;   // log((cz - z0) / z0), the wind-profile numerator
+    double ew;      // lwarg^1.36: the layer's factor of u_z^1.36
+    double cz;      // layer centre height above the snow surface
 };
+constexpr int kRowTerms = 7;  // doubles per row of Susp::slow_rows
 
 // Per-face values the saltation pass hands to the row assembly, [FV_COUNT][Tp].
 enum FaceValue {
-    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QSUB, FV_C1R, FV_LR, FV_LU, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0,
+    // FV_QC, FV_QL: the face's factors of the two sublimation terms; FV_EF:
+    // its factor of the particle-velocity term 3 cos(pi/4) 0.005 u_z^1.36
+    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QC, FV_QL, FV_EF, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0,
     FV_COUNT
 };
 
@@ -164,7 +171,7 @@ struct Susp {
     double* face_v;   // [FV_COUNT][Tp] saltation pass results
     int32_t* slow_list;  // [Tp] faces with a saltation layer (hs > 0)
     int* n_slow;      // device count of slow_list
-    double* slow_rows;   // [8][R] layer terms of those faces' rows
+    double* slow_rows;   // [kRowTerms][R] layer terms of those faces' rows
     double* band;     // [6][R]
     double* rhs;      // [R]
     double* x;        // [R]

@@ -87,7 +87,7 @@ __device__ __forceinline__ double dot2(double ax, double ay, double bx, double b
 // (PBSM3D.cpp:1003-1028, 1113-1120, 1157): mean particle radius and mass,
 // radius of the mean-mass particle, settling velocity, the log(cz) factor of
 // the undersaturation, the radiation term and the mixing length; and the
-// wind-profile logarithm log((cz - z0)/z0) with its own logarithm.
+// wind-profile logarithm log((cz - z0)/z0) with its 1.36th power.
 // hz_minus_d0 is the reference's Z_out - (snow depth + z0) of
 // log_scale_wind (Atmosphere.cpp:32-38).
 __device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double z0, double settling_scale,
@@ -96,22 +96,24 @@ __device__ __forceinline__ void cz_coeffs(double cz, double hz_minus_d0, double 
     const double rm = 4.6e-5 * exp_t(-0.258 * lcz, t);             // 4.6e-5 cz^-0.258
     const double ia = rcp_t(4.08 + 12.6 * cz);                       // 1 / mm_alpha
     const double mm = 4. / 3. * M_PI * kRhoIce * rm * rm * rm * (1.0 + 3.0 * ia + 2. * (ia * ia));
-    o.inv_mm = rcp_t(mm);
+    const double inv_mm = rcp_t(mm);
     const double lq = 0.3333333 * log_t((3.0 * mm) * (1.0 / (4 * M_PI * kRhoIce)), t);
     const double r_z = exp_t(lq, t);                                 // (3 mm / 4 pi rho)^0.3333333
     double omega = P.settling_velocity;
     if (!P.do_fixed_settling) omega = 1.1e7 * exp_t(1.8 * lq, t);   // 1.1e7 r_z^1.8
     o.omega = omega * settling_scale;
     // the radiation term, or with iterative_subl, whose rate has no radiation
-    // term, the mean radius itself
-    o.Qr = P.iterative_subl ? rm : 0.9 * M_PI * rm * rm * 120.0;
+    // term, the mean radius itself; over the particle mass
+    o.qr_m = (P.iterative_subl ? rm : 0.9 * M_PI * rm * rm * 120.0) * inv_mm;
     const double sigfac = 1.019 + 0.027 * lcz;
     const double kz = kKappa * (cz + z0);
     o.l = kz * 40.0 * rcp_t(kz + 40.0);
     o.rz2nu = 2.0 * r_z * (1.0 / 1.88e-5);                          // Re = rz2nu * Vr
-    o.rsig = r_z * sigfac;
+    o.rsig_m = r_z * sigfac * inv_mm;
     o.lwarg = log_t(hz_minus_d0 * rcp_t(z0), t);
-    o.llw = log_t(o.lwarg, t);
+    // u_z^1.36 = (uref / logden)^1.36 lwarg^1.36: the face's factor times
+    // this one, so the row needs no exp (lwarg <= 0 gives NaN, as log does)
+    o.ew = exp_t(1.36 * log_t(o.lwarg, t), t);
     o.cz = cz;
 }
 
@@ -333,9 +335,12 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             const double sdz0 = snow_depth + z0;
             const double logden = log_t((kZUR - sdz0) * rcp_t(z0), mt);
             const double inv_logden = rcp_t(logden);
-            // log(u_z) = log(uref) - log(logden) + log(log((cz - z0)/z0)), so
-            // u_z^1.36 costs one exp per row
-            const double lu_face = uref > 0.0 ? log_t(uref, mt) - log_t(logden, mt) : 0.0;
+            // u_z^1.36 = (uref / logden)^1.36 lwarg^1.36: this face's factor,
+            // with the constants of the particle-velocity term 3 cos(pi/4) 0.005 u_z^1.36
+            const double ef = uref > 0.0 ? (0.015 * P.cos_pi_4) * exp_t(1.36 * (log_t(uref, mt) - log_t(logden, mt)), mt)
+                                         : 0.0;
+            // the two sublimation terms' per-face factors
+            const double qc = P.iterative_subl ? q_sub : q_sub * c1r, ql = P.iterative_subl ? 0.0 : q_sub * LR;
             double v1 = 0, v2 = 0;
             v1 += ux * ux;
             v2 += uy * uy;
@@ -345,10 +350,9 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             fv[FV_USTAR * Tp + i] = ustar;
             fv[FV_UTH * Tp + i] = uth;
             fv[FV_CSALT * Tp + i] = c_salt;
-            fv[FV_QSUB * Tp + i] = q_sub;
-            fv[FV_C1R * Tp + i] = c1r;
-            fv[FV_LR * Tp + i] = LR;
-            fv[FV_LU * Tp + i] = lu_face;
+            fv[FV_QC * Tp + i] = qc;
+            fv[FV_QL * Tp + i] = ql;
+            fv[FV_EF * Tp + i] = ef;
             fv[FV_INVLOGDEN * Tp + i] = inv_logden;
             if (P.z0_ustar_coupling) fv[FV_Z0 * Tp + i] = z0;
             // lateral faces: udotm_f = u_z * k_f with k_f = (u_hat . m_f) / |u_hat|
@@ -387,14 +391,13 @@ __global__ void __launch_bounds__(kBlock) k_salt_rows(Params P, Forcing F, Susp 
         cz_coeffs(cz, cz + snow_depth - (snow_depth + z0), z0, mp.settling_scale, P, mt, o);
         const int64_t r = (int64_t)z * Tp + i;
         double* w = A.slow_rows + r;
-        w[0 * R] = o.inv_mm;
-        w[1 * R] = o.omega;
-        w[2 * R] = o.Qr;
-        w[3 * R] = o.l;
-        w[4 * R] = o.rz2nu;
-        w[5 * R] = o.rsig;
-        w[6 * R] = o.lwarg;
-        w[7 * R] = o.llw;
+        w[0 * R] = o.omega;
+        w[1 * R] = o.qr_m;
+        w[2 * R] = o.l;
+        w[3 * R] = o.rz2nu;
+        w[4 * R] = o.rsig_m;
+        w[5 * R] = o.lwarg;
+        w[6 * R] = o.ew;
     }
 }
 
@@ -443,11 +446,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         const double ustar = fv[FV_USTAR * Tp + i];
         const double uth = fv[FV_UTH * Tp + i];
         const double c_salt = fv[FV_CSALT * Tp + i];
-        const double q_sub = fv[FV_QSUB * Tp + i];
-        const double c1r = fv[FV_C1R * Tp + i];
-        const double LR = fv[FV_LR * Tp + i];
-        const double lu_face = fv[FV_LU * Tp + i];
+        const double qc = fv[FV_QC * Tp + i];
+        const double ql = fv[FV_QL * Tp + i];
+        const double ef = fv[FV_EF * Tp + i];
         const double inv_logden = fv[FV_INVLOGDEN * Tp + i];
+        const double kxr = 0.015 * P.cos_pi_4;  // 3 cos(pi/4) 0.005
         const bool saltation = S.saltation[i];
         const double uref = F.UR[i];
         double snow_depth = F.sd[i];
@@ -497,40 +500,47 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
         const long long b001 = __double_as_longlong(0.01);
         const bool uref_pos = uref > 0.0;
         double prev_up = 0.0, prev_ib = 1.0;
+        float prev_up32 = 0.f, prev_ib32 = 1.f;
         unsigned long long face_max = 0;
         for (int z = 0; z < P.L; ++z) {
             const int64_t r = (int64_t)z * Tp + i;
             // layer terms: the member's table row, or this row of pass 2
-            const double* lp = fast ? &tab[z].inv_mm : A.slow_rows + r;
+            const double* lp = fast ? &tab[z].omega : A.slow_rows + r;
             const int64_t ls = fast ? 1 : R;
-            const double inv_mm = lp[0], omega = lp[ls], Qr = lp[2 * ls], lmix = lp[3 * ls];
-            const double rz2nu = lp[4 * ls], rsig = lp[5 * ls], lwarg = lp[6 * ls], llw = lp[7 * ls];
+            const double omega = lp[0], qr_m = lp[ls], lmix = lp[2 * ls], rz2nu = lp[3 * ls];
+            const double rsig_m = lp[4 * ls], lwarg = lp[5 * ls], ew = lp[6 * ls];
             // the layer centre is only needed by the canopy and 50 m tests,
             // which the per-face flags usually settle
             const bool need_cz = in_canopy_possible || !all_below_zur;
             const double cz = need_cz ? z * P.dz + hs + P.dz / 2. : 0.0;
-            double u_z, xrz;
+            // u_z and xr = 3 cos(pi/4) 0.005 u_z^1.36: in the open below 50 m
+            // with a positive wind, the face's factor times the layer's (no
+            // exp per row); else u_z^1.36 directly (a branch, not a select)
+            double u_z, xr = 0.0;
+            bool direct = true;
             if (in_canopy_possible && saltation && cz < height_diff) {
                 u_z = 2.8 * uth;
-                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             } else if (in_canopy_possible && cz < height_diff) {
                 u_z = 0.01;
-                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             } else if (all_below_zur || cz + snow_depth < kZUR) {
                 // log_scale_wind(uref, 50, hz, snow_depth, z0), clamped at 0.01 m/s
                 const double u_raw = uref * lwarg * inv_logden;
                 const long long ub = __double_as_longlong(u_raw);
                 const bool above = ub > b001 && ub <= 0x7ff0000000000000ll;  // 0.01 < u_raw, not NaN
                 u_z = above ? u_raw : 0.01;
-                xrz = (above && uref_pos) ? 0.005 * exp_t(1.36 * (lu_face + llw), mt) : 0.005 * pow_t(u_z, 1.36, mt);
+                if (above && uref_pos) {
+                    xr = ef * ew;
+                    direct = false;
+                }
             } else {
                 u_z = fmax(0.01, uref);
-                xrz = 0.005 * pow_t(u_z, 1.36, mt);
             }
-            const double Vr = omega + 3.0 * xrz * P.cos_pi_4;
+            if (direct) xr = kxr * pow_t(u_z, 1.36, mt);
+            const double Vr = omega + xr;
             const double Nu = 1.79 + 0.606 * sqrt(rz2nu * Vr);
-            const double dmdtz = P.iterative_subl ? q_sub * (Qr * Nu) : q_sub * (c1r * Nu * rsig - Qr * LR);
-            double csubl = dmdtz * inv_mm;
+            // dm/dt / mm (PBSM3D.cpp:1113-1120 regrouped: the face factors qc, ql
+            // times the layer factors over the mass)
+            double csubl = P.iterative_subl ? qc * Nu * qr_m : fma(qc * Nu, rsig_m, -ql * qr_m);
             const double w = omega;
             double K34;
             if (P.rouault)
@@ -574,25 +584,43 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             A.rhs[r] = b;
             A.x[r] = 0.0;
             // Thomas factorisation of the column: beta_z = d_z - l_z * up_{z-1}
-            const double lz = (z == 0) ? 0.0 : lo * prev_ib;
-            const double beta = (z == 0) ? dg : dg - lz * prev_up;
-            const double ib = rcp_t(beta);
-            A.fac_l[r] = lz;
-            A.fac_ib[r] = ib;
+            float l32 = 0.f, ib32 = 1.f;
+            const float up32 = P.mixed ? f32_rn(up) : 0.f;
+            if (P.fac64) {
+                const double lz = (z == 0) ? 0.0 : lo * prev_ib;
+                const double beta = (z == 0) ? dg : dg - lz * prev_up;
+                const double ib = rcp_t(beta);
+                A.fac_l[r] = lz;
+                A.fac_ib[r] = ib;
+                if (P.mixed) {
+                    l32 = f32_rn(lz);
+                    ib32 = f32_rn(ib);
+                }
+                prev_ib = ib;
+                if (nonfinite(ib)) bad = true;
+            } else {
+                // MIXED, no FP64 factors needed: the FP32 preconditioner's own
+                // factorisation of the FP32-rounded column, on the FP32 pipe.
+                // It only preconditions; the refinement's FP64 residual decides.
+                const float dg32 = f32_rn(dg);
+                l32 = (z == 0) ? 0.f : f32_rn(lo) * prev_ib32;
+                ib32 = __frcp_rn((z == 0) ? dg32 : __fmaf_rn(-l32, prev_up32, dg32));
+                prev_ib32 = ib32;
+            }
             if (P.mixed) {
                 A.lat32[r] = f32_rn(lat[0]);
                 A.lat32[R + r] = f32_rn(lat[1]);
                 A.lat32[2 * R + r] = f32_rn(lat[2]);
-                A.l32[r] = f32_rn(lz);
-                A.ib32[r] = f32_rn(ib);
-                A.up32[r] = f32_rn(up);
+                A.l32[r] = l32;
+                A.ib32[r] = ib32;
+                A.up32[r] = up32;
             }
             prev_up = up;
-            prev_ib = ib;
+            prev_up32 = up32;
             vmax_bits = max(vmax_bits, abs_bits(b));
             face_max = max(face_max, abs_bits(b));
             if (nonfinite(dg) | nonfinite(b) | nonfinite(lat[0]) | nonfinite(lat[1]) | nonfinite(lat[2]) |
-                nonfinite(lo) | nonfinite(up) | nonfinite(ib))
+                nonfinite(lo) | nonfinite(up))
                 bad = true;
         }
         if (Mb.n > 1) atomicMax(&mb_max[mem], face_max);

@@ -417,8 +417,13 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const d
                                                      const int32_t* __restrict__ nbr, const double* __restrict__ x,
                                                      const double* __restrict__ b, double* __restrict__ r,
                                                      V* __restrict__ rv, V* __restrict__ rhv, V* __restrict__ pv,
-                                                     V* __restrict__ vv, MScal* ms, double* part) {
+                                                     V* __restrict__ vv, MScal* ms, double* part, int first,
+                                                     const int* __restrict__ sweep) {
     const int64_t Tp = P.Tp, R = P.R;
+    // (b, b) and (b, r) serve the first refinement sweep only (the target's
+    // norm and the warm start's scale): two FP64 FMAs a row fewer after it.
+    // The sweep number is the host's (first) or, in a graph, the controller's.
+    const bool full = sweep ? *sweep == 0 : first != 0;
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
@@ -450,15 +455,19 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const d
                     vv[k] = 0;
                 }
                 acc[0] += rk * rk;
-                acc[1] += b[k] * b[k];
-                acc[2] += b[k] * rk;
+                if (full) {
+                    acc[1] += b[k] * b[k];
+                    acc[2] += b[k] * rk;
+                }
             }
         }
         double tot[3];
         if (member_totals<3>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
             ms[m].rnorm2 = tot[0];
-            ms[m].bnorm2 = tot[1];
-            ms[m].red0 = tot[2];
+            if (full) {
+                ms[m].bnorm2 = tot[1];
+                ms[m].red0 = tot[2];
+            }
         }
         a = ae;
     }
@@ -1320,10 +1329,10 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         prof_begin(c, s);
         if (c.P.mixed)
             k_residual<float><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
-                                                    c.p32, c.v32, c.msR, part);
+                                                    c.p32, c.v32, c.msR, part, sweeps == 0, nullptr);
         else
             k_residual<double><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh,
-                                                     c.p, c.v, c.msR, part);
+                                                     c.p, c.v, c.msR, part, sweeps == 0, nullptr);
         prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 88 : 96) + act * 12);
         int rc = read_members(c, s, c.msR);
         if (rc) return rc;
@@ -2316,10 +2325,10 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
         cudaStream_t t = G.cap[depth + 1];
         if (mixed)
             k_residual<float><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
-                                                    c.p32, c.v32, c.msR, part);
+                                                    c.p32, c.v32, c.msR, part, 1, &G.ctl->sweep);
         else
             k_residual<double><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
-                                                     c.v, c.msR, part);
+                                                     c.v, c.msR, part, 1, &G.ctl->sweep);
         if (warm) {
             CondBody wb;
             if (wb.begin(t, G.cap[depth + 2], h.h[H_WARM], cudaGraphCondTypeIf)) return 1;
