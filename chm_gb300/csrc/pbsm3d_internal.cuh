@@ -466,6 +466,48 @@ __device__ __forceinline__ bool block_partials_last(double (&v)[NT], double* par
     return true;
 }
 
+// Maxima of non-negative values (no order to fix): as block_partials_last,
+// the last block reducing all partials with every thread.
+template <int NT>
+__device__ __forceinline__ bool block_partials_last_max(double (&v)[NT], double* partials, unsigned* counter,
+                                                        double (&tot)[NT]) {
+    __shared__ double shm[NT][32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    auto block_max = [&](double (&x)[NT]) {
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            const double w = warp_max(x[k]);
+            if (lane == 0) shm[k][wid] = w;
+        }
+        __syncthreads();
+        if (wid == 0) {
+#pragma unroll
+            for (int k = 0; k < NT; ++k) x[k] = warp_max(lane < nw ? shm[k][lane] : 0.0);
+        }
+        __syncthreads();
+    };
+    block_max(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NT; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NT; ++k) {
+        double m = 0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) m = fmax(m, __ldcg(&partials[k * gridDim.x + b]));
+        tot[k] = m;
+    }
+    block_max(tot);
+    if (threadIdx.x == 0) *counter = 0u;
+    return true;
+}
+
 // Same for FP32 per-thread values: the warp-level sums stay in FP32 (off the
 // FP64 pipe); each warp's sum is widened to FP64 for the block and grid sums.
 __device__ __forceinline__ float warp_sum_f(float v) {

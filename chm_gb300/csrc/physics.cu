@@ -633,37 +633,10 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
     // ||rhs||_inf (as the bit pattern of a non-negative double, whose integer
     // order is its numeric order) and the NaN/Inf flag: last block finalises
     const double vmax = __longlong_as_double((long long)vmax_bits), vnan = bad ? 1.0 : 0.0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __shared__ double shm[2][kBlock / 32];
-    double a = warp_max(vmax), bn = warp_max(vnan);
-    if (lane == 0) {
-        shm[0][wid] = a;
-        shm[1][wid] = bn;
-    }
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        double m0 = 0, m1 = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-            m0 = fmax(m0, shm[0][k]);
-            m1 = fmax(m1, shm[1][k]);
-        }
-        partials[blockIdx.x] = m0;
-        partials[gridDim.x + blockIdx.x] = m1;
-        __threadfence();
-        last = atomicAdd(&sc->counter[0], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        double m0 = 0, m1 = 0;
-        for (int k = 0; k < (int)gridDim.x; ++k) {
-            m0 = fmax(m0, __ldcg(&partials[k]));
-            m1 = fmax(m1, __ldcg(&partials[gridDim.x + k]));
-        }
-        sc->rhs_max = m0;
-        sc->nan_flag = m1;
-        sc->counter[0] = 0u;
+    double mv[2] = {vmax, vnan}, tot[2];
+    if (block_partials_last_max<2>(mv, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rhs_max = tot[0];
+        sc->nan_flag = tot[1];
     }
 }
 
@@ -751,37 +724,10 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
         for (int m = threadIdx.x; m < Mb.n; m += blockDim.x)
             if (mb_max[m]) atomicMax(&Mb.dep_max[m], mb_max[m]);
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __shared__ double shm[2][kBlock / 32];
-    double a = warp_max(vmax), bn = warp_max(vnan);
-    if (lane == 0) {
-        shm[0][wid] = a;
-        shm[1][wid] = bn;
-    }
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        double m0 = 0, m1 = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-            m0 = fmax(m0, shm[0][k]);
-            m1 = fmax(m1, shm[1][k]);
-        }
-        partials[blockIdx.x] = m0;
-        partials[gridDim.x + blockIdx.x] = m1;
-        __threadfence();
-        last = atomicAdd(&sc->counter[0], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        double m0 = 0, m1 = 0;
-        for (int k = 0; k < (int)gridDim.x; ++k) {
-            m0 = fmax(m0, __ldcg(&partials[k]));
-            m1 = fmax(m1, __ldcg(&partials[gridDim.x + k]));
-        }
-        sc->rhs_max = m0;
-        sc->nan_flag = m1;
-        sc->counter[0] = 0u;
+    double mv[2] = {vmax, vnan}, tot[2];
+    if (block_partials_last_max<2>(mv, partials, &sc->counter[0], tot) && threadIdx.x == 0) {
+        sc->rhs_max = tot[0];
+        sc->nan_flag = tot[1];
     }
 }
 
@@ -815,34 +761,9 @@ __global__ void __launch_bounds__(kBlock) k_update(Params P, Faces G, Forcing F,
         v[2] += area * (mass - q * P.dt);
         v[3] += P.dt * rres[i];
     }
-    double w[5] = {v[0], v[1], v[2], v[3], snow};
-    __shared__ double sh[5][kBlock / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = 0; k < 5; ++k) {
-        double s = warp_sum(w[k]);
-        if (lane == 0) sh[k][wid] = s;
-    }
-    __syncthreads();
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < 5; ++k) {
-            double s = 0;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sh[k][q];
-            partials[k * gridDim.x + blockIdx.x] = s;
-        }
-        __threadfence();
-        last = atomicAdd(&sc->counter[1], 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        for (int k = 0; k < 5; ++k) {
-            double s = 0;
-            for (int q = 0; q < (int)gridDim.x; ++q) s += __ldcg(&partials[k * gridDim.x + q]);
-            ledger[k] = s;
-        }
-        sc->counter[1] = 0u;
-    }
+    double w[5] = {v[0], v[1], v[2], v[3], snow}, tot[5];
+    if (block_partials_last<5>(w, partials, &sc->counter[1], tot) && threadIdx.x == 0)
+        for (int k = 0; k < 5; ++k) ledger[k] = tot[k];
 }
 
 // The drift consumer of CHM's snow models on the device (snobal.cpp:363-387
