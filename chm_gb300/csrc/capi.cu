@@ -410,7 +410,8 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     A.fac_ib = dalloc<double>(c, R, ok);
     c.r = dalloc<double>(c, R, ok);
     if (P.mixed) {
-        A.lat32 = dalloc<float>(c, 3 * R, ok);
+        A.uz32 = dalloc<float>(c, R, ok);
+        A.l01 = dalloc<float>(c, (size_t)6 * Tp, ok);
         A.l32 = dalloc<float>(c, R, ok);
         A.ib32 = dalloc<float>(c, R, ok);
         A.up32 = dalloc<float>(c, R, ok);

@@ -174,36 +174,52 @@ struct FeatSrc {
     double dz;
 };
 
-__device__ __forceinline__ void row_features(const FeatSrc& s, int64_t i, int z, float (&f)[kFeat]) {
+// The features are BF16 inputs after standardisation, so they are formed in
+// FP32 from the FP64 system (one conversion per value; FP64 divisions and
+// log10 would cost the GB300's slow FP64 pipe ~80 instructions a row).  They
+// come in two halves, features 0-7 and 8-13, so that the fused inference can
+// give a row's halves to two threads; the training path forms both.
+__device__ __forceinline__ float feat_inv_diag(const FeatSrc& s, int64_t r) {
+    const float d = (float)s.band[r];
+    const float ad = fabsf(d) > 0.0f ? fabsf(d) : 1.0f;
+    return 1.0f / ad;
+}
+
+__device__ __forceinline__ void row_features_lo(const FeatSrc& s, int64_t i, int z, float* f) {
     const int64_t r = (int64_t)z * s.Tp + i;
-    const double d = s.band[r];
-    const double ad = fabs(d) > 0 ? fabs(d) : 1.0;
-    const double inv = 1.0 / ad;
-    const double up = s.band[5 * s.R + r], lo = s.band[4 * s.R + r];
-    double latc = 0.0;
-    double lat[3];
+    const float inv = feat_inv_diag(s, r);
+    f[0] = (z + 0.5f) / (float)s.L;
+    f[1] = log10f(fmaxf((float)s.u_z[r], 1e-3f));
+    f[2] = (float)s.csubl[r] * ((float)s.dz * 1e3f);
+    f[3] = (float)s.band[5 * s.R + r] * inv;
+    f[4] = (float)s.band[4 * s.R + r] * inv;
+    for (int j = 0; j < 3; ++j) f[5 + j] = (float)s.band[(1 + j) * s.R + r] * inv;
+}
+
+__device__ __forceinline__ void row_features_hi(const FeatSrc& s, int64_t i, int z, float* f) {
+    const int64_t r = (int64_t)z * s.Tp + i;
+    const float inv = feat_inv_diag(s, r);
+    const float up = (float)s.band[5 * s.R + r], lo = (float)s.band[4 * s.R + r];
+    float latc = 0.0f;
     for (int j = 0; j < 3; ++j) {
-        lat[j] = s.band[(1 + j) * s.R + r];
         const int32_t nb = s.nbr[j * s.Tp + i];
-        if (nb >= 0) latc += lat[j] * s.cprev[(int64_t)z * s.Tp + nb];
+        if (nb >= 0) latc += (float)s.band[(1 + j) * s.R + r] * (float)s.cprev[(int64_t)z * s.Tp + nb];
     }
-    const double above = z + 1 < s.L ? s.cprev[r + s.Tp] : 0.0;
-    const double below = z > 0 ? s.cprev[r - s.Tp] : 0.0;
-    const double d0 = fabs(s.band[i]) > 0 ? fabs(s.band[i]) : 1.0;
-    f[0] = (float)((z + 0.5) / s.L);
-    f[1] = (float)log10(fmax(s.u_z[r], 1e-3));
-    f[2] = (float)(s.csubl[r] * s.dz * 1e3);
-    f[3] = (float)(up * inv);
-    f[4] = (float)(lo * inv);
-    f[5] = (float)(lat[0] * inv);
-    f[6] = (float)(lat[1] * inv);
-    f[7] = (float)(lat[2] * inv);
-    f[8] = (float)(s.rhs[r] * inv * kCScale);
-    f[9] = (float)(s.cprev[r] * kCScale);
-    f[10] = (float)(latc * inv * kCScale);
-    f[11] = (float)(up * above * inv * kCScale);
-    f[12] = (float)(lo * below * inv * kCScale);
-    f[13] = (float)(s.rhs[i] / d0 * kCScale);
+    const float above = z + 1 < s.L ? (float)s.cprev[r + s.Tp] : 0.0f;
+    const float below = z > 0 ? (float)s.cprev[r - s.Tp] : 0.0f;
+    const float b0 = fabsf((float)s.band[i]);
+    const float d0 = b0 > 0.0f ? b0 : 1.0f;
+    f[0] = (float)s.rhs[r] * inv * kCScale;
+    f[1] = (float)s.cprev[r] * kCScale;
+    f[2] = latc * inv * kCScale;
+    f[3] = up * above * inv * kCScale;
+    f[4] = lo * below * inv * kCScale;
+    f[5] = (float)s.rhs[i] / d0 * kCScale;
+}
+
+__device__ __forceinline__ void row_features(const FeatSrc& s, int64_t i, int z, float (&f)[kFeat]) {
+    row_features_lo(s, i, z, f);
+    row_features_hi(s, i, z, f + 8);
 }
 
 // features [rows][14] (raw, un-standardised) and target [rows] = c * 1e2, rows in reference order
@@ -240,13 +256,20 @@ struct InferArgs {
 };
 
 constexpr int kInferSmem = 16384 + 32768 + 32768 + 16384 + 32768 + 1024;
+constexpr int kInferThreads = 256;
 
 // Weights -> SW128 tiles (R = 128 rows).  W0 has K = 16 (2 chunks per row).
 __device__ __forceinline__ void stage_weights(unsigned char* t, const bf16* W, int K) {
     load_tile(t, W, K, 0, 128, 0, K / 8);
 }
 
-__global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
+// 256 threads: warps w and w + 4 read the same TMEM lanes (rows 32 (w % 4)
+// ...) and split the epilogue's 128 columns between them, so each SM
+// sub-partition has two warps to interleave the epilogue's dependent chains
+// (with one, ncu showed the kernel stalled on fixed-latency waits with the
+// tensor pipe ~6% busy).  Each of a row's two threads forms half its
+// features; x0 comes from the first 128 threads.
+__global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sW0 = base;
@@ -276,7 +299,9 @@ __global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
     }
     __syncthreads();
     const uint32_t tmem = tmem_slot;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    const int row = threadIdx.x & 127, half = warp >> 2;  // this thread's tile row; column half
+    const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    __shared__ float yh[128];  // the second column half's head partial per row
     const uint32_t idesc = tc::idesc_bf16(128, kHid);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH);
     const uint32_t aW0 = tc::smem_u32(sW0), aW1 = tc::smem_u32(sW1), aW2 = tc::smem_u32(sW2);
@@ -285,7 +310,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
     uint32_t phase = 0;
     bool ok = true;
     for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int64_t q = tile * 128 + threadIdx.x;  // reference-order row of this thread
+        const int64_t q = tile * 128 + row;  // reference-order row of this thread
         const bool valid = q < rows;
         int z = 0;
         int64_t i = 0;
@@ -293,19 +318,24 @@ __global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
             z = (int)(q / a.T);
             i = q - (int64_t)z * a.T;
         }
-        // features -> standardised -> bf16 -> X row (16 columns, 2 chunks)
+        // features -> standardised -> bf16 -> X row: this thread's half of
+        // the 16 columns (features 0-7, or 8-13 and two zero pads), one chunk
         {
-            float f[kFeat];
-            if (valid) row_features(a.src, i, z, f);
-            __align__(16) bf16 xb[16];
-            for (int k = 0; k < 16; ++k) {
+            float f[8];
+            if (valid) {
+                if (half == 0)
+                    row_features_lo(a.src, i, z, f);
+                else
+                    row_features_hi(a.src, i, z, f);
+            }
+            __align__(16) bf16 xb[8];
+            for (int k = 0; k < 8; ++k) {
+                const int col = half * 8 + k;
                 float v = 0.0f;
-                if (valid && k < kFeat) v = (f[k] - a.fmean[k]) * a.fscale[k];
+                if (valid && col < kFeat) v = (f[k] - a.fmean[col]) * a.fscale[col];
                 xb[k] = __float2bfloat16_rn(v);
             }
-            const uint4* xs = reinterpret_cast<const uint4*>(xb);
-            *reinterpret_cast<uint4*>(sX + tc::sw128_chunk(threadIdx.x, 0, 128)) = xs[0];
-            *reinterpret_cast<uint4*>(sX + tc::sw128_chunk(threadIdx.x, 1, 128)) = xs[1];
+            *reinterpret_cast<uint4*>(sX + tc::sw128_chunk(row, half, 128)) = *reinterpret_cast<const uint4*>(xb);
         }
         float y = 0.0f;
         for (int layer = 0; layer < 3 && ok; ++layer) {
@@ -334,9 +364,10 @@ __global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
             }
             phase ^= 1u;
             tc::fence_after_sync();
-            // epilogue: bias + ReLU; layers 0, 1 -> H (bf16); layer 2 -> head dot
+            // epilogue, this thread's column half: bias + ReLU; layers 0, 1 -> H
+            // (bf16); layer 2 -> head dot
 #pragma unroll 1
-            for (int c0 = 0; c0 < kHid; c0 += 32) {
+            for (int c0 = half * (kHid / 2); c0 < (half + 1) * (kHid / 2); c0 += 32) {
                 float v[32];
                 tc::tmem_ld32(lane_addr + (uint32_t)c0, v);
                 if (layer < 2) {
@@ -346,16 +377,19 @@ __global__ void __launch_bounds__(128) k_mlp_infer(InferArgs a) {
                     const uint4* hs = reinterpret_cast<const uint4*>(hb);
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc)
-                        *reinterpret_cast<uint4*>(sH + tc::sw128_chunk(threadIdx.x, c0 / 8 + cc, 128)) = hs[cc];
+                        *reinterpret_cast<uint4*>(sH + tc::sw128_chunk(row, c0 / 8 + cc, 128)) = hs[cc];
                 } else {
 #pragma unroll
                     for (int j = 0; j < 32; ++j) y += fmaxf(v[j] + sb[2][c0 + j], 0.0f) * sw3[c0 + j];
                 }
             }
         }
-        if (ok && valid) {
+        // head: the first half's partial plus the second's, in that order
+        if (half == 1) yh[row] = y;
+        __syncthreads();
+        if (ok && valid && half == 0) {
             const int64_t r = (int64_t)z * a.src.Tp + i;
-            a.x0[r] = a.src.cprev[r] + (double)((y + a.b3) / kCScale);
+            a.x0[r] = a.src.cprev[r] + (double)((y + yh[row] + a.b3) / kCScale);
         }
     }
     tc::fence_before_sync();
@@ -628,7 +662,7 @@ int launch_mlp_infer(Ctx& c, cudaStream_t s, double* x0) {
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, sms));
     PBSM_CUDA_TRY(cudaMemsetAsync(&c.gbar->err, 0, sizeof(int), s));
     prof_begin(c, s);
-    k_mlp_infer<<<grid, 128, kInferSmem, s>>>(a);
+    k_mlp_infer<<<grid, kInferThreads, kInferSmem, s>>>(a);
     // per row: 14 feature inputs (~12 doubles read) + x0 written; weights once per CTA
     prof_end(c, s, PBSM3D_K_MLP, c.P.T * c.P.L * (12 * 8 + 8));
     PBSM_CUDA_TRY(cudaGetLastError());

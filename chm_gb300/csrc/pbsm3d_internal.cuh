@@ -179,8 +179,10 @@ struct Susp {
     double* csubl;    // [R]
     double* fac_l;    // [R]
     double* fac_ib;   // [R]
-    // MIXED: FP32 copies of the lateral bands and the column factors
-    float* lat32;     // [3][R]
+    // MIXED: the FP32 operator.  Its lateral bands are not stored: a row's
+    // lat_f = u_z L1_f + L0_f comes from its u_z and its face's constants
+    float* uz32;      // [R] u_z
+    float* l01;       // [6][Tp] L0_0..2, L1_0..2 of each face
     float* l32;       // [R]
     float* ib32;      // [R]
     float* up32;      // [R]

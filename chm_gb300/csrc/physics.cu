@@ -430,7 +430,9 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
                 A.fac_l[r] = 0.0;
                 A.fac_ib[r] = 1.0;
                 if (P.mixed) {
-                    for (int k = 0; k < 3; ++k) A.lat32[k * R + r] = 0.f;
+                    A.uz32[r] = 0.f;
+                    if (z == 0)
+                        for (int k = 0; k < 6; ++k) A.l01[k * Tp + i] = 0.f;
                     A.l32[r] = 0.f;
                     A.ib32[r] = 1.f;
                     A.up32[r] = 0.f;
@@ -489,6 +491,12 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             L0[f] = has ? al[f] : 0.0;
             L1[f] = (has && !out_f[f]) ? -Ak[f] : 0.0;
         }
+        if (P.mixed)
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                A.l01[f * Tp + i] = f32_rn(L0[f]);
+                A.l01[(3 + f) * Tp + i] = f32_rn(L1[f]);
+            }
         const double ust_dc = P.snow_diffusion_const * ustar;
         // Per-face versions of the per-row branch tests (no FP64 compare per
         // row): the canopy test cz < height_diff can only hold when
@@ -608,9 +616,7 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
                 prev_ib32 = ib32;
             }
             if (P.mixed) {
-                A.lat32[r] = f32_rn(lat[0]);
-                A.lat32[R + r] = f32_rn(lat[1]);
-                A.lat32[2 * R + r] = f32_rn(lat[2]);
+                A.uz32[r] = f32_rn(u_z);
                 A.l32[r] = l32;
                 A.ib32[r] = ib32;
                 A.up32[r] = up32;

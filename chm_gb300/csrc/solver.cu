@@ -73,13 +73,60 @@ namespace {
 
 template <typename V>
 struct Op {
-    const V* lat;    // [3][R]
+    const V* lat;    // [3][R] lateral bands (FP64; null in FP32)
     const V* l;      // [R] forward multipliers
     const V* ib;     // [R] inverse pivots
     const V* up;     // [R] above band
     const int32_t* nbr;  // [3][Tp]
     int64_t Tp, R;
     int L;
+    const float* uz;   // FP32: [R] u_z of each row
+    const float* l01;  // FP32: [6][Tp] L0_f, L1_f of each face
+};
+
+// Values a row, and bytes a face, of the lateral couplings (traffic counts).
+template <typename V>
+constexpr int64_t kLatRow = sizeof(V) == 4 ? 1 : 3;
+template <typename V>
+constexpr int64_t kLatFace = sizeof(V) == 4 ? 24 : 0;
+
+// The lateral couplings of one face's rows.  FP64 reads the stored bands.
+// FP32 recomputes lat_f = u_z L1_f + L0_f from the row's u_z and the face's
+// six constants (loaded once per column): 4 bytes a row instead of 12.
+template <typename V>
+struct LatFace;
+template <>
+struct LatFace<double> {
+    const double* lat;
+    int64_t R;
+    // a row's bands, each loaded where it is used
+    struct Row {
+        const double* p;
+        int64_t R;
+        __device__ __forceinline__ double operator[](int j) const { return p[j * R]; }
+    };
+    __device__ __forceinline__ LatFace(const Op<double>& op, int64_t) : lat(op.lat), R(op.R) {}
+    __device__ __forceinline__ Row row(int64_t k) const { return Row{lat + k, R}; }
+};
+template <>
+struct LatFace<float> {
+    const float* uz;
+    float a0, a1, a2, b0, b1, b2;  // L0_f, L1_f
+    struct Row {
+        float u, a0, a1, a2, b0, b1, b2;
+        __device__ __forceinline__ float operator[](int j) const {
+            return j == 0 ? fmaf(u, b0, a0) : j == 1 ? fmaf(u, b1, a1) : fmaf(u, b2, a2);
+        }
+    };
+    __device__ __forceinline__ LatFace(const Op<float>& op, int64_t i) : uz(op.uz) {
+        a0 = op.l01[i];
+        a1 = op.l01[op.Tp + i];
+        a2 = op.l01[2 * op.Tp + i];
+        b0 = op.l01[3 * op.Tp + i];
+        b1 = op.l01[4 * op.Tp + i];
+        b2 = op.l01[5 * op.Tp + i];
+    }
+    __device__ __forceinline__ Row row(int64_t k) const { return Row{uz[k], a0, a1, a2, b0, b1, b2}; }
 };
 
 enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3 };
@@ -250,7 +297,7 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* 
 // from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
 // so the lateral kernels that follow take w in place of u.
 template <typename V, bool WRITE_W>
-__global__ void __launch_bounds__(kBlock, (sizeof(V) == 4 && !WRITE_W) ? 8 : 6) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
+__global__ void __launch_bounds__(kBlock, 6) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
                                                      const V* __restrict__ zin, V* __restrict__ w,
                                                      V* __restrict__ zout, const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
@@ -262,14 +309,18 @@ __global__ void __launch_bounds__(kBlock, (sizeof(V) == 4 && !WRITE_W) ? 8 : 6) 
         const int64_t i = tl.start[t] + threadIdx.x;
         if (i >= tl.start[t + 1]) continue;
         const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+        // FP32: the face's six coupling constants stay in registers over the
+        // column (40 a thread with four layers in flight, no spills)
+        const LatFace<V> lf(op, i);
 #pragma unroll 4
         for (int z = 0; z < op.L; ++z) {
             const int64_t base = (int64_t)z * op.Tp;
             const int64_t k = base + i;
+            const auto la = lf.row(k);
             V wk = u[k];
-            if (n0 >= 0) wk -= op.lat[k] * zin[base + n0];
-            if (n1 >= 0) wk -= op.lat[op.R + k] * zin[base + n1];
-            if (n2 >= 0) wk -= op.lat[2 * op.R + k] * zin[base + n2];
+            if (n0 >= 0) wk -= la[0] * zin[base + n0];
+            if (n1 >= 0) wk -= la[1] * zin[base + n1];
+            if (n2 >= 0) wk -= la[2] * zin[base + n2];
             if (WRITE_W) w[k] = wk;  // only the last step's w is read (by the lateral kernel)
             g[z * blockDim.x + threadIdx.x] = wk;
         }
@@ -283,15 +334,17 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const 
                                               const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
                                               V (&acc)[2]) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+    const LatFace<V> lf(op, i);
     // layers are independent here: unrolled so their loads overlap
 #pragma unroll 4
     for (int z = 0; z < op.L; ++z) {
         const int64_t base = (int64_t)z * op.Tp;
         const int64_t k = base + i;
+        const auto la = lf.row(k);
         V yk = u[k];
-        if (n0 >= 0) yk += op.lat[k] * zz[base + n0];
-        if (n1 >= 0) yk += op.lat[op.R + k] * zz[base + n1];
-        if (n2 >= 0) yk += op.lat[2 * op.R + k] * zz[base + n2];
+        if (n0 >= 0) yk += la[0] * zz[base + n0];
+        if (n1 >= 0) yk += la[1] * zz[base + n1];
+        if (n2 >= 0) yk += la[2] * zz[base + n2];
         y[k] = yk;
         acc[0] += a[k] * yk;
         if (NT > 1) acc[1] += yk * yk;
@@ -1040,11 +1093,12 @@ template <typename V>
 Op<V> make_op(Ctx& c);
 template <>
 Op<double> make_op<double>(Ctx& c) {
-    return Op<double>{c.A.band + c.P.R, c.A.fac_l, c.A.fac_ib, c.A.band + 5 * c.P.R, c.F.nbr, c.P.Tp, c.P.R, c.P.L};
+    return Op<double>{c.A.band + c.P.R, c.A.fac_l, c.A.fac_ib, c.A.band + 5 * c.P.R, c.F.nbr, c.P.Tp, c.P.R, c.P.L,
+                      nullptr, nullptr};
 }
 template <>
 Op<float> make_op<float>(Ctx& c) {
-    return Op<float>{c.A.lat32, c.A.l32, c.A.ib32, c.A.up32, c.F.nbr, c.P.Tp, c.P.R, c.P.L};
+    return Op<float>{nullptr, c.A.l32, c.A.ib32, c.A.up32, c.F.nbr, c.P.Tp, c.P.R, c.P.L, c.A.uz32, c.A.l01};
 }
 
 int read_scalars(Ctx& c, cudaStream_t s, Scalars* dev) {
@@ -1116,7 +1170,12 @@ const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl
             k_bicg_neu<V, true><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
         else
             k_bicg_neu<V, false><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
-        if (prof) prof_end(c, s, PBSM3D_K_NEUMANN, rows * (last ? 10 : 9) * sizeof(V) + rows / c.P.L * 12);
+        // per row u, z in, z out, the lateral couplings (3 bands, or u_z in
+        // FP32), 3 column factors, w on the last step; per face the ids (and
+        // the FP32 couplings' 6 constants)
+        if (prof)
+            prof_end(c, s, PBSM3D_K_NEUMANN,
+                     rows * ((last ? 7 : 6) + kLatRow<V>) * sizeof(V) + rows / c.P.L * (12 + kLatFace<V>));
         std::swap(a, b);
     }
     return K > 0 ? w : u;
@@ -1175,14 +1234,14 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             const V* up = launch_neumann<V>(c, s, op, tl, gc, smem, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
-            prof_end(c, s, PBSM3D_K_BICG_V, rows * 7 * sv_ + act * 12);
+            prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
             k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, neumann_first(c, zs, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
             const V* us = launch_neumann<V>(c, s, op, tl, gc, smem, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
-            prof_end(c, s, PBSM3D_K_BICG_T, rows * 6 * sv_ + act * 12);
+            prof_end(c, s, PBSM3D_K_BICG_T, rows * (3 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
             k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
