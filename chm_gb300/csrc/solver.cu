@@ -2438,9 +2438,13 @@ int capture_scg(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& 
     CondBody loop;
     if (loop.begin(s, G.cap[depth + 1], h.h[H_DLOOP], cudaGraphCondTypeWhile)) return 1;
     cudaStream_t t = G.cap[depth + 1];
-    k_scg_x<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
-    k_scg_q<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
-    k_ctl_inner<<<1, kBlock, 0, t>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_DLOOP, 3, h);
+    // two CG iterations per pass of the loop body, one controller: a member
+    // that stops in the first is skipped by the second (its scalars say done)
+    for (int k = 0; k < 2; ++k) {
+        k_scg_x<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+        k_scg_q<V><<<g, kBlock, 0, t>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
+    }
+    k_ctl_inner<<<1, kBlock, 0, t>>>(G.ctl, ms, sc, tl, c.act_buf, G.nact, H_DLOOP, 5, h);
     return loop.end();
 }
 
