@@ -865,7 +865,8 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     const int64_t T = c.P.T, rows = T * c.P.L;
     // the three passes count as one assembly; the algorithmic bytes are those
     // of the whole step: per face 8 forcing + 133 B geometry in, Qsalt + flag
-    // out; per row 12 doubles out (+6 floats MIXED)
+    // out (+6 floats of coupling constants MIXED); per row 10 doubles out, 2
+    // more with the FP64 column factors, 4 floats MIXED
     prof_begin(c, s);
     cudaMemsetAsync(c.A.n_slow, 0, sizeof(int), s);
     // the wind inputs on the device (scale_wind_vert, fetchr), when asked for
@@ -875,7 +876,9 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     k_salt_faces<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
     k_salt_rows<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Fo, c.A, c.Mb);
     k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
-    prof_end(c, s, PBSM3D_K_ASSEMBLE, T * (64 + 133 + 9) + rows * (96 + (c.P.mixed ? 24 : 0)));
+    prof_end(c, s, PBSM3D_K_ASSEMBLE,
+             T * (64 + 133 + 9 + (c.P.mixed ? 24 : 0)) +
+                 rows * (80 + (c.P.fac64 ? 16 : 0) + (c.P.mixed ? 16 : 0)));
     c.launches += c.asm_kernels;
 }
 
