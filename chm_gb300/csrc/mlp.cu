@@ -255,37 +255,49 @@ struct InferArgs {
     int* err;
 };
 
-constexpr int kInferSmem = 16384 + 32768 + 32768 + 16384 + 32768 + 1024;
-constexpr int kInferThreads = 256;
+constexpr int kGroups = 2, kGroupThreads = 256, kInferThreads = kGroups * kGroupThreads;
+// the weights, then each group's X (128 x 16, 128-byte rows) and H (128 x 128)
+constexpr int kInferSmem = 16384 + 32768 + 32768 + kGroups * (16384 + 32768) + 1024;
 
 // Weights -> SW128 tiles (R = 128 rows).  W0 has K = 16 (2 chunks per row).
 __device__ __forceinline__ void stage_weights(unsigned char* t, const bf16* W, int K) {
     load_tile(t, W, K, 0, 128, 0, K / 8);
 }
 
-// 256 threads: warps w and w + 4 read the same TMEM lanes (rows 32 (w % 4)
-// ...) and split the epilogue's 128 columns between them, so each SM
-// sub-partition has two warps to interleave the epilogue's dependent chains
-// (with one, ncu showed the kernel stalled on fixed-latency waits with the
-// tensor pipe ~6% busy).  Each of a row's two threads forms half its
-// features; x0 comes from the first 128 threads.
+// Two groups of 256 threads, each with its own 128-row tile in flight: its
+// own X and H buffers in shared memory, its own 128 TMEM columns, mbarrier and
+// named barrier, the weights shared.  While one group forms features or runs
+// its epilogue on the CUDA cores, the other's MMAs can run.  Within a group,
+// warps w and w + 4 read the same TMEM lanes (rows 32 (w % 4) ...): each of a
+// row's two threads forms half its features and takes half the epilogue's 128
+// columns.  (One 128-thread tile at a time stalled on fixed-latency waits with
+// the tensor pipe ~6% busy.)
+__device__ __forceinline__ void group_sync(int grp) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(kGroupThreads) : "memory");
+}
+
 __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sW0 = base;
     unsigned char* sW1 = sW0 + 16384;
     unsigned char* sW2 = sW1 + 32768;
-    unsigned char* sX = sW2 + 32768;
-    unsigned char* sH = sX + 16384;
-    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ __align__(8) unsigned long long mbar[kGroups];
     __shared__ uint32_t tmem_slot;
     __shared__ float sb[3][kHid];
     __shared__ float sw3[kHid];
+    __shared__ float yh[kGroups][128];  // the second column half's head partial per row
+    __shared__ int s_ok[kGroups];
     const int warp = threadIdx.x >> 5;
-    const uint32_t mb = tc::smem_u32(&mbar);
-    if (threadIdx.x == 0) tc::mbar_init(mb, 1);
+    const int grp = threadIdx.x / kGroupThreads, gt = threadIdx.x % kGroupThreads, gwarp = gt >> 5;
+    const int row = gt & 127, half = gwarp >> 2;  // this thread's tile row; column half
+    unsigned char* sX = sW2 + 32768 + grp * (16384 + 32768);
+    unsigned char* sH = sX + 16384;
+    const uint32_t mb = tc::smem_u32(&mbar[grp]);
+    if (threadIdx.x == 0)
+        for (int g = 0; g < kGroups; ++g) tc::mbar_init(tc::smem_u32(&mbar[g]), 1);
     if (warp == 0) {
-        tc::tmem_alloc(tc::smem_u32(&tmem_slot), 128);
+        tc::tmem_alloc(tc::smem_u32(&tmem_slot), 128 * kGroups);
         tc::tmem_relinquish();
     }
     stage_weights(sW0, a.W0, 16);
@@ -298,10 +310,8 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
         sw3[k] = a.w3[k];
     }
     __syncthreads();
-    const uint32_t tmem = tmem_slot;
-    const int row = threadIdx.x & 127, half = warp >> 2;  // this thread's tile row; column half
+    const uint32_t tmem = tmem_slot + (uint32_t)(grp * 128);  // this group's columns
     const uint32_t lane_addr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    __shared__ float yh[128];  // the second column half's head partial per row
     const uint32_t idesc = tc::idesc_bf16(128, kHid);
     const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH);
     const uint32_t aW0 = tc::smem_u32(sW0), aW1 = tc::smem_u32(sW1), aW2 = tc::smem_u32(sW2);
@@ -309,7 +319,8 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
     const int64_t ntiles = (rows + 127) / 128;
     uint32_t phase = 0;
     bool ok = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    for (int64_t tile = (int64_t)blockIdx.x * kGroups + grp; tile < ntiles && ok;
+         tile += (int64_t)gridDim.x * kGroups) {
         const int64_t q = tile * 128 + row;  // reference-order row of this thread
         const bool valid = q < rows;
         int z = 0;
@@ -341,8 +352,8 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
         for (int layer = 0; layer < 3 && ok; ++layer) {
             tc::fence_proxy_async();
             tc::fence_before_sync();
-            __syncthreads();
-            if (threadIdx.x == 0) {
+            group_sync(grp);
+            if (gt == 0) {
                 tc::fence_after_sync();
                 if (layer == 0) {
                     tc::mma_bf16(tmem, tc::desc_kstep(aX, 0, 128), tc::desc_kstep(aW0, 0, 128), idesc, 0u);
@@ -356,9 +367,15 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
             }
             __syncwarp();
             const bool waited = tc::mbar_wait(mb, phase, kMmaWaitNs);
-            ok = __syncthreads_and(waited) != 0;  // uniform across the CTA
+            // uniform across the group: every thread leaves together on a timeout
+            if (gt == 0) s_ok[grp] = 1;
+            group_sync(grp);
+            if (!waited) s_ok[grp] = 0;
+            group_sync(grp);
+            ok = s_ok[grp] != 0;
+            group_sync(grp);
             if (!ok) {
-                if (threadIdx.x == 0) atomicExch(a.err, 1);
+                if (gt == 0) atomicExch(a.err, 1);
                 tc::mbar_wait(mb, phase, kMmaWaitNs);
                 break;
             }
@@ -385,16 +402,16 @@ __global__ void __launch_bounds__(kInferThreads) k_mlp_infer(InferArgs a) {
             }
         }
         // head: the first half's partial plus the second's, in that order
-        if (half == 1) yh[row] = y;
-        __syncthreads();
+        if (half == 1) yh[grp][row] = y;
+        group_sync(grp);
         if (ok && valid && half == 0) {
             const int64_t r = (int64_t)z * a.src.Tp + i;
-            a.x0[r] = a.src.cprev[r] + (double)((y + yh[row] + a.b3) / kCScale);
+            a.x0[r] = a.src.cprev[r] + (double)((y + yh[grp][row] + a.b3) / kCScale);
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+    if (warp == 0) tc::tmem_dealloc(tmem_slot, 128 * kGroups);
 }
 
 // ---------------------------------------------------------------- training kernels
@@ -659,7 +676,7 @@ int launch_mlp_infer(Ctx& c, cudaStream_t s, double* x0) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t tiles = (c.P.T * c.P.L + 127) / 128;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, sms));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + kGroups - 1) / kGroups, sms));
     PBSM_CUDA_TRY(cudaMemsetAsync(&c.gbar->err, 0, sizeof(int), s));
     prof_begin(c, s);
     k_mlp_infer<<<grid, kInferThreads, kInferSmem, s>>>(a);
