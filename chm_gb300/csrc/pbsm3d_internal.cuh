@@ -333,6 +333,10 @@ struct Ctx {
     std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
     int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
+    // co-resident blocks per SM of the polynomial-preconditioner step over
+    // those of the column kernels: its grid is the column kernels' scaled so
+    // that it too is one wave (no second, partial wave)
+    double neu_scale[2] = {1.0, 1.0};
     // autotuner (cfg.autotune): one-wave grids, the candidate being timed,
     // per-iteration times of the candidates; tuned = a choice is in force
     int wave_col[2] = {1, 1}, wave_red[2] = {1, 1};

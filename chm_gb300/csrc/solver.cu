@@ -1163,6 +1163,9 @@ const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl
     const int K = c.cfg.neumann;
     V* a = (K & 1) ? ztmp : zfinal;
     V* b = (K & 1) ? zfinal : ztmp;
+    // the column kernels' grid gc (a wave of theirs, or the tuned multiple)
+    // scaled to this kernel's residency
+    gc = std::max(1, std::min(gc, (int)(gc * c.neu_scale[sizeof(V) == 4] + 0.5)));
     for (int j = 0; j < K; ++j) {
         const bool last = j == K - 1;
         if (prof) prof_begin(c, s);
@@ -1330,6 +1333,12 @@ int configure_solver_kernels(Ctx& c) {
     if ((rc = wave((const void*)k_bicg_p<float>, s32, c.grid_col[1]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
+    {
+        int gn[2];
+        if ((rc = wave((const void*)k_bicg_neu<double, false>, s64, gn[0]))) return rc;
+        if ((rc = wave((const void*)k_bicg_neu<float, false>, s32, gn[1]))) return rc;
+        for (int k = 0; k < 2; ++k) c.neu_scale[k] = std::min(1.0, (double)gn[k] / (double)c.grid_col[k]);
+    }
     for (int k = 0; k < 2; ++k) {
         c.wave_col[k] = c.grid_col[k];
         c.wave_red[k] = c.grid_red[k];
