@@ -333,6 +333,7 @@ struct Ctx {
     std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
     int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
+    int grid_cg[2] = {1, 1};   // the tile CG's kernels (k_scg_x, k_scg_q): one wave
     // co-resident blocks per SM of the polynomial-preconditioner step over
     // those of the column kernels: its grid is the column kernels' scaled so
     // that it too is one wave (no second, partial wave)

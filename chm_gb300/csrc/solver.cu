@@ -921,7 +921,7 @@ __global__ void __launch_bounds__(kBlock) k_scg_start(Tiles tl, int64_t Tp, DepS
 
 // q = A z + beta q, p = z + beta p; alpha = rho / (p, q)
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_scg_q(Tiles tl, int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
+__global__ void __launch_bounds__(kBlock, 6) k_scg_q(Tiles tl, int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
                                                   MScal* ms, Scalars* sc, double* part) {
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
@@ -1334,6 +1334,15 @@ int configure_solver_kernels(Ctx& c) {
     if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
     {
+        // the tile CG: one wave of its two per-iteration kernels
+        int gx[2], gq[2];
+        if ((rc = wave((const void*)k_scg_x<double>, 0, gx[0]))) return rc;
+        if ((rc = wave((const void*)k_scg_x<float>, 0, gx[1]))) return rc;
+        if ((rc = wave((const void*)k_scg_q<double>, 0, gq[0]))) return rc;
+        if ((rc = wave((const void*)k_scg_q<float>, 0, gq[1]))) return rc;
+        for (int k = 0; k < 2; ++k) c.grid_cg[k] = std::min(gx[k], gq[k]);
+    }
+    {
         int gn[2];
         if ((rc = wave((const void*)k_bicg_neu<double, false>, s64, gn[0]))) return rc;
         if ((rc = wave((const void*)k_bicg_neu<float, false>, s32, gn[1]))) return rc;
@@ -1665,7 +1674,7 @@ static int scg_iterations(Ctx& c, cudaStream_t s, DepSys<V> D, MScal* ms, Scalar
     int rc = set_active(c, s, active);
     if (rc) return rc;
     Tiles tl = c.tiles;
-    int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+    int g = std::max(1, std::min(c.grid_cg[sizeof(V) == 4], tl.nact));
     int64_t act = active_faces(c);
     prof_begin(c, s);
     k_scg_start<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
@@ -1697,7 +1706,7 @@ static int scg_iterations(Ctx& c, cudaStream_t s, DepSys<V> D, MScal* ms, Scalar
         if (changed) {
             if ((rc = set_active(c, s, active))) return rc;
             tl = c.tiles;
-            g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+            g = std::max(1, std::min(c.grid_cg[sizeof(V) == 4], tl.nact));
             act = active_faces(c);
         }
         chunk = std::min(32, chunk * 2);
@@ -2440,7 +2449,7 @@ template <typename V>
 int capture_scg(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& tl, DepSys<V> D, MScal* ms,
                 Scalars* sc) {
     cudaStream_t s = G.cap[depth];
-    const int g = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
+    const int g = std::max(1, std::min(c.grid_cg[sizeof(V) == 4], tl.ntiles));
     double* part = c.tile_part;
     k_scg_start<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
     k_scg_q<V><<<g, kBlock, 0, s>>>(tl, c.P.Tp, D, c.F.nbr, ms, sc, part);
