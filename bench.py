@@ -617,7 +617,7 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg2", choices=sorted(synth.CONFIGS))
+    ap.add_argument("--config", default="tri1m", choices=sorted(synth.CONFIGS))
     ap.add_argument("--variants", default="plain_fp64,mixed,previous,learned,graph_previous,plain_fp64_neumann5,"
                                           "previous_neumann5,graph_previous_neumann5,graph_learned_neumann5",
                     help="comma list of %s; the fastest meeting residual 1e-8 is the headline" % ",".join(VARIANTS))

@@ -277,13 +277,13 @@ def consume_drift(swe, depth, drift_mass, drift_density: float = 300.0):
 # Named configurations of the measurement plan.
 CONFIGS = {
     # ~8.1k faces in a 5 km square, 5 layers (CPU reference case)
-    "cfg1": dict(n_points=4096, side=5000.0, nLayer=5),
+    "tri8k": dict(n_points=4096, side=5000.0, nLayer=5),
     # ~1.05M faces in a 70 km square, 10 layers
-    "cfg2": dict(n_points=524288, side=70000.0, nLayer=10),
+    "tri1m": dict(n_points=524288, side=70000.0, nLayer=10),
     # the same point density at a quarter of the size (~262k faces), for
     # profiler captures that must stay small
-    "cfg2q": dict(n_points=131072, side=35000.0, nLayer=10),
+    "tri262k": dict(n_points=131072, side=35000.0, nLayer=10),
     # the learned-warm-start configuration's size: ~4.2M faces at the same
     # point density, 10 layers
-    "cfg5": dict(n_points=2097152, side=140000.0, nLayer=10),
+    "tri4m": dict(n_points=2097152, side=140000.0, nLayer=10),
 }

@@ -21,7 +21,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(warmstart.WEIGHTS_FILE))
     ap.add_argument("--seeds", default="1001,1002,1003")
-    ap.add_argument("--config", default="cfg2q")
+    ap.add_argument("--config", default="tri262k")
     ap.add_argument("--steps-per-seed", type=int, default=8)
     ap.add_argument("--rows-per-step", type=int, default=250000)
     ap.add_argument("--train-steps", type=int, default=3000)

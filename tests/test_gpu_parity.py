@@ -300,7 +300,7 @@ def test_full_size_properties(cuda_lib):
     """1M faces x 10 layers: FP64 residual recomputed on the host from the
     exported system, the mass ledger, non-negative clamped concentrations."""
     import scipy.sparse as sp
-    cfg = synth.CONFIGS["cfg2"]
+    cfg = synth.CONFIGS["tri1m"]
     w = synth.Workload(cfg["n_points"], cfg["side"], seed=1)
     m = gpu_module(w.mesh, 10)
     out = m.run(w.forcing(0), 3600.0, want_c=True)
