@@ -492,7 +492,12 @@ def run_ensemble(args, dist: Dist, rank: int, world: int, local_rank: int, membe
     faces_total = dist.sum(float(T * args.steps))
     head = min(results, key=lambda k: results[k]["t_max"])
     ctx = ctxs[head]
-    # e2e through the C ABI with pinned host forcing and host outputs
+    # e2e through the C ABI with pinned host forcing and host outputs, the
+    # head form's context alone on the GPU (as a user runs it: with the other
+    # forms' contexts still resident, ~27 GB each, the host transfers ran ~30%
+    # slower per step)
+    for k in [k for k in ctxs if k != head]:
+        lib.pbsm3d_destroy(ctxs.pop(k))
     del dev_forcing, fdescs
     torch.cuda.empty_cache()
     pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in forcing_at(s).items()}
