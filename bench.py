@@ -275,7 +275,10 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     t_dev = results[head]["t_dev"]
     stats = results[head]["stats"]
 
-    # ---- e2e (headline form): host pinned forcing in, host outputs back, copies timed
+    # ---- e2e (headline form): host pinned forcing in, host outputs back, copies
+    # timed, the head form's context alone on the GPU (as a user runs it)
+    for k in [k for k in ctxs if k != head]:
+        lib.pbsm3d_destroy(ctxs.pop(k))
     pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in fs.items()} for fs in host_forcing]
     pin_out = {k: torch.empty(T, dtype=torch.float64).pin_memory() for k in out_names}
     o_host = capi.Outputs()
