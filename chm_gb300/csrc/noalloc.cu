@@ -14,9 +14,16 @@
 //
 // Its address is looked up with cudaGetSymbolAddress once per device, by the
 // first call made with that device current, and cached; make that first call
-// before any stream capture.  All calls share the one array: calls that
-// overlap on a device (other host threads, other streams) race on it.  Each
-// call clears the part that must start at zero (the reduction counters).
+// before any stream capture.  The cache remembers the device context it was
+// taken in (cuCtxGetId, reached through cudaGetDriverEntryPointByVersion, so
+// the library needs no link to the driver library): after a cudaDeviceReset
+// the next call looks the address up again in the new context.  Where the
+// driver has no context ids the address is kept for the process, and the
+// device must not be reset after the first call.  All calls share the one
+// array: calls that overlap on a device (other host threads, other streams)
+// race on it.  Each call clears the part that must start at zero (the
+// reduction counters).
+#include <cuda.h>
 #include <math.h>
 
 #include <algorithm>
@@ -162,7 +169,39 @@ __global__ void __launch_bounds__(kBlock) k_na_resid(DepIn D, NaView W) {
 }
 
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_dev[64] = {};
+struct ScratchAddr {
+    unsigned char* ptr = nullptr;
+    unsigned long long ctx_id = 0;  // context the address was taken in (0: unknown)
+};
+ScratchAddr g_scratch_dev[64];
+
+// The id of the current device context, 0 when there is none or the driver
+// cannot say.  *known tells whether the driver offers context ids at all.
+unsigned long long current_context_id(bool* known) {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess && f1 && f2) {
+            get_current = reinterpret_cast<GetCurrent>(f1);
+            get_id = reinterpret_cast<GetId>(f2);
+        }
+        resolved = true;
+    }
+    *known = get_current != nullptr;
+    if (!get_current) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 // failure messages go where pbsm3d_last_error(NULL) reads them
 struct NoallocError {
@@ -201,19 +240,24 @@ extern "C" int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* n
     }
     unsigned char* base = nullptr;
     {
-        // once per device, with that device current: the device address of
-        // the scratch array (its name in host code is only a stand-in)
+        // once per device (and again after a reset of it), with that device
+        // current: the device address of the scratch array (its name in host
+        // code is only a stand-in)
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_dev[dev]) {
+        bool ids = false;
+        const unsigned long long ctx = current_context_id(&ids);
+        ScratchAddr& a = g_scratch_dev[dev];
+        if (!a.ptr || (ids && (ctx == 0 || ctx != a.ctx_id))) {
             void* ptr = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
             if (e != cudaSuccess || !ptr) {
                 g_noalloc_error = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
                 return PBSM3D_ERR_CUDA;
             }
-            g_scratch_dev[dev] = static_cast<unsigned char*>(ptr);
+            a.ptr = static_cast<unsigned char*>(ptr);
+            a.ctx_id = current_context_id(&ids);
         }
-        base = g_scratch_dev[dev];
+        base = a.ptr;
     }
     NaView W = view_of(base);
     DepIn D{n_faces, neighbor, diag, off, rhs, x};
@@ -224,15 +268,31 @@ extern "C" int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* n
         g_noalloc_error = "cudaMemsetAsync failed";
         return PBSM3D_ERR_CUDA;
     }
+    auto launch_failed = [](const char* what) {
+        const cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) return false;
+        g_noalloc_error = std::string(what) + ": " + cudaGetErrorString(e);
+        return true;
+    };
     k_na_init<<<grid, kBlock, 0, s>>>(D, W, tol, maxit);
+    if (launch_failed("launch of the solver's first kernel")) return PBSM3D_ERR_CUDA;
     Scalars h{};
     int it_done = 0;
-    while (true) {
+    // Each batch runs 8 iterations and the device stops itself at maxit, so
+    // a solve whose kernels run reports done within maxit / 8 + 1 batches;
+    // a state that stops advancing is a CUDA failure, never an endless poll.
+    const int64_t max_polls = (int64_t)maxit / 8 + 2;
+    for (int64_t poll = 0;; ++poll) {
+        if (poll >= max_polls) {
+            g_noalloc_error = "deposition solver state did not advance (kernels did not run)";
+            return PBSM3D_ERR_CUDA;
+        }
         for (int k = 0; k < 8; ++k) {
             k_na_q<<<grid, kBlock, 0, s>>>(D, W);
             k_na_x<<<grid, kBlock, 0, s>>>(D, W);
             k_na_p<<<grid, kBlock, 0, s>>>(D, W);
         }
+        if (launch_failed("launch of the solver's iteration kernels")) return PBSM3D_ERR_CUDA;
         if (cudaMemcpy(&h, W.sc, sizeof(Scalars), cudaMemcpyDeviceToHost) != cudaSuccess) {
             g_noalloc_error = std::string("CUDA error: ") + cudaGetErrorString(cudaGetLastError());
             return PBSM3D_ERR_CUDA;
@@ -243,6 +303,7 @@ extern "C" int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* n
     const double bn2 = h.bnorm2;
     const int status = h.done;
     k_na_resid<<<grid, kBlock, 0, s>>>(D, W);
+    if (launch_failed("launch of the residual kernel")) return PBSM3D_ERR_CUDA;
     if (cudaMemcpy(&h, W.sc, sizeof(Scalars), cudaMemcpyDeviceToHost) != cudaSuccess) {
         g_noalloc_error = std::string("CUDA error: ") + cudaGetErrorString(cudaGetLastError());
         return PBSM3D_ERR_CUDA;

@@ -646,7 +646,11 @@ constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 // flags[t], reads block t's partials and the block sums them in block order
 // (deterministic).  Partials alternate between two buffers by epoch parity:
 // a block can only publish epoch e+2 after every block has published e+1,
-// i.e. after every block has finished reading epoch e.  The wait is bounded:
+// i.e. after every block has finished reading epoch e.  A reader therefore
+// waits until flags[b] is AT LEAST its epoch (wraparound-safe difference):
+// block b may already have left this all-reduce and published e+1 before a
+// slow reader first loads its flag, and its epoch-e partials stay valid in
+// the other buffer until every block has published e+1.  The wait is bounded:
 // after kBarrierLimitNs a block sets *err and every block leaves at its next
 // all-reduce, so a broken co-residency assumption ends in an error, never a
 // hang.  Returns false when the kernel must exit.
@@ -668,7 +672,7 @@ __device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, 
     for (int k = 0; k < NT; ++k) t[k] = 0.0;
     for (int b = threadIdx.x; b < G; b += blockDim.x) {
         const unsigned long long t0 = global_timer_ns();
-        while (ld_relaxed_u32(&flags[b * kFlagStride]) != epoch) {
+        while ((int)(ld_relaxed_u32(&flags[b * kFlagStride]) - epoch) < 0) {
             if (*(volatile int*)err) {
                 ok = 0;
                 break;

@@ -502,9 +502,14 @@ int pbsm3d_timer_elapsed(pbsm3d_ctx* ctx, int32_t a, int32_t b, double* ms);
  * Work space is a fixed static device array sized for at most 1,048,576
  * faces (32 MiB, held by every device that loads the library until exit);
  * larger n_faces returns PBSM3D_ERR_INVALID_ARG.  The first call on a device
- * looks up that array's address (make it before any stream capture); calls
- * that overlap on one device race on the shared array.  Runs on the legacy
- * default stream and returns when done.  Messages: pbsm3d_last_error(NULL).
+ * looks up that array's address (make it before any stream capture), and
+ * the first call after a cudaDeviceReset looks it up again where the driver
+ * reports context ids (CUDA 12+ drivers); with an older driver, do not reset
+ * the device after the first call.  Calls that overlap on one device race on
+ * the shared array.  Runs on the legacy default stream and returns when done,
+ * after at most maxit iterations: a launch failure returns PBSM3D_ERR_CUDA,
+ * a solve that reaches maxit above tol PBSM3D_ERR_NOT_CONVERGED (with *iters
+ * and *rel_residual set).  Messages: pbsm3d_last_error(NULL).
  */
 int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* neighbor, const double* diag,
                                     const double* off, const double* rhs, double* x, double tol, int32_t maxit,
