@@ -12,9 +12,15 @@ An element-step is one face advanced one timestep.
 value: device-resident forcing (uploaded before the timed region), K steps
 timed with CUDA events on the library's stream, barrier + synchronize on both
 sides, max over ranks.  e2e: the same K steps through the C ABI with host
-(pinned) forcing and host outputs, copies inside the timed region.
+(pinned) forcing and host outputs, copies inside the timed region.  The
+headline (value, e2e) is the fastest form in FP64 arithmetic, the reference's
+precision; the fastest FP32-inner/FP64-refined form is reported beside it
+("mixed_precision"), with every form's per-field error against the plain FP64
+form's fields.
 --impl reference: the CPU restatement of the reference (oracle, GMRES(30) +
-ILUT, tol 1e-8) on this machine's host cores, rank 0 only.
+ILUT, tol 1e-8, zero initial guess) on this machine's host cores, rank 0
+only, over the same warm-up and timed steps and the same snow-state
+trajectory (each step's drift_mass applied by snobal's rule) as the GPU arm.
 """
 from __future__ import annotations
 
@@ -162,15 +168,22 @@ def forcing_desc(arrs: dict, on_device: int, keep: list):
 
 VARIANTS = {
     # name: config overrides (all reach relative residual 1e-8 in FP64)
+    # -- FP64 arithmetic throughout (the reference's precision); x0 is zero
+    # (the reference's choice) or the previous step's field
     "plain_fp64": {"precision": capi.FP64},
+    # the polynomial (truncated Neumann) preconditioners: order 5 (or K) in the
+    # suspension solve, order 1 in the deposition CG
+    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
+    "fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "neumann": 5,
+                               "dep_neumann": 1},
+    # the same step as one CUDA-graph launch with device-side control
+    "graph_fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                     "neumann": 5, "dep_neumann": 1},
+    # -- FP32 inner solves inside FP64 iterative refinement
     "mixed": {"precision": capi.MIXED},
     "previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS},
     "learned": {"precision": capi.MIXED, "warm_start": capi.X0_LEARNED},
-    # the same step as one CUDA-graph launch with device-side control
     "graph_previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1},
-    # with the polynomial (truncated Neumann) preconditioners: order 5 (or K) in the
-    # suspension solve, order 1 in the deposition CG
-    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
     "previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "neumann": 5, "dep_neumann": 1},
     "graph_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                 "neumann": 5, "dep_neumann": 1},
@@ -183,6 +196,60 @@ VARIANTS = {
 }
 
 
+FIELDS = ("Qsalt", "Qsusp", "Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "sum_drift")
+OUT_NAMES = FIELDS + ("pbsm_more_than_avail", "blowingsnow_probability")
+
+
+def field_errors(a: dict, ref: dict) -> dict:
+    """Per-field error of one form's fields against the reference form's:
+    max-rel (max |a-b| / max |b|), L2-rel (||a-b|| / ||b||) and floored
+    per-element relative error (max |a-b| / max(|b|, 1e-3 max |b|))."""
+    out = {}
+    for k in ref:
+        x = np.asarray(a[k], dtype=np.float64)
+        y = np.asarray(ref[k], dtype=np.float64)
+        ok = np.isfinite(y) & (np.abs(y + 9999.0) > 1e-6)
+        x, y = x[ok], y[ok]
+        d = np.abs(x - y)
+        m = float(np.abs(y).max()) if y.size else 0.0
+        l2 = float(np.linalg.norm(y))
+        out[k] = {"max_rel": float(d.max() / m) if m > 0 else float(d.max(initial=0.0)),
+                  "l2_rel": float(np.linalg.norm(x - y) / l2) if l2 > 0 else float(np.linalg.norm(x - y)),
+                  "elem_rel_floored": float((d / np.maximum(np.abs(y), 1e-3 * m)).max()) if m > 0 else 0.0}
+    return out
+
+
+def is_fp64(name: str) -> bool:
+    return VARIANTS[name].get("precision", capi.FP64) == capi.FP64
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def workload_config(args, T: int, L: int) -> dict:
+    """The workload as both arms name it (identical dicts: same workload)."""
+    return {"workload": f"{args.config}: {T} faces x {L} layers, {args.warmup} warm-up + {args.steps} hourly steps, "
+                        f"snow state advanced by each step's drift_mass (snobal's rule), Weibull wind scale "
+                        f"{args.wind} m/s, seed {args.seed}",
+            "faces": T, "layers": L, "dt_s": 3600.0, "rel_residual": 1e-8,
+            "l2": "working set larger than L2 (no flush needed)"}
+
+
 def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     import torch
     torch.cuda.set_device(local_rank)
@@ -191,21 +258,28 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     T = w.mesh.n_faces
     nsteps = args.warmup + args.steps
     # swe and snow depth stay on the device between steps (pbsm3d_set_snow):
-    # each step's drift_mass feeds the next step's snow state
+    # each step's drift_mass feeds the next step's snow state; one extra
+    # step after the timed ones gives every form's c field for the error report
     host_forcing = [{k: v for k, v in w.forcing(s).arrays().items() if k not in ("swe", "snowdepthavg")}
-                    for s in range(nsteps)]
+                    for s in range(nsteps + 1)]
     swe0, depth0 = np.ascontiguousarray(w.swe), np.ascontiguousarray(w.depth)
     keep = []
     desc = capi.mesh_desc(w.mesh, keep)
     # device-resident forcing for every step, uploaded before timing
     dev_forcing = [{k: torch.from_numpy(a).cuda() for k, a in fs.items()} for fs in host_forcing]
-    out_names = ("Qsalt", "Qsusp", "Qsubl", "Qsubl_mass", "sum_subl", "drift_mass", "sum_drift",
-                 "pbsm_more_than_avail", "blowingsnow_probability")
-    dev_out = {k: torch.empty(T, dtype=torch.float64, device="cuda") for k in out_names}
-    o_dev = capi.Outputs()
-    for k, t in dev_out.items():
-        setattr(o_dev, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
-    o_dev.on_device = 1
+    dev_out = {k: torch.empty(T, dtype=torch.float64, device="cuda") for k in OUT_NAMES}
+    dev_c = torch.empty(T * L, dtype=torch.float64, device="cuda")
+
+    def out_desc(with_c: bool):
+        o = capi.Outputs()
+        for k, t in dev_out.items():
+            setattr(o, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+        if with_c:
+            o.c = C.cast(C.c_void_p(dev_c.data_ptr()), C.POINTER(C.c_double))
+        o.on_device = 1
+        return o
+
+    o_dev, o_dev_c = out_desc(False), out_desc(True)
     fdescs = [forcing_desc(d, 1, keep) for d in dev_forcing]
     torch.cuda.synchronize()
     st = capi.Stats()
@@ -248,13 +322,14 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
         return t, stats
 
     names = args.variants.split(",")
-    if "learned" in names:
+    if "learned" in " ".join(names):
         from chm_gb300 import warmstart
         if not warmstart.WEIGHTS_FILE.exists():
-            names.remove("learned")
+            names = [n for n in names if "learned" not in n]
     sampler = ClockSampler(local_rank)
     results = {}
     ctxs = {}
+    fields = {}
     for name in names:
         ctx = make_ctx(VARIANTS[name])
         ctxs[name] = ctx
@@ -266,73 +341,111 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
             time.sleep(0.3)
         t_dev, stats = timed(ctx, fdescs, o_dev, 0)
         results[name] = {"t_dev": t_dev, "t_max": dist.max(t_dev), "stats": stats}
+        # the last timed step's fields, then one more (untimed) step with c
+        f_last = {k: dev_out[k].cpu().numpy().copy() for k in FIELDS}
+        step(ctx, fdescs[nsteps], o_dev_c)
+        torch.cuda.synchronize()
+        f_last["c"] = dev_c.cpu().numpy().copy()
+        fields[name] = f_last
     clocks = sampler.stop()
     faces_total = dist.sum(float(T * args.steps))
     ok = [n for n in names if max(s["susp_rel_residual"] for s in results[n]["stats"]) <= 1e-8]
-    head = min(ok or names, key=lambda n: results[n]["t_max"])
-    ctx = ctxs[head]
+    fp64_ok = [n for n in ok if is_fp64(n)] or [n for n in names if is_fp64(n)] or names
+    mixed_ok = [n for n in ok if not is_fp64(n)]
+    # the headline is the fastest form in FP64 arithmetic (the reference's
+    # precision); the fastest mixed form is reported beside it
+    head = min(fp64_ok, key=lambda n: results[n]["t_max"])
+    mixed_head = min(mixed_ok, key=lambda n: results[n]["t_max"]) if mixed_ok else None
     t_max = results[head]["t_max"]
-    t_dev = results[head]["t_dev"]
     stats = results[head]["stats"]
+    ref_form = "plain_fp64" if "plain_fp64" in fields else head
+    errors = {n: field_errors(fields[n], fields[ref_form]) for n in names if n != ref_form}
 
-    # ---- e2e (headline form): host pinned forcing in, host outputs back, copies
-    # timed, the head form's context alone on the GPU (as a user runs it)
-    for k in [k for k in ctxs if k != head]:
-        lib.pbsm3d_destroy(ctxs.pop(k))
-    pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in fs.items()} for fs in host_forcing]
-    pin_out = {k: torch.empty(T, dtype=torch.float64).pin_memory() for k in out_names}
-    o_host = capi.Outputs()
-    for k, t in pin_out.items():
-        setattr(o_host, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
-    o_host.on_device = 0
-    hdescs = []
-    for d in pin_f:
-        f = capi.ForcingDesc()
-        for k, t in d.items():
-            setattr(f, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
-        f.on_device = 0
-        hdescs.append(f)
-    step(ctx, hdescs[0], o_host)
-    t_e2e_dev, _ = timed(ctx, hdescs, o_host, 2)
-    t_e2e = dist.max(t_e2e_dev)
+    # ---- e2e: host pinned forcing in, host outputs back, copies timed, the
+    # measured form's context alone on the GPU (as a user runs it)
+    def e2e_of(name):
+        for k in [k for k in ctxs if k != name]:
+            lib.pbsm3d_destroy(ctxs.pop(k))
+        if name not in ctxs:  # a fresh context, warmed up like the timed one
+            ctxs[name] = make_ctx(VARIANTS[name])
+            for s in range(args.warmup):
+                step(ctxs[name], fdescs[s], o_dev)
+            torch.cuda.synchronize()
+        ctx = ctxs[name]
+        pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in fs.items()} for fs in host_forcing]
+        pin_out = {k: torch.empty(T, dtype=torch.float64).pin_memory() for k in OUT_NAMES}
+        o_host = capi.Outputs()
+        for k, t in pin_out.items():
+            setattr(o_host, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+        o_host.on_device = 0
+        hdescs = []
+        for d in pin_f:
+            f = capi.ForcingDesc()
+            for k, t in d.items():
+                setattr(f, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
+            f.on_device = 0
+            hdescs.append(f)
+        step(ctx, hdescs[0], o_host)
+        t_e2e_dev, _ = timed(ctx, hdescs, o_host, 2)
+        lib.pbsm3d_destroy(ctxs.pop(name))
+        return dist.max(t_e2e_dev)
+
+    # per-kernel figures come from host-driven forms (a graph replay has no
+    # per-launch events): the fastest profiled form of each precision
+    def profiled_twin(pool):
+        prof = [n for n in pool if all(s["profiled"] for s in results[n]["stats"])]
+        return min(prof, key=lambda n: results[n]["t_max"]) if prof else None
+
+    prof_name = profiled_twin([head]) or profiled_twin([n for n in names if is_fp64(n)])
+    mixed_prof = profiled_twin([mixed_head]) if mixed_head else None
+    if mixed_head and not mixed_prof:
+        mixed_prof = profiled_twin([n for n in names if not is_fp64(n)])
+    t_e2e = e2e_of(head)
+    t_e2e_mixed = e2e_of(mixed_head) if mixed_head else None
     h2d = 8 * T * len(host_forcing[0])
-    d2h = 8 * T * len(out_names)
+    d2h = 8 * T * len(OUT_NAMES)
     for c in ctxs.values():
         lib.pbsm3d_destroy(c)
 
-    # ---- roofline of the dominant kernel class (events around each launch);
-    # a graph-mode step has no per-launch events: use the fastest profiled form
-    profiled = [n for n in names if all(s["profiled"] for s in results[n]["stats"])]
-    if not profiled:  # only graph forms asked for: no per-kernel figures
-        prof_name = None
-        profiled = [head]
-    else:
-        prof_name = head if head in profiled else min(profiled, key=lambda n: results[n]["t_max"])
-    stats_p = results[prof_name or head]["stats"]
-    kern_ms = np.sum([s["kern_ms"] for s in stats_p], axis=0)
-    kern_bytes = np.sum([s["kern_bytes"] for s in stats_p], axis=0)
-    kern_n = np.sum([s["kern_launches"] for s in stats_p], axis=0)
-    top = int(np.argmax(kern_ms))
     peak, peak_kind = measured_peak()
-    achieved = float(kern_bytes[top]) / (float(kern_ms[top]) / 1e3) / 1e9 if kern_ms[top] > 0 else 0.0
-    traffic = None
+    traffic_tab = {}
     prof_file = ROOT / "profiles" / "traffic.json"
     if prof_file.exists():
         try:
-            tr = json.loads(prof_file.read_text())
-            key = f"{capi.KERNELS[top]}:{args.config}"
-            if key in tr:
-                traffic = tr[key]
+            traffic_tab = json.loads(prof_file.read_text())
         except Exception:
-            traffic = None
-    total_ms = float(np.sum(kern_ms))
-    kernels = {capi.KERNELS[k]: {"ms": round(float(kern_ms[k]), 3), "launches": int(kern_n[k]),
-                                 "GBps": round(float(kern_bytes[k]) / (float(kern_ms[k]) / 1e3) / 1e9, 1)
-                                 if kern_ms[k] > 0 else None,
-                                 "share": round(float(kern_ms[k]) / total_ms, 4) if total_ms > 0 else None}
-               for k in range(len(capi.KERNELS)) if kern_n[k] > 0}
-    alg_bytes = float(np.sum([s["bytes_moved"] for s in stats_p]))
-    t_prof = results[prof_name or head]["t_dev"]
+            traffic_tab = {}
+
+    def kernel_figures(pname):
+        """Per-class event timing of one host-driven form: the dominant
+        class's roofline, every class's time/share/GBps, the step's roofline."""
+        if pname is None:
+            return None, None, None
+        sp = results[pname]["stats"]
+        kern_ms = np.sum([s["kern_ms"] for s in sp], axis=0)
+        kern_bytes = np.sum([s["kern_bytes"] for s in sp], axis=0)
+        kern_n = np.sum([s["kern_launches"] for s in sp], axis=0)
+        top = int(np.argmax(kern_ms))
+        achieved = float(kern_bytes[top]) / (float(kern_ms[top]) / 1e3) / 1e9 if kern_ms[top] > 0 else 0.0
+        total_ms = float(np.sum(kern_ms))
+        kernels = {capi.KERNELS[k]: {"ms": round(float(kern_ms[k]), 3), "launches": int(kern_n[k]),
+                                     "GBps": round(float(kern_bytes[k]) / (float(kern_ms[k]) / 1e3) / 1e9, 1)
+                                     if kern_ms[k] > 0 else None,
+                                     "share": round(float(kern_ms[k]) / total_ms, 4) if total_ms > 0 else None}
+                   for k in range(len(capi.KERNELS)) if kern_n[k] > 0}
+        tkey = f"{capi.KERNELS[top]}:{'fp64' if is_fp64(pname) else 'fp32'}:{args.config}"
+        roof = {"bound": "hbm", "kernel": capi.KERNELS[top], "achieved": round(achieved, 1), "peak": peak,
+                "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": traffic_tab.get(tkey), "variant": pname}
+        alg_bytes = float(np.sum([s["bytes_moved"] for s in sp]))
+        t_prof = results[pname]["t_dev"]
+        step_roof = {"alg_GB_per_step": round(alg_bytes / args.steps / 1e9, 3),
+                     "achieved_GBps": round(alg_bytes / t_prof / 1e9, 1),
+                     "frac": round(alg_bytes / t_prof / 1e9 / peak, 4), "variant": pname}
+        return roof, step_roof, kernels
+
+    roof, step_roof, kernels = kernel_figures(prof_name)
+    mroof, mstep_roof, mkernels = kernel_figures(mixed_prof)
 
     def solver_summary(sts):
         return {"susp_iters_mean": float(np.mean([s["susp_iters"] for s in sts])),
@@ -341,38 +454,49 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 "dep_refinements_mean": float(np.mean([s["dep_refinements"] for s in sts])),
                 "saltating_faces_mean": float(np.mean([s["n_slow_faces"] for s in sts])),
                 "susp_rel_residual_max": float(np.max([s["susp_rel_residual"] for s in sts])),
+                "ledger_residual_max": float(np.max([abs(s["ledger_residual"]) for s in sts])),
                 "ms_coefficients": float(np.mean([s["ms_coefficients"] for s in sts])),
                 "ms_susp_solve": float(np.mean([s["ms_susp_solve"] for s in sts])),
                 "ms_dep_solve": float(np.mean([s["ms_dep_solve"] for s in sts]))}
 
+    def worst(errs):
+        return {k: max(v[k] for v in errs.values()) for k in ("max_rel", "l2_rel", "elem_rel_floored")}
+
     res = {
         "metric": METRIC, "value": faces_total / t_max, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "plain_fp64" else "f64+f32",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Delaunay mesh and forcing of the reference's benchmark shape)",
-        "config": {"workload": f"{args.config}: {T} faces x {L} layers, hourly steps with the snow state kept on "
-                               f"the device, Weibull wind scale {args.wind} m/s, seed {args.seed}+rank",
-                   "faces": T, "layers": L, "variant": head,
-                   "solver": "BiCGStab, column-Thomas right preconditioner, rel. residual 1e-8; deposition CG 1e-10",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "working set larger than L2 (no flush needed)"},
+        "config": workload_config(args, T, L),
+        "variant": head,
+        "solver": "BiCGStab, right-preconditioned (column Thomas, or order-K truncated Neumann), rel. residual "
+                  "1e-8; deposition CG to 1e-10; FP64 arithmetic",
+        "parallelism": f"replicas x{world}",
         "e2e": {"value": faces_total / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "variant": head},
         "gpu_launches": int(sum(s["gpu_launches"] for s in stats)),
-        "roofline": {"bound": "hbm", "kernel": capi.KERNELS[top], "achieved": round(achieved, 1),
-                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": traffic, "variant": prof_name},
-        "step_roofline": {"alg_GB_per_step": round(alg_bytes / args.steps / 1e9, 3),
-                          "achieved_GBps": round(alg_bytes / t_prof / 1e9, 1),
-                          "frac": round(alg_bytes / t_prof / 1e9 / peak, 4), "variant": prof_name},
+        "roofline": roof,
+        "step_roofline": step_roof,
         "kernels": kernels,
-        "solver": solver_summary(stats),
-        **({} if prof_name else {"roofline": None, "step_roofline": None, "kernels": None}),
+        "solver_stats": solver_summary(stats),
+        "mixed_precision": None if mixed_head is None else {
+            "variant": mixed_head, "dtype": "f64+f32", "value": faces_total / results[mixed_head]["t_max"],
+            "ms_per_step": results[mixed_head]["t_max"] / args.steps * 1e3,
+            "e2e": {"value": faces_total / t_e2e_mixed, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "speedup_vs_fp64_headline": t_max / results[mixed_head]["t_max"],
+            "field_error_vs": ref_form, "field_error": errors.get(mixed_head),
+            "roofline": mroof, "step_roofline": mstep_roof, "kernels": mkernels},
+        "field_error_vs": f"{ref_form} (FP64, zero initial guess: the reference's solve), fields of the last timed "
+                          f"step and c of one step after it",
         "variants": {n: {"value": faces_total / results[n]["t_max"],
                          "ms_per_step": results[n]["t_max"] / args.steps * 1e3,
+                         "dtype": "f64" if is_fp64(n) else "f64+f32",
                          "speedup_vs_plain_fp64": (results["plain_fp64"]["t_max"] / results[n]["t_max"]
                                                    if "plain_fp64" in results else None),
-                         **solver_summary(results[n]["stats"])} for n in names},
+                         **solver_summary(results[n]["stats"]),
+                         **({"field_error_worst": worst(errors[n])} if n in errors else {})}
+                     for n in names},
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -568,54 +692,102 @@ def run_ensemble(args, dist: Dist, rank: int, world: int, local_rank: int, membe
     }
 
 
+def _cpu_one_step(w, L, forcing, threads: int, nblocks: int) -> float:
+    """Seconds for one oracle step at a given thread count and ILUT block count."""
+    from oracle import pyoracle
+    lib = pyoracle.load()
+    prev = lib.oracle_set_threads(threads)
+    try:
+        o = pyoracle.Oracle(w.mesh, nLayer=L, solver={"nblocks": nblocks})
+        t0 = time.perf_counter()
+        o.step(forcing, 3600.0, want_c=False)
+        dt = time.perf_counter() - t0
+        o.close()
+    finally:
+        lib.oracle_set_threads(prev)
+    return dt
+
+
+ILUT_NOTE = ("the port factorises ILUT over {nb} row blocks, as {nb} reference MPI ranks do (Ifpack2 factorises each "
+             "rank's own rows); one reference rank factorises globally: 'one_rank' (1 block, {nc} threads) and "
+             "'one_core' (1 block, 1 thread) time that")
+
+
 def cpu_baseline(w, L, args) -> dict:
     """The oracle (C++ restatement of the reference, GMRES(30)+ILUT, tol 1e-8)
-    timed on this host's cores over one step of the same workload."""
+    timed on this host's cores: one step of the same workload with all cores,
+    and one with a single core and a global ILUT."""
     cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     from oracle import pyoracle
-    o = pyoracle.Oracle(w.mesh, nLayer=L, solver={"nblocks": cores})
     f = w.forcing(args.warmup)
-    t0 = time.perf_counter()
-    _, st = o.step(f, 3600.0, want_c=False)
-    dt = time.perf_counter() - t0
-    o.close()
+    dt = _cpu_one_step(w, L, f, cores, cores)
+    dt1 = _cpu_one_step(w, L, f, 1, 1)
     T = w.mesh.n_faces
-    return {"value": T / dt, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", cores)), "kind": "port",
+    return {"value": T / dt, "unit": UNIT, "cores": cores, "kind": "port", "cpu_model": cpu_model(),
             "sample": f"1 step of the same {T}-face x {L}-layer workload ({dt:.1f} s; GMRES(30)+ILUT over "
-                      f"{cores} blocks, {st['susp_iters']} suspension iterations)"}
+                      f"{cores} blocks on {cores} threads)",
+            "ilut": ILUT_NOTE.format(nb=cores, nc=cores),
+            "one_core": {"value": T / dt1, "unit": UNIT, "cores": 1, "sample": f"1 step, 1 ILUT block ({dt1:.1f} s)"}}
 
 
 def run_reference(args, rank: int, world: int) -> dict | None:
+    """The reference's CPU path (the oracle: the C++ restatement, GMRES(30) +
+    ILUT, tol 1e-8, zero initial guess) on this host's cores, over the same
+    steps, forcing and snow-state trajectory as the GPU arm."""
     if rank != 0:
         return None
     cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     from oracle import pyoracle
     w, L = make_workload(args, 0)
     T = w.mesh.n_faces
+    nsteps = args.warmup + args.steps
+    forcings = [{k: v for k, v in w.forcing(s).arrays().items() if k not in ("swe", "snowdepthavg")}
+                for s in range(nsteps)]
+    lib = pyoracle.load()
+    lib.oracle_set_threads(cores)
     o = pyoracle.Oracle(w.mesh, nLayer=L, solver={"nblocks": cores})
-    budget = args.ref_budget
-    for s in range(min(args.warmup, 1)):
-        o.step(w.forcing(s), 3600.0, want_c=False)
-    t0 = time.perf_counter()
+    # warm-up and timed steps run back to back on one trajectory; the timer
+    # covers the timed steps only
+    from chm_gb300.synth import consume_drift
+    swe, depth = w.swe.copy(), w.depth.copy()
+    iters, dep_iters, times = [], [], []
+    t_start = time.perf_counter()
     done = 0
-    iters = []
-    for s in range(args.steps):
-        _, st = o.step(w.forcing(args.warmup + s), 3600.0, want_c=False)
-        iters.append(st["susp_iters"])
-        done += 1
-        if time.perf_counter() - t0 > budget:
+    for s in range(nsteps):
+        f = dict(forcings[s])
+        f["swe"], f["snowdepthavg"] = swe, depth
+        t0 = time.perf_counter()
+        out, st = o.step(f, 3600.0, want_c=False)
+        swe, depth = consume_drift(swe, depth, out["drift_mass"], 300.0)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+            iters.append(st["susp_iters"])
+            dep_iters.append(st["dep_iters"])
+            done += 1
+        if time.perf_counter() - t_start > args.ref_budget:
             break
-    dt = time.perf_counter() - t0
-    v = T * done / dt
-    sample = (f"{done} of {args.steps} steps of the {T}-face x {L}-layer workload ({dt:.1f} s, "
-              f"GMRES(30)+ILUT over {cores} blocks, mean {np.mean(iters):.1f} suspension iterations)")
-    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1),
-            "ms_per_step": dt / done * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{args.config}: {T} faces x {L} layers, hourly steps", "faces": T, "layers": L},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+    o.close()
+    dt = float(np.sum(times)) if times else float("nan")
+    v = T * done / dt if done else 0.0
+    f1 = dict(forcings[min(args.warmup, nsteps - 1)])
+    f1["swe"], f1["snowdepthavg"] = w.swe, w.depth
+    dt_rank = _cpu_one_step(w, L, f1, cores, 1)
+    dt_core = _cpu_one_step(w, L, f1, 1, 1) if not args.no_one_core else None
+    sample = (f"{done} of {args.steps} timed steps (after {args.warmup} warm-up steps) of the {T}-face x {L}-layer "
+              f"workload on the GPU arm's snow-state trajectory ({dt:.1f} s; GMRES(30)+ILUT over {cores} blocks, "
+              f"{cores} threads, mean {np.mean(iters):.1f} suspension and {np.mean(dep_iters):.1f} deposition "
+              f"iterations)")
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": done, "warmup": args.warmup,
+            "ms_per_step": dt / max(done, 1) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(args, T, L),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                             "cpu_model": cpu_model(), "ilut": ILUT_NOTE.format(nb=cores, nc=cores),
+                             "one_rank": {"value": T / dt_rank, "unit": UNIT, "cores": cores,
+                                          "sample": f"1 step, 1 ILUT block, {cores} threads ({dt_rank:.1f} s)"},
+                             "one_core": None if dt_core is None else {
+                                 "value": T / dt_core, "unit": UNIT, "cores": 1,
+                                 "sample": f"1 step, 1 ILUT block, 1 thread ({dt_core:.1f} s)"}},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -626,12 +798,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="tri1m", choices=sorted(synth.CONFIGS))
-    ap.add_argument("--variants", default="plain_fp64,mixed,previous,learned,graph_previous,plain_fp64_neumann5,"
+    ap.add_argument("--variants", default="plain_fp64,plain_fp64_neumann5,fp64_previous_neumann5,"
+                                          "graph_fp64_previous_neumann5,mixed,previous,learned,graph_previous,"
                                           "previous_neumann5,graph_previous_neumann5,graph_learned_neumann5",
-                    help="comma list of %s; the fastest meeting residual 1e-8 is the headline" % ",".join(VARIANTS))
+                    help="comma list of %s; the fastest FP64 form meeting residual 1e-8 is the headline, the "
+                         "fastest mixed form is reported beside it" % ",".join(VARIANTS))
     ap.add_argument("--wind", type=float, default=8.0)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--ref-budget", type=float, default=120.0)
+    ap.add_argument("--ref-budget", type=float, default=600.0,
+                    help="seconds after which the reference arm stops taking steps")
+    ap.add_argument("--no-one-core", action="store_true", help="reference arm: skip the 1-core step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--members", type=int, default=0,
                     help="batched-ensemble workload with this many member meshes (0: the single 1M-face mesh)")

@@ -18,9 +18,13 @@
 //    absolute).  Accurate to a few 1e-16 absolute; callers use it where an
 //    absolute error of that size is harmless (arguments of exp, or arguments
 //    far from 1).
-//  * rcp: the hardware reciprocal estimate of the high word (PTX
-//    rcp.approx.ftz.f64) refined by two Newton steps, then one residual
-//    correction of the quotient.
+//  * rcp: the hardware reciprocal estimate (PTX rcp.approx.ftz.f64, about
+//    23 correct bits) refined by two Newton-Raphson steps on f(y) = 1/y - x,
+//    y <- y + y (1 - x y), each of which squares the relative error.
+//  * div: a * rcp(b), then one correction of the quotient by its residual,
+//    q + (a - b q) rcp(b) (P. Markstein, "Computation of elementary
+//    functions on the IBM RISC System/6000 processor", IBM J. Res. Dev.
+//    34(1), 1990).
 //
 // Arguments outside the fast ranges (non-positive, subnormal, huge, NaN,
 // Inf) take the CUDA library function, so special values behave as before.
@@ -96,7 +100,8 @@ __device__ __forceinline__ double log_t(double x, const MathTables& t) {
     return hi + lo;
 }
 
-// 1/x for finite non-zero normal x (|x| in [2^-1000, 2^1000]), else 1.0/x.
+// 1/x for finite non-zero normal x (|x| in [2^-1000, 2^1000]), else 1.0/x:
+// the hardware estimate and two Newton-Raphson steps y <- y + y (1 - x y).
 __device__ __forceinline__ double rcp_t(double x) {
     const unsigned long long ax = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
     if (ax < 0x0170000000000000ull || ax >= 0x7e70000000000000ull) return 1.0 / x;
@@ -109,7 +114,7 @@ __device__ __forceinline__ double rcp_t(double x) {
     return y;
 }
 
-// a / b with one residual correction of a * rcp(b) (within 1 ulp).
+// a / b: q = a rcp(b) corrected once by its residual (Markstein 1990), within 1 ulp.
 __device__ __forceinline__ double div_t(double a, double b) {
     const double y = rcp_t(b);
     const double q = a * y;

@@ -515,6 +515,31 @@ int pbsm3d_deposition_solve_noalloc(int64_t n_faces, const int32_t* neighbor, co
                                     const double* off, const double* rhs, double* x, double tol, int32_t maxit,
                                     int32_t* iters, double* rel_residual);
 
+/*
+ * Validation of the library's table-driven FP64 routines.  No counterpart in
+ * the reference: the assembly evaluates exp, log, x^y, 1/x and a/b with its
+ * own routines (Tang's table-driven exp and log, a Newton-Raphson-refined
+ * reciprocal) and rounds FP64 to FP32 on the integer pipe; this evaluates
+ * one of them, or the CUDA function it stands in for, elementwise over n
+ * device values: out[i] = f(a[i]) or f(a[i], b[i]) (b only for DIV and POW).
+ * Synchronous, on the legacy default stream.
+ */
+enum {
+    PBSM3D_MATH_EXP = 0,
+    PBSM3D_MATH_LOG = 1,
+    PBSM3D_MATH_RCP = 2,
+    PBSM3D_MATH_DIV = 3,
+    PBSM3D_MATH_POW = 4,
+    PBSM3D_MATH_F32 = 5,       /* (double)(float) rounding on the integer pipe */
+    PBSM3D_MATH_CUDA_EXP = 6,  /* CUDA's exp, log, 1.0/x, a/b, pow, (float) */
+    PBSM3D_MATH_CUDA_LOG = 7,
+    PBSM3D_MATH_CUDA_RCP = 8,
+    PBSM3D_MATH_CUDA_DIV = 9,
+    PBSM3D_MATH_CUDA_POW = 10,
+    PBSM3D_MATH_CUDA_F32 = 11
+};
+int pbsm3d_math_eval(int32_t fn, int64_t n, const double* a, const double* b, double* out);
+
 /* Message of the last failure on this context (or of the last failed create
  * when ctx is NULL). */
 const char* pbsm3d_last_error(const pbsm3d_ctx* ctx);

@@ -960,6 +960,12 @@ int oracle_face_neighbors(int64_t nv, int64_t nt, const int32_t* tri, int32_t* n
     return 0;
 }
 
+int oracle_set_threads(int n) {
+    const int prev = omp_get_max_threads();
+    if (n > 0) omp_set_num_threads(n);
+    return prev;
+}
+
 void oracle_solver_defaults(oracle_solver_cfg* s) {
     s->restart = 30;
     s->maxit = 1000;

@@ -48,6 +48,9 @@ int oracle_create(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg, oracle
 void oracle_destroy(oracle_ctx* ctx);
 void oracle_solver_defaults(oracle_solver_cfg* s);
 int oracle_set_solver(oracle_ctx* ctx, const oracle_solver_cfg* s);
+/* OpenMP threads of the process's later parallel regions (the CPU timing at
+ * a stated core count); returns the count in effect before the call. */
+int oracle_set_threads(int n);
 const char* oracle_last_error(const oracle_ctx* ctx);
 
 /* Whole step (PBSM3D::run). */

@@ -46,6 +46,8 @@ def load():
     lib.oracle_solver_defaults.argtypes = [C.POINTER(SolverCfg)]
     lib.oracle_solver_defaults.restype = None
     lib.oracle_set_solver.argtypes = [vp, C.POINTER(SolverCfg)]
+    lib.oracle_set_threads.argtypes = [C.c_int]
+    lib.oracle_set_threads.restype = C.c_int
     lib.oracle_last_error.argtypes = [vp]
     lib.oracle_last_error.restype = C.c_char_p
     lib.oracle_step.argtypes = [vp, C.POINTER(capi.ForcingDesc), C.c_double, C.POINTER(capi.Outputs),
