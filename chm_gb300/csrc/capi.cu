@@ -754,6 +754,18 @@ int pbsm3d_set_profiling(pbsm3d_ctx* h, int32_t on) {
     return 0;
 }
 
+int pbsm3d_arm_wait_timeout_test(pbsm3d_ctx* h, int32_t withhold_block, double limit_ms) {
+    if (!h || withhold_block < 0 || !(limit_ms > 0.0) || limit_ms > 2000.0) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    if (c.tiles.n > 1 || c.cfg.graph) {
+        c.err = "the wait-timeout test needs a single-mesh, host-driven context (persistent deposition CG)";
+        return PBSM3D_ERR_INVALID_ARG;
+    }
+    c.test_withhold = withhold_block;
+    c.test_limit_ns = (unsigned long long)(limit_ms * 1e6);
+    return 0;
+}
+
 int pbsm3d_timer_mark(pbsm3d_ctx* h, int32_t slot) {
     if (!h || slot < 0 || slot >= 16) return PBSM3D_ERR_INVALID_ARG;
     Ctx& c = h->c;

@@ -357,6 +357,11 @@ struct Ctx {
     int coop_blocks;   // co-resident blocks of the persistent CG kernel
     int coop_blocks32 = 0;  // ... of its FP32 instance (MIXED)
     unsigned* cg_flags;     // [kMaxCgBlocks][32] all-reduce flags of the persistent CG
+    // the timeout test (pbsm3d_arm_wait_timeout_test): for the next
+    // persistent CG launch only, a block that publishes no flag and the wait
+    // limit in ns (0: none armed)
+    int test_withhold = -1;
+    unsigned long long test_limit_ns = 0;
     // MIXED deposition: FP32 matrix (diag, off[3], dinv), right-hand side and
     // the five CG vectors, [11][Tp]
     float* dep32 = nullptr;

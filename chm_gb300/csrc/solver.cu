@@ -640,6 +640,14 @@ constexpr int kCgBlock = 512;
 constexpr int kCgBlocksPerSm = 2;
 constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 
+// The bounded waits of the persistent CG: their limit, and one block that
+// publishes no flag at all (-1: none; set only by the timeout test, whose
+// other blocks' waits then run out and end the kernel with *err set).
+struct GridWait {
+    unsigned long long limit_ns;
+    int withhold;
+};
+
 // All-reduce of NT per-thread values over a cooperative grid, identical in
 // every block, without atomics: block b writes its partials and then
 // releases flags[b] = epoch; thread t < gridDim of every block waits for
@@ -651,12 +659,13 @@ constexpr int kFlagStride = 32;  // one 128-byte line per block flag
 // block b may already have left this all-reduce and published e+1 before a
 // slow reader first loads its flag, and its epoch-e partials stay valid in
 // the other buffer until every block has published e+1.  The wait is bounded:
-// after kBarrierLimitNs a block sets *err and every block leaves at its next
-// all-reduce, so a broken co-residency assumption ends in an error, never a
-// hang.  Returns false when the kernel must exit.
+// after gw.limit_ns (kBarrierLimitNs outside the timeout test) a block sets
+// *err and every block leaves at its next all-reduce, so a broken
+// co-residency assumption ends in an error, never a hang.  Returns false
+// when the kernel must exit.
 template <int NT>
 __device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, unsigned epoch, int* err,
-                            double (&tot)[NT]) {
+                            const GridWait& gw, double (&tot)[NT]) {
     __shared__ double bc[NT];
     __shared__ int ok;
     block_sum<NT>(v);
@@ -664,7 +673,7 @@ __device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, 
     double* pp = partials + (size_t)(epoch & 1u) * 4 * G;
     if (threadIdx.x == 0) {
         for (int k = 0; k < NT; ++k) pp[k * G + blockIdx.x] = v[k];
-        st_release_u32(&flags[blockIdx.x * kFlagStride], epoch);
+        if ((int)blockIdx.x != gw.withhold) st_release_u32(&flags[blockIdx.x * kFlagStride], epoch);
         ok = 1;
     }
     __syncthreads();
@@ -677,7 +686,7 @@ __device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, 
                 ok = 0;
                 break;
             }
-            if (global_timer_ns() - t0 > kBarrierLimitNs) {
+            if (global_timer_ns() - t0 > gw.limit_ns) {
                 atomicExch(err, 1);
                 ok = 0;
                 break;
@@ -734,11 +743,19 @@ __device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __re
 // CG in one cooperative launch, Jacobi or polynomial preconditioner; at 1M
 // faces its vectors and matrix (~100 MB in FP64) stay in L2.  Two all-reduces
 // per iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
-// (q is updated from A z by the recurrence q = A z + beta q).
+// (q is updated from A z by the recurrence q = A z + beta q).  Measured
+// slower at 1M faces, and dropped: a form with one all-reduce per iteration
+// (Chronopoulos-Gear recurrences, contiguous row runs per block and a
+// point-to-point wait for the blocks owning neighbour rows), 2.95 against
+// 2.55 ms per FP64 solve, whose polynomial preconditioner rebuilds each
+// neighbour's new residual from three vectors instead of two (the iteration
+// is bound by those gathered loads, not by the all-reduce it saves); and an
+// all-reduce whose partials are staged in shared memory for one warp to
+// sum, 2.65 ms (its 24 KB of shared memory is L1 the gathers lose).
 template <typename V>
-__global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr,
-                                                          double* partials, unsigned* flags, int* err, Scalars* sc,
-                                                          double tol, int maxit) {
+__global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm)
+    k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr, double* partials, unsigned* flags,
+                    int* err, Scalars* sc, double tol, int maxit, GridWait gw) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     unsigned epoch = 0;
@@ -759,7 +776,7 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int6
             acc[2] += bi * bi;
         }
         for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
-        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
+        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, gw, t3)) return;
         V zq = 0;
         for (int64_t i = i0; i < Tp; i += stride) {
             V qi = D.diag[i] * D.zz[i];
@@ -772,7 +789,7 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int6
             zq += D.zz[i] * qi;
         }
         double a1[1] = {(double)zq}, t1[1];
-        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, t1)) return;
+        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, gw, t1)) return;
         t3[1] = t1[0];
     } else {
         V acc[3] = {0, 0, 0};
@@ -795,7 +812,7 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int6
             acc[2] += bi * bi;
         }
         for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
-        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, t3)) return;
+        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, gw, t3)) return;
     }
     double rho = t3[0];
     const double bb = t3[2];
@@ -826,7 +843,7 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int6
             a2[0] = (double)acc[0];
             a2[1] = (double)acc[1];
         }
-        if (!grid_totals<2>(a2, partials, flags, ++epoch, err, t2)) return;
+        if (!grid_totals<2>(a2, partials, flags, ++epoch, err, gw, t2)) return;
         ++it;
         rr = t2[1];
         if (rr <= target2) {
@@ -862,7 +879,7 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm) k_cg_persistent(int6
             }
             a1[0] = (double)acc;
         }
-        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, t1)) return;
+        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, gw, t1)) return;
         if (!(t1[0] > 0.0)) {
             status = 2;
             break;
@@ -1589,7 +1606,14 @@ static int launch_cg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* s
     int64_t Tp = c.P.Tp;
     double* part = c.red.partials;
     int* err = &c.gbar->err;
-    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit};
+    GridWait gw{kBarrierLimitNs, -1};
+    if (c.test_limit_ns) {  // armed by the timeout test, for this launch only
+        gw.limit_ns = c.test_limit_ns;
+        gw.withhold = std::min(std::max(c.test_withhold, 0), blocks - 1);
+        c.test_limit_ns = 0;
+        c.test_withhold = -1;
+    }
+    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit, &gw};
     PBSM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_persistent<V>, dim3(blocks), dim3(kCgBlock), args,
                                               0, s));
     int rc = read_scalars(c, s, sc);
@@ -1597,7 +1621,7 @@ static int launch_cg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* s
     int e = 0;
     PBSM_CUDA_TRY(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) {
-        c.err = "deposition solve: grid all-reduce timed out";
+        c.err = "deposition solve: grid all-reduce timed out (a block's wait ran out)";
         return PBSM3D_ERR_CUDA;
     }
     return 0;

@@ -482,6 +482,20 @@ int pbsm3d_mlp_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t
  * and fills pbsm3d_stats.kern_*. */
 int pbsm3d_set_profiling(pbsm3d_ctx* ctx, int32_t on);
 
+/*
+ * Test of the device-side wait limits.  No counterpart in the reference,
+ * whose failure path is a solver exception (PBSM3D.cpp:1690-1705).  Every
+ * wait of the persistent deposition CG (one cooperative launch whose blocks
+ * synchronise through flags in global memory) is bounded; this arms, for the
+ * next such launch of this context only, a block (withhold_block, clamped to
+ * the grid) that publishes none of its flags, and a wait limit of limit_ms
+ * (at most 2000; the default limit is 2 s).  The other blocks' waits run
+ * out, every block leaves, and that step returns PBSM3D_ERR_CUDA ("grid
+ * all-reduce timed out") with the context usable for the next step.
+ * Single-mesh, host-driven contexts only (PBSM3D_ERR_INVALID_ARG otherwise).
+ */
+int pbsm3d_arm_wait_timeout_test(pbsm3d_ctx* ctx, int32_t withhold_block, double limit_ms);
+
 /* Device-side timing of a region on the context's stream (measurement
  * plumbing): pbsm3d_timer_mark records CUDA event `slot` (0..15) on the
  * stream; pbsm3d_timer_elapsed waits for both and returns the milliseconds
