@@ -58,16 +58,17 @@ def _ptr(t):
 
 
 def collect(seeds, n_points: int, side: float, nLayer: int, steps: int, rows_per_step: int, wind: float = 8.0,
-            rng_seed: int = 0):
+            rng_seed: int = 0, workloads=None):
     """(features, targets) as CUDA tensors: `rows_per_step` random rows of
     every step of plain FP64 solves on the seeded meshes (c_prev of the first
-    step is zero, as in a cold start)."""
+    step is zero, as in a cold start).  `workloads`, when given, are the
+    seeds' prebuilt workloads (in seed order)."""
     import torch
     lib = capi.load()
     rng = np.random.default_rng(rng_seed)
     feats, targs = [], []
-    for seed in seeds:
-        w = synth.Workload(n_points, side, seed=seed, wind_scale=wind)
+    for k, seed in enumerate(seeds):
+        w = workloads[k] if workloads is not None else synth.Workload(n_points, side, seed=seed, wind_scale=wind)
         m = PBSM3D({"nLayer": str(nLayer)})
         m.init(w.mesh)
         rows = w.mesh.n_faces * nLayer
@@ -183,10 +184,10 @@ def features(module: PBSM3D):
 
 
 def train_from_solutions(train_seeds, n_points, side, nLayer, steps_per_seed, rows_per_step, train_steps, lr=1e-3,
-                         batch=8192, seed=0, wind=8.0):
+                         batch=8192, seed=0, wind=8.0, workloads=None):
     """Collect plain-solver solutions on the training seeds and fit the MLP on the GPU."""
     feat, targ = collect(train_seeds, n_points, side, nLayer, steps_per_seed, rows_per_step, wind=wind,
-                         rng_seed=seed)
+                         rng_seed=seed, workloads=workloads)
     mean, scale = feature_stats(feat)
     tr = Trainer(init_params(seed), mean, scale, batch=batch)
     losses = tr.train(feat, targ, train_steps, lr, seed)

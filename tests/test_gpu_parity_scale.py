@@ -61,10 +61,11 @@ EXACT_TOL = 1e-9    # fields the solves do not change
 TIGHT_TOL = 1e-8
 LEDGER_TOL = 1e-10
 
-# the forms the benchmark reports: the reference-like solve, the fastest
-# FP64 form (the headline) and the fastest FP32-inner/FP64-refined form
+# the forms the benchmark reports: the reference-like solve, the FP64 forms
+# that compete for the headline and the fastest FP32-inner/FP64-refined form
 FORMS = {
     "plain_fp64": {},
+    "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
     "graph_fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                      "neumann": 5, "dep_neumann": 1},
     "graph_mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
