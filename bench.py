@@ -219,6 +219,13 @@ def field_errors(a: dict, ref: dict) -> dict:
     return out
 
 
+def column_geometry(lib, ctx) -> dict:
+    """The column kernels' launch geometry in force (autotuned by default)."""
+    w, l, t = C.c_int32(), C.c_int32(), C.c_int32()
+    lib.pbsm3d_get_column_geometry(ctx, C.byref(w), C.byref(l), C.byref(t))
+    return {"faces_per_block": w.value, "lanes_per_column": l.value, "tuned": bool(t.value)}
+
+
 def is_fp64(name: str) -> bool:
     return VARIANTS[name].get("precision", capi.FP64) == capi.FP64
 
@@ -340,7 +347,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
             sampler.start()
             time.sleep(0.3)
         t_dev, stats = timed(ctx, fdescs, o_dev, 0)
-        results[name] = {"t_dev": t_dev, "t_max": dist.max(t_dev), "stats": stats}
+        results[name] = {"t_dev": t_dev, "t_max": dist.max(t_dev), "stats": stats, "geometry": column_geometry(lib, ctx)}
         # the last timed step's fields, then one more (untimed) step with c
         f_last = {k: dev_out[k].cpu().numpy().copy() for k in FIELDS}
         step(ctx, fdescs[nsteps], o_dev_c)
@@ -495,6 +502,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                          "speedup_vs_plain_fp64": (results["plain_fp64"]["t_max"] / results[n]["t_max"]
                                                    if "plain_fp64" in results else None),
                          **solver_summary(results[n]["stats"]),
+                         "column_geometry": results[n]["geometry"],
                          **({"field_error_worst": worst(errors[n])} if n in errors else {})}
                      for n in names},
         "clocks": clocks,
@@ -614,7 +622,7 @@ def run_ensemble(args, dist: Dist, rank: int, world: int, local_rank: int, membe
             sampler.start()
             time.sleep(0.3)
         t_dev, stats = timed(ctx, fdescs, o_dev, 0)
-        results[name] = {"t_dev": t_dev, "t_max": dist.max(t_dev), "stats": stats}
+        results[name] = {"t_dev": t_dev, "t_max": dist.max(t_dev), "stats": stats, "geometry": column_geometry(lib, ctx)}
     clocks = sampler.stop()
     faces_total = dist.sum(float(T * args.steps))
     head = min(results, key=lambda k: results[k]["t_max"])
@@ -687,7 +695,7 @@ def run_ensemble(args, dist: Dist, rank: int, world: int, local_rank: int, membe
         "kernels": kernels,
         "variants": {k: {"value": faces_total / v["t_max"], "ms_per_step": v["t_max"] / args.steps * 1e3,
                          "speedup_vs_plain_fp64": results["plain_fp64"]["t_max"] / v["t_max"],
-                         **summary(v["stats"])} for k, v in results.items()},
+                         "column_geometry": v["geometry"], **summary(v["stats"])} for k, v in results.items()},
         "clocks": clocks,
     }
 

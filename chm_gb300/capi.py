@@ -120,7 +120,7 @@ EXPORTS = [
     "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr", "pbsm3d_mesh_read",
     "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error", "pbsm3d_get_debug",
     "pbsm3d_set_stations", "pbsm3d_uniform_wind", "pbsm3d_math_eval",
-    "pbsm3d_arm_wait_timeout_test",
+    "pbsm3d_arm_wait_timeout_test", "pbsm3d_set_column_geometry", "pbsm3d_get_column_geometry",
 ]
 
 _lib = None
@@ -209,6 +209,10 @@ def load(path: Path | None = None):
     lib.pbsm3d_deposition_solve_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, vp, C.c_double, C.c_int32,
                                                     C.POINTER(C.c_int32), _dp]
     lib.pbsm3d_deposition_solve_noalloc.restype = C.c_int
+    lib.pbsm3d_set_column_geometry.argtypes = [vp, C.c_int32, C.c_int32]
+    lib.pbsm3d_set_column_geometry.restype = C.c_int
+    lib.pbsm3d_get_column_geometry.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    lib.pbsm3d_get_column_geometry.restype = C.c_int
     lib.pbsm3d_arm_wait_timeout_test.argtypes = [vp, C.c_int32, C.c_double]
     lib.pbsm3d_arm_wait_timeout_test.restype = C.c_int
     lib.pbsm3d_math_eval.argtypes = [C.c_int32, C.c_int64, vp, vp, vp]

@@ -140,6 +140,7 @@ void pbsm3d_config_defaults(pbsm3d_config* cfg) {
     cfg->fetch_I = 0.06;
     cfg->dep_tol = 1e-10;
     cfg->inner_tol = 1e-4;
+    cfg->autotune = 1;
 }
 
 const char* pbsm3d_last_error(const pbsm3d_ctx* ctx) {
@@ -751,6 +752,29 @@ void pbsm3d_destroy(pbsm3d_ctx* h) {
 int pbsm3d_set_profiling(pbsm3d_ctx* h, int32_t on) {
     if (!h) return PBSM3D_ERR_INVALID_ARG;
     h->c.prof = on != 0;
+    return 0;
+}
+
+int pbsm3d_set_column_geometry(pbsm3d_ctx* h, int32_t width, int32_t lanes) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    Ctx& c = h->c;
+    for (int gi = 0; gi < kNumColGeoms; ++gi)
+        if (kColGeom[gi].W == width && kColGeom[gi].LC == lanes) {
+            if (c.graph && c.geom != gi) graph_destroy(c);  // captured with the old geometry
+            c.geom = gi;
+            c.tuned = true;
+            return 0;
+        }
+    c.err = "column geometry must be width 64, 128 or 256 and lanes 1, 2 or 4";
+    return PBSM3D_ERR_INVALID_ARG;
+}
+
+int pbsm3d_get_column_geometry(const pbsm3d_ctx* h, int32_t* width, int32_t* lanes, int32_t* tuned) {
+    if (!h) return PBSM3D_ERR_INVALID_ARG;
+    const Ctx& c = h->c;
+    if (width) *width = kColGeom[c.geom].W;
+    if (lanes) *lanes = kColGeom[c.geom].LC;
+    if (tuned) *tuned = c.tuned ? 1 : 0;
     return 0;
 }
 

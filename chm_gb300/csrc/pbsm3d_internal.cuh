@@ -33,6 +33,12 @@ constexpr int kMaxLayers = 64;
 constexpr int kMaxTerms = 4;
 constexpr int kMaxMembers = 256;
 constexpr int kMaxCgBlocks = 1024;  // blocks of a cooperative CG launch
+// launch geometries of the column kernels: W faces a block, LC lanes a face column
+struct ColGeom {
+    int W, LC;
+};
+constexpr int kNumColGeoms = 9;
+extern const ColGeom kColGeom[kNumColGeoms];
 
 // Configuration scalars every kernel sees (passed by value).
 struct Params {
@@ -270,8 +276,7 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow);
 void graph_destroy(Ctx& c);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);
-int tuned_waves(Ctx& c);             // autotuner: the choice cached for this shape (0 = none)
-void apply_waves(Ctx& c, int mult);
+int tuned_geometry(Ctx& c);          // autotuner: the choice cached for this shape (-1 = none)
 int configure_cg(Ctx& c);
 int jacobi_sweep(Ctx& c, cudaStream_t s, const double* xi, double* xo);
 // mlp.cu
@@ -331,18 +336,16 @@ struct Ctx {
     MScal* ms_host = nullptr;
     double* tile_part = nullptr;  // [4][ntiles]
     std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
-    int grid_col[2] = {1, 1};  // BiCGStab column-solve kernels, [FP64, FP32]: one wave
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
     int grid_cg[2] = {1, 1};   // the tile CG's kernels (k_scg_x, k_scg_q): one wave
-    // co-resident blocks per SM of the polynomial-preconditioner step over
-    // those of the column kernels: its grid is the column kernels' scaled so
-    // that it too is one wave (no second, partial wave)
-    double neu_scale[2] = {1.0, 1.0};
-    // autotuner (cfg.autotune): one-wave grids, the candidate being timed,
-    // per-iteration times of the candidates; tuned = a choice is in force
-    int wave_col[2] = {1, 1}, wave_red[2] = {1, 1};
+    // column kernels (p, s, polynomial step): one wave of blocks at each
+    // geometry, [p/s or polynomial step][FP64, FP32][geometry]; the geometry
+    // in force; the autotuner's state (cfg.autotune): next candidate, best
+    // time per iteration and per face of each, tuned = a choice is in force
+    int grid_geom[2][2][kNumColGeoms] = {};
+    int geom = 0;
     int tune_cand = 0;
-    float tune_ms[3] = {0, 0, 0};
+    float tune_ms[kNumColGeoms] = {};
     bool tuned = false;
     // ledger partial sums
     double* ledger;    // device [8]

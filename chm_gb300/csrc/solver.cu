@@ -36,37 +36,55 @@
 namespace pbsm {
 
 // ---------------------------------------------------------------- launch-geometry autotuner
-// The batched Krylov kernels walk their tiles with grid-stride loops, so the
-// grid is free: the tuner times 1, 2 and 4 waves of co-resident blocks on the
-// first suspension solve's own iterations (one polling chunk each) and keeps
-// the fastest.  The choice is remembered per problem shape for the process.
-constexpr int kTuneWaves[3] = {1, 2, 4};
+// The column kernels (k_bicg_p, k_bicg_s, k_bicg_neu) run at one of nine
+// geometries: slices of W = 256, 128 or 64 faces a block, with 1, 2 or 4
+// lanes per face column (blocks of W x lanes threads).  Their arithmetic
+// does not depend on the geometry (bit-identical results), so the tuner
+// times the candidates on the first solves' own iterations, one iteration
+// each (the default timed first and last, its faster time counts), and keeps
+// the fastest if it beats the default by more than 2%.  The choice is
+// remembered per problem shape for the process.  The reduction kernels
+// (lateral gathers with their dot products, x update) keep one fixed
+// geometry: theirs decides the order of the floating-point sums.
+const ColGeom kColGeom[kNumColGeoms] = {{256, 1}, {128, 1}, {64, 1}, {256, 2}, {128, 2},
+                                        {64, 2},  {256, 4}, {128, 4}, {64, 4}};
+// timing order: the default first and again last
+constexpr int kTuneOrder[kNumColGeoms + 1] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 0};
 
 struct TuneKey {
     int64_t Tp;
-    int L, n, mixed;
+    int L, n, mixed, neumann;
     bool operator<(const TuneKey& o) const {
-        return std::tie(Tp, L, n, mixed) < std::tie(o.Tp, o.L, o.n, o.mixed);
+        return std::tie(Tp, L, n, mixed, neumann) < std::tie(o.Tp, o.L, o.n, o.mixed, o.neumann);
     }
 };
 static std::mutex g_tune_mu;
 static std::map<TuneKey, int> g_tune;
 
-static TuneKey tune_key(const Ctx& c) { return TuneKey{c.P.Tp, c.P.L, c.tiles.n, c.P.mixed}; }
-
-int tuned_waves(Ctx& c) {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(tune_key(c));
-    if (it == g_tune.end()) return 0;
-    return it->second;
+static TuneKey tune_key(const Ctx& c) {
+    return TuneKey{c.P.Tp, c.P.L, c.tiles.n, c.P.mixed, c.cfg.neumann > 0 ? 1 : 0};
 }
 
-void apply_waves(Ctx& c, int mult) {
-    for (int k = 0; k < 2; ++k) {
-        c.grid_col[k] = std::min(c.wave_col[k] * mult, std::max(1, c.tiles.ntiles));
-        c.grid_red[k] = std::min(c.wave_red[k] * mult, c.grid_faces);  // within the partials workspace
-    }
+int tuned_geometry(Ctx& c) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(c));
+    return it == g_tune.end() ? -1 : it->second;
+}
+
+// One more candidate timed (ms per iteration per active face); after the
+// last, the choice.
+static void tune_record(Ctx& c, float ms) {
+    const int g = kTuneOrder[c.tune_cand];
+    if (c.tune_ms[g] <= 0.f || ms < c.tune_ms[g]) c.tune_ms[g] = ms;
+    if (++c.tune_cand < kNumColGeoms + 1) return;
+    int best = 0;
+    for (int k = 1; k < kNumColGeoms; ++k)
+        if (c.tune_ms[k] < c.tune_ms[best]) best = k;
+    if (!(c.tune_ms[best] < 0.98f * c.tune_ms[0])) best = 0;
+    c.geom = best;
     c.tuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_key(c)] = best;
 }
 
 namespace {
@@ -131,21 +149,20 @@ struct LatFace<float> {
 
 enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3 };
 
-// z = B^{-1} u for one column, u already in smem column g[z*bd + tid].
+// z = B^{-1} u for one column, u already in smem column g[z*bd + col].
 template <typename V>
-__device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V* zout) {
-    const int bd = blockDim.x, tid = threadIdx.x;
+__device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V* zout, int bd, int col) {
     V prev = 0;
     for (int z = 0; z < op.L; ++z) {
         const int64_t r = (int64_t)z * op.Tp + i;
-        V gz = g[z * bd + tid] - op.l[r] * prev;
-        g[z * bd + tid] = gz;
+        V gz = g[z * bd + col] - op.l[r] * prev;
+        g[z * bd + col] = gz;
         prev = gz;
     }
     V y = 0;
     for (int z = op.L - 1; z >= 0; --z) {
         const int64_t r = (int64_t)z * op.Tp + i;
-        y = (g[z * bd + tid] - op.up[r] * y) * op.ib[r];
+        y = (g[z * bd + col] - op.up[r] * y) * op.ib[r];
         zout[r] = y;
     }
 }
@@ -168,6 +185,18 @@ __device__ __forceinline__ TileRange block_tiles(const Tiles& tl) {
     const int64_t n = tl.nact_dev ? *tl.nact_dev : tl.nact, g = gridDim.x, b = blockIdx.x;
     return TileRange{(int)(b * n / g), (int)((b + 1) * n / g)};
 }
+// Slices of the column kernels: each active tile (<= kBlock faces) is cut
+// into S = kBlock / W slices of W faces; block b owns the contiguous run
+// [u0, u1) of the nact * S slices.  A slice's face column is handled by LC
+// lanes: thread t takes face t % W of the slice, lane t / W.
+struct SliceRange {
+    int u0, u1;
+};
+__device__ __forceinline__ SliceRange block_slices(const Tiles& tl, int S) {
+    const int64_t n = (int64_t)(tl.nact_dev ? *tl.nact_dev : tl.nact) * S, g = gridDim.x, b = blockIdx.x;
+    return SliceRange{(int)(b * n / g), (int)((b + 1) * n / g)};
+}
+
 // End (exclusive, in active-list positions) of the segment that starts at
 // position a with tile t of member m.
 __device__ __forceinline__ int segment_end(const Tiles& tl, const TileRange& br, int a, int t, int m) {
@@ -243,51 +272,83 @@ __device__ __forceinline__ void member_stop(MScal* ms, int m, int st, Scalars* s
     if (atomicAdd(&sc->counter[2], 1u) + 1u == (unsigned)n) sc->done = DONE_CONVERGED;
 }
 
+// The column kernels (p, s and the polynomial-preconditioner step) compute
+// each row from that row's own inputs and each column's Thomas solve in one
+// thread, so the launch geometry -- slice width W and lanes per face column
+// LC -- changes which thread does the work, never the arithmetic: every
+// geometry gives bit-identical results (the autotuner relies on it).  With
+// LC > 1 the lanes split the column's layers for the row-wise part, and lane
+// 0 then runs the Thomas solve from shared memory.
+template <int LC>
+struct ColLanes {
+    int f, lane;
+    __device__ __forceinline__ explicit ColLanes(int W) : f(threadIdx.x & (W - 1)), lane(threadIdx.x / W) {}
+};
+template <>
+struct ColLanes<1> {
+    int f, lane;
+    __device__ __forceinline__ explicit ColLanes(int) : f(threadIdx.x), lane(0) {}
+};
+// slices of a tile: S = kBlock / W = 1 << sh
+__device__ __forceinline__ int slice_shift(int W) { return W == kBlock ? 0 : W == kBlock / 2 ? 1 : 2; }
+
 // p = r + beta (p - omega v); zp = B^{-1} p
-template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_p(Op<V> op, Tiles tl, const V* __restrict__ r, V* __restrict__ p,
-                                                   const V* __restrict__ v, V* __restrict__ zp,
-                                                   const MScal* __restrict__ ms) {
+template <typename V, int LC>
+__global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_p(Op<V> op, Tiles tl, int W, const V* __restrict__ r,
+                                                        V* __restrict__ p, const V* __restrict__ v,
+                                                        V* __restrict__ zp, const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
-    const TileRange br = block_tiles(tl);
-    for (int a = br.a0; a < br.a1; ++a) {
-        const int t = tl.act[a], m = tl.member[t];
+    const ColLanes<LC> cl(W);
+    const int sh = slice_shift(W);
+    const SliceRange br = block_slices(tl, 1 << sh);
+    for (int u = br.u0; u < br.u1; ++u) {
+        const int t = tl.act[u >> sh], m = tl.member[t];
         if (ms[m].done) continue;
-        const int64_t i = tl.start[t] + threadIdx.x;
-        if (i >= tl.start[t + 1]) continue;
+        const int64_t i = tl.start[t] + (int64_t)(u & ((1 << sh) - 1)) * W + cl.f;
+        const bool valid = i < tl.start[t + 1];
+        if (LC == 1 && !valid) continue;  // no block barrier with one lane
         const V beta = (V)ms[m].beta, omega = (V)ms[m].omega;
-        for (int z = 0; z < op.L; ++z) {
-            const int64_t k = (int64_t)z * op.Tp + i;
-            const V pk = r[k] + beta * (p[k] - omega * v[k]);
-            p[k] = pk;
-            g[z * blockDim.x + threadIdx.x] = pk;
-        }
-        column_solve(op, i, g, zp);
+        if (valid)
+            for (int z = cl.lane; z < op.L; z += LC) {
+                const int64_t k = (int64_t)z * op.Tp + i;
+                const V pk = r[k] + beta * (p[k] - omega * v[k]);
+                p[k] = pk;
+                g[z * W + cl.f] = pk;
+            }
+        if (LC > 1) __syncthreads();
+        if (valid && cl.lane == 0) column_solve(op, i, g, zp, W, cl.f);
+        if (LC > 1) __syncthreads();
     }
 }
 
 // s = r - alpha v; zs = B^{-1} s
-template <typename V>
-__global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* __restrict__ r,
-                                                   const V* __restrict__ v, V* __restrict__ s, V* __restrict__ zs,
-                                                   const MScal* __restrict__ ms) {
+template <typename V, int LC>
+__global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op<V> op, Tiles tl, int W, const V* __restrict__ r,
+                                                        const V* __restrict__ v, V* __restrict__ s,
+                                                        V* __restrict__ zs, const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
-    const TileRange br = block_tiles(tl);
-    for (int a = br.a0; a < br.a1; ++a) {
-        const int t = tl.act[a], m = tl.member[t];
+    const ColLanes<LC> cl(W);
+    const int sh = slice_shift(W);
+    const SliceRange br = block_slices(tl, 1 << sh);
+    for (int u = br.u0; u < br.u1; ++u) {
+        const int t = tl.act[u >> sh], m = tl.member[t];
         if (ms[m].done) continue;
-        const int64_t i = tl.start[t] + threadIdx.x;
-        if (i >= tl.start[t + 1]) continue;
+        const int64_t i = tl.start[t] + (int64_t)(u & ((1 << sh) - 1)) * W + cl.f;
+        const bool valid = i < tl.start[t + 1];
+        if (LC == 1 && !valid) continue;  // no block barrier with one lane
         const V alpha = (V)ms[m].alpha;
-        for (int z = 0; z < op.L; ++z) {
-            const int64_t k = (int64_t)z * op.Tp + i;
-            const V sk = r[k] - alpha * v[k];
-            s[k] = sk;
-            g[z * blockDim.x + threadIdx.x] = sk;
-        }
-        column_solve(op, i, g, zs);
+        if (valid)
+            for (int z = cl.lane; z < op.L; z += LC) {
+                const int64_t k = (int64_t)z * op.Tp + i;
+                const V sk = r[k] - alpha * v[k];
+                s[k] = sk;
+                g[z * W + cl.f] = sk;
+            }
+        if (LC > 1) __syncthreads();
+        if (valid && cl.lane == 0) column_solve(op, i, g, zs, W, cl.f);
+        if (LC > 1) __syncthreads();
     }
 }
 
@@ -296,35 +357,42 @@ __global__ void __launch_bounds__(kBlock) k_bicg_s(Op<V> op, Tiles tl, const V* 
 // Linear Systems, section 12.3): w = u - N zin, zout = B^{-1} w.  Starting
 // from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
 // so the lateral kernels that follow take w in place of u.
-template <typename V, bool WRITE_W>
-__global__ void __launch_bounds__(kBlock, 6) k_bicg_neu(Op<V> op, Tiles tl, const V* __restrict__ u,
-                                                     const V* __restrict__ zin, V* __restrict__ w,
-                                                     V* __restrict__ zout, const MScal* __restrict__ ms) {
+template <typename V, bool WRITE_W, int LC>
+__global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
+    k_bicg_neu(Op<V> op, Tiles tl, int W, const V* __restrict__ u, const V* __restrict__ zin, V* __restrict__ w,
+               V* __restrict__ zout, const MScal* __restrict__ ms) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
-    const TileRange br = block_tiles(tl);
-    for (int a = br.a0; a < br.a1; ++a) {
-        const int t = tl.act[a], m = tl.member[t];
+    const ColLanes<LC> cl(W);
+    const int sh = slice_shift(W);
+    const SliceRange br = block_slices(tl, 1 << sh);
+    for (int uu = br.u0; uu < br.u1; ++uu) {
+        const int t = tl.act[uu >> sh], m = tl.member[t];
         if (ms[m].done) continue;
-        const int64_t i = tl.start[t] + threadIdx.x;
-        if (i >= tl.start[t + 1]) continue;
-        const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
-        // FP32: the face's six coupling constants stay in registers over the
-        // column (40 a thread with four layers in flight, no spills)
-        const LatFace<V> lf(op, i);
+        const int64_t i = tl.start[t] + (int64_t)(uu & ((1 << sh) - 1)) * W + cl.f;
+        const bool valid = i < tl.start[t + 1];
+        if (LC == 1 && !valid) continue;  // no block barrier with one lane
+        if (valid) {
+            const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
+            // FP32: the face's six coupling constants stay in registers over the
+            // column (40 a thread with four layers in flight, no spills)
+            const LatFace<V> lf(op, i);
 #pragma unroll 4
-        for (int z = 0; z < op.L; ++z) {
-            const int64_t base = (int64_t)z * op.Tp;
-            const int64_t k = base + i;
-            const auto la = lf.row(k);
-            V wk = u[k];
-            if (n0 >= 0) wk -= la[0] * zin[base + n0];
-            if (n1 >= 0) wk -= la[1] * zin[base + n1];
-            if (n2 >= 0) wk -= la[2] * zin[base + n2];
-            if (WRITE_W) w[k] = wk;  // only the last step's w is read (by the lateral kernel)
-            g[z * blockDim.x + threadIdx.x] = wk;
+            for (int z = cl.lane; z < op.L; z += LC) {
+                const int64_t base = (int64_t)z * op.Tp;
+                const int64_t k = base + i;
+                const auto la = lf.row(k);
+                V wk = u[k];
+                if (n0 >= 0) wk -= la[0] * zin[base + n0];
+                if (n1 >= 0) wk -= la[1] * zin[base + n1];
+                if (n2 >= 0) wk -= la[2] * zin[base + n2];
+                if (WRITE_W) w[k] = wk;  // only the last step's w is read (by the lateral kernel)
+                g[z * W + cl.f] = wk;
+            }
         }
-        column_solve(op, i, g, zout);
+        if (LC > 1) __syncthreads();
+        if (valid && cl.lane == 0) column_solve(op, i, g, zout, W, cl.f);
+        if (LC > 1) __syncthreads();
     }
 }
 
@@ -579,7 +647,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_sweep(Op<double> op, const do
             if (n2 >= 0) u -= op.lat[2 * op.R + k] * xi[base + n2];
             g[z * blockDim.x + threadIdx.x] = u;
         }
-        column_solve(op, i, g, xo);
+        column_solve(op, i, g, xo, (int)blockDim.x, (int)threadIdx.x);
     }
 }
 
@@ -1178,22 +1246,62 @@ int64_t active_faces_of(const Ctx& c, const std::vector<char>& conv) {
 // K steps of the polynomial preconditioner on u, whose B^-1 u the column
 // kernel wrote to z0 (chosen so that the last step writes zfinal); returns
 // the vector the lateral kernel adds N zfinal to (u, or the last u - N z).
+// Launch of a column kernel at geometry gi: grid = one wave of its own
+// residency (c.grid_geom), capped by the slices to do (all tiles' in graph
+// mode, where the active count lives on the device).
 template <typename V>
-const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gc, size_t smem, const V* u,
-                        V* zfinal, V* w, V* ztmp, const MScal* ms, int64_t rows, bool prof) {
+static int col_grid(const Ctx& c, const Tiles& tl, int gi, bool neu) {
+    const int S = kBlock / kColGeom[gi].W;
+    const int units = (tl.nact_dev ? tl.ntiles : tl.nact) * S;
+    return std::max(1, std::min(c.grid_geom[neu ? 1 : 0][sizeof(V) == 4][gi], units));
+}
+
+template <typename V>
+void launch_col_p(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* r, V* p, const V* v,
+                  V* zp, const MScal* ms) {
+    const ColGeom G = kColGeom[gi];
+    const int grid = col_grid<V>(c, tl, gi, false);
+    const size_t smem = (size_t)c.P.L * G.W * sizeof(V);
+    if (G.LC == 1) k_bicg_p<V, 1><<<grid, G.W, smem, s>>>(op, tl, G.W, r, p, v, zp, ms);
+    else if (G.LC == 2) k_bicg_p<V, 2><<<grid, 2 * G.W, smem, s>>>(op, tl, G.W, r, p, v, zp, ms);
+    else k_bicg_p<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, p, v, zp, ms);
+}
+
+template <typename V>
+void launch_col_s(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* r, const V* v, V* sv,
+                  V* zs, const MScal* ms) {
+    const ColGeom G = kColGeom[gi];
+    const int grid = col_grid<V>(c, tl, gi, false);
+    const size_t smem = (size_t)c.P.L * G.W * sizeof(V);
+    if (G.LC == 1) k_bicg_s<V, 1><<<grid, G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
+    else if (G.LC == 2) k_bicg_s<V, 2><<<grid, 2 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
+    else k_bicg_s<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
+}
+
+template <typename V, bool WRITE_W>
+static void launch_neu_step(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* u,
+                            const V* zin, V* w, V* zout, const MScal* ms) {
+    const ColGeom G = kColGeom[gi];
+    const int grid = col_grid<V>(c, tl, gi, true);
+    const size_t smem = (size_t)c.P.L * G.W * sizeof(V);
+    if (G.LC == 1) k_bicg_neu<V, WRITE_W, 1><<<grid, G.W, smem, s>>>(op, tl, G.W, u, zin, w, zout, ms);
+    else if (G.LC == 2) k_bicg_neu<V, WRITE_W, 2><<<grid, 2 * G.W, smem, s>>>(op, tl, G.W, u, zin, w, zout, ms);
+    else k_bicg_neu<V, WRITE_W, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, u, zin, w, zout, ms);
+}
+
+template <typename V>
+const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* u, V* zfinal,
+                        V* w, V* ztmp, const MScal* ms, int64_t rows, bool prof) {
     const int K = c.cfg.neumann;
     V* a = (K & 1) ? ztmp : zfinal;
     V* b = (K & 1) ? zfinal : ztmp;
-    // the column kernels' grid gc (a wave of theirs, or the tuned multiple)
-    // scaled to this kernel's residency
-    gc = std::max(1, std::min(gc, (int)(gc * c.neu_scale[sizeof(V) == 4] + 0.5)));
     for (int j = 0; j < K; ++j) {
         const bool last = j == K - 1;
         if (prof) prof_begin(c, s);
         if (last)
-            k_bicg_neu<V, true><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
+            launch_neu_step<V, true>(c, s, op, tl, gi, u, a, w, b, ms);
         else
-            k_bicg_neu<V, false><<<gc, kBlock, smem, s>>>(op, tl, u, a, w, b, ms);
+            launch_neu_step<V, false>(c, s, op, tl, gi, u, a, w, b, ms);
         // per row u, z in, z out, the lateral couplings (3 bands, or u_z in
         // FP32), 3 column factors, w on the last step; per face the ids (and
         // the FP32 couplings' 6 constants)
@@ -1204,6 +1312,7 @@ const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl
     }
     return K > 0 ? w : u;
 }
+
 template <typename V>
 V* neumann_first(Ctx& c, V* zfinal, V* ztmp) { return (c.cfg.neumann & 1) ? ztmp : zfinal; }
 
@@ -1211,7 +1320,6 @@ template <typename V, typename X>
 int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V* r, V* rh, V* p, V* v, V* sv,
                         V* tv, V* zp, V* zs, V* nw, V* nz, int& iters) {
     Op<V> op = make_op<V>(c);
-    const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
     double* part = c.tile_part;
     const int64_t sv_ = sizeof(V), sx = sizeof(X);
     std::vector<char> active(c.tiles.n);
@@ -1221,7 +1329,6 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         if (rc) return rc;
     }
     Tiles tl = c.tiles;
-    int gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
     int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
     int chunk = 4;
     int before = 0;
@@ -1239,12 +1346,11 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
     while (true) {
         const int64_t rows = act * c.P.L;
         const bool timing = !c.tuned;
+        // the column kernels' geometry: the candidate under test (one
+        // iteration a chunk while tuning), else the chosen one
+        const int gi = timing ? kTuneOrder[c.tune_cand] : c.geom;
         if (timing) {
-            // this chunk runs the candidate under test, at a fixed length
-            const int mult = kTuneWaves[c.tune_cand];
-            gc = std::max(1, std::min(c.wave_col[sizeof(V) == 4] * mult, tl.nact));
-            gr = std::max(1, std::min(std::min(c.wave_red[sizeof(V) == 4] * mult, c.grid_faces), tl.nact));
-            chunk = 4;
+            chunk = 1;
             if (!te[0]) {
                 PBSM_CUDA_TRY(cudaEventCreate(&te[0]));
                 PBSM_CUDA_TRY(cudaEventCreate(&te[1]));
@@ -1253,16 +1359,16 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         }
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
-            k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, neumann_first(c, zp, nz), ms);
+            launch_col_p<V>(c, s, op, tl, gi, r, p, v, neumann_first(c, zp, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
-            const V* up = launch_neumann<V>(c, s, op, tl, gc, smem, p, zp, nw, nz, ms, rows, true);
+            const V* up = launch_neumann<V>(c, s, op, tl, gi, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
-            k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, neumann_first(c, zs, nz), ms);
+            launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
-            const V* us = launch_neumann<V>(c, s, op, tl, gc, smem, sv, zs, nw, nz, ms, rows, true);
+            const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
             prof_end(c, s, PBSM3D_K_BICG_T, rows * (3 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
@@ -1276,24 +1382,11 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         const int ran = c.sc_host->iter - before;
         before = c.sc_host->iter;
         if (timing && ran == chunk) {
-            // a full chunk: its time per iteration decides
-            // per iteration and per active face: in an ensemble, later chunks
-            // carry fewer members
+            // a full chunk: its time per iteration and per active face (in
+            // an ensemble later chunks carry fewer members) decides
             float ms = 0;
             PBSM_CUDA_TRY(cudaEventElapsedTime(&ms, te[0], te[1]));
-            c.tune_ms[c.tune_cand] = ms / chunk / (float)std::max<int64_t>(1, act);
-            if (++c.tune_cand == 3) {
-                int best = 0;
-                for (int k = 1; k < 3; ++k)
-                    if (c.tune_ms[k] < c.tune_ms[best]) best = k;
-                apply_waves(c, kTuneWaves[best]);
-                std::lock_guard<std::mutex> lk(g_tune_mu);
-                g_tune[tune_key(c)] = kTuneWaves[best];
-            }
-        }
-        if (c.tuned) {
-            gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
-            gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+            tune_record(c, ms / chunk / (float)std::max<int64_t>(1, act));
         }
         // launches after the last member stopped returned at once: not counted
         const int idle = chunk - ran - (c.sc_host->done && ran < chunk ? 1 : 0);
@@ -1311,12 +1404,11 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             if (changed) {
                 if ((rc = set_active(c, s, active))) return rc;
                 tl = c.tiles;
-                gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.nact));
                 gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
             }
             act = active_faces(c);
         }
-        chunk = std::min(16, chunk * 2);
+        chunk = c.tuned ? std::min(16, chunk * 2) : 1;
     }
     for (auto e : te)
         if (e) cudaEventDestroy(e);
@@ -1331,27 +1423,46 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
 int configure_solver_kernels(Ctx& c) {
     const int s64 = c.P.L * kBlock * 8, s32 = c.P.L * kBlock * 4;
     PBSM_CUDA_TRY(cudaFuncSetAttribute(k_jacobi_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_p<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_s<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s64));
-    PBSM_CUDA_TRY(cudaFuncSetAttribute(k_bicg_neu<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, s32));
-    // one full wave of co-resident blocks per kernel (grid-stride loops do the rest)
     int dev = 0, sms = 0;
     PBSM_CUDA_TRY(cudaGetDevice(&dev));
     PBSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    auto wave = [&](const void* f, int smem, int& out) -> int {
+    // one full wave of co-resident blocks per kernel (grid-stride loops do the rest)
+    auto wave_of = [&](const void* f, int block, int smem, int& out) -> int {
         int per = 0;
-        PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, kBlock, smem));
-        out = std::max(1, std::min(c.grid_faces, sms * std::max(per, 1)));
+        PBSM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, block, smem));
+        out = std::max(1, sms * std::max(per, 1));
         return 0;
     };
     int rc;
-    if ((rc = wave((const void*)k_bicg_p<double>, s64, c.grid_col[0]))) return rc;
-    if ((rc = wave((const void*)k_bicg_p<float>, s32, c.grid_col[1]))) return rc;
+    // the column kernels at every geometry: shared-memory opt-in and one wave
+    auto col_kernels = [&](auto vtag, int prec, int smax) -> int {
+        using V = decltype(vtag);
+        const void* kp[3] = {(const void*)k_bicg_p<V, 1>, (const void*)k_bicg_p<V, 2>, (const void*)k_bicg_p<V, 4>};
+        const void* ks[3] = {(const void*)k_bicg_s<V, 1>, (const void*)k_bicg_s<V, 2>, (const void*)k_bicg_s<V, 4>};
+        const void* kn0[3] = {(const void*)k_bicg_neu<V, false, 1>, (const void*)k_bicg_neu<V, false, 2>,
+                              (const void*)k_bicg_neu<V, false, 4>};
+        const void* kn1[3] = {(const void*)k_bicg_neu<V, true, 1>, (const void*)k_bicg_neu<V, true, 2>,
+                              (const void*)k_bicg_neu<V, true, 4>};
+        for (int l = 0; l < 3; ++l)
+            for (const void* f : {kp[l], ks[l], kn0[l], kn1[l]})
+                PBSM_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+        for (int gi = 0; gi < kNumColGeoms; ++gi) {
+            const ColGeom G = kColGeom[gi];
+            const int l = G.LC == 1 ? 0 : G.LC == 2 ? 1 : 2;
+            const int smem = c.P.L * G.W * (int)sizeof(V);
+            int r1;
+            if ((r1 = wave_of(kp[l], G.W * G.LC, smem, c.grid_geom[0][prec][gi]))) return r1;
+            if ((r1 = wave_of(kn0[l], G.W * G.LC, smem, c.grid_geom[1][prec][gi]))) return r1;
+        }
+        return 0;
+    };
+    if ((rc = col_kernels(double{}, 0, s64))) return rc;
+    if ((rc = col_kernels(float{}, 1, s32))) return rc;
+    auto wave = [&](const void* f, int smem, int& out) -> int {
+        int r1 = wave_of(f, kBlock, smem, out);
+        out = std::min(out, c.grid_faces);
+        return r1;
+    };
     if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
     if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
     {
@@ -1363,21 +1474,15 @@ int configure_solver_kernels(Ctx& c) {
         if ((rc = wave((const void*)k_scg_q<float>, 0, gq[1]))) return rc;
         for (int k = 0; k < 2; ++k) c.grid_cg[k] = std::min(gx[k], gq[k]);
     }
-    {
-        int gn[2];
-        if ((rc = wave((const void*)k_bicg_neu<double, false>, s64, gn[0]))) return rc;
-        if ((rc = wave((const void*)k_bicg_neu<float, false>, s32, gn[1]))) return rc;
-        for (int k = 0; k < 2; ++k) c.neu_scale[k] = std::min(1.0, (double)gn[k] / (double)c.grid_col[k]);
-    }
-    for (int k = 0; k < 2; ++k) {
-        c.wave_col[k] = c.grid_col[k];
-        c.wave_red[k] = c.grid_red[k];
-    }
+    c.geom = 0;
     c.tuned = !c.cfg.autotune;
     if (!c.tuned) {
         // a choice made for this shape by an earlier context of the process
-        const int mult = tuned_waves(c);
-        if (mult > 0) apply_waves(c, mult);
+        const int gi = tuned_geometry(c);
+        if (gi >= 0) {
+            c.geom = gi;
+            c.tuned = true;
+        }
     }
     return 0;
 }
@@ -2397,15 +2502,13 @@ template <typename V, typename X>
 void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, Scalars* sc, X* x, V* r, V* rh,
                             V* p, V* v, V* sv, V* tv, V* zp, V* zs, V* nw, V* nz) {
     Op<V> op = make_op<V>(c);
-    const size_t smem = (size_t)c.P.L * kBlock * sizeof(V);
-    const int gc = std::max(1, std::min(c.grid_col[sizeof(V) == 4], tl.ntiles));
     const int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
     double* part = c.tile_part;
-    k_bicg_p<V><<<gc, kBlock, smem, s>>>(op, tl, r, p, v, neumann_first(c, zp, nz), ms);
-    const V* up = launch_neumann<V>(c, s, op, tl, gc, smem, p, zp, nw, nz, ms, 0, false);
+    launch_col_p<V>(c, s, op, tl, c.geom, r, p, v, neumann_first(c, zp, nz), ms);
+    const V* up = launch_neumann<V>(c, s, op, tl, c.geom, p, zp, nw, nz, ms, 0, false);
     k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
-    k_bicg_s<V><<<gc, kBlock, smem, s>>>(op, tl, r, v, sv, neumann_first(c, zs, nz), ms);
-    const V* us = launch_neumann<V>(c, s, op, tl, gc, smem, sv, zs, nw, nz, ms, 0, false);
+    launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms);
+    const V* us = launch_neumann<V>(c, s, op, tl, c.geom, sv, zs, nw, nz, ms, 0, false);
     k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
     k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
 }

@@ -126,9 +126,12 @@ typedef struct pbsm3d_config {
                                bit 1 = no block-Jacobi sweep after the learned guess; 0 */
     int32_t graph;          /* 1: run each step as one CUDA-graph launch with device-side control
                                (conditional nodes; no host round trip inside the step); 0 */
-    int32_t autotune;       /* 1: the first suspension solve times the batched Krylov kernels at 1, 2
-                               and 4 waves of blocks per SM on its own iterations and keeps the
-                               fastest (shared by later contexts of the same shape); 0 */
+    int32_t autotune;       /* 1: the first suspension solves time the column kernels (the vector
+                               updates fused with the column Thomas solves, and the polynomial-
+                               preconditioner steps) at nine launch geometries -- slices of 256, 128
+                               or 64 faces a block, 1, 2 or 4 threads a face column -- one iteration
+                               each, and keep the fastest (shared by later contexts of the same
+                               shape).  Every geometry gives bit-identical results; 1 */
     int32_t neumann;        /* order K (0..9) of the polynomial preconditioner of the suspension
                                Krylov solve: M^-1 = B^-1 sum_{j<=K} (-N B^-1)^j, B the column
                                (tridiagonal) blocks, N the lateral couplings; 0 = B^-1 alone.
@@ -481,6 +484,17 @@ int pbsm3d_mlp_gemm_bf16(const uint16_t* A, const uint16_t* B, float* C, int32_t
  * the step records an event pair around each launch on the context's stream
  * and fills pbsm3d_stats.kern_*. */
 int pbsm3d_set_profiling(pbsm3d_ctx* ctx, int32_t on);
+
+/*
+ * Launch geometry of the suspension solve's column kernels.  No counterpart
+ * in the reference (its Krylov solve is Belos/Tpetra's, LinearAlgebra.cpp:
+ * 228-252).  set: fix the geometry (width 256, 128 or 64 faces a block;
+ * lanes 1, 2 or 4 threads a face column), which also ends autotuning; the
+ * results do not depend on it, bit for bit.  get: the geometry in force and
+ * whether it is final (tuned = 1) or still being tuned.
+ */
+int pbsm3d_set_column_geometry(pbsm3d_ctx* ctx, int32_t width, int32_t lanes);
+int pbsm3d_get_column_geometry(const pbsm3d_ctx* ctx, int32_t* width, int32_t* lanes, int32_t* tuned);
 
 /*
  * Test of the device-side wait limits.  No counterpart in the reference,
