@@ -174,6 +174,8 @@ VARIANTS = {
     # the polynomial (truncated Neumann) preconditioners: order 5 (or K) in the
     # suspension solve, order 1 in the deposition CG
     "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
+    "plain_fp64_neumann3": {"precision": capi.FP64, "neumann": 3, "dep_neumann": 1},
+    "plain_fp64_neumann7": {"precision": capi.FP64, "neumann": 7, "dep_neumann": 1},
     "fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "neumann": 5,
                                "dep_neumann": 1},
     # the same step as one CUDA-graph launch with device-side control
