@@ -176,6 +176,7 @@ VARIANTS = {
     "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
     "plain_fp64_neumann3": {"precision": capi.FP64, "neumann": 3, "dep_neumann": 1},
     "plain_fp64_neumann7": {"precision": capi.FP64, "neumann": 7, "dep_neumann": 1},
+    "plain_fp64_neumann9": {"precision": capi.FP64, "neumann": 9, "dep_neumann": 1},
     "fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "neumann": 5,
                                "dep_neumann": 1},
     # the same step as one CUDA-graph launch with device-side control
@@ -808,8 +809,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="tri1m", choices=sorted(synth.CONFIGS))
-    ap.add_argument("--variants", default="plain_fp64,plain_fp64_neumann5,fp64_previous_neumann5,"
-                                          "graph_fp64_previous_neumann5,mixed,previous,learned,graph_previous,"
+    ap.add_argument("--variants", default="plain_fp64,plain_fp64_neumann5,plain_fp64_neumann7,plain_fp64_neumann9,"
+                                          "fp64_previous_neumann5,graph_fp64_previous_neumann5,mixed,previous,"
+                                          "learned,graph_previous,"
                                           "previous_neumann5,graph_previous_neumann5,graph_learned_neumann5",
                     help="comma list of %s; the fastest FP64 form meeting residual 1e-8 is the headline, the "
                          "fastest mixed form is reported beside it" % ",".join(VARIANTS))

@@ -82,6 +82,10 @@ void free_all(Ctx& c) {
     c.ms_host = nullptr;
     if (c.stream) cudaStreamDestroy(c.stream);
     c.stream = nullptr;
+    if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+    c.copy_stream = nullptr;
+    for (auto& e : c.copy_ev)
+        if (e) cudaEventDestroy(e);
 }
 
 // SoA [3][Tp] from row-major [n][3]
@@ -292,6 +296,16 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     }
     for (auto& e : c.ev) cudaEventCreate(&e);
     for (auto& e : c.user_ev) cudaEventCreate(&e);
+    // outputs that are final before the deposition solve go to the host on a
+    // second stream while the solve runs
+    if (cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.copy_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c.copy_ev[1], cudaEventDisableTiming) != cudaSuccess) {
+        g_create_error = "cudaStreamCreate failed";
+        free_all(c);
+        delete h;
+        return PBSM3D_ERR_CUDA;
+    }
     if (cudaMallocHost(&c.sc_host, sizeof(Scalars)) != cudaSuccess ||
         cudaMallocHost(&c.n_slow_host, sizeof(int)) != cudaSuccess ||
         cudaMallocHost(&c.ms_host, sizeof(MScal) * members.size()) != cudaSuccess) {
@@ -902,12 +916,17 @@ static int copy_in(Ctx& c, double* dst, const double* src, int on_device) {
                                   c.stream));
     return 0;
 }
-static int copy_out(Ctx& c, double* dst, const double* src, int on_device) {
+static int copy_out(Ctx& c, double* dst, const double* src, int on_device, cudaStream_t s = nullptr) {
     if (!dst) return 0;
     PBSM_CUDA_TRY(cudaMemcpyAsync(dst, src, c.P.T * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                  c.stream));
+                                  s ? s : c.stream));
     return 0;
 }
+
+// Output k of the step (pbsm3d_outputs order) is final once the suspension
+// post has run: Qsalt, Qsusp, Qsubl, Qsubl_mass, sum_subl, blowing-snow
+// probability (and c).  The others change in the deposition update.
+static bool final_after_post(int k) { return k <= 4 || k == 8; }
 
 static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0;
@@ -975,6 +994,15 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
                                    (f->p_snow_hours ? 1 : 0));
 
     double susp_rhs_max = 0.0, dep_rhs_max = 0.0;
+    bool early_out = false;  // some host outputs already copied on the second stream
+    // whatever path leaves the step, no copy into the caller's buffers outlives it
+    struct CopyGuard {
+        Ctx& c;
+        const bool& on;
+        ~CopyGuard() {
+            if (on) cudaStreamSynchronize(c.copy_stream);
+        }
+    } copy_guard{c, early_out};
     // graph mode; with the autotuner on, the first step runs host-driven so
     // that the geometry is tuned before the graph is built
     if (c.cfg.graph && c.tuned) {
@@ -1043,9 +1071,36 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         c.dep_target_scale2 = 1.0;
         if (c.Mb.n > 1 && (rc = member_presence(c, s, 1))) return rc;
         if (c.deposition_present) {
+            if (out && !out->on_device) {
+                // host outputs already final: copied on the second stream
+                // while the deposition solve runs
+                double* outs[9] = {out->Qsalt, out->Qsusp, out->Qsubl, out->Qsubl_mass, out->sum_subl,
+                                   out->drift_mass, out->sum_drift, out->pbsm_more_than_avail,
+                                   out->blowingsnow_probability};
+                const double* srcs[9] = {c.S.Qsalt, c.S.Qsusp, c.S.Qsubl, c.S.Qsubl_mass, c.S.sum_subl,
+                                         c.S.drift_mass, c.S.sum_drift, c.S.more, c.S.bsp};
+                PBSM_CUDA_TRY(cudaEventRecord(c.copy_ev[0], s));
+                PBSM_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.copy_ev[0], 0));
+                early_out = true;
+                for (int k = 0; k < 9; ++k)
+                    if (final_after_post(k) && (rc = copy_out(c, outs[k], srcs[k], 0, c.copy_stream))) break;
+                if (!rc && out->c)
+                    rc = cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L,
+                                           cudaMemcpyDeviceToHost, c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
+                if (!rc) rc = cudaEventRecord(c.copy_ev[1], c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
+                if (rc) {
+                    cudaStreamSynchronize(c.copy_stream);
+                    c.err = "output copy failed";
+                    return rc;
+                }
+            }
             rc = solve_deposition(c, s, st);
             PBSM_CUDA_TRY(cudaGetLastError());
-            if (rc) return rc;
+            if (rc) {
+                // no copy into the caller's buffers outlives the call
+                if (early_out) cudaStreamSynchronize(c.copy_stream);
+                return rc;
+            }
         }
         PBSM_CUDA_TRY(cudaEventRecord(c.ev[5], s));
         launch_update(c, s);
@@ -1061,7 +1116,10 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         const double* srcs[9] = {c.S.Qsalt, c.S.Qsusp, c.S.Qsubl, c.S.Qsubl_mass, c.S.sum_subl,
                                  c.S.drift_mass, c.S.sum_drift, c.S.more, c.S.bsp};
         for (int k = 0; k < 9; ++k) {
-            if ((rc = copy_out(c, outs[k], srcs[k], od))) return rc;
+            if (!(early_out && final_after_post(k)) && (rc = copy_out(c, outs[k], srcs[k], od))) {
+                if (early_out) cudaStreamSynchronize(c.copy_stream);
+                return rc;
+            }
             if (outs[k] && !od) d2h += c.P.T * 8;
         }
         if (c.S.sub) {
@@ -1074,13 +1132,15 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         }
         if (out->c) {
             // layer-major with stride n_faces (the device stride is the padded Tp)
-            PBSM_CUDA_TRY(cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L,
-                                            od ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+            if (!early_out)
+                PBSM_CUDA_TRY(cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L,
+                                                od ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
             if (!od) d2h += c.P.T * c.P.L * 8;
         }
     }
     double ledger[8] = {0};
     PBSM_CUDA_TRY(cudaMemcpyAsync(ledger, c.ledger, 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (early_out) PBSM_CUDA_TRY(cudaStreamWaitEvent(s, c.copy_ev[1], 0));
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[7], s));
     PBSM_CUDA_TRY(cudaStreamSynchronize(s));
     if (st) {

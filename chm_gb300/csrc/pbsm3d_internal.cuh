@@ -369,6 +369,8 @@ struct Ctx {
     // the five CG vectors, [11][Tp]
     float* dep32 = nullptr;
     cudaStream_t stream;
+    cudaStream_t copy_stream = nullptr;  // host copies of outputs final before the deposition solve
+    cudaEvent_t copy_ev[2] = {nullptr, nullptr};
     cudaEvent_t ev[16];
     cudaEvent_t user_ev[16];
     std::vector<void*> allocations;

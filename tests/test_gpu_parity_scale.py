@@ -66,6 +66,8 @@ LEDGER_TOL = 1e-10
 FORMS = {
     "plain_fp64": {},
     "plain_fp64_neumann5": {"precision": capi.FP64, "neumann": 5, "dep_neumann": 1},
+    "plain_fp64_neumann7": {"precision": capi.FP64, "neumann": 7, "dep_neumann": 1},
+    "plain_fp64_neumann9": {"precision": capi.FP64, "neumann": 9, "dep_neumann": 1},
     "graph_fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                      "neumann": 5, "dep_neumann": 1},
     "graph_mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
