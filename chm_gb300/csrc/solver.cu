@@ -1371,7 +1371,10 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
-            prof_end(c, s, PBSM3D_K_BICG_T, rows * (3 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
+            // u, s, t and the gathered zs a row (u is s itself without the
+            // polynomial preconditioner, the last step's w with it)
+            prof_end(c, s, PBSM3D_K_BICG_T,
+                     rows * ((c.cfg.neumann > 0 ? 4 : 3) + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
             k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_X, rows * (2 * sx + 6 * sv_));
