@@ -23,7 +23,7 @@ class ChmMesh:
                                   C.byref(h))
         if rc != 0:
             raise capi.MeshError(f"pbsm3d_mesh_read: {capi.STATUS_NAMES.get(rc, rc)}: "
-                                 f"{lib.pbsm3d_mesh_last_error().decode()}")
+                                 f"{lib.pbsm3d_mesh_last_error().decode(errors='replace')}")
         try:
             d = capi.MeshDesc()
             lib.pbsm3d_mesh_describe(h, C.byref(d))

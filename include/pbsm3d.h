@@ -412,8 +412,13 @@ int pbsm3d_uniform_wind(pbsm3d_ctx* ctx, const double* station_U_R, const double
  * table).  Geographic meshes return PBSM3D_ERR_UNSUPPORTED; malformed files
  * PBSM3D_ERR_BAD_MESH with the reason in pbsm3d_mesh_last_error().
  * pbsm3d_mesh_describe fills a description whose arrays point into the mesh
- * (valid until pbsm3d_mesh_free).  The HDF5 mesh and partition formats are not
- * read.
+ * (valid until pbsm3d_mesh_free).  CHM's HDF5 mesh and parameter files
+ * (triangulation.cpp:724-1035, 1237-1383: /mesh/vertex, /mesh/elem,
+ * /mesh/neighbor, root attributes "/mesh/...", /parameters/<name>) are read
+ * too, either path of the pair, chosen by the file's signature, with no HDF5
+ * library (the subset of the format those files use).  One file of a
+ * multi-process partition (is_partition, or cell_global_id out of file
+ * order) is refused: the step runs on the whole mesh.
  */
 /*
  * Diagnostics of the last step by the names debug_output gives them in the
