@@ -467,7 +467,9 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 "ledger_residual_max": float(np.max([abs(s["ledger_residual"]) for s in sts])),
                 "ms_coefficients": float(np.mean([s["ms_coefficients"] for s in sts])),
                 "ms_susp_solve": float(np.mean([s["ms_susp_solve"] for s in sts])),
-                "ms_dep_solve": float(np.mean([s["ms_dep_solve"] for s in sts]))}
+                "ms_post": float(np.mean([s["ms_post"] for s in sts])),
+                "ms_dep_solve": float(np.mean([s["ms_dep_solve"] for s in sts])),
+                "ms_update": float(np.mean([s["ms_update"] for s in sts]))}
 
     def worst(errs):
         return {k: max(v[k] for v in errs.values()) for k in ("max_rel", "l2_rel", "elem_rel_floored")}

@@ -1157,12 +1157,21 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         st->dep_rel_residual = c.dep_relres;
         st->susp_rhs_max = susp_rhs_max;
         st->dep_rhs_max = dep_rhs_max;
-        st->ms_coefficients = ev_ms(c.ev[1], c.ev[2]);
-        st->ms_susp_solve = ev_ms(c.ev[2], c.ev[3]);
-        st->ms_post = ev_ms(c.ev[3], c.ev[4]);
+        if (c.cfg.graph && c.tuned && c.graph_phases) {
+            // one graph launch: the phases from the device stamps in the graph
+            st->ms_coefficients = c.graph_phase_ms[0];
+            st->ms_susp_solve = c.graph_phase_ms[1];
+            st->ms_post = c.graph_phase_ms[2];
+            st->ms_dep_solve = c.graph_phase_ms[3];
+            st->ms_update = c.graph_phase_ms[4];
+        } else {
+            st->ms_coefficients = ev_ms(c.ev[1], c.ev[2]);
+            st->ms_susp_solve = ev_ms(c.ev[2], c.ev[3]);
+            st->ms_post = ev_ms(c.ev[3], c.ev[4]);
+            st->ms_dep_solve = ev_ms(c.ev[4], c.ev[5]);
+            st->ms_update = ev_ms(c.ev[5], c.ev[6]);
+        }
         st->ms_dep_assembly = 0;
-        st->ms_dep_solve = ev_ms(c.ev[4], c.ev[5]);
-        st->ms_update = ev_ms(c.ev[5], c.ev[6]);
         st->ms_total = ev_ms(c.ev[0], c.ev[7]);
         if (c.deposition_present) {
             st->ledger_divergence = ledger[0];

@@ -322,6 +322,11 @@ struct Ctx {
     const int* graph_dep_flag = nullptr;  // set only while the graph is captured
     struct StepGraph* graph = nullptr;
     double graph_rhs_max[2] = {0, 0};  // graph mode: ||rhs||_inf of the two systems
+    // graph mode with profiling: the step's phase times from device stamps
+    // (assembly, suspension solve, post + deposition assembly, deposition
+    // solve, update)
+    bool graph_phases = false;
+    double graph_phase_ms[5] = {0, 0, 0, 0, 0};
     // device-resident snow state (pbsm3d_set_snow): swe and depth live in Fo.swe / Fo.sd
     bool snow_state = false;
     double drift_density = 300.0;

@@ -2000,6 +2000,8 @@ namespace {
 
 constexpr int kGuardMax = 200000;
 
+constexpr int kGraphStamps = 6;
+
 struct StepCtl {
     int ok, err;  // err: PBSM3D_ERR_* of the failure, 0 while ok
     int susp_present, dep_present;
@@ -2007,9 +2009,24 @@ struct StepCtl {
     int guard, n_active;
     int kernels;  // kernels the graph executed this step (tallied by the controllers)
     double susp_relres, dep_relres, susp_rhs_max, dep_rhs_max, gamma_sum;
+    // with profiling on: %globaltimer at the phase boundaries (start, after
+    // the assembly, the suspension solve, the post and deposition assembly,
+    // the deposition solve, the update); 0 where a phase did not run
+    unsigned long long stamp[kGraphStamps];
     int conv[kMaxMembers], dconv[kMaxMembers];
     double bb[kMaxMembers], dbb[kMaxMembers];
 };
+
+// A phase boundary of the step graph, stamped from the device clock by a
+// one-thread kernel (kernel nodes are allowed inside conditional bodies,
+// event-record nodes are not).  Slot 0 also clears the others.
+__global__ void k_stamp(StepCtl* ctl, int slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (slot == 0)
+        for (int k = 1; k < kGraphStamps; ++k) ctl->stamp[k] = 0;
+    ctl->stamp[slot] = t;
+}
 
 // The conditional handles of the step graph.  A form without a warm start
 // or without the mixed deposition refinement has no node for those handles;
@@ -2461,6 +2478,7 @@ struct StepGraph {
     StepCtl* ctl_host = nullptr;  // pinned
     int* nact = nullptr;         // device
     cudaStream_t cap[8] = {};
+    bool profiled = false;       // captured with the phase stamps
 };
 
 namespace {
@@ -2664,7 +2682,13 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
     int bad = 0;
     PBSM_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     c.graph_dep_flag = &G.ctl->dep_present;
+    // phase stamps when the context profiles (the host path's per-launch
+    // events have no graph equivalent)
+    auto stamp = [&](cudaStream_t st, int slot) {
+        if (prof) k_stamp<<<1, 1, 0, st>>>(G.ctl, slot);
+    };
     {
+        stamp(s, 0);
         cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s);
         if (c.Mb.n > 1) {
             cudaMemsetAsync(c.Mb.rhs_max, 0, c.Mb.n * 8, s);
@@ -2673,6 +2697,7 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
         launch_assemble_suspension(c, s);
         k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, c.asm_kernels, h);
         if (c.Mb.n > 1) launch_member_mask_norm(c, s, 0);
+        stamp(s, 1);
         CondBody ok1;
         bad |= ok1.begin(s, G.cap[1], h.h[H_OK1], cudaGraphCondTypeIf);
         if (!bad) {
@@ -2696,6 +2721,7 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
                                            : capture_suspension<double>(c, G, h, 2, tl);
                 bad |= susp.end();
             }
+            stamp(t, 2);
             k_ctl_mid<<<1, 32, 0, t>>>(G.ctl, h);
             CondBody ok2;
             bad |= ok2.begin(t, G.cap[2], h.h[H_OK2], cudaGraphCondTypeIf);
@@ -2704,17 +2730,20 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
                 launch_post_and_assemble_deposition(c, u);
                 k_ctl_dep_begin<<<1, 32, 0, u>>>(G.ctl, c.sc, c.Mb, c.Mb.n, own_snow ? 2 : 1, h);
                 if (c.Mb.n > 1) launch_member_mask_norm(c, u, 1);
+                stamp(u, 3);
                 CondBody dep;
                 bad |= dep.begin(u, G.cap[3], h.h[H_DEP], cudaGraphCondTypeIf);
                 if (!bad) {
                     bad |= capture_deposition(c, G, h, 3, tl);
                     bad |= dep.end();
                 }
+                stamp(u, 4);
                 CondBody ok3;
                 bad |= ok3.begin(u, G.cap[3], h.h[H_OK3], cudaGraphCondTypeIf);
                 if (!bad) {
                     launch_update(c, G.cap[3]);
                     if (own_snow) launch_consume_drift(c, G.cap[3]);
+                    stamp(G.cap[3], 5);
                     bad |= ok3.end();
                 }
                 bad |= ok2.end();
@@ -2742,6 +2771,7 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
     G.graph = g;
     G.exec = exec;
     G.own_snow = own_snow;
+    G.profiled = prof;
     G.dt = c.P.dt;
     return 0;
 }
@@ -2774,7 +2804,7 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
         }
     }
     StepGraph& G = *c.graph;
-    if (!G.exec || G.dt != c.P.dt || G.own_snow != own_snow) {
+    if (!G.exec || G.dt != c.P.dt || G.own_snow != own_snow || G.profiled != c.prof) {
         if (G.exec) {
             cudaGraphExecDestroy(G.exec);
             cudaGraphDestroy(G.graph);
@@ -2804,6 +2834,18 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
     c.launches = k.kernels;  // kernels the one graph launch executed
     c.graph_rhs_max[0] = k.susp_rhs_max;
     c.graph_rhs_max[1] = k.dep_rhs_max;
+    // phase times from the stamps (a phase that did not run counts 0; the
+    // next stamp that did run closes the span)
+    for (int p = 0; p < kGraphStamps - 1; ++p) c.graph_phase_ms[p] = 0.0;
+    c.graph_phases = G.profiled && k.stamp[0] != 0;
+    if (c.graph_phases) {
+        unsigned long long prev = k.stamp[0];
+        for (int p = 1; p < kGraphStamps; ++p)
+            if (k.stamp[p] >= prev && k.stamp[p] != 0) {
+                c.graph_phase_ms[p - 1] = (double)(k.stamp[p] - prev) * 1e-6;
+                prev = k.stamp[p];
+            }
+    }
     if (k.err) {
         c.err = k.err == PBSM3D_ERR_NAN_INPUT ? "NaN in an assembled system (check the forcing)"
                                               : "a Krylov solve failed to converge";

@@ -433,3 +433,24 @@ def test_native_mesh_reader_end_to_end(cuda_lib, oracle_lib, tmp_path):
     for k in FIELDS:
         assert relerr(out[k], ref[k]) < FIELD_TOL, (k, relerr(out[k], ref[k]))
     m.close()
+
+
+@pytest.mark.parametrize("solver", [{}, {"precision": 1, "warm_start": 1, "neumann": 5, "dep_neumann": 1}],
+                         ids=["fp64", "mixed_previous_neumann5"])
+def test_graph_phase_times(cuda_lib, solver):
+    """With profiling on, a graph-mode step (one launch) reports its phases --
+    assembly, suspension solve, post with the deposition assembly, deposition
+    solve, update -- from device-clock stamps at the phase boundaries; they
+    are positive and add up to about the step."""
+    w = synth.Workload(2048, 3500.0, seed=9)
+    m = gpu_module(w.mesh, 5, graph=1, **solver)
+    m.set_profiling(True)
+    for s in range(5):
+        m.run(w.forcing(s), 3600.0)
+        w.apply_drift(m.state()["drift_mass"])
+    st = m.last_stats
+    assert st["susp_iters"] > 0 and st["deposition_present"]
+    phases = [st[k] for k in ("ms_coefficients", "ms_susp_solve", "ms_post", "ms_dep_solve", "ms_update")]
+    assert all(p > 0 for p in phases), phases
+    assert 0.5 * st["ms_total"] <= sum(phases) <= 1.05 * st["ms_total"], (phases, st["ms_total"])
+    m.close()
