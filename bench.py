@@ -182,6 +182,9 @@ VARIANTS = {
     # the same step as one CUDA-graph launch with device-side control
     "graph_fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                      "neumann": 5, "dep_neumann": 1},
+    "graph_fp64_neumann7": {"precision": capi.FP64, "graph": 1, "neumann": 7, "dep_neumann": 1},
+    "graph_fp64_previous_neumann7": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                     "neumann": 7, "dep_neumann": 1},
     # -- FP32 inner solves inside FP64 iterative refinement
     "mixed": {"precision": capi.MIXED},
     "previous": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS},
@@ -372,15 +375,14 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     errors = {n: field_errors(fields[n], fields[ref_form]) for n in names if n != ref_form}
 
     # ---- e2e: host pinned forcing in, host outputs back, copies timed, the
-    # measured form's context alone on the GPU (as a user runs it)
+    # measured form's context alone on the GPU (as a user runs it), on the
+    # same steps of the same snow trajectory as the device-resident timing:
+    # a fresh context from the initial snow state, warmed up the same way
+    # (the warm-up steps with host buffers too)
     def e2e_of(name):
-        for k in [k for k in ctxs if k != name]:
+        for k in list(ctxs):
             lib.pbsm3d_destroy(ctxs.pop(k))
-        if name not in ctxs:  # a fresh context, warmed up like the timed one
-            ctxs[name] = make_ctx(VARIANTS[name])
-            for s in range(args.warmup):
-                step(ctxs[name], fdescs[s], o_dev)
-            torch.cuda.synchronize()
+        ctxs[name] = make_ctx(VARIANTS[name])
         ctx = ctxs[name]
         pin_f = [{k: torch.from_numpy(a).pin_memory() for k, a in fs.items()} for fs in host_forcing]
         pin_out = {k: torch.empty(T, dtype=torch.float64).pin_memory() for k in OUT_NAMES}
@@ -395,10 +397,12 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 setattr(f, k, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)))
             f.on_device = 0
             hdescs.append(f)
-        step(ctx, hdescs[0], o_host)
-        t_e2e_dev, _ = timed(ctx, hdescs, o_host, 2)
+        for s in range(args.warmup):
+            step(ctx, hdescs[s], o_host)
+        torch.cuda.synchronize()
+        t_e2e_dev, sts = timed(ctx, hdescs, o_host, 2)
         lib.pbsm3d_destroy(ctxs.pop(name))
-        return dist.max(t_e2e_dev)
+        return dist.max(t_e2e_dev), sts
 
     # per-kernel figures come from host-driven forms (a graph replay has no
     # per-launch events): the fastest profiled form of each precision
@@ -410,8 +414,8 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     mixed_prof = profiled_twin([mixed_head]) if mixed_head else None
     if mixed_head and not mixed_prof:
         mixed_prof = profiled_twin([n for n in names if not is_fp64(n)])
-    t_e2e = e2e_of(head)
-    t_e2e_mixed = e2e_of(mixed_head) if mixed_head else None
+    t_e2e, e2e_stats = e2e_of(head)
+    t_e2e_mixed, e2e_stats_mixed = e2e_of(mixed_head) if mixed_head else (None, None)
     h2d = 8 * T * len(host_forcing[0])
     d2h = 8 * T * len(OUT_NAMES)
     for c in ctxs.values():
@@ -471,6 +475,12 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 "ms_dep_solve": float(np.mean([s["ms_dep_solve"] for s in sts])),
                 "ms_update": float(np.mean([s["ms_update"] for s in sts]))}
 
+    def phase_means(sts):
+        # the step's phases (the graph forms' device-clock stamps, the host
+        # path's events) and the part outside them: host copies and waits
+        ks = ("ms_coefficients", "ms_susp_solve", "ms_post", "ms_dep_solve", "ms_update", "ms_total")
+        return {k: round(float(np.mean([s[k] for s in sts])), 3) for k in ks}
+
     def worst(errs):
         return {k: max(v[k] for v in errs.values()) for k in ("max_rel", "l2_rel", "elem_rel_floored")}
 
@@ -485,7 +495,8 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                   "1e-8; deposition CG to 1e-10; FP64 arithmetic",
         "parallelism": f"replicas x{world}",
         "e2e": {"value": faces_total / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "variant": head},
+                "d2h_bytes_per_step": d2h, "variant": head, "ms_per_step": t_e2e / args.steps * 1e3,
+                "phases_ms": phase_means(e2e_stats)},
         "gpu_launches": int(sum(s["gpu_launches"] for s in stats)),
         "roofline": roof,
         "step_roofline": step_roof,
@@ -495,7 +506,8 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
             "variant": mixed_head, "dtype": "f64+f32", "value": faces_total / results[mixed_head]["t_max"],
             "ms_per_step": results[mixed_head]["t_max"] / args.steps * 1e3,
             "e2e": {"value": faces_total / t_e2e_mixed, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": t_e2e_mixed / args.steps * 1e3,
+                    "phases_ms": phase_means(e2e_stats_mixed)},
             "speedup_vs_fp64_headline": t_max / results[mixed_head]["t_max"],
             "field_error_vs": ref_form, "field_error": errors.get(mixed_head),
             "roofline": mroof, "step_roofline": mstep_roof, "kernels": mkernels},
@@ -812,7 +824,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="tri1m", choices=sorted(synth.CONFIGS))
     ap.add_argument("--variants", default="plain_fp64,plain_fp64_neumann5,plain_fp64_neumann7,plain_fp64_neumann9,"
-                                          "fp64_previous_neumann5,graph_fp64_previous_neumann5,mixed,previous,"
+                                          "fp64_previous_neumann5,graph_fp64_previous_neumann5,graph_fp64_neumann7,"
+                                          "graph_fp64_previous_neumann7,mixed,previous,"
                                           "learned,graph_previous,"
                                           "previous_neumann5,graph_previous_neumann5,graph_learned_neumann5",
                     help="comma list of %s; the fastest FP64 form meeting residual 1e-8 is the headline, the "

@@ -928,6 +928,53 @@ static int copy_out(Ctx& c, double* dst, const double* src, int on_device, cudaS
 // probability (and c).  The others change in the deposition update.
 static bool final_after_post(int k) { return k <= 4 || k == 8; }
 
+// Whether the outputs that are final after the post can be copied to the
+// host while the step goes on: host outputs in page-locked memory (a copy
+// into pageable memory returns only when it is done, so queued early it
+// would hold the host, and the rest of the step, until then).
+static bool early_copies(const pbsm3d_outputs* out) {
+    if (!out || out->on_device) return false;
+    const void* ptrs[7] = {out->Qsalt, out->Qsusp, out->Qsubl, out->Qsubl_mass, out->sum_subl,
+                           out->blowingsnow_probability, out->c};
+    bool any = false;
+    for (const void* p : ptrs) {
+        if (!p) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+        any = true;
+    }
+    return any;
+}
+
+// Queue the host copies of the outputs that are final after the post (and
+// c) on the second stream, after the work queued so far on s; copy_ev[1]
+// marks their end and `early` records that they are in flight.
+static int copy_final_outputs(Ctx& c, cudaStream_t s, const pbsm3d_outputs* out, bool& early) {
+    double* outs[9] = {out->Qsalt, out->Qsusp, out->Qsubl, out->Qsubl_mass, out->sum_subl,
+                       out->drift_mass, out->sum_drift, out->pbsm_more_than_avail, out->blowingsnow_probability};
+    const double* srcs[9] = {c.S.Qsalt, c.S.Qsusp, c.S.Qsubl, c.S.Qsubl_mass, c.S.sum_subl,
+                             c.S.drift_mass, c.S.sum_drift, c.S.more, c.S.bsp};
+    PBSM_CUDA_TRY(cudaEventRecord(c.copy_ev[0], s));
+    PBSM_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.copy_ev[0], 0));
+    early = true;
+    int rc = 0;
+    for (int k = 0; k < 9; ++k)
+        if (final_after_post(k) && (rc = copy_out(c, outs[k], srcs[k], 0, c.copy_stream))) break;
+    if (!rc && out->c)
+        rc = cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L, cudaMemcpyDeviceToHost,
+                               c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
+    if (!rc) rc = cudaEventRecord(c.copy_ev[1], c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
+    if (rc) {
+        cudaStreamSynchronize(c.copy_stream);
+        c.err = "output copy failed";
+    }
+    return rc;
+}
+
 static float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0;
     cudaEventElapsedTime(&ms, a, b);
@@ -1006,9 +1053,13 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     // graph mode; with the autotuner on, the first step runs host-driven so
     // that the geometry is tuned before the graph is built
     if (c.cfg.graph && c.tuned) {
-        // the whole device part of the step as one CUDA-graph launch
+        // the device part of the step as the step graph's two launches; host
+        // outputs final after the post are copied while part 2 runs (on a
+        // failed step they may hold the post's fields or the last step's)
         PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
-        if ((rc = graph_step(c, s, own_snow))) return rc;
+        std::function<int()> between;
+        if (early_copies(out)) between = [&]() { return copy_final_outputs(c, s, out, early_out); };
+        if ((rc = graph_step(c, s, own_snow, between))) return rc;
         for (int k = 2; k <= 6; ++k) PBSM_CUDA_TRY(cudaEventRecord(c.ev[k], s));
         susp_rhs_max = c.graph_rhs_max[0];
         dep_rhs_max = c.graph_rhs_max[1];
@@ -1071,29 +1122,9 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         c.dep_target_scale2 = 1.0;
         if (c.Mb.n > 1 && (rc = member_presence(c, s, 1))) return rc;
         if (c.deposition_present) {
-            if (out && !out->on_device) {
-                // host outputs already final: copied on the second stream
-                // while the deposition solve runs
-                double* outs[9] = {out->Qsalt, out->Qsusp, out->Qsubl, out->Qsubl_mass, out->sum_subl,
-                                   out->drift_mass, out->sum_drift, out->pbsm_more_than_avail,
-                                   out->blowingsnow_probability};
-                const double* srcs[9] = {c.S.Qsalt, c.S.Qsusp, c.S.Qsubl, c.S.Qsubl_mass, c.S.sum_subl,
-                                         c.S.drift_mass, c.S.sum_drift, c.S.more, c.S.bsp};
-                PBSM_CUDA_TRY(cudaEventRecord(c.copy_ev[0], s));
-                PBSM_CUDA_TRY(cudaStreamWaitEvent(c.copy_stream, c.copy_ev[0], 0));
-                early_out = true;
-                for (int k = 0; k < 9; ++k)
-                    if (final_after_post(k) && (rc = copy_out(c, outs[k], srcs[k], 0, c.copy_stream))) break;
-                if (!rc && out->c)
-                    rc = cudaMemcpy2DAsync(out->c, c.P.T * 8, c.A.x, c.P.Tp * 8, c.P.T * 8, c.P.L,
-                                           cudaMemcpyDeviceToHost, c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
-                if (!rc) rc = cudaEventRecord(c.copy_ev[1], c.copy_stream) == cudaSuccess ? 0 : PBSM3D_ERR_CUDA;
-                if (rc) {
-                    cudaStreamSynchronize(c.copy_stream);
-                    c.err = "output copy failed";
-                    return rc;
-                }
-            }
+            // host outputs already final: copied on the second stream while
+            // the deposition solve runs
+            if (early_copies(out) && (rc = copy_final_outputs(c, s, out, early_out))) return rc;
             rc = solve_deposition(c, s, st);
             PBSM_CUDA_TRY(cudaGetLastError());
             if (rc) {

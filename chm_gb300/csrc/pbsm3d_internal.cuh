@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -272,7 +273,9 @@ void launch_uniform_wind(Ctx& c, cudaStream_t s, double* U_R, double* vw_dir);
 int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 // graph mode: the device part of a step as one CUDA-graph launch (built on
 // first use); fills the iteration/residual fields of c like the host path
-int graph_step(Ctx& c, cudaStream_t s, bool own_snow);
+// One step as the two launches of the step graph; `between` (may be empty)
+// runs on the host after part 1 is queued and before part 2 is.
+int graph_step(Ctx& c, cudaStream_t s, bool own_snow, const std::function<int()>& between);
 void graph_destroy(Ctx& c);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);

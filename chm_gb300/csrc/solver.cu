@@ -820,10 +820,14 @@ __device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __re
 // is bound by those gathered loads, not by the all-reduce it saves); and an
 // all-reduce whose partials are staged in shared memory for one warp to
 // sum, 2.65 ms (its 24 KB of shared memory is L1 the gathers lose).
+//
+// `dyn`, when set, holds the stopping target (target2, relative to (b, b))
+// and the iteration limit in device memory, written by a controller kernel
+// of the step graph; otherwise tol and maxit are the launch's own.
 template <typename V>
 __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm)
     k_cg_persistent(int64_t Tp, DepSys<V> D, const int32_t* __restrict__ nbr, double* partials, unsigned* flags,
-                    int* err, Scalars* sc, double tol, int maxit, GridWait gw) {
+                    int* err, Scalars* sc, double tol, int maxit, GridWait gw, const MScal* dyn) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     unsigned epoch = 0;
@@ -884,7 +888,8 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm)
     }
     double rho = t3[0];
     const double bb = t3[2];
-    const double target2 = tol * tol * bb;
+    const double target2 = (dyn ? dyn->target2 : tol * tol) * bb;
+    if (dyn) maxit = dyn->maxit;
     int status = 0, it = 0;
     double rr = bb;
     if (bb == 0.0) status = 1;
@@ -1721,7 +1726,8 @@ static int launch_cg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* s
         c.test_limit_ns = 0;
         c.test_withhold = -1;
     }
-    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit, &gw};
+    const MScal* dyn = nullptr;
+    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit, &gw, &dyn};
     PBSM_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_cg_persistent<V>, dim3(blocks), dim3(kCgBlock), args,
                                               0, s));
     int rc = read_scalars(c, s, sc);
@@ -1993,8 +1999,9 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
 // Krylov loops stop at their iteration limits, the refinement loops after
 // 64 (suspension) or 8 (deposition) sweeps, and a guard counter over all
 // loop bodies ends every loop and records an error past kGuardMax.  The
-// deposition solve runs as per-member tile CG (no cooperative launch inside
-// the graph).
+// deposition solve of one mesh is the host path's cooperative CG kernel (its
+// own loop, bounded by its iteration limit and its waits); an ensemble's is
+// the per-member tile CG.
 
 namespace {
 
@@ -2307,6 +2314,18 @@ __global__ void k_ctl_mid(StepCtl* ctl, Handles h) {
     hset(h, H_OK2, ctl->ok ? 1u : 0u);
 }
 
+// Start of the step graph's second part: part 1's outcome in the control
+// block opens this part's conditional nodes (the deposition solve when the
+// step is ok and a deposition system is present, the update when ok).
+__global__ void k_ctl_part2(StepCtl* ctl, Handles h) {
+    if (threadIdx.x != 0) return;
+    ctl->kernels += 1;
+    const bool ok = ctl->ok != 0;
+    hset(h, H_OK2, ok ? 1u : 0u);
+    hset(h, H_DEP, ok && ctl->dep_present ? 1u : 0u);
+    hset(h, H_OK3, ok ? 1u : 0u);
+}
+
 // Deposition CG states (plain: target tol relative to ||b_m||; mixed inner:
 // itol relative to ||r_m||), all members active unless converged.
 __global__ void k_ctl_dcg_init(StepCtl* ctl, MScal* ms, Scalars* sc, Tiles tl, int32_t* act, int* nact, double tol,
@@ -2347,7 +2366,10 @@ __global__ void k_ctl_dres_init(StepCtl* ctl, MScal* msR, Tiles tl, int32_t* act
 }
 
 // End of the plain deposition solve: every member's true residual.
-__global__ void k_ctl_dep_end(StepCtl* ctl, const MScal* msR, const Scalars* sc, int n, double tol, Handles h) {
+// cg_err: the cooperative CG's error word (null for the tile CG); set when
+// one of its bounded grid waits ran out.
+__global__ void k_ctl_dep_end(StepCtl* ctl, const MScal* msR, const Scalars* sc, int n, double tol,
+                              const int* cg_err, Handles h) {
     if (threadIdx.x != 0) return;
     double worst = 0.0;
     bool ok = true;
@@ -2359,10 +2381,11 @@ __global__ void k_ctl_dep_end(StepCtl* ctl, const MScal* msR, const Scalars* sc,
     ctl->dep_relres = sqrt(worst);
     ctl->dep_iters = sc->iter;
     ctl->dep_sweeps = 1;
-    ctl->kernels += 1;
-    if (!ok) {
+    ctl->kernels += cg_err ? 2 : 1;  // this (and the cooperative CG)
+    const bool timed_out = cg_err && *(volatile const int*)cg_err;
+    if (!ok || timed_out) {
         ctl->ok = 0;
-        ctl->err = PBSM3D_ERR_NOT_CONVERGED;
+        ctl->err = timed_out ? PBSM3D_ERR_CUDA : PBSM3D_ERR_NOT_CONVERGED;
         hset(h, H_OK3, 0u);
     }
 }
@@ -2386,8 +2409,10 @@ __global__ void k_ctl_dmix_init(StepCtl* ctl, MScal* msR, Tiles tl, int32_t* act
 
 // Mixed deposition, after a residual pass: convergence per member, then the
 // next FP32 inner solve's states or the end of the refinement.
+// `solve_kernels`: the kernels of one inner solve before its first loop
+// pass (zero, CG start, first q), or 1 for the cooperative CG.
 __global__ void k_ctl_dmix_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Tiles tl, int32_t* act,
-                                 int* nact, double tol, int maxit, Handles h) {
+                                 int* nact, double tol, int maxit, int solve_kernels, Handles h) {
     __shared__ int active[kMaxMembers];
     __shared__ int s_all, s_go;
     const int n = tl.n;
@@ -2444,15 +2469,17 @@ __global__ void k_ctl_dmix_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* s
         sc->counter[2] = (unsigned)nd;
         sc->iter = 0;
         ctl->n_active = n - nd;
-        ctl->kernels += 3;  // zero, CG start, first q
+        ctl->kernels += solve_kernels;
         hset(h, H_DOUTER, 1u);
         hset(h, H_DINNER, 1u);
         hset(h, H_DLOOP, 1u);
     }
 }
 
-// Mixed deposition: end of an inner solve.
-__global__ void k_ctl_dmix_sweep_end(StepCtl* ctl, const Scalars* sc, MScal* msR, Tiles tl, int32_t* act, int* nact) {
+// Mixed deposition: end of an inner solve (cg_err as in k_ctl_dep_end: a
+// timed-out cooperative CG ends the refinement with an error).
+__global__ void k_ctl_dmix_sweep_end(StepCtl* ctl, const Scalars* sc, MScal* msR, Tiles tl, int32_t* act, int* nact,
+                                     const int* cg_err, Handles h) {
     __shared__ int active[kMaxMembers];
     for (int m = threadIdx.x; m < tl.n; m += blockDim.x) {
         active[m] = !ctl->dconv[m];
@@ -2464,14 +2491,22 @@ __global__ void k_ctl_dmix_sweep_end(StepCtl* ctl, const Scalars* sc, MScal* msR
         ctl->dep_iters += sc->iter;
         ctl->dep_sweeps += 1;
         ctl->kernels += 2;  // the correction and this
+        if (cg_err && *(volatile const int*)cg_err) {
+            ctl->ok = 0;
+            ctl->err = PBSM3D_ERR_CUDA;
+            stop_all(h);
+            hset(h, H_OK3, 0u);
+        }
     }
 }
 
 }  // namespace
 
 struct StepGraph {
-    cudaGraph_t graph = nullptr;
+    cudaGraph_t graph = nullptr;  // part 1: assembly through the post
     cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph2 = nullptr;  // part 2: deposition solve and update
+    cudaGraphExec_t exec2 = nullptr;
     double dt = -1.0;
     bool own_snow = false;
     StepCtl* ctl = nullptr;      // device
@@ -2618,6 +2653,38 @@ int capture_scg(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& 
     return loop.end();
 }
 
+// The single-mesh CG as one cooperative kernel node (the host path's
+// kernel; cooperative launches are allowed in conditional bodies): the
+// flags and the error word are cleared by memset nodes before it.
+template <typename V>
+int capture_pcg(Ctx& c, cudaStream_t s, DepSys<V> D, int blocks, Scalars* sc, double tol, int maxit,
+                const MScal* dyn) {
+    if (cudaMemsetAsync(c.cg_flags, 0, sizeof(unsigned) * kFlagStride * (size_t)blocks, s) != cudaSuccess) return 1;
+    if (cudaMemsetAsync(&c.gbar->err, 0, sizeof(int), s) != cudaSuccess) return 1;
+    int64_t Tp = c.P.Tp;
+    double* part = c.red.partials;
+    int* err = &c.gbar->err;
+    GridWait gw{kBarrierLimitNs, -1};
+    void* args[] = {&Tp, &D, &c.F.nbr, &part, &c.cg_flags, &err, &sc, &tol, &maxit, &gw, &dyn};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cudaLaunchConfig_t lc{};
+    lc.gridDim = dim3(blocks);
+    lc.blockDim = dim3(kCgBlock);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = s;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    return cudaLaunchKernelExC(&lc, (const void*)k_cg_persistent<V>, args) != cudaSuccess;
+}
+
+// Whether the graph's deposition solve is the cooperative CG: one mesh,
+// and the device runs cooperative launches.
+static bool graph_pcg(const Ctx& c) {
+    return c.tiles.n == 1 && (c.P.mixed ? c.coop_blocks32 : c.coop_blocks) > 0;
+}
+
 // The deposition solve (inside IF dep).
 int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const Tiles& tl) {
     cudaStream_t s = G.cap[depth];
@@ -2626,13 +2693,19 @@ int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     Scalars* sc = c.sc + 2;
     const int gr = std::max(1, std::min(c.grid_red[0], tl.ntiles));
     double* part = c.tile_part;
+    const bool pcg = graph_pcg(c);
+    int* cg_err = pcg ? &c.gbar->err : nullptr;
     if (!c.P.mixed) {
         DepSys<double> D = dep_sys64(c);
-        k_ctl_dcg_init<<<1, kBlock, 0, s>>>(G.ctl, c.ms0, sc, tl, c.act_buf, G.nact, tol, c.cfg.dep_maxit, h);
-        if (capture_scg<double>(c, G, h, depth, tl, D, c.ms0, sc)) return 1;
+        if (pcg) {
+            if (capture_pcg<double>(c, s, D, c.coop_blocks, sc, tol, c.cfg.dep_maxit, nullptr)) return 1;
+        } else {
+            k_ctl_dcg_init<<<1, kBlock, 0, s>>>(G.ctl, c.ms0, sc, tl, c.act_buf, G.nact, tol, c.cfg.dep_maxit, h);
+            if (capture_scg<double>(c, G, h, depth, tl, D, c.ms0, sc)) return 1;
+        }
         k_ctl_dres_init<<<1, kBlock, 0, s>>>(G.ctl, c.msR, tl, c.act_buf, G.nact, 0);
         k_sdep_resid<<<gr, kBlock, 0, s>>>(tl, c.P, c.D, c.F.nbr, nullptr, c.dr, c.msR, part);
-        k_ctl_dep_end<<<1, 32, 0, s>>>(G.ctl, c.msR, sc, tl.n, tol, h);
+        k_ctl_dep_end<<<1, 32, 0, s>>>(G.ctl, c.msR, sc, tl.n, tol, cg_err, h);
         return 0;
     }
     float* f = c.dep32;
@@ -2647,32 +2720,63 @@ int capture_deposition(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
         cudaStream_t t = G.cap[depth + 1];
         k_sdep_resid<<<gr, kBlock, 0, t>>>(tl, c.P, c.D, c.F.nbr, r32, c.dr, c.msR, part);
         k_ctl_dmix_outer<<<1, kBlock, 0, t>>>(G.ctl, c.msR, c.ms1, sc, tl, c.act_buf, G.nact, tol,
-                                              std::min(c.cfg.dep_maxit, 500), h);
+                                              std::min(c.cfg.dep_maxit, 500), pcg ? 1 : 3, h);
         CondBody inner;
         if (inner.begin(t, G.cap[depth + 2], h.h[H_DINNER], cudaGraphCondTypeIf)) return 1;
         {
             cudaStream_t u = G.cap[depth + 2];
-            k_zero<float><<<c.grid_faces, kBlock, 0, u>>>(Tp, D32.x);
-            if (capture_scg<float>(c, G, h, depth + 2, tl, D32, c.ms1, sc)) return 1;
+            if (pcg) {
+                // the kernel starts from x = 0 itself; target and limit from ms1
+                if (capture_pcg<float>(c, u, D32, c.coop_blocks32, sc, 0.0, 0, c.ms1)) return 1;
+            } else {
+                k_zero<float><<<c.grid_faces, kBlock, 0, u>>>(Tp, D32.x);
+                if (capture_scg<float>(c, G, h, depth + 2, tl, D32, c.ms1, sc)) return 1;
+            }
             k_dep_add<<<c.grid_faces, kBlock, 0, u>>>(c.P, c.D, D32.x);
-            k_ctl_dmix_sweep_end<<<1, kBlock, 0, u>>>(G.ctl, sc, c.msR, tl, c.act_buf, G.nact);
+            k_ctl_dmix_sweep_end<<<1, kBlock, 0, u>>>(G.ctl, sc, c.msR, tl, c.act_buf, G.nact, cg_err, h);
         }
         if (inner.end()) return 1;
     }
     return outer.end();
 }
 
+// The step graph is two graphs launched back to back: part 1 runs the
+// assembly, the suspension solve and the column post (with the deposition
+// rows); part 2 the deposition solve and the update.  Between the two
+// launches the host can queue copies of the outputs that are final after
+// the post on a second stream, which then overlap part 2.  Each part owns
+// its conditional handles; a controller at the start of part 2 opens its
+// nodes from part 1's outcome in the control block.
+constexpr unsigned kPart1Handles = (1u << H_OK1) | (1u << H_SUSP) | (1u << H_OUTER) | (1u << H_WARM) |
+                                   (1u << H_INNER) | (1u << H_ILOOP) | (1u << H_OK2);
+constexpr unsigned kPart2Handles = (1u << H_OK2) | (1u << H_DEP) | (1u << H_DOUTER) | (1u << H_DINNER) |
+                                   (1u << H_DLOOP) | (1u << H_OK3);
+
 int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
-    cudaGraph_t g;
-    PBSM_CUDA_TRY(cudaGraphCreate(&g, 0));
-    Handles h{};
+    cudaGraph_t g1 = nullptr, g2 = nullptr;
+    auto fail = [&](const char* what, cudaError_t e) {
+        if (g1) cudaGraphDestroy(g1);
+        if (g2) cudaGraphDestroy(g2);
+        c.err = std::string(what) + cudaGetErrorString(e);
+        return PBSM3D_ERR_CUDA;
+    };
+    cudaError_t e = cudaGraphCreate(&g1, 0);
+    if (e == cudaSuccess) e = cudaGraphCreate(&g2, 0);
+    if (e != cudaSuccess) return fail("creating the step graph failed: ", e);
     const bool warm = c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1);
-    h.valid = (1u << H_COUNT) - 1u;
-    if (!warm) h.valid &= ~(1u << H_WARM);
-    if (!c.P.mixed) h.valid &= ~((1u << H_DOUTER) | (1u << H_DINNER));
-    for (int id = 0; id < H_COUNT; ++id)
-        if (h.valid & (1u << id))
-            PBSM_CUDA_TRY(cudaGraphConditionalHandleCreate(&h.h[id], g, 0, cudaGraphCondAssignDefault));
+    unsigned valid = (1u << H_COUNT) - 1u;
+    if (!warm) valid &= ~(1u << H_WARM);
+    if (!c.P.mixed) valid &= ~((1u << H_DOUTER) | (1u << H_DINNER));
+    if (graph_pcg(c)) valid &= ~(1u << H_DLOOP);  // no tile-CG loop
+    Handles h1{}, h2{};
+    h1.valid = valid & kPart1Handles;
+    h2.valid = valid & kPart2Handles;
+    for (int id = 0; id < H_COUNT && e == cudaSuccess; ++id) {
+        if (h1.valid & (1u << id)) e = cudaGraphConditionalHandleCreate(&h1.h[id], g1, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess && (h2.valid & (1u << id)))
+            e = cudaGraphConditionalHandleCreate(&h2.h[id], g2, 0, cudaGraphCondAssignDefault);
+    }
+    if (e != cudaSuccess) return fail("creating the step graph's conditional handles failed: ", e);
     const bool prof = c.prof;
     c.prof = false;  // per-launch events are a host-path feature
     Tiles tl = c.tiles;
@@ -2680,14 +2784,15 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
     tl.nact = 0;
     cudaStream_t s = G.cap[0];
     int bad = 0;
-    PBSM_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-    c.graph_dep_flag = &G.ctl->dep_present;
     // phase stamps when the context profiles (the host path's per-launch
     // events have no graph equivalent)
     auto stamp = [&](cudaStream_t st, int slot) {
         if (prof) k_stamp<<<1, 1, 0, st>>>(G.ctl, slot);
     };
-    {
+    c.graph_dep_flag = &G.ctl->dep_present;
+    // ---- part 1: assembly, suspension solve, post and deposition rows
+    e = cudaStreamBeginCaptureToGraph(s, g1, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
         stamp(s, 0);
         cudaMemcpyAsync(c.x_prev, c.A.x, c.P.R * 8, cudaMemcpyDeviceToDevice, s);
         if (c.Mb.n > 1) {
@@ -2695,15 +2800,15 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
             cudaMemsetAsync(c.Mb.dep_max, 0, c.Mb.n * 8, s);
         }
         launch_assemble_suspension(c, s);
-        k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, c.asm_kernels, h);
+        k_ctl_begin<<<1, 32, 0, s>>>(G.ctl, c.sc, c.Mb, c.Mb.n, c.asm_kernels, h1);
         if (c.Mb.n > 1) launch_member_mask_norm(c, s, 0);
         stamp(s, 1);
         CondBody ok1;
-        bad |= ok1.begin(s, G.cap[1], h.h[H_OK1], cudaGraphCondTypeIf);
+        bad |= ok1.begin(s, G.cap[1], h1.h[H_OK1], cudaGraphCondTypeIf);
         if (!bad) {
             cudaStream_t t = G.cap[1];
             CondBody susp;
-            bad |= susp.begin(t, G.cap[2], h.h[H_SUSP], cudaGraphCondTypeIf);
+            bad |= susp.begin(t, G.cap[2], h1.h[H_SUSP], cudaGraphCondTypeIf);
             if (!bad) {
                 cudaStream_t u = G.cap[2];
                 if (c.cfg.warm_start == PBSM3D_X0_PREVIOUS)
@@ -2717,59 +2822,76 @@ int build_step_graph(Ctx& c, StepGraph& G, bool own_snow) {
                     }
                 }
                 if (c.Mb.n > 1 && c.cfg.warm_start != PBSM3D_X0_ZERO) launch_member_zero(c, u, c.A.x);
-                if (!bad) bad |= c.P.mixed ? capture_suspension<float>(c, G, h, 2, tl)
-                                           : capture_suspension<double>(c, G, h, 2, tl);
+                if (!bad) bad |= c.P.mixed ? capture_suspension<float>(c, G, h1, 2, tl)
+                                           : capture_suspension<double>(c, G, h1, 2, tl);
                 bad |= susp.end();
             }
             stamp(t, 2);
-            k_ctl_mid<<<1, 32, 0, t>>>(G.ctl, h);
+            k_ctl_mid<<<1, 32, 0, t>>>(G.ctl, h1);
             CondBody ok2;
-            bad |= ok2.begin(t, G.cap[2], h.h[H_OK2], cudaGraphCondTypeIf);
+            bad |= ok2.begin(t, G.cap[2], h1.h[H_OK2], cudaGraphCondTypeIf);
             if (!bad) {
                 cudaStream_t u = G.cap[2];
                 launch_post_and_assemble_deposition(c, u);
-                k_ctl_dep_begin<<<1, 32, 0, u>>>(G.ctl, c.sc, c.Mb, c.Mb.n, own_snow ? 2 : 1, h);
+                // decides the deposition's presence in the control block
+                // (its handles belong to part 2)
+                k_ctl_dep_begin<<<1, 32, 0, u>>>(G.ctl, c.sc, c.Mb, c.Mb.n, own_snow ? 2 : 1, h1);
                 if (c.Mb.n > 1) launch_member_mask_norm(c, u, 1);
                 stamp(u, 3);
-                CondBody dep;
-                bad |= dep.begin(u, G.cap[3], h.h[H_DEP], cudaGraphCondTypeIf);
-                if (!bad) {
-                    bad |= capture_deposition(c, G, h, 3, tl);
-                    bad |= dep.end();
-                }
-                stamp(u, 4);
-                CondBody ok3;
-                bad |= ok3.begin(u, G.cap[3], h.h[H_OK3], cudaGraphCondTypeIf);
-                if (!bad) {
-                    launch_update(c, G.cap[3]);
-                    if (own_snow) launch_consume_drift(c, G.cap[3]);
-                    stamp(G.cap[3], 5);
-                    bad |= ok3.end();
-                }
                 bad |= ok2.end();
             }
             bad |= ok1.end();
         }
+        cudaGraph_t out;
+        const cudaError_t ee = cudaStreamEndCapture(s, &out);
+        if (ee != cudaSuccess) e = ee;
+    }
+    // ---- part 2: deposition solve and update
+    if (e == cudaSuccess && !bad) {
+        e = cudaStreamBeginCaptureToGraph(s, g2, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+            k_ctl_part2<<<1, 32, 0, s>>>(G.ctl, h2);
+            CondBody ok2;
+            bad |= ok2.begin(s, G.cap[1], h2.h[H_OK2], cudaGraphCondTypeIf);
+            if (!bad) {
+                cudaStream_t t = G.cap[1];
+                CondBody dep;
+                bad |= dep.begin(t, G.cap[2], h2.h[H_DEP], cudaGraphCondTypeIf);
+                if (!bad) {
+                    bad |= capture_deposition(c, G, h2, 2, tl);
+                    bad |= dep.end();
+                }
+                stamp(t, 4);
+                CondBody ok3;
+                bad |= ok3.begin(t, G.cap[2], h2.h[H_OK3], cudaGraphCondTypeIf);
+                if (!bad) {
+                    launch_update(c, G.cap[2]);
+                    if (own_snow) launch_consume_drift(c, G.cap[2]);
+                    stamp(G.cap[2], 5);
+                    bad |= ok3.end();
+                }
+                bad |= ok2.end();
+            }
+            cudaGraph_t out;
+            const cudaError_t ee = cudaStreamEndCapture(s, &out);
+            if (ee != cudaSuccess) e = ee;
+        }
     }
     c.graph_dep_flag = nullptr;
     c.prof = prof;
-    cudaGraph_t out;
-    const cudaError_t e = cudaStreamEndCapture(s, &out);
-    if (bad || e != cudaSuccess) {
-        cudaGraphDestroy(g);
-        c.err = std::string("building the step graph failed: ") + cudaGetErrorString(e != cudaSuccess ? e
-                                                                                       : cudaGetLastError());
-        return PBSM3D_ERR_CUDA;
+    if (bad || e != cudaSuccess)
+        return fail("building the step graph failed: ", e != cudaSuccess ? e : cudaGetLastError());
+    cudaGraphExec_t x1 = nullptr, x2 = nullptr;
+    e = cudaGraphInstantiate(&x1, g1, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&x2, g2, 0);
+    if (e != cudaSuccess) {
+        if (x1) cudaGraphExecDestroy(x1);
+        return fail("instantiating the step graph failed: ", e);
     }
-    cudaGraphExec_t exec;
-    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
-    if (ei != cudaSuccess) {
-        cudaGraphDestroy(g);
-        c.err = std::string("instantiating the step graph failed: ") + cudaGetErrorString(ei);
-        return PBSM3D_ERR_CUDA;
-    }
-    G.graph = g;
-    G.exec = exec;
+    G.graph = g1;
+    G.exec = x1;
+    G.graph2 = g2;
+    G.exec2 = x2;
     G.own_snow = own_snow;
     G.profiled = prof;
     G.dt = c.P.dt;
@@ -2783,6 +2905,8 @@ void graph_destroy(Ctx& c) {
     StepGraph& G = *c.graph;
     if (G.exec) cudaGraphExecDestroy(G.exec);
     if (G.graph) cudaGraphDestroy(G.graph);
+    if (G.exec2) cudaGraphExecDestroy(G.exec2);
+    if (G.graph2) cudaGraphDestroy(G.graph2);
     for (auto& st : G.cap)
         if (st) cudaStreamDestroy(st);
     if (G.ctl_host) cudaFreeHost(G.ctl_host);
@@ -2790,7 +2914,7 @@ void graph_destroy(Ctx& c) {
     c.graph = nullptr;
 }
 
-int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
+int graph_step(Ctx& c, cudaStream_t s, bool own_snow, const std::function<int()>& between) {
     if (!c.graph) {
         c.graph = new StepGraph();
         StepGraph& G = *c.graph;
@@ -2808,8 +2932,10 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
         if (G.exec) {
             cudaGraphExecDestroy(G.exec);
             cudaGraphDestroy(G.graph);
-            G.exec = nullptr;
-            G.graph = nullptr;
+            cudaGraphExecDestroy(G.exec2);
+            cudaGraphDestroy(G.graph2);
+            G.exec = G.exec2 = nullptr;
+            G.graph = G.graph2 = nullptr;
         }
         // the capture streams must follow s's earlier work
         PBSM_CUDA_TRY(cudaStreamSynchronize(s));
@@ -2818,6 +2944,14 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
         c.bytes = 0;
     }
     PBSM_CUDA_TRY(cudaGraphLaunch(G.exec, s));
+    if (between) {
+        const int rc = between();
+        if (rc) {
+            cudaStreamSynchronize(s);
+            return rc;
+        }
+    }
+    PBSM_CUDA_TRY(cudaGraphLaunch(G.exec2, s));
     PBSM_CUDA_TRY(cudaMemcpyAsync(G.ctl_host, G.ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, s));
     PBSM_CUDA_TRY(cudaStreamSynchronize(s));
     const StepCtl& k = *G.ctl_host;
@@ -2848,6 +2982,7 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow) {
     }
     if (k.err) {
         c.err = k.err == PBSM3D_ERR_NAN_INPUT ? "NaN in an assembled system (check the forcing)"
+                : k.err == PBSM3D_ERR_CUDA    ? "deposition solve: grid all-reduce timed out (a block's wait ran out)"
                                               : "a Krylov solve failed to converge";
         return k.err;
     }

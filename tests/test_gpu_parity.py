@@ -454,3 +454,35 @@ def test_graph_phase_times(cuda_lib, solver):
     assert all(p > 0 for p in phases), phases
     assert 0.5 * st["ms_total"] <= sum(phases) <= 1.05 * st["ms_total"], (phases, st["ms_total"])
     m.close()
+
+
+@pytest.mark.parametrize("solver", [{}, {"precision": 1, "warm_start": 1, "neumann": 5, "dep_neumann": 1},
+                                    {"graph": 1, "neumann": 5, "dep_neumann": 1},
+                                    {"graph": 1, "precision": 1, "warm_start": 1, "neumann": 5, "dep_neumann": 1}],
+                         ids=["fp64", "mixed_previous_neumann5", "graph_fp64_neumann5", "graph_mixed_previous_neumann5"])
+def test_pinned_host_outputs(cuda_lib, solver):
+    """Host outputs in page-locked memory: the outputs final after the column
+    post (and c) go to the host on a second stream while the deposition solve
+    runs (host-driven), or between the step graph's two launches (graph
+    mode).  Every output equals, bit for bit, the one a twin context writes
+    to pageable memory after the step, over coupled steps with the device
+    snow state."""
+    torch = pytest.importorskip("torch")
+    w = synth.Workload(2048, 3500.0, seed=21)
+    L = 5
+    mods = [gpu_module(w.mesh, L, **solver) for _ in range(2)]
+    n = mods[0].n_faces
+    keys = list(mods[0].output_keys())
+    pinned = {k: torch.empty(n, dtype=torch.float64).pin_memory().numpy() for k in keys}
+    pinned["c"] = torch.empty(L * n, dtype=torch.float64).pin_memory().numpy()
+    for m in mods:
+        m.set_snow(w.swe.copy(), w.depth.copy())
+    for s in range(5):
+        fa = {k: v for k, v in w.forcing(s).arrays().items() if k not in ("swe", "snowdepthavg")}
+        a = mods[0].run(fa, 3600.0, outputs=pinned)
+        b = mods[1].run(fa, 3600.0, want_c=True)
+        assert mods[0].last_stats["deposition_present"] == 1
+        for k in keys + ["c"]:
+            np.testing.assert_array_equal(a[k], b[k], err_msg=f"step {s} {k}")
+    for m in mods:
+        m.close()

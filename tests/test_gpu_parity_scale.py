@@ -70,6 +70,9 @@ FORMS = {
     "plain_fp64_neumann9": {"precision": capi.FP64, "neumann": 9, "dep_neumann": 1},
     "graph_fp64_previous_neumann5": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                      "neumann": 5, "dep_neumann": 1},
+    "graph_fp64_neumann7": {"precision": capi.FP64, "graph": 1, "neumann": 7, "dep_neumann": 1},
+    "graph_fp64_previous_neumann7": {"precision": capi.FP64, "warm_start": capi.X0_PREVIOUS, "graph": 1,
+                                     "neumann": 7, "dep_neumann": 1},
     "graph_mixed_previous_neumann5": {"precision": capi.MIXED, "warm_start": capi.X0_PREVIOUS, "graph": 1,
                                       "neumann": 5, "dep_neumann": 1},
 }
@@ -77,6 +80,8 @@ MIXED_FORMS = {
     "mixed": {"precision": capi.MIXED},
     "graph_mixed_previous_neumann5": FORMS["graph_mixed_previous_neumann5"],
 }
+# the wind sweep also runs the fastest FP64 form
+SWEEP_FORMS = {**MIXED_FORMS, "graph_fp64_previous_neumann7": FORMS["graph_fp64_previous_neumann7"]}
 # solved tightly: the assembled systems, not the stopping rule, are compared
 TIGHT = {"plain_fp64_tight": {"susp_tol": 1e-11, "dep_tol": 1e-13, "susp_maxit": 5000, "dep_maxit": 5000},
          "mixed_tight": {"precision": capi.MIXED, "susp_tol": 1e-11, "dep_tol": 1e-13, "susp_maxit": 5000,
@@ -244,13 +249,14 @@ def test_tri1m_coupled_steps(cuda_lib, tri1m_wind8, name):
 
 @pytest.mark.parametrize("wind", [4.0, 14.0])
 def test_tri1m_wind_sweep_mixed(cuda_lib, oracle_lib, tri1m_mesh, wind):
-    """The FP32-inner / FP64-refined forms at 1M faces where advection is
-    weak (4 m/s) and dominant (14 m/s), two coupled steps."""
+    """The FP32-inner / FP64-refined forms (and the fastest FP64 form) at 1M
+    faces where advection is weak (4 m/s) and dominant (14 m/s), two coupled
+    steps."""
     cfg = synth.CONFIGS["tri1m"]
     w = synth.Workload(cfg["n_points"], cfg["side"], seed=1, wind_scale=wind, mesh=tri1m_mesh)
     L = cfg["nLayer"]
     exact, reflike = references(w, L, 2, f"tri1m/wind{wind:g}")
-    for name, solver in {**MIXED_FORMS, "mixed_tight": TIGHT["mixed_tight"]}.items():
+    for name, solver in {**SWEEP_FORMS, "mixed_tight": TIGHT["mixed_tight"]}.items():
         for s, (out, st) in enumerate(gpu_trajectory(w, L, solver, len(exact))):
             check_fields(f"tri1m/wind{wind:g}/{name}/step{s}", out, exact[s], st,
                          None if name in TIGHT else reflike[s])
