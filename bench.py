@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import statistics
@@ -325,9 +326,11 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     def timed(ctx, descs, odesc, slot):
         dist.barrier()
         torch.cuda.synchronize()
+        gc.disable()  # no collector pause of the harness between two steps
         lib.pbsm3d_timer_mark(ctx, slot)
         stats = [step(ctx, descs[s], odesc) for s in range(args.warmup, nsteps)]
         lib.pbsm3d_timer_mark(ctx, slot + 1)
+        gc.enable()
         torch.cuda.synchronize()
         lib.pbsm3d_timer_elapsed(ctx, slot, slot + 1, C.byref(ms))
         t = ms.value / 1000.0
@@ -479,7 +482,11 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
         # the step's phases (the graph forms' device-clock stamps, the host
         # path's events) and the part outside them: host copies and waits
         ks = ("ms_coefficients", "ms_susp_solve", "ms_post", "ms_dep_solve", "ms_update", "ms_total")
-        return {k: round(float(np.mean([s[k] for s in sts])), 3) for k in ks}
+        out = {k: round(float(np.mean([s[k] for s in sts])), 3) for k in ks}
+        rest = [s["ms_total"] - sum(s[k] for k in ks[:-1]) for s in sts]
+        out["outside_phases_ms"] = [round(float(np.min(rest)), 3), round(float(np.median(rest)), 3),
+                                    round(float(np.max(rest)), 3)]
+        return out
 
     def worst(errs):
         return {k: max(v[k] for v in errs.values()) for k in ("max_rel", "l2_rel", "elem_rel_floored")}
@@ -619,9 +626,11 @@ def run_ensemble(args, dist: Dist, rank: int, world: int, local_rank: int, membe
     def timed(ctx, descs_, odesc, slot):
         dist.barrier()
         torch.cuda.synchronize()
+        gc.disable()  # no collector pause of the harness between two steps
         lib.pbsm3d_timer_mark(ctx, slot)
         stats = [step(ctx, descs_[s], odesc) for s in range(args.warmup, nsteps)]
         lib.pbsm3d_timer_mark(ctx, slot + 1)
+        gc.enable()
         torch.cuda.synchronize()
         lib.pbsm3d_timer_elapsed(ctx, slot, slot + 1, C.byref(ms))
         dist.barrier()

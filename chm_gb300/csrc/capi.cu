@@ -1042,14 +1042,17 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
 
     double susp_rhs_max = 0.0, dep_rhs_max = 0.0;
     bool early_out = false;  // some host outputs already copied on the second stream
+    bool graph_run = false;  // the step graph is queued on s (its outcome comes after the sync)
     // whatever path leaves the step, no copy into the caller's buffers outlives it
     struct CopyGuard {
         Ctx& c;
         const bool& on;
+        const bool& queued;
         ~CopyGuard() {
             if (on) cudaStreamSynchronize(c.copy_stream);
+            if (queued) cudaStreamSynchronize(c.stream);
         }
-    } copy_guard{c, early_out};
+    } copy_guard{c, early_out, graph_run};
     // graph mode; with the autotuner on, the first step runs host-driven so
     // that the geometry is tuned before the graph is built
     if (c.cfg.graph && c.tuned) {
@@ -1057,12 +1060,14 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
         // outputs final after the post are copied while part 2 runs (on a
         // failed step they may hold the post's fields or the last step's)
         PBSM_CUDA_TRY(cudaEventRecord(c.ev[1], s));
+        // Nothing waits for the graph here: the remaining output copies
+        // follow it on s, and its outcome is read after the step's one
+        // synchronisation below.
         std::function<int()> between;
         if (early_copies(out)) between = [&]() { return copy_final_outputs(c, s, out, early_out); };
+        graph_run = true;
         if ((rc = graph_step(c, s, own_snow, between))) return rc;
         for (int k = 2; k <= 6; ++k) PBSM_CUDA_TRY(cudaEventRecord(c.ev[k], s));
-        susp_rhs_max = c.graph_rhs_max[0];
-        dep_rhs_max = c.graph_rhs_max[1];
     } else {
         // the previous step's solution (the assembly zeroes x, as the reference's
         // zeroSystem does): kept for the warm starts and the MLP features
@@ -1174,6 +1179,12 @@ int pbsm3d_step(pbsm3d_ctx* h, const pbsm3d_forcing* f, double dt, const pbsm3d_
     if (early_out) PBSM_CUDA_TRY(cudaStreamWaitEvent(s, c.copy_ev[1], 0));
     PBSM_CUDA_TRY(cudaEventRecord(c.ev[7], s));
     PBSM_CUDA_TRY(cudaStreamSynchronize(s));
+    if (graph_run) {
+        graph_run = false;
+        if ((rc = graph_finish(c))) return rc;  // the output buffers' contents are unspecified
+        susp_rhs_max = c.graph_rhs_max[0];
+        dep_rhs_max = c.graph_rhs_max[1];
+    }
     if (st) {
         memset(st, 0, sizeof(*st));
         st->suspension_present = c.suspension_present;

@@ -510,10 +510,6 @@ __global__ void k_fold_w0(const float* dW0pad, float* gW0) {
     for (int k = threadIdx.x; k < kFeat; k += blockDim.x) gW0[o * kFeat + k] += dW0pad[o * 16 + k];
 }
 
-__global__ void k_zero_f(float* p, int n) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) p[k] = 0.0f;
-}
-
 }  // namespace
 
 // ---------------------------------------------------------------- host side

@@ -274,8 +274,12 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 // graph mode: the device part of a step as one CUDA-graph launch (built on
 // first use); fills the iteration/residual fields of c like the host path
 // One step as the two launches of the step graph; `between` (may be empty)
-// runs on the host after part 1 is queued and before part 2 is.
+// runs on the host after part 1 is queued and before part 2 is.  The step's
+// control block comes back with the queued work: after the caller's
+// synchronisation of s, graph_finish reads it (iterations, residuals, the
+// step's error).
 int graph_step(Ctx& c, cudaStream_t s, bool own_snow, const std::function<int()>& between);
+int graph_finish(Ctx& c);
 void graph_destroy(Ctx& c);
 int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st);
 int configure_solver_kernels(Ctx& c);

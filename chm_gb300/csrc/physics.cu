@@ -441,7 +441,6 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
             continue;
         }
         const int mem = Mb.face_member[i];
-        const Member mp = Mb.prm[mem];
         const CzCoef* tab = A.cztab + (int64_t)mem * P.L;
         const double* fv = A.face_v;
         const double hs = fv[FV_HS * Tp + i];

@@ -2152,12 +2152,10 @@ __global__ void k_ctl_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Ti
                             double tol, double inner_tol, int maxit, int mixed, Handles h) {
     __shared__ int active[kMaxMembers];
     __shared__ int s_all, s_finite, s_go;
-    __shared__ double s_worst;
     const int n = tl.n;
     if (threadIdx.x == 0) {
         s_all = 1;
         s_finite = 1;
-        s_worst = 0.0;
     }
     __syncthreads();
     for (int m = threadIdx.x; m < n; m += blockDim.x) {
@@ -2953,8 +2951,12 @@ int graph_step(Ctx& c, cudaStream_t s, bool own_snow, const std::function<int()>
     }
     PBSM_CUDA_TRY(cudaGraphLaunch(G.exec2, s));
     PBSM_CUDA_TRY(cudaMemcpyAsync(G.ctl_host, G.ctl, sizeof(StepCtl), cudaMemcpyDeviceToHost, s));
-    PBSM_CUDA_TRY(cudaStreamSynchronize(s));
-    const StepCtl& k = *G.ctl_host;
+    return 0;
+}
+
+int graph_finish(Ctx& c) {
+    const StepCtl& k = *c.graph->ctl_host;
+    const StepGraph& G = *c.graph;
     c.suspension_present = k.susp_present;
     c.deposition_present = k.dep_present;
     c.susp_iters = k.susp_iters;

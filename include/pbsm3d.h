@@ -332,7 +332,13 @@ int pbsm3d_ensemble_create(int32_t n_members, const pbsm3d_mesh_desc* meshes, co
 int pbsm3d_member_offsets(const pbsm3d_ctx* ctx, int64_t* offsets);
 
 /* One timestep of dt seconds (global_param->dt(), integer seconds in CHM).
- * Replaces PBSM3D::run.  stats may be NULL. */
+ * Replaces PBSM3D::run.  stats may be NULL.  Host output buffers in
+ * page-locked memory let the outputs that are final after the column post
+ * (Qsalt, Qsusp, Qsubl, Qsubl_mass, sum_subl, blowingsnow_probability, c)
+ * reach the host while the deposition solve runs; with pageable buffers
+ * every output is copied after the step.  After an error return the output
+ * buffers' contents are unspecified; a step that fails before the column
+ * post (NaN input, suspension solve) leaves the module state unchanged. */
 int pbsm3d_step(pbsm3d_ctx* ctx, const pbsm3d_forcing* forcing, double dt,
                 const pbsm3d_outputs* out, pbsm3d_stats* stats);
 
@@ -511,7 +517,8 @@ int pbsm3d_get_column_geometry(const pbsm3d_ctx* ctx, int32_t* width, int32_t* l
  * (at most 2000; the default limit is 2 s).  The other blocks' waits run
  * out, every block leaves, and that step returns PBSM3D_ERR_CUDA ("grid
  * all-reduce timed out") with the context usable for the next step.
- * Single-mesh, host-driven contexts only (PBSM3D_ERR_INVALID_ARG otherwise).
+ * Single-mesh, host-driven contexts only (PBSM3D_ERR_INVALID_ARG otherwise;
+ * a graph-mode context's wait limit is fixed when its graph is captured).
  */
 int pbsm3d_arm_wait_timeout_test(pbsm3d_ctx* ctx, int32_t withhold_block, double limit_ms);
 
