@@ -469,7 +469,9 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     // the polynomial deposition preconditioner reads the previous residual
     // of its neighbours while the new one is written: a second buffer
     if (cfg.dep_neumann && !P.mixed) c.dr2 = dalloc<double>(c, Tp, ok);
-    if (P.mixed) c.dep32 = dalloc<float>(c, (size_t)(cfg.dep_neumann ? 12 : 11) * Tp, ok);
+    // the persistent CG's scaling d^-1/2 and scaled couplings
+    if (!P.mixed) c.dscale = dalloc<double>(c, (size_t)4 * Tp, ok);
+    if (P.mixed) c.dep32 = dalloc<float>(c, (size_t)16 * Tp, ok);
     c.cg_flags = dalloc<unsigned>(c, (size_t)kMaxCgBlocks * 32, ok);
     c.sc = dalloc<Scalars>(c, 4, ok);
     c.red.partials = dalloc<double>(c, (size_t)8 * c.red.nblocks, ok);

@@ -319,7 +319,8 @@ struct Ctx {
     float *nw32 = nullptr, *nz32 = nullptr;
     // deposition CG vectors [Tp]
     double *dr, *dz_, *dp, *dq;
-    double* dr2 = nullptr;  // second residual buffer of the polynomial deposition CG (FP64)
+    double* dr2 = nullptr;     // second residual buffer of the polynomial deposition tile CG (FP64)
+    double* dscale = nullptr;  // [4][Tp] the persistent CG's d^-1/2 and scaled couplings (FP64)
     // reductions
     Scalars* sc;       // device
     Scalars* sc_host;  // pinned mirror

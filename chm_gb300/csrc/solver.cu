@@ -716,61 +716,142 @@ struct GridWait {
     int withhold;
 };
 
-// All-reduce of NT per-thread values over a cooperative grid, identical in
-// every block, without atomics: block b writes its partials and then
-// releases flags[b] = epoch; thread t < gridDim of every block waits for
-// flags[t], reads block t's partials and the block sums them in block order
-// (deterministic).  Partials alternate between two buffers by epoch parity:
-// a block can only publish epoch e+2 after every block has published e+1,
-// i.e. after every block has finished reading epoch e.  A reader therefore
-// waits until flags[b] is AT LEAST its epoch (wraparound-safe difference):
-// block b may already have left this all-reduce and published e+1 before a
-// slow reader first loads its flag, and its epoch-e partials stay valid in
-// the other buffer until every block has published e+1.  The wait is bounded:
-// after gw.limit_ns (kBarrierLimitNs outside the timeout test) a block sets
-// *err and every block leaves at its next all-reduce, so a broken
-// co-residency assumption ends in an error, never a hang.  Returns false
-// when the kernel must exit.
+// Warp sums of NT FP64 values (identical order in every call: deterministic);
+// every lane ends with the totals.  The FP64 pipe of this GPU issues a small
+// fraction of the FP32 rate, so two values share the first butterfly step:
+// each half-warp adds one of them, and the four remaining steps carry one
+// value a lane -- 5 FP64 adds a lane instead of 10.
+__device__ __forceinline__ void warp_sums(double (&v)[1]) { v[0] = warp_sum(v[0]); }
+__device__ __forceinline__ void warp_sums(double (&v)[2]) {
+    const bool lo = (threadIdx.x & 31) < 16;
+    double keep = lo ? v[0] : v[1];
+    keep += __shfl_xor_sync(0xffffffffu, lo ? v[1] : v[0], 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+    v[0] = __shfl_sync(0xffffffffu, keep, 0);
+    v[1] = __shfl_sync(0xffffffffu, keep, 16);
+}
+// First level of a block reduction: FP32 values are summed in FP32 across
+// the warp (off the FP64 pipe), then widened.
 template <int NT>
-__device__ bool grid_totals(double (&v)[NT], double* partials, unsigned* flags, unsigned epoch, int* err,
-                            const GridWait& gw, double (&tot)[NT]) {
-    __shared__ double bc[NT];
-    __shared__ int ok;
-    block_sum<NT>(v);
+__device__ __forceinline__ void warp_level(const double (&v)[NT], double (&w)[NT]) {
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w[k] = v[k];
+    warp_sums(w);
+}
+template <int NT>
+__device__ __forceinline__ void warp_level(const float (&v)[NT], double (&w)[NT]) {
+#pragma unroll
+    for (int k = 0; k < NT; ++k) w[k] = (double)warp_sum_f(v[k]);
+}
+
+// All-reduce of NT per-thread values over a cooperative grid, identical in
+// every block, without atomics.  (1) Warp sums go to shared memory; (2) warp
+// 0 adds them, and its lane 0 writes the block's partials and then releases
+// flags[b] = epoch; (3) thread t < gridDim of every block waits for flags[t]
+// and loads block t's partials, the warps holding them sum them, and (4)
+// warp 0 adds those warp sums: the same order in every block
+// (deterministic).  Lane 0 of warp 0 then runs `fin` on the totals -- the
+// solver's scalar step (divisions, stopping tests), once a block instead of
+// once a thread -- and its NX results (as double and as V) and status are
+// broadcast.  Three block barriers a call.  FP64 operations are kept few
+// (transposed warp sums, one warp for the block and grid levels, scalar work
+// in one lane), since on this GPU they, not the flag latency, bound an
+// all-reduce of many blocks.
+// Partials alternate between two buffers by epoch parity: a block can only
+// publish epoch e+2 after every block has published e+1, i.e. after every
+// block has finished reading epoch e.  A reader therefore waits until
+// flags[b] is AT LEAST its epoch (wraparound-safe difference): block b may
+// already have left this all-reduce and published e+1 before a slow reader
+// first loads its flag, and its epoch-e partials stay valid in the other
+// buffer until every block has published e+1.  The wait is bounded: after
+// gw.limit_ns (kBarrierLimitNs outside the timeout test) a block sets *err
+// and every block leaves at its next all-reduce, so a broken co-residency
+// assumption ends in an error, never a hang.  Returns false when the kernel
+// must exit.
+template <int NT, int NX, typename V, typename Fin>
+__device__ bool grid_totals(const V (&v)[NT], double* partials, unsigned* flags, unsigned epoch, int* err,
+                            const GridWait& gw, double (&out)[NX], V (&outv)[NX], int& st, Fin fin) {
+    __shared__ double shw[NT][32], shg[NT][32], bx[NX];
+    __shared__ V bv[NX];
+    __shared__ int bad, good_all, bst;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
     const int G = gridDim.x;
     double* pp = partials + (size_t)(epoch & 1u) * 4 * G;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < NT; ++k) pp[k * G + blockIdx.x] = v[k];
-        if ((int)blockIdx.x != gw.withhold) st_release_u32(&flags[blockIdx.x * kFlagStride], epoch);
-        ok = 1;
+    {
+        double w[NT];
+        warp_level<NT>(v, w);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) shw[k][wid] = w[k];
+        if (threadIdx.x == 0) bad = 0;
     }
     __syncthreads();
+    if (wid == 0) {
+        double b[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) b[k] = lane < nw ? shw[k][lane] : 0.0;
+        warp_sums(b);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NT; ++k) pp[k * G + blockIdx.x] = b[k];
+            if ((int)blockIdx.x != gw.withhold) st_release_u32(&flags[blockIdx.x * kFlagStride], epoch);
+        }
+    }
     double t[NT];
+#pragma unroll
     for (int k = 0; k < NT; ++k) t[k] = 0.0;
     for (int b = threadIdx.x; b < G; b += blockDim.x) {
         const unsigned long long t0 = global_timer_ns();
+        bool ok = true;
         while ((int)(ld_relaxed_u32(&flags[b * kFlagStride]) - epoch) < 0) {
             if (*(volatile int*)err) {
-                ok = 0;
+                ok = false;
                 break;
             }
             if (global_timer_ns() - t0 > gw.limit_ns) {
                 atomicExch(err, 1);
-                ok = 0;
+                ok = false;
                 break;
             }
         }
+        if (!ok) bad = 1;
         asm volatile("fence.acq_rel.gpu;" ::: "memory");
+#pragma unroll
         for (int k = 0; k < NT; ++k) t[k] += __ldcg(&pp[k * G + b]);
     }
-    block_sum<NT>(t);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < NT; ++k) bc[k] = t[k];
+    if (wid * 32 < G) {
+        warp_sums(t);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) shg[k][wid] = t[k];
+    }
     __syncthreads();
-    for (int k = 0; k < NT; ++k) tot[k] = bc[k];
-    const bool good = ok != 0;
+    if (wid == 0) {
+        const int ng = min(nw, (G + 31) >> 5);
+        double g[NT];
+#pragma unroll
+        for (int k = 0; k < NT; ++k) g[k] = lane < ng ? shg[k][lane] : 0.0;
+        warp_sums(g);
+        if (lane == 0) {
+            double o[NX];
+            bst = fin(g, o);
+#pragma unroll
+            for (int k = 0; k < NX; ++k) {
+                bx[k] = o[k];
+                bv[k] = (V)o[k];
+            }
+            good_all = !bad;
+        }
+    }
     __syncthreads();
-    return good;
+#pragma unroll
+    for (int k = 0; k < NX; ++k) {
+        out[k] = bx[k];
+        outv[k] = bv[k];
+    }
+    st = bst;
+    return good_all != 0;
 }
 
 // The deposition system in one precision.
@@ -778,23 +859,26 @@ template <typename V>
 struct DepSys {
     const V* diag;      // [Tp]
     const V* off;       // [3][Tp]
-    const V* dinv;      // [Tp] Jacobi preconditioner
+    const V* dinv;      // [Tp] Jacobi preconditioner (per-member tile CG)
     const V* b;         // [Tp]
     V* x;               // [Tp] solution (starts at 0)
     V *r, *zz, *p, *q;  // [Tp] work
     V* r2;              // [Tp] second residual buffer; non-null selects the polynomial preconditioner
+    V* s;               // [Tp] d^-1/2, the symmetric scaling of the persistent CG
+    V* offs;            // [3][Tp] scaled couplings s_i a_ij s_j of the persistent CG
 };
 
-// The preconditioner z = M^-1 r at row i.  Jacobi: z_i = r_i / d_i.  With
-// D.r2 set, the order-1 truncated Neumann series of the Jacobi splitting
-// A = D - R (Saad, Iterative Methods for Sparse Linear Systems, 2nd ed.,
-// sec. 12.3.1): M^-1 = D^-1 + D^-1 R D^-1, symmetric, and positive definite
-// because the spectral radius of D^-1 R is below 1 for this strictly
-// diagonally dominant matrix with non-positive off-diagonals; about half the
-// iterations of Jacobi.  The neighbours' residuals are recomputed from the
-// previous iteration's r and q (rn = r - alpha q), so z needs no grid-wide
-// wait between the residual update and the dot products; the new residual
-// goes to the other buffer, since neighbours still read the old one.
+// The preconditioner z = M^-1 r at row i of the per-member tile CG.  Jacobi:
+// z_i = r_i / d_i.  With D.r2 set, the order-1 truncated Neumann series of
+// the Jacobi splitting A = D - R (Saad, Iterative Methods for Sparse Linear
+// Systems, 2nd ed., sec. 12.3.1): M^-1 = D^-1 + D^-1 R D^-1, symmetric, and
+// positive definite because the spectral radius of D^-1 R is below 1 for
+// this strictly diagonally dominant matrix with non-positive off-diagonals;
+// about half the iterations of Jacobi.  The neighbours' residuals are
+// recomputed from the previous iteration's r and q (rn = r - alpha q), so z
+// needs no grid-wide wait between the residual update and the dot products;
+// the new residual goes to the other buffer, since neighbours still read the
+// old one.
 template <typename V>
 __device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __restrict__ nbr, int64_t Tp, int64_t i,
                                          V rn, const V* __restrict__ rin, const V* __restrict__ q, V al) {
@@ -808,18 +892,33 @@ __device__ __forceinline__ V dep_precond(const DepSys<V>& D, const int32_t* __re
     return D.dinv[i] * acc;
 }
 
+__device__ __forceinline__ double rsqrt_v(double d) { return rsqrt(d); }
+__device__ __forceinline__ float rsqrt_v(float d) { return rsqrtf(d); }
+
 // CG in one cooperative launch, Jacobi or polynomial preconditioner; at 1M
-// faces its vectors and matrix (~100 MB in FP64) stay in L2.  Two all-reduces
-// per iteration: (r, z) and (r, r) after the x/r update, (p, q) after q = A p
-// (q is updated from A z by the recurrence q = A z + beta q).  Measured
-// slower at 1M faces, and dropped: a form with one all-reduce per iteration
-// (Chronopoulos-Gear recurrences, contiguous row runs per block and a
-// point-to-point wait for the blocks owning neighbour rows), 2.95 against
-// 2.55 ms per FP64 solve, whose polynomial preconditioner rebuilds each
-// neighbour's new residual from three vectors instead of two (the iteration
-// is bound by those gathered loads, not by the all-reduce it saves); and an
-// all-reduce whose partials are staged in shared memory for one warp to
-// sum, 2.65 ms (its 24 KB of shared memory is L1 the gathers lose).
+// faces its vectors and matrix (~100 MB in FP64) stay in L2.
+//
+// On this GPU the FP64 pipe, not memory or the grid all-reduce, bounds the
+// FP64 iteration, so the iteration is arranged for few FP64 operations:
+// - CG runs on the symmetrically scaled system S A S y = S b, S = D^-1/2
+//   (x = S y), whose diagonal is one: the Jacobi preconditioner becomes the
+//   identity and the order-1 Neumann polynomial M^-1 = D^-1 + D^-1 R D^-1
+//   (A = D - R; Saad, Iterative Methods for Sparse Linear Systems, 2nd ed.,
+//   sec. 12.3.1) becomes I + S R S.  In exact arithmetic the iterates are
+//   those of the unscaled preconditioned CG, x_k = S y_k; the stopping test
+//   uses the unscaled residual, ||r||^2 = sum d_i r^_i^2.
+// - The polynomial's z = M^-1 r is carried by the recurrence z -= alpha
+//   M^-1 q (from r -= alpha q), so an iteration gathers the neighbours' q
+//   only, and no second residual buffer is needed.
+// - Two all-reduces per iteration: (r, z) and (r, r) after the x/r/z update,
+//   (p, q) after q = A z + beta q.
+// 15 FP64 operations a row and iteration with the polynomial (21 unscaled).
+// Measured slower at 1M faces and dropped: a form with one all-reduce per
+// iteration (Chronopoulos-Gear recurrences, contiguous row runs per block
+// and a point-to-point wait for the blocks owning neighbour rows), whose
+// polynomial rebuilt each neighbour's new residual from three vectors; and
+// an all-reduce whose partials are staged in shared memory for one warp to
+// sum (its 24 KB of shared memory is L1 the gathers lose).
 //
 // `dyn`, when set, holds the stopping target (target2, relative to (b, b))
 // and the iteration limit in device memory, written by a controller kernel
@@ -830,135 +929,169 @@ __global__ void __launch_bounds__(kCgBlock, kCgBlocksPerSm)
                     int* err, Scalars* sc, double tol, int maxit, GridWait gw, const MScal* dyn) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool poly = D.r2 != nullptr;
+    V *x = D.x, *r = D.r, *p = D.p, *q = D.q, *s = D.s, *offs = D.offs;
+    V* z = poly ? D.zz : D.r;  // Jacobi: z = r in the scaled system
     unsigned epoch = 0;
-    // init: r = b, z = D^-1 b, p = z, q = A z
-    double a3[3], t3[3];
-    if (D.r2) {
-        // polynomial preconditioner: z = M^-1 b needs the neighbours' b
-        // only, but A z needs their z, hence a second phase
-        V acc[3] = {0, 0, 0};
+    int st = 0;
+    const auto total = [](const double (&g)[1], double (&o)[1]) {
+        o[0] = g[0];
+        return 0;
+    };
+    // set-up 1: s = d^-1/2, r = s b, y = 0; (b, b)
+    double bb, rho, rr;
+    V alpha = 0;  // in the vector precision (converted once, in one lane)
+    {
+        V a[1] = {0};
         for (int64_t i = i0; i < Tp; i += stride) {
-            const V bi = D.b[i];
-            const V zi = dep_precond<V>(D, nbr, Tp, i, bi, D.b, nullptr, V(0));
-            D.r[i] = bi;
-            D.zz[i] = zi;
-            D.p[i] = zi;
-            D.x[i] = 0;
-            acc[0] += bi * zi;
-            acc[2] += bi * bi;
+            const V bi = D.b[i], si = rsqrt_v(D.diag[i]);
+            s[i] = si;
+            r[i] = si * bi;
+            x[i] = 0;
+            a[0] += bi * bi;
         }
-        for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
-        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, gw, t3)) return;
-        V zq = 0;
-        for (int64_t i = i0; i < Tp; i += stride) {
-            V qi = D.diag[i] * D.zz[i];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int32_t nb = nbr[j * Tp + i];
-                if (nb >= 0) qi += D.off[j * Tp + i] * D.zz[nb];
-            }
-            D.q[i] = qi;
-            zq += D.zz[i] * qi;
-        }
-        double a1[1] = {(double)zq}, t1[1];
-        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, gw, t1)) return;
-        t3[1] = t1[0];
-    } else {
-        V acc[3] = {0, 0, 0};
-        for (int64_t i = i0; i < Tp; i += stride) {
-            const V bi = D.b[i];
-            const V zi = D.dinv[i] * bi;
-            V qi = D.diag[i] * zi;
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int32_t nb = nbr[j * Tp + i];
-                if (nb >= 0) qi += D.off[j * Tp + i] * (D.dinv[nb] * D.b[nb]);
-            }
-            D.r[i] = bi;
-            D.zz[i] = zi;
-            D.p[i] = zi;
-            D.q[i] = qi;
-            D.x[i] = 0;
-            acc[0] += bi * zi;
-            acc[1] += zi * qi;
-            acc[2] += bi * bi;
-        }
-        for (int k = 0; k < 3; ++k) a3[k] = (double)acc[k];
-        if (!grid_totals<3>(a3, partials, flags, ++epoch, err, gw, t3)) return;
+        double o[1];
+        V ov[1];
+        if (!grid_totals<1, 1>(a, partials, flags, ++epoch, err, gw, o, ov, st, total)) return;
+        bb = o[0];
     }
-    double rho = t3[0];
-    const double bb = t3[2];
+    // set-up 2 (every s is visible): the scaled couplings (0 without a
+    // neighbour), z = M^-1 r, p = z; (r, z)
+    {
+        V a[1] = {0};
+        for (int64_t i = i0; i < Tp; i += stride) {
+            const V si = s[i], ri = r[i];
+            V zi = ri;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                V o = 0;
+                if (nb >= 0) {
+                    o = si * D.off[j * Tp + i] * s[nb];
+                    if (poly) zi -= o * r[nb];
+                }
+                offs[j * Tp + i] = o;
+            }
+            if (poly) z[i] = zi;
+            p[i] = zi;
+            a[0] += ri * zi;
+        }
+        double o[1];
+        V ov[1];
+        if (!grid_totals<1, 1>(a, partials, flags, ++epoch, err, gw, o, ov, st, total)) return;
+        rho = o[0];
+    }
     const double target2 = (dyn ? dyn->target2 : tol * tol) * bb;
     if (dyn) maxit = dyn->maxit;
-    int status = 0, it = 0;
-    double rr = bb;
-    if (bb == 0.0) status = 1;
-    else if (!(t3[1] > 0.0)) status = 2;
-    double alpha = status ? 0.0 : rho / t3[1];
-    while (status == 0) {
-        double a2[2], t2[2];
-        {
-            const V al = (V)alpha;
-            V acc[2] = {0, 0};
-            // polynomial preconditioner: the residual alternates between
-            // two buffers (read the old, write the new)
-            const V* rin = (D.r2 && (it & 1)) ? D.r2 : D.r;
-            V* rout = D.r2 ? ((it & 1) ? D.r : D.r2) : D.r;
-            for (int64_t i = i0; i < Tp; i += stride) {
-                D.x[i] += al * D.p[i];
-                const V ri = rin[i] - al * D.q[i];
-                rout[i] = ri;
-                const V zi = dep_precond<V>(D, nbr, Tp, i, ri, rin, D.q, al);
-                D.zz[i] = zi;
-                acc[0] += ri * zi;
-                acc[1] += ri * ri;
+    // set-up 3: q = A p; (p, q), alpha = (r, z) / (p, q)
+    {
+        V a[1] = {0};
+        for (int64_t i = i0; i < Tp; i += stride) {
+            const V pi = p[i];
+            V qi = pi;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int32_t nb = nbr[j * Tp + i];
+                if (nb >= 0) qi += offs[j * Tp + i] * p[nb];
             }
-            a2[0] = (double)acc[0];
-            a2[1] = (double)acc[1];
+            q[i] = qi;
+            a[0] += pi * qi;
         }
-        if (!grid_totals<2>(a2, partials, flags, ++epoch, err, gw, t2)) return;
-        ++it;
-        rr = t2[1];
-        if (rr <= target2) {
-            status = 1;
-            break;
-        }
-        if (!isfinite(rr)) {
-            status = 2;
-            break;
-        }
-        if (it >= maxit) {
-            status = 3;
-            break;
-        }
-        const double beta = t2[0] / rho;
-        rho = t2[0];
-        double a1[1], t1[1];
+        double o[1];
+        V ov[1];
+        const auto first = [bb, rho](const double (&g)[1], double (&o)[1]) {
+            o[0] = 0.0;
+            if (bb == 0.0) return 1;
+            if (!(g[0] > 0.0)) return 2;
+            o[0] = rho / g[0];
+            return 0;
+        };
+        if (!grid_totals<1, 1>(a, partials, flags, ++epoch, err, gw, o, ov, st, first)) return;
+        alpha = ov[0];
+    }
+    int status = st, it = 0;
+    rr = bb;
+    while (status == 0) {
+        // y += alpha p, r -= alpha q, z -= alpha M^-1 q; (r, z) and the
+        // unscaled (r, r); then the stopping tests and beta in one lane
         {
-            const V be = (V)beta;
-            V acc = 0;
+            const V al = alpha;
+            V a[2] = {0, 0};
             for (int64_t i = i0; i < Tp; i += stride) {
-                V az = D.diag[i] * D.zz[i];
+                x[i] += al * p[i];
+                const V qi = q[i];
+                const V ri = r[i] - al * qi;
+                r[i] = ri;
+                V zi = ri;
+                if (poly) {
+                    V mq = qi;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        const int32_t nb = nbr[j * Tp + i];
+                        if (nb >= 0) mq -= offs[j * Tp + i] * q[nb];
+                    }
+                    zi = z[i] - al * mq;
+                    z[i] = zi;
+                }
+                a[0] += ri * zi;
+                a[1] += ri * ri * D.diag[i];
+            }
+            const int itn = it + 1;
+            const auto step = [=](const double (&g)[2], double (&o)[3]) {
+                o[0] = g[0];
+                o[1] = g[1];
+                o[2] = 0.0;
+                if (g[1] <= target2) return 1;
+                if (!isfinite(g[1])) return 2;
+                if (itn >= maxit) return 3;
+                o[2] = g[0] / rho;  // beta
+                return 0;
+            };
+            double o[3];
+            V ov[3];
+            if (!grid_totals<2, 3>(a, partials, flags, ++epoch, err, gw, o, ov, st, step)) return;
+            it = itn;
+            rr = o[1];
+            if (st) {
+                status = st;
+                break;
+            }
+            rho = o[0];
+            // p = z + beta p, q = A z + beta q; (p, q), alpha = rho / (p, q)
+            const V be = ov[2];
+            V b1[1] = {0};
+            for (int64_t i = i0; i < Tp; i += stride) {
+                const V zi = z[i];
+                V az = zi;
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     const int32_t nb = nbr[j * Tp + i];
-                    if (nb >= 0) az += D.off[j * Tp + i] * D.zz[nb];
+                    if (nb >= 0) az += offs[j * Tp + i] * z[nb];
                 }
-                const V pi = D.zz[i] + be * D.p[i];
-                const V qi = az + be * D.q[i];
-                D.p[i] = pi;
-                D.q[i] = qi;
-                acc += pi * qi;
+                const V pi = zi + be * p[i];
+                const V qi = az + be * q[i];
+                p[i] = pi;
+                q[i] = qi;
+                b1[0] += pi * qi;
             }
-            a1[0] = (double)acc;
+            const auto step2 = [rho](const double (&g)[1], double (&o)[1]) {
+                o[0] = 0.0;
+                if (!(g[0] > 0.0)) return 2;
+                o[0] = rho / g[0];
+                return 0;
+            };
+            double o2[1];
+            V ov2[1];
+            if (!grid_totals<1, 1>(b1, partials, flags, ++epoch, err, gw, o2, ov2, st, step2)) return;
+            if (st) {
+                status = st;
+                break;
+            }
+            alpha = ov2[0];
         }
-        if (!grid_totals<1>(a1, partials, flags, ++epoch, err, gw, t1)) return;
-        if (!(t1[0] > 0.0)) {
-            status = 2;
-            break;
-        }
-        alpha = rho / t1[0];
     }
+    // back to the unscaled solution x = S y
+    for (int64_t i = i0; i < Tp; i += stride) x[i] *= s[i];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         sc->iter = it;
         sc->done = status;
@@ -1697,15 +1830,24 @@ int configure_cg(Ctx& c) {
 // The deposition CG's system and work vectors, FP64 and (MIXED) FP32; the
 // second residual buffer exists with dep_neumann only.
 static DepSys<double> dep_sys64(Ctx& c) {
-    return DepSys<double>{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x, c.dr, c.dz_, c.dp, c.dq, c.dr2};
+    return DepSys<double>{c.D.diag, c.D.off, c.D.dinv, c.D.rhs, c.D.x,           c.dr,
+                          c.dz_,    c.dp,    c.dq,     c.dr2,  c.dscale, c.dscale + c.P.Tp};
 }
 
 static DepSys<float> dep_sys32(Ctx& c) {
     const int64_t Tp = c.P.Tp;
     float* f = c.dep32;
-    return DepSys<float>{f,          f + Tp,     f + 4 * Tp, f + 5 * Tp, f + 6 * Tp,
-                         f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp, c.cfg.dep_neumann ? f + 11 * Tp : nullptr};
+    return DepSys<float>{f,          f + Tp,     f + 4 * Tp, f + 5 * Tp,  f + 6 * Tp,
+                         f + 7 * Tp, f + 8 * Tp, f + 9 * Tp, f + 10 * Tp, c.cfg.dep_neumann ? f + 11 * Tp : nullptr,
+                         f + 12 * Tp, f + 13 * Tp};
 }
+
+// Algorithmic bytes of the persistent CG per face: each array touched once
+// per phase, the neighbour gathers as reads of the same vector.  Set-up:
+// 23 values + 24 B of neighbour ids; an iteration with the polynomial
+// preconditioner: 20 values + 24 B of ids, with Jacobi 15 values + 12 B.
+static int64_t cg_setup_bytes(int vb) { return 23 * vb + 24; }
+static int64_t cg_iter_bytes(int vb, bool poly) { return poly ? 20 * vb + 24 : 15 * vb + 12; }
 
 // One cooperative CG launch on system D; returns the status and iterations in sc.
 template <typename V>
@@ -1769,7 +1911,7 @@ static int solve_deposition_mixed(Ctx& c, cudaStream_t s, double tol) {
         prof_begin(c, s);
         if ((rc = launch_cg<float>(c, s, D32, c.coop_blocks32, sc, itol, std::min(c.cfg.dep_maxit, 500)))) return rc;
         const int inner = c.sc_host->iter;
-        prof_end(c, s, PBSM3D_K_CG, T * 48 + (int64_t)inner * T * 74);
+        prof_end(c, s, PBSM3D_K_CG, T * (cg_setup_bytes(4) + (int64_t)inner * cg_iter_bytes(4, c.cfg.dep_neumann)));
         c.dep_iters += inner;
         c.dep_refinements += 1;
         prof_begin(c, s);
@@ -1974,7 +2116,7 @@ int solve_deposition(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
     if (rc) return rc;
     const int done = c.sc_host->done;
     c.dep_iters = c.sc_host->iter;
-    prof_end(c, s, PBSM3D_K_CG, T * 96 + (int64_t)c.dep_iters * T * 148);
+    prof_end(c, s, PBSM3D_K_CG, T * (cg_setup_bytes(8) + (int64_t)c.dep_iters * cg_iter_bytes(8, c.cfg.dep_neumann)));
     const double bn2 = c.sc_host->bnorm2;
     prof_begin(c, s);
     k_cg_resid<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.D, c.F.nbr, c.dr, sc, part);
