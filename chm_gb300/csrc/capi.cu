@@ -423,6 +423,12 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     A.csubl = dalloc<double>(c, R, ok);
     A.fac_l = dalloc<double>(c, R, ok);
     A.fac_ib = dalloc<double>(c, R, ok);
+    A.fac_u = dalloc<double>(c, R, ok);
+    if (!P.mixed && cfg.neumann > 0) {
+        A.fac_piv = dalloc<double>(c, R, ok);
+        A.latp = dalloc<double>(c, (size_t)3 * R, ok);
+        c.nu64 = dalloc<double>(c, R, ok);
+    }
     c.r = dalloc<double>(c, R, ok);
     if (P.mixed) {
         A.uz32 = dalloc<float>(c, R, ok);

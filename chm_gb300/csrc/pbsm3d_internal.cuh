@@ -184,8 +184,15 @@ struct Susp {
     double* x;        // [R]
     double* u_z;      // [R]
     double* csubl;    // [R]
+    // FP64 Thomas factors of the column tridiagonals: the inverse pivots ib,
+    // and the off-diagonals scaled by them (ib_z lo_z, ib_z up_z)
     double* fac_l;    // [R]
     double* fac_ib;   // [R]
+    double* fac_u;    // [R]
+    // FP64 with the polynomial preconditioner: the pivots and the lateral
+    // bands scaled by ib (null otherwise)
+    double* fac_piv = nullptr;  // [R]
+    double* latp = nullptr;     // [3][R]
     // MIXED: the FP32 operator.  Its lateral bands are not stored: a row's
     // lat_f = u_z L1_f + L0_f comes from its u_z and its face's constants
     float* uz32;      // [R] u_z
@@ -316,6 +323,7 @@ struct Ctx {
     float *r32, *rh32, *p32, *v32, *s32, *t32, *zp32, *zs32, *x32;
     // polynomial preconditioner (neumann > 0): the last u - N z and the other z, [R] each
     double *nw = nullptr, *nz = nullptr;
+    double* nu64 = nullptr;  // FP64 with neumann > 0: ib * u, read by the polynomial steps [R]
     float *nw32 = nullptr, *nz32 = nullptr;
     // deposition CG vectors [Tp]
     double *dr, *dz_, *dp, *dq;

@@ -429,6 +429,11 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
                 A.csubl[r] = 0.0;
                 A.fac_l[r] = 0.0;
                 A.fac_ib[r] = 1.0;
+                A.fac_u[r] = 0.0;
+                if (A.latp) {
+                    A.fac_piv[r] = 1.0;
+                    for (int k = 0; k < 3; ++k) A.latp[k * R + r] = 0.0;
+                }
                 if (P.mixed) {
                     A.uz32[r] = 0.f;
                     if (z == 0)
@@ -597,8 +602,17 @@ __global__ void __launch_bounds__(kBlock, 2) k_assemble_suspension(Params P, Fac
                 const double lz = (z == 0) ? 0.0 : lo * prev_ib;
                 const double beta = (z == 0) ? dg : dg - lz * prev_up;
                 const double ib = rcp_t(beta);
-                A.fac_l[r] = lz;
+                // the factors scaled by the inverse pivot (the FP64 column
+                // solve's form), and for the FP64 polynomial steps the pivot
+                // and the lateral bands times ib
+                A.fac_l[r] = ib * lo;
                 A.fac_ib[r] = ib;
+                A.fac_u[r] = ib * up;
+                if (A.latp) {
+                    A.fac_piv[r] = beta;
+#pragma unroll
+                    for (int f = 0; f < 3; ++f) A.latp[f * R + r] = ib * lat[f];
+                }
                 if (P.mixed) {
                     l32 = f32_rn(lz);
                     ib32 = f32_rn(ib);
@@ -864,8 +878,9 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     const int64_t T = c.P.T, rows = T * c.P.L;
     // the three passes count as one assembly; the algorithmic bytes are those
     // of the whole step: per face 8 forcing + 133 B geometry in, Qsalt + flag
-    // out (+6 floats of coupling constants MIXED); per row 10 doubles out, 2
-    // more with the FP64 column factors, 4 floats MIXED
+    // out (+6 floats of coupling constants MIXED); per row 10 doubles out, 3
+    // more with the FP64 column factors, 4 more with the FP64 polynomial
+    // preconditioner's scaled bands and pivot, 4 floats MIXED
     prof_begin(c, s);
     cudaMemsetAsync(c.A.n_slow, 0, sizeof(int), s);
     // the wind inputs on the device (scale_wind_vert, fetchr), when asked for
@@ -877,7 +892,7 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
     prof_end(c, s, PBSM3D_K_ASSEMBLE,
              T * (64 + 133 + 9 + (c.P.mixed ? 24 : 0)) +
-                 rows * (80 + (c.P.fac64 ? 16 : 0) + (c.P.mixed ? 16 : 0)));
+                 rows * (80 + (c.P.fac64 ? 24 : 0) + (c.A.latp ? 32 : 0) + (c.P.mixed ? 16 : 0)));
     c.launches += c.asm_kernels;
 }
 

@@ -92,14 +92,20 @@ namespace {
 template <typename V>
 struct Op {
     const V* lat;    // [3][R] lateral bands (FP64; null in FP32)
-    const V* l;      // [R] forward multipliers
+    const V* l;      // [R] forward multipliers (FP64: scaled, ib_z lo_z)
     const V* ib;     // [R] inverse pivots
-    const V* up;     // [R] above band
+    const V* up;     // [R] above band (FP64: scaled, ib_z up_z)
     const int32_t* nbr;  // [3][Tp]
     int64_t Tp, R;
     int L;
     const float* uz;   // FP32: [R] u_z of each row
     const float* l01;  // FP32: [6][Tp] L0_f, L1_f of each face
+    // FP64 with the polynomial preconditioner: the lateral bands scaled by
+    // the row's inverse pivot, the pivots, and the buffer of the scaled
+    // vector ib * u that the steps read (null otherwise)
+    const V* latp = nullptr;  // [3][R]
+    const V* piv = nullptr;   // [R]
+    V* nu = nullptr;          // [R]
 };
 
 // Values a row, and bytes a face, of the lateral couplings (traffic counts).
@@ -150,6 +156,12 @@ struct LatFace<float> {
 enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3 };
 
 // z = B^{-1} u for one column, u already in smem column g[z*bd + col].
+// FP32: the Thomas sweeps on (l, ib, up), 3 operations a row.  FP64, whose
+// pipe bounds these kernels on this GPU: the caller stores ib * u, and the
+// sweeps run on the factors scaled by the inverse pivots (B = L D U', so
+// D^-1 L^-1 u = L''^-1 (D^-1 u) with L'' = D^-1 L D unit lower, sub-diagonal
+// ib_z lo_z, and U' = D^-1 U unit upper, super-diagonal ib_z up_z): 2
+// operations a row.
 template <typename V>
 __device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V* zout, int bd, int col) {
     V prev = 0;
@@ -162,8 +174,23 @@ __device__ __forceinline__ void column_solve(const Op<V>& op, int64_t i, V* g, V
     V y = 0;
     for (int z = op.L - 1; z >= 0; --z) {
         const int64_t r = (int64_t)z * op.Tp + i;
-        y = (g[z * bd + col] - op.up[r] * y) * op.ib[r];
+        if constexpr (sizeof(V) == 8)
+            y = g[z * bd + col] - op.up[r] * y;
+        else
+            y = (g[z * bd + col] - op.up[r] * y) * op.ib[r];
         zout[r] = y;
+    }
+}
+// The column solve's input for row k: u itself (FP32) or ib * u (FP64),
+// which the polynomial steps of an FP64 solve also read (op.nu).
+template <typename V>
+__device__ __forceinline__ V column_in(const Op<V>& op, int64_t k, V u) {
+    if constexpr (sizeof(V) == 8) {
+        const V g = u * op.ib[k];
+        if (op.nu) op.nu[k] = g;
+        return g;
+    } else {
+        return u;
     }
 }
 
@@ -314,7 +341,7 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_p(Op
                 const int64_t k = (int64_t)z * op.Tp + i;
                 const V pk = r[k] + beta * (p[k] - omega * v[k]);
                 p[k] = pk;
-                g[z * W + cl.f] = pk;
+                g[z * W + cl.f] = column_in(op, k, pk);
             }
         if (LC > 1) __syncthreads();
         if (valid && cl.lane == 0) column_solve(op, i, g, zp, W, cl.f);
@@ -344,7 +371,7 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op
                 const int64_t k = (int64_t)z * op.Tp + i;
                 const V sk = r[k] - alpha * v[k];
                 s[k] = sk;
-                g[z * W + cl.f] = sk;
+                g[z * W + cl.f] = column_in(op, k, sk);
             }
         if (LC > 1) __syncthreads();
         if (valid && cl.lane == 0) column_solve(op, i, g, zs, W, cl.f);
@@ -356,7 +383,10 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op
 // C = N B^-1 (a truncated Neumann series; Saad, Iterative Methods for Sparse
 // Linear Systems, section 12.3): w = u - N zin, zout = B^{-1} w.  Starting
 // from zin = B^{-1} u, K steps give zout = M^-1 u, and A zout = w + N zout,
-// so the lateral kernels that follow take w in place of u.
+// so the lateral kernels that follow take w in place of u.  FP64 works on
+// ib * w = ib * u - (ib N) zin from the stored ib * u and the scaled bands
+// (5 FP64 operations a row instead of 6); its last step writes w = piv * (ib
+// * w) for the lateral kernel.
 template <typename V, bool WRITE_W, int LC>
 __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
     k_bicg_neu(Op<V> op, Tiles tl, int W, const V* __restrict__ u, const V* __restrict__ zin, V* __restrict__ w,
@@ -376,7 +406,9 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
             const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
             // FP32: the face's six coupling constants stay in registers over the
             // column (40 a thread with four layers in flight, no spills)
-            const LatFace<V> lf(op, i);
+            Op<V> opn = op;
+            if constexpr (sizeof(V) == 8) opn.lat = op.latp;
+            const LatFace<V> lf(opn, i);
 #pragma unroll 4
             for (int z = cl.lane; z < op.L; z += LC) {
                 const int64_t base = (int64_t)z * op.Tp;
@@ -386,7 +418,12 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
                 if (n0 >= 0) wk -= la[0] * zin[base + n0];
                 if (n1 >= 0) wk -= la[1] * zin[base + n1];
                 if (n2 >= 0) wk -= la[2] * zin[base + n2];
-                if (WRITE_W) w[k] = wk;  // only the last step's w is read (by the lateral kernel)
+                if (WRITE_W) {  // only the last step's w is read (by the lateral kernel)
+                    if constexpr (sizeof(V) == 8)
+                        w[k] = wk * op.piv[k];
+                    else
+                        w[k] = wk;
+                }
                 g[z * W + cl.f] = wk;
             }
         }
@@ -645,7 +682,7 @@ __global__ void __launch_bounds__(kBlock) k_jacobi_sweep(Op<double> op, const do
             if (n0 >= 0) u -= op.lat[k] * xi[base + n0];
             if (n1 >= 0) u -= op.lat[op.R + k] * xi[base + n1];
             if (n2 >= 0) u -= op.lat[2 * op.R + k] * xi[base + n2];
-            g[z * blockDim.x + threadIdx.x] = u;
+            g[z * blockDim.x + threadIdx.x] = u * op.ib[k];
         }
         column_solve(op, i, g, xo, (int)blockDim.x, (int)threadIdx.x);
     }
@@ -1320,8 +1357,12 @@ template <typename V>
 Op<V> make_op(Ctx& c);
 template <>
 Op<double> make_op<double>(Ctx& c) {
-    return Op<double>{c.A.band + c.P.R, c.A.fac_l, c.A.fac_ib, c.A.band + 5 * c.P.R, c.F.nbr, c.P.Tp, c.P.R, c.P.L,
-                      nullptr, nullptr};
+    Op<double> op{c.A.band + c.P.R, c.A.fac_l, c.A.fac_ib, c.A.fac_u, c.F.nbr, c.P.Tp, c.P.R, c.P.L,
+                  nullptr,          nullptr};
+    op.latp = c.A.latp;
+    op.piv = c.A.fac_piv;
+    op.nu = c.A.latp ? c.nu64 : nullptr;
+    return op;
 }
 template <>
 Op<float> make_op<float>(Ctx& c) {
@@ -1433,19 +1474,22 @@ const V* launch_neumann(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl
     const int K = c.cfg.neumann;
     V* a = (K & 1) ? ztmp : zfinal;
     V* b = (K & 1) ? zfinal : ztmp;
+    const V* un = op.nu ? op.nu : u;  // FP64: the steps read ib * u
     for (int j = 0; j < K; ++j) {
         const bool last = j == K - 1;
         if (prof) prof_begin(c, s);
         if (last)
-            launch_neu_step<V, true>(c, s, op, tl, gi, u, a, w, b, ms);
+            launch_neu_step<V, true>(c, s, op, tl, gi, un, a, w, b, ms);
         else
-            launch_neu_step<V, false>(c, s, op, tl, gi, u, a, w, b, ms);
+            launch_neu_step<V, false>(c, s, op, tl, gi, un, a, w, b, ms);
         // per row u, z in, z out, the lateral couplings (3 bands, or u_z in
-        // FP32), 3 column factors, w on the last step; per face the ids (and
-        // the FP32 couplings' 6 constants)
+        // FP32), the column factors (3 in FP32, 2 scaled ones in FP64), w on
+        // the last step (FP64: and the pivot); per face the ids (and the FP32
+        // couplings' 6 constants)
+        const int64_t vals = sizeof(V) == 8 ? (last ? 7 : 5) : (last ? 7 : 6);
         if (prof)
             prof_end(c, s, PBSM3D_K_NEUMANN,
-                     rows * ((last ? 7 : 6) + kLatRow<V>) * sizeof(V) + rows / c.P.L * (12 + kLatFace<V>));
+                     rows * (vals + kLatRow<V>) * sizeof(V) + rows / c.P.L * (12 + kLatFace<V>));
         std::swap(a, b);
     }
     return K > 0 ? w : u;
@@ -1498,14 +1542,14 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         for (int k = 0; k < chunk; ++k) {
             prof_begin(c, s);
             launch_col_p<V>(c, s, op, tl, gi, r, p, v, neumann_first(c, zp, nz), ms);
-            prof_end(c, s, PBSM3D_K_BICG_P, rows * 8 * sv_);
+            prof_end(c, s, PBSM3D_K_BICG_P, rows * (8 + (op.nu ? 1 : 0)) * sv_);
             const V* up = launch_neumann<V>(c, s, op, tl, gi, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
             launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms);
-            prof_end(c, s, PBSM3D_K_BICG_S, rows * 7 * sv_);
+            prof_end(c, s, PBSM3D_K_BICG_S, rows * (7 + (op.nu ? 1 : 0)) * sv_);
             const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
             k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
