@@ -85,6 +85,13 @@ class Dist:
         return float(t.item())
 
 
+def fp64_rate(lib):
+    """The GPU's FP64 FMA rate (thread operations a second), measured by the
+    library's probe; None when it fails."""
+    r = C.c_double(0.0)
+    return r.value if lib.pbsm3d_fp64_rate(C.byref(r)) == 0 and r.value > 0 else None
+
+
 def measured_peak():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -268,6 +275,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     import torch
     torch.cuda.set_device(local_rank)
     lib = capi.load()
+    fma_rate = fp64_rate(lib)
     w, L = make_workload(args, rank)
     T = w.mesh.n_faces
     nsteps = args.warmup + args.steps
@@ -464,6 +472,39 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
     roof, step_roof, kernels = kernel_figures(prof_name)
     mroof, mstep_roof, mkernels = kernel_figures(mixed_prof)
 
+    def fp64_figures(pname, kern, rows, rate):
+        """The FP64 kernels' bound on this GPU is the FP64 pipe: each class's
+        FP64 thread operations per row (ncu-measured, profiles/fp64_ops.json)
+        times the rows of its launches over its event time, against the
+        measured FMA rate (FMA = 2 flops)."""
+        if pname is None or not is_fp64(pname) or not kern or not rate:
+            return None
+        try:
+            tab = json.loads((ROOT / "profiles" / "fp64_ops.json").read_text())
+        except Exception:
+            return None
+        K = VARIANTS[pname].get("neumann", 0)
+        out = {}
+        for cls, fig in kern.items():
+            per_row = tab.get(f"{cls}:fp64")
+            if per_row is None or not fig["ms"]:
+                continue
+            if isinstance(per_row, dict):  # the polynomial steps: K-1 intermediate, 1 last
+                per_row = ((K - 1) * per_row["mid"] + per_row["last"]) / K if K > 0 else None
+            if per_row is None:
+                continue
+            gflops = 2.0 * per_row * rows * fig["launches"] / (fig["ms"] / 1e3) / 1e9
+            out[cls] = {"fp64_ops_per_row": round(per_row, 3), "achieved_gflops": round(gflops, 1),
+                        "frac": round(gflops / (2.0 * rate / 1e9), 4)}
+        if not out:
+            return None
+        top = max(out, key=lambda c: kern[c]["ms"])
+        return {"bound": "fp64_pipe", "kernel": top, "achieved": out[top]["achieved_gflops"],
+                "peak": round(2.0 * rate / 1e9, 1), "peak_kind": "measured (pbsm3d_fp64_rate: FMA chains, FMA = 2)",
+                "unit": "GFLOP/s", "frac": out[top]["frac"], "variant": pname, "classes": out}
+
+    fp64_roof = fp64_figures(prof_name, kernels, T * L, fma_rate)
+
     def solver_summary(sts):
         return {"susp_iters_mean": float(np.mean([s["susp_iters"] for s in sts])),
                 "susp_refinements_mean": float(np.mean([s["susp_refinements"] for s in sts])),
@@ -506,6 +547,7 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 "phases_ms": phase_means(e2e_stats)},
         "gpu_launches": int(sum(s["gpu_launches"] for s in stats)),
         "roofline": roof,
+        "fp64_roofline": fp64_roof,
         "step_roofline": step_roof,
         "kernels": kernels,
         "solver_stats": solver_summary(stats),

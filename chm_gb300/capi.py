@@ -119,7 +119,7 @@ EXPORTS = [
     "pbsm3d_mlp_gemm_bf16", "pbsm3d_mlp_predict", "pbsm3d_ensemble_create", "pbsm3d_member_offsets",
     "pbsm3d_set_snow", "pbsm3d_get_snow", "pbsm3d_scale_wind_vert", "pbsm3d_fetchr", "pbsm3d_mesh_read",
     "pbsm3d_mesh_describe", "pbsm3d_mesh_arrays", "pbsm3d_mesh_free", "pbsm3d_mesh_last_error", "pbsm3d_get_debug",
-    "pbsm3d_set_stations", "pbsm3d_uniform_wind", "pbsm3d_math_eval",
+    "pbsm3d_set_stations", "pbsm3d_uniform_wind", "pbsm3d_math_eval", "pbsm3d_fp64_rate",
     "pbsm3d_arm_wait_timeout_test", "pbsm3d_set_column_geometry", "pbsm3d_get_column_geometry",
 ]
 
@@ -217,6 +217,8 @@ def load(path: Path | None = None):
     lib.pbsm3d_arm_wait_timeout_test.restype = C.c_int
     lib.pbsm3d_math_eval.argtypes = [C.c_int32, C.c_int64, vp, vp, vp]
     lib.pbsm3d_math_eval.restype = C.c_int
+    lib.pbsm3d_fp64_rate.argtypes = [C.POINTER(C.c_double)]
+    lib.pbsm3d_fp64_rate.restype = C.c_int
     lib.pbsm3d_last_error.argtypes = [vp]
     lib.pbsm3d_last_error.restype = C.c_char_p
     lib.pbsm3d_destroy.argtypes = [vp]

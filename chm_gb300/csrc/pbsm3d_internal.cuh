@@ -448,6 +448,45 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+// Warp sums of NT FP64 values, every lane ending with the totals (the same
+// order in every call: deterministic).  The FP64 pipe of this GPU issues a
+// small fraction of the FP32 rate, so the values share the first butterfly
+// steps: with two, each half-warp adds one of them and the four remaining
+// steps carry one value a lane (5 FP64 adds a lane instead of 10); with
+// three, the quarter-warps take v0, v1, v2 and a zero after two shared steps
+// (6 instead of 15).
+__device__ __forceinline__ void warp_sums(double (&v)[1]) { v[0] = warp_sum(v[0]); }
+__device__ __forceinline__ void warp_sums(double (&v)[2]) {
+    const bool lo = (threadIdx.x & 31) < 16;
+    double keep = lo ? v[0] : v[1];
+    keep += __shfl_xor_sync(0xffffffffu, lo ? v[1] : v[0], 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+    v[0] = __shfl_sync(0xffffffffu, keep, 0);
+    v[1] = __shfl_sync(0xffffffffu, keep, 16);
+}
+__device__ __forceinline__ void warp_sums(double (&v)[3]) {
+    const int lane = threadIdx.x & 31;
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0;
+    // lanes < 16 carry (v0, v1), lanes >= 16 carry (v2, 0)
+    double a = h16 ? v[2] : v[0], b = h16 ? 0.0 : v[1];
+    a += __shfl_xor_sync(0xffffffffu, h16 ? v[0] : v[2], 16);
+    b += __shfl_xor_sync(0xffffffffu, h16 ? v[1] : 0.0, 16);
+    // lanes with bit 3 clear keep a, the others b
+    double c = h8 ? b : a;
+    c += __shfl_xor_sync(0xffffffffu, h8 ? a : b, 8);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    v[0] = __shfl_sync(0xffffffffu, c, 0);
+    v[1] = __shfl_sync(0xffffffffu, c, 8);
+    v[2] = __shfl_sync(0xffffffffu, c, 16);
+}
+template <int NT>
+__device__ __forceinline__ void warp_sums(double (&v)[NT]) {
+#pragma unroll
+    for (int k = 0; k < NT; ++k) v[k] = warp_sum(v[k]);
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -459,18 +498,20 @@ template <int NT>
 __device__ __forceinline__ void block_sum(double (&v)[NT]) {
     __shared__ double sh[NT][32];  // up to 1024 threads
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    {
+        double w[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) {
-        double w = warp_sum(v[k]);
-        if (lane == 0) sh[k][wid] = w;
+        for (int k = 0; k < NT; ++k) w[k] = v[k];
+        warp_sums(w);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) sh[k][wid] = w[k];
     }
     __syncthreads();
     if (wid == 0) {
 #pragma unroll
-        for (int k = 0; k < NT; ++k) {
-            double w = lane < (int)(blockDim.x >> 5) ? sh[k][lane] : 0.0;
-            v[k] = warp_sum(w);
-        }
+        for (int k = 0; k < NT; ++k) v[k] = lane < (int)(blockDim.x >> 5) ? sh[k][lane] : 0.0;
+        warp_sums(v);
     }
     __syncthreads();
 }

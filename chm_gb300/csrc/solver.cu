@@ -200,7 +200,6 @@ __device__ __forceinline__ V column_in(const Op<V>& op, int64_t k, V u) {
 // once.  Tiles of members that are done are skipped.
 
 __device__ __forceinline__ float wsum(float v) { return warp_sum_f(v); }
-__device__ __forceinline__ double wsum(double v) { return warp_sum(v); }
 
 // Block b owns the contiguous run [a0, a1) of the active-tile list (whole
 // members, ascending tiles); within it each run of one member's tiles is a
@@ -241,10 +240,20 @@ __device__ bool member_totals(V (&v)[NT], double* part, const Tiles& tl, int ts,
     __shared__ double shp[NT][32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if constexpr (sizeof(V) == 8) {
+        double w[NT];
 #pragma unroll
-    for (int k = 0; k < NT; ++k) {
-        const V w = wsum(v[k]);
-        if (lane == 0) shp[k][wid] = (double)w;
+        for (int k = 0; k < NT; ++k) w[k] = v[k];
+        warp_sums(w);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < NT; ++k) shp[k][wid] = w[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < NT; ++k) {
+            const V w = wsum(v[k]);
+            if (lane == 0) shp[k][wid] = (double)w;
+        }
     }
     __syncthreads();
     // one member: the finaliser reads only the segment heads (block starts),
@@ -753,21 +762,6 @@ struct GridWait {
     int withhold;
 };
 
-// Warp sums of NT FP64 values (identical order in every call: deterministic);
-// every lane ends with the totals.  The FP64 pipe of this GPU issues a small
-// fraction of the FP32 rate, so two values share the first butterfly step:
-// each half-warp adds one of them, and the four remaining steps carry one
-// value a lane -- 5 FP64 adds a lane instead of 10.
-__device__ __forceinline__ void warp_sums(double (&v)[1]) { v[0] = warp_sum(v[0]); }
-__device__ __forceinline__ void warp_sums(double (&v)[2]) {
-    const bool lo = (threadIdx.x & 31) < 16;
-    double keep = lo ? v[0] : v[1];
-    keep += __shfl_xor_sync(0xffffffffu, lo ? v[1] : v[0], 16);
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
-    v[0] = __shfl_sync(0xffffffffu, keep, 0);
-    v[1] = __shfl_sync(0xffffffffu, keep, 16);
-}
 // First level of a block reduction: FP32 values are summed in FP32 across
 // the warp (off the FP64 pipe), then widened.
 template <int NT>

@@ -580,6 +580,13 @@ enum {
 };
 int pbsm3d_math_eval(int32_t fn, int64_t n, const double* a, const double* b, double* out);
 
+/* The GPU's FP64 fused multiply-add rate (thread operations a second),
+ * measured on the current device by a kernel of independent FMA chains that
+ * touches no memory (about 10 ms).  Measurement plumbing for the FP64
+ * roofline of the FP64 kernels, whose bound on this GPU is the FP64 pipe; no
+ * reference counterpart. */
+int pbsm3d_fp64_rate(double* fma_per_s);
+
 /* Message of the last failure on this context (or of the last failed create
  * when ctx is NULL). */
 const char* pbsm3d_last_error(const pbsm3d_ctx* ctx);

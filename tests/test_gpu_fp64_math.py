@@ -138,3 +138,17 @@ def test_f32_rounding(cuda_lib, rng):
                         np.nextafter(mid, np.inf), np.array([0.0, -0.0, 1e-40, -1e-45, 3.5e38, 3.4028235e38,
                                                               np.inf, -np.inf, np.nan])])
     assert same_bits(ev(cuda_lib, F32, x), ev(cuda_lib, CF32, x))
+
+
+def test_fp64_rate_probe(cuda_lib):
+    """pbsm3d_fp64_rate measures the FP64 FMA rate that bounds the FP64
+    kernels; the bench's FP64 roofline divides by it.  It must land near the
+    GPU's FP64 pipe rate: 2 FMA a clock per SM (1.26 TFLOP/s on 152 SMs at
+    2.07 GHz), within what clock states allow."""
+    torch = pytest.importorskip("torch")
+    rate = C.c_double(0.0)
+    assert cuda_lib.pbsm3d_fp64_rate(C.byref(rate)) == capi.OK, cuda_lib.pbsm3d_last_error(None)
+    props = torch.cuda.get_device_properties(0)
+    nominal = 2.0 * props.multi_processor_count * 2.07e9
+    assert 0.3 * nominal < rate.value < 1.2 * nominal, (rate.value, nominal)
+    assert cuda_lib.pbsm3d_fp64_rate(None) == capi.ERR_INVALID_ARG
