@@ -366,6 +366,7 @@ struct Ctx {
     int grid_geom[2][2][kNumColGeoms] = {};
     int geom = 0;
     int tune_cand = 0;
+    int bicg_hint[2] = {4, 4};  // iterations of the last host-driven BiCGStab call (FP64, FP32): the first chunk
     float tune_ms[kNumColGeoms] = {};
     bool tuned = false;
     // ledger partial sums

@@ -1506,7 +1506,15 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
     }
     Tiles tl = c.tiles;
     int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
-    int chunk = 4;
+    // iterations are launched in chunks between polls of the device's
+    // stopping flag; launches after it stops return at once but still cost
+    // a launch each (5 + 2K a polynomial-preconditioned iteration).  The
+    // first chunk is the previous solve's count; later ones grow by a
+    // quarter of the iterations done, so an overshoot stays small.
+    const int hint = sizeof(V) == 4 ? 1 : 0;
+    int chunk = std::max(1, std::min(16, c.bicg_hint[hint]));
+    int done_iters = 0;
+    const int per_it = 5 + (c.cfg.neumann > 0 ? 2 * c.cfg.neumann : 0);  // profiled launches an iteration
     int before = 0;
     {
         int rc = read_scalars(c, s, sc);
@@ -1567,9 +1575,11 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             PBSM_CUDA_TRY(cudaEventElapsedTime(&ms, te[0], te[1]));
             tune_record(c, ms / chunk / (float)std::max<int64_t>(1, act));
         }
-        // launches after the last member stopped returned at once: not counted
-        const int idle = chunk - ran - (c.sc_host->done && ran < chunk ? 1 : 0);
-        if (idle > 0) prof_drop(c, 5 * idle);
+        // launches after the last member stopped returned at once: not
+        // counted (their bytes would inflate the classes' rates)
+        done_iters += ran;
+        const int idle = chunk - ran;
+        if (idle > 0) prof_drop(c, per_it * idle);
         if (c.sc_host->done) break;
         if (tl.n > 1) {
             // members that stopped leave the active-tile list
@@ -1587,11 +1597,12 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             }
             act = active_faces(c);
         }
-        chunk = c.tuned ? std::min(16, chunk * 2) : 1;
+        chunk = c.tuned ? std::max(1, std::min(16, done_iters / 4)) : 1;
     }
     for (auto e : te)
         if (e) cudaEventDestroy(e);
     iters = c.sc_host->iter;
+    c.bicg_hint[hint] = std::max(1, done_iters);
     return 0;
 }
 
