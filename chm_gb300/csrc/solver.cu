@@ -442,16 +442,24 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
     }
 }
 
-// y = u + N z for the column of face i, with (a, y) [and (y, y)]
-template <typename V, int NT>
-__device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const V* __restrict__ u,
+// Lanes per face column of the lateral kernels (k_bicg_v, k_bicg_t2): the
+// column's layers are split over them, so a block of kBlock * kLatLanes
+// threads keeps twice the independent gathers in flight per face.  Their
+// launch geometry is fixed (it decides the order of the dot products' sums).
+constexpr int kLatLanes = 2;
+
+// y = u + N z for layers lane, lane + LC, ... of the column of face i, with
+// (a, y) [and (y, y)]
+template <typename V, int NT, int LC>
+__device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int lane, const V* __restrict__ u,
                                               const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
                                               V (&acc)[2]) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
     const LatFace<V> lf(op, i);
     // layers are independent here: unrolled so their loads overlap
-#pragma unroll 4
-    for (int z = 0; z < op.L; ++z) {
+    constexpr int kUnroll = LC == 1 ? 4 : 2;
+#pragma unroll kUnroll
+    for (int z = lane; z < op.L; z += LC) {
         const int64_t base = (int64_t)z * op.Tp;
         const int64_t k = base + i;
         const auto la = lf.row(k);
@@ -467,7 +475,7 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, const 
 
 // v = p + N zp; rv = (rhat, v); alpha = rho / rv
 template <typename V>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
                                                       const V* __restrict__ zp, V* __restrict__ v,
                                                       const V* __restrict__ rh, MScal* ms, Scalars* sc,
                                                       double* part) {
@@ -481,8 +489,8 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, Tiles tl, const 
         }
         V acc[2] = {0, 0};
         for (int t = ts; t < te; ++t) {
-            const int64_t i = tl.start[t] + threadIdx.x;
-            if (i < tl.start[t + 1]) lateral_apply<V, 1>(op, i, p, zp, v, rh, acc);
+            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+            if (i < tl.start[t + 1]) lateral_apply<V, 1, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, acc);
         }
         V a1[1] = {acc[0]};
         double tot[1];
@@ -500,7 +508,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_v(Op<V> op, Tiles tl, const 
 // t = u + N zs (u = s, or the preconditioner's last s - N z); ts = (t, s),
 // tt = (t, t); omega = ts / tt
 template <typename V>
-__global__ void __launch_bounds__(kBlock, 5) k_bicg_t2(Op<V> op, Tiles tl, const V* __restrict__ u,
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_t2(Op<V> op, Tiles tl, const V* __restrict__ u,
                                                        const V* __restrict__ zs, V* __restrict__ tv,
                                                        const V* __restrict__ s, MScal* ms, double* part) {
     const TileRange br = block_tiles(tl);
@@ -513,8 +521,8 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_t2(Op<V> op, Tiles tl, const
         }
         V acc[2] = {0, 0};
         for (int t = ts; t < te; ++t) {
-            const int64_t i = tl.start[t] + threadIdx.x;
-            if (i < tl.start[t + 1]) lateral_apply<V, 2>(op, i, u, zs, tv, s, acc);
+            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+            if (i < tl.start[t + 1]) lateral_apply<V, 2, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, s, acc);
         }
         double tot[2];
         if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
@@ -1506,6 +1514,7 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
     }
     Tiles tl = c.tiles;
     int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+    int gl = std::max(1, std::min(c.grid_lat[sizeof(V) == 4], tl.nact));
     // iterations are launched in chunks between polls of the device's
     // stopping flag; launches after it stops return at once but still cost
     // a launch each (5 + 2K a polynomial-preconditioned iteration).  The
@@ -1547,14 +1556,14 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             prof_end(c, s, PBSM3D_K_BICG_P, rows * (8 + (op.nu ? 1 : 0)) * sv_);
             const V* up = launch_neumann<V>(c, s, op, tl, gi, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
-            k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
+            k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
             prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
             launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * (7 + (op.nu ? 1 : 0)) * sv_);
             const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
-            k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
+            k_bicg_t2<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
             // u, s, t and the gathered zs a row (u is s itself without the
             // polynomial preconditioner, the last step's w with it)
             prof_end(c, s, PBSM3D_K_BICG_T,
@@ -1594,6 +1603,7 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
                 if ((rc = set_active(c, s, active))) return rc;
                 tl = c.tiles;
                 gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.nact));
+                gl = std::max(1, std::min(c.grid_lat[sizeof(V) == 4], tl.nact));
             }
             act = active_faces(c);
         }
@@ -1653,8 +1663,13 @@ int configure_solver_kernels(Ctx& c) {
         out = std::min(out, c.grid_faces);
         return r1;
     };
-    if ((rc = wave((const void*)k_bicg_v<double>, 0, c.grid_red[0]))) return rc;
-    if ((rc = wave((const void*)k_bicg_v<float>, 0, c.grid_red[1]))) return rc;
+    if ((rc = wave((const void*)k_bicg_x<double, double>, 0, c.grid_red[0]))) return rc;
+    if ((rc = wave((const void*)k_bicg_x<float, float>, 0, c.grid_red[1]))) return rc;
+    for (int k = 0; k < 2; ++k) {
+        const void* f = k ? (const void*)k_bicg_v<float> : (const void*)k_bicg_v<double>;
+        if ((rc = wave_of(f, kBlock * kLatLanes, 0, c.grid_lat[k]))) return rc;
+        c.grid_lat[k] = std::min(c.grid_lat[k], c.grid_faces);
+    }
     {
         // the tile CG: one wave of its two per-iteration kernels
         int gx[2], gq[2];
@@ -2748,13 +2763,14 @@ void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, 
                             V* p, V* v, V* sv, V* tv, V* zp, V* zs, V* nw, V* nz) {
     Op<V> op = make_op<V>(c);
     const int gr = std::max(1, std::min(c.grid_red[sizeof(V) == 4], tl.ntiles));
+    const int gl = std::max(1, std::min(c.grid_lat[sizeof(V) == 4], tl.ntiles));
     double* part = c.tile_part;
     launch_col_p<V>(c, s, op, tl, c.geom, r, p, v, neumann_first(c, zp, nz), ms);
     const V* up = launch_neumann<V>(c, s, op, tl, c.geom, p, zp, nw, nz, ms, 0, false);
-    k_bicg_v<V><<<gr, kBlock, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
+    k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
     launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms);
     const V* us = launch_neumann<V>(c, s, op, tl, c.geom, sv, zs, nw, nz, ms, 0, false);
-    k_bicg_t2<V><<<gr, kBlock, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
+    k_bicg_t2<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
     k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
 }
 
