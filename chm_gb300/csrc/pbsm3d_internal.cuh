@@ -359,6 +359,7 @@ struct Ctx {
     std::vector<double> member_bb;  // ||b_m||^2 of the current suspension solve
     int grid_red[2] = {1, 1};  // BiCGStab gather + reduction kernels
     int grid_lat[2] = {1, 1};  // the lateral kernels (v, t), kLatLanes lanes a face
+    int grid_res = 1;          // the FP64 residual kernel, kLatLanes lanes a face
     int grid_cg[2] = {1, 1};   // the tile CG's kernels (k_scg_x, k_scg_q): one wave
     // column kernels (p, s, polynomial step): one wave of blocks at each
     // geometry, [p/s or polynomial step][FP64, FP32][geometry]; the geometry

@@ -31,6 +31,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "fp64_math.cuh"
 #include "pbsm3d_internal.cuh"
 
 namespace pbsm {
@@ -588,7 +589,8 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, Tiles t
 // rhat = r, p = v = 0.  Members marked done in ms are skipped (their x is
 // final).
 template <typename V>
-__global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const double* __restrict__ band,
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2)
+    k_residual(Params P, Tiles tl, const double* __restrict__ band,
                                                      const int32_t* __restrict__ nbr, const double* __restrict__ x,
                                                      const double* __restrict__ b, double* __restrict__ r,
                                                      V* __restrict__ rv, V* __restrict__ rhv, V* __restrict__ pv,
@@ -608,11 +610,14 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const d
             continue;
         }
         double acc[3] = {0, 0, 0};
+        // kLatLanes lanes a face column, splitting its layers (as the lateral kernels)
+        const int lane = threadIdx.x / kBlock;
         for (int t = ts; t < te; ++t) {
-            const int64_t i = tl.start[t] + threadIdx.x;
+            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
             if (i >= tl.start[t + 1]) continue;
             const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
-            for (int z = 0; z < P.L; ++z) {
+#pragma unroll 1
+            for (int z = lane; z < P.L; z += kLatLanes) {
                 const int64_t base = (int64_t)z * Tp;
                 const int64_t k = base + i;
                 double ax = band[k] * x[k];
@@ -624,8 +629,10 @@ __global__ void __launch_bounds__(kBlock) k_residual(Params P, Tiles tl, const d
                 const double rk = b[k] - ax;
                 r[k] = rk;
                 if (rv) {
-                    rv[k] = (V)rk;
-                    rhv[k] = (V)rk;
+                    // FP32 copies rounded on the integer pipe (bit-identical to the cast)
+                    const V rc = sizeof(V) == 4 ? (V)f32_rn(rk) : (V)rk;
+                    rv[k] = rc;
+                    rhv[k] = rc;
                     pv[k] = 0;
                     vv[k] = 0;
                 }
@@ -1665,6 +1672,8 @@ int configure_solver_kernels(Ctx& c) {
     };
     if ((rc = wave((const void*)k_bicg_x<double, double>, 0, c.grid_red[0]))) return rc;
     if ((rc = wave((const void*)k_bicg_x<float, float>, 0, c.grid_red[1]))) return rc;
+    if ((rc = wave_of((const void*)k_residual<float>, kBlock * kLatLanes, 0, c.grid_res))) return rc;
+    c.grid_res = std::min(c.grid_res, c.grid_faces);
     for (int k = 0; k < 2; ++k) {
         const void* f = k ? (const void*)k_bicg_v<float> : (const void*)k_bicg_v<double>;
         if ((rc = wave_of(f, kBlock * kLatLanes, 0, c.grid_lat[k]))) return rc;
@@ -1734,12 +1743,13 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         }
         const Tiles tl = c.tiles;
         const int gr = std::max(1, std::min(c.grid_red[0], tl.nact));
+        const int gq = std::max(1, std::min(c.grid_res, tl.nact));
         prof_begin(c, s);
         if (c.P.mixed)
-            k_residual<float><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
+            k_residual<float><<<gq, kBlock * kLatLanes, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
                                                     c.p32, c.v32, c.msR, part, sweeps == 0, nullptr);
         else
-            k_residual<double><<<gr, kBlock, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh,
+            k_residual<double><<<gq, kBlock * kLatLanes, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh,
                                                      c.p, c.v, c.msR, part, sweeps == 0, nullptr);
         prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 88 : 96) + act * 12);
         int rc = read_members(c, s, c.msR);
@@ -2780,6 +2790,7 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     cudaStream_t s = G.cap[depth];
     const int n = tl.n;
     const int gr = std::max(1, std::min(c.grid_red[0], tl.ntiles));
+    const int gq = std::max(1, std::min(c.grid_res, tl.ntiles));
     double* part = c.tile_part;
     const bool mixed = c.P.mixed;
     const int warm = c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1);
@@ -2793,10 +2804,10 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     {
         cudaStream_t t = G.cap[depth + 1];
         if (mixed)
-            k_residual<float><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
+            k_residual<float><<<gq, kBlock * kLatLanes, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
                                                     c.p32, c.v32, c.msR, part, 1, &G.ctl->sweep);
         else
-            k_residual<double><<<gr, kBlock, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
+            k_residual<double><<<gq, kBlock * kLatLanes, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
                                                      c.v, c.msR, part, 1, &G.ctl->sweep);
         if (warm) {
             CondBody wb;
