@@ -72,11 +72,11 @@ extern "C" int pbsm3d_fp64_rate(double* fma_per_s) {
     cudaEvent_t ev[2] = {nullptr, nullptr};
     if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
     if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
-    // two resident waves of 256-thread blocks a SM; a warm-up launch of the
-    // same length lets the clocks settle, then the best of three
+    // two resident waves of 256-thread blocks a SM; warm-up launches let the
+    // clocks settle, then the best of three
     const int grid = 8 * sms, iters = 4096;
     float best = 0.f;
-    if (e == cudaSuccess) {
+    for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {  // ~0.1 s of load: the clocks settle
         k_fp64_rate<<<grid, 256>>>(iters, 0.999999, 1e-6);
         e = cudaGetLastError();
     }
