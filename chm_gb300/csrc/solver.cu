@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
 // column's layers are split over them, so a block of kBlock * kLatLanes
 // threads keeps twice the independent gathers in flight per face.  Their
 // launch geometry is fixed (it decides the order of the dot products' sums).
-constexpr int kLatLanes = 4;
+constexpr int kLatLanes = 2;
 
 // y = u + N z for layers lane, lane + LC, ... of the column of face i, with
 // (a, y) [and (y, y)]
@@ -476,7 +476,7 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int la
 
 // v = p + N zp; rv = (rhat, v); alpha = rho / rv
 template <typename V>
-__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : kLatLanes == 2 ? 2 : 1) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
                                                       const V* __restrict__ zp, V* __restrict__ v,
                                                       const V* __restrict__ rh, MScal* ms, Scalars* sc,
                                                       double* part) {
@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : kLatL
 // t = u + N zs (u = s, or the preconditioner's last s - N z); ts = (t, s),
 // tt = (t, t); omega = ts / tt
 template <typename V>
-__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : kLatLanes == 2 ? 2 : 1) k_bicg_t2(Op<V> op, Tiles tl, const V* __restrict__ u,
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_t2(Op<V> op, Tiles tl, const V* __restrict__ u,
                                                        const V* __restrict__ zs, V* __restrict__ tv,
                                                        const V* __restrict__ s, MScal* ms, double* part) {
     const TileRange br = block_tiles(tl);
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, Tiles t
 // rhat = r, p = v = 0.  Members marked done in ms are skipped (their x is
 // final).
 template <typename V>
-__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : kLatLanes == 2 ? 2 : 1)
+__global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2)
     k_residual(Params P, Tiles tl, const double* __restrict__ band,
                                                      const int32_t* __restrict__ nbr, const double* __restrict__ x,
                                                      const double* __restrict__ b, double* __restrict__ r,
