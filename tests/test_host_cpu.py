@@ -210,3 +210,88 @@ def test_consume_drift_rule():
     s, d = consume_drift(swe, depth, dm, 300.0)
     np.testing.assert_allclose(s, [80.0, 130.0, 0.0, 50.0, 6.0, 80.0])
     np.testing.assert_allclose(d, [0.5 - 20.0 / 200.0, 0.5 + 30.0 / 300.0, 0.0, 0.2, 6.0 / 300.0, 0.4])
+
+
+def _deposition_like_system(n_points=3000, seed=5):
+    """A deposition-shaped SPD system on a synthetic mesh: diag = area +
+    eps sum E/dx, off = -eps E/dx across each shared edge (PBSM3D.cpp:1546-1592)."""
+    from chm_gb300 import synth
+    w = synth.Workload(n_points, 6000.0, seed=seed)
+    m = w.mesh
+    nb = np.asarray(m.neighbor)
+    E = np.asarray(m.edge_length)
+    c = np.asarray(m.center)[:, :2]
+    area = np.asarray(m.area)
+    off = np.zeros((m.n_faces, 3))
+    diag = area.copy()
+    for j in range(3):
+        k = nb[:, j]
+        ok = k >= 0
+        wgt = 820.0 * E[ok, j] / np.linalg.norm(c[ok] - c[k[ok]], axis=1)
+        diag[ok] += wgt
+        off[ok, j] = -wgt
+    return nb, diag, off, np.random.default_rng(seed).standard_normal(m.n_faces) * area
+
+
+def _apply(nb, d, off, v):
+    y = d * v
+    for j in range(3):
+        ok = nb[:, j] >= 0
+        y[ok] += off[ok, j] * v[nb[ok, j]]
+    return y
+
+
+@pytest.mark.parametrize("poly", [False, True])
+def test_scaled_recurrence_cg_is_the_preconditioned_cg(poly):
+    """The persistent deposition CG runs on S A S (S = D^-1/2) with the
+    polynomial preconditioner's z carried by z -= alpha M^-1 q.  In exact
+    arithmetic its iterates are those of the unscaled preconditioned CG
+    (Jacobi, or M^-1 = D^-1 + D^-1 R D^-1); in FP64 both stop at the same
+    iteration of the unscaled-residual test and agree to rounding."""
+    nb, d, off, b = _deposition_like_system()
+    tol = 1e-10
+    dinv = 1.0 / d
+
+    def M(r):  # unscaled preconditioner
+        if not poly:
+            return dinv * r
+        acc = r.copy()
+        for j in range(3):
+            ok = nb[:, j] >= 0
+            acc[ok] -= off[ok, j] * dinv[nb[ok, j]] * r[nb[ok, j]]
+        return dinv * acc
+
+    x = np.zeros_like(b); r = b.copy(); z = M(r); p = z.copy(); rho = r @ z; bb = b @ b
+    for it_ref in range(1, 500):
+        q = _apply(nb, d, off, p); al = rho / (p @ q)
+        x += al * p; r -= al * q
+        if r @ r <= tol * tol * bb:
+            break
+        z = M(r); rn = r @ z; p = z + rn / rho * p; rho = rn
+
+    s = 1.0 / np.sqrt(d)
+    offs = np.zeros_like(off)
+    for j in range(3):
+        ok = nb[:, j] >= 0
+        offs[ok, j] = s[ok] * off[ok, j] * s[nb[ok, j]]
+
+    def shifted(v, sign):  # v + sign * (offs gathered)
+        y = v.copy()
+        for j in range(3):
+            ok = nb[:, j] >= 0
+            y[ok] += sign * offs[ok, j] * v[nb[ok, j]]
+        return y
+
+    y = np.zeros_like(b); rh = s * b
+    zh = shifted(rh, -1.0) if poly else rh.copy()
+    ph = zh.copy(); rho = rh @ zh; qh = shifted(ph, 1.0); al = rho / (ph @ qh)
+    for it in range(1, 500):
+        y += al * ph; rh = rh - al * qh
+        zh = zh - al * shifted(qh, -1.0) if poly else rh
+        if (rh * rh) @ d <= tol * tol * bb:
+            break
+        rz = rh @ zh; be = rz / rho; rho = rz
+        ph = zh + be * ph; qh = shifted(zh, 1.0) + be * qh; al = rho / (ph @ qh)
+    assert it == it_ref
+    np.testing.assert_allclose(s * y, x, rtol=0, atol=1e-12 * np.abs(x).max())
+    assert np.linalg.norm(b - _apply(nb, d, off, s * y)) <= 1.01 * tol * np.sqrt(bb)
