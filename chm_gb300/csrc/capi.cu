@@ -275,7 +275,7 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     P.z0_ustar_coupling = cfg.z0_ustar_coupling != 0;
     P.iterative_subl = cfg.iterative_subl != 0;
     P.subgrid = (cfg.use_subgrid_topo ? 1 : 0) | (cfg.use_subgrid_topo_V2 ? 2 : 0);
-    c.asm_kernels = 3 + (P.subgrid ? 1 : 0) + (cfg.derive_wind ? 2 : 0) + (cfg.derive_fetch ? 1 : 0);
+    c.asm_kernels = 4 + (P.subgrid ? 1 : 0) + (cfg.derive_wind ? 2 : 0) + (cfg.derive_fetch ? 1 : 0);
     c.member_offsets = offsets;
     c.member_z0.resize(members.size());
     for (size_t m = 0; m < members.size(); ++m) c.member_z0[m] = members[m].z0;

@@ -151,7 +151,9 @@ constexpr int kRowTerms = 7;  // doubles per row of Susp::slow_rows
 enum FaceValue {
     // FV_QC, FV_QL: the face's factors of the two sublimation terms; FV_EF:
     // its factor of the particle-velocity term 3 cos(pi/4) 0.005 u_z^1.36
-    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QC, FV_QL, FV_EF, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0,
+    // FV_LAMBDA: the roughness element density of a saltating face (pass 1
+    // to its saltation terms, pass 1b)
+    FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QC, FV_QL, FV_EF, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0, FV_LAMBDA,
     FV_COUNT
 };
 

@@ -202,14 +202,10 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
         bool slow = false;
         if (i < P.T) {
             const Member mp = Mb.prm[Mb.face_member[i]];
-            double fetch = 1000;
-            if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
             const double uref = F.UR[i];
             double snow_depth = F.sd[i];
             snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
             const double u2 = F.U2[i];
-            double swe = F.swe[i];
-            swe = is_nan_chm(swe) ? 0 : swe;
             double height_diff = smax(0.0, G.canopy[i] - snow_depth);
             if (!P.enable_veg) height_diff = 0;
             double ustar = 1.3;
@@ -245,69 +241,30 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                 z0 = smax(mp.z0, 0.6131702345e-2 * ustar * ustar + .5 * lambda);
             if (!saltation) ustar = smax(0.01, kKappa * uref / mp.log_zur_z0);
             ustar = smax(0.01, ustar);
-            double hs = 0;
-            if (saltation) hs = 0.08436 * pow_t(ustar, 1.27, mt);
+            // the saltation terms (hs, c_salt, Qsalt, the over-erosion check)
+            // of the saltating faces run in pass 1b over their compacted list,
+            // so that warps do not carry them for the ~70% of faces without
+            // saltation; the other faces are final here
             slow = saltation;  // hs > 0
-            double Qsalt = 0;
-            double c_salt = 0;
             const double t = F.t[i] + 273.15;
             double vx, vy;
             bearing_to_cartesian(F.dir[i], vx, vy);
             const double ux = -vx, uy = -vy;
-            double mx[3], my[3], Ej[3];
+            double mx[3], my[3];
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 mx[j] = G.mx[j * Tp + i];
                 my[j] = G.my[j * Tp + i];
-                Ej[j] = G.E[j * Tp + i];
             }
+            double* fv = A.face_v;
             if (saltation) {
-                const double rho_f = std_dry_air_density(G.zc[i], t, mt);
-                const double Beta = 202.0, mB = 0.16;
-                const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
-                const double tau_n_ratio = __ddiv_rn(mbl, __dadd_rn(1.0, mbl));
-                // the bracket cancels near the threshold: no contraction here
-                const double bracket =
-                    __dsub_rn(__dsub_rn(1.0, tau_n_ratio), __ddiv_rn(__dmul_rn(uth, uth), __dmul_rn(ustar, ustar)));
-                c_salt = __dmul_rn(__ddiv_rn(rho_f, __dmul_rn(3.29, ustar)), bracket);
-                if (c_salt < 0 || isnan(c_salt)) {
-                    c_salt = 0;
-                    saltation = false;
-                }
-                if (P.use_exp_fetch && fetch < 500) {
-                    const double fetch_ref = 500, mu = 3.0;
-                    c_salt *= 1.0 - exp(-mu * fetch / fetch_ref);
-                } else if (P.use_tanh_fetch && fetch <= 300.) {
-                    c_salt *= P.Lc_tanh;  // 0.5*tanh(0.01333*fetch_ref - 2)+0.5 with fetch_ref = 300
-                }
-                if (P.use_PomLi) {  // PBSM3D.cpp:848-865
-                    const double z10 = 10. + snow_depth;
-                    const double u10 = z10 < kZUR ? log_scale_wind(uref, kZUR, z10, snow_depth, mp.z0) : uref;
-                    const double Ah = F.psh[i];
-                    const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
-                    const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
-                    const double z0v = (stalkN * stalkD * height_diff) / 2.0;
-                    const double us = u10 / sqrt((1 + 340.0 * z0v));
-                    const double Pu10 = 1.0 / (1.0 + exp((sqrt(M_PI) * (u_mean - us)) / delta));
-                    S.bsp[i] = Pu10;
-                    c_salt *= Pu10;
-                }
-                if (P.subgrid) c_salt *= S.sub[SG_FRAC * Tp + i];  // :867-870
-                const double uhs = 2.8 * uth;
-                Qsalt = c_salt * uhs * hs;
-                double mass = 0;
-                for (int j = 0; j < 3; ++j) {
-                    const double udm = __dadd_rn(__dmul_rn(ux, mx[j]), __dmul_rn(uy, my[j]));
-                    mass = __dadd_rn(mass, __dmul_rn(__dmul_rn(-Ej[j], Qsalt), udm));
-                }
-                mass = __dmul_rn(__ddiv_rn(mass, G.area[i]), P.dt);
-                if (mass < 0 && fabs(mass) > swe) {
-                    c_salt = 0;
-                    Qsalt = c_salt * uhs * hs;
-                }
+                fv[FV_LAMBDA * Tp + i] = lambda;
+            } else {
+                fv[FV_HS * Tp + i] = 0.0;
+                fv[FV_CSALT * Tp + i] = 0.0;
+                S.Qsalt[i] = 0.0;
+                S.saltation[i] = false;
             }
-            S.Qsalt[i] = Qsalt;
-            S.saltation[i] = saltation;
 
             // per-face constants of the layer loop.  Division by a per-face or
             // constant value becomes a product with its reciprocal and the
@@ -345,11 +302,8 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             v1 += ux * ux;
             v2 += uy * uy;
             const double inv_nrm = rcp_t(sqrt(v1 + v2));
-            double* fv = A.face_v;
-            fv[FV_HS * Tp + i] = hs;
             fv[FV_USTAR * Tp + i] = ustar;
             fv[FV_UTH * Tp + i] = uth;
-            fv[FV_CSALT * Tp + i] = c_salt;
             fv[FV_QC * Tp + i] = qc;
             fv[FV_QL * Tp + i] = ql;
             fv[FV_EF * Tp + i] = ef;
@@ -367,6 +321,86 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
             base = __shfl_sync(0xffffffffu, base, 0);
             if (slow) A.slow_list[base + __popc(ball & ((1u << lane) - 1u))] = (int32_t)i;
         }
+    }
+}
+
+// Pass 1b, one thread per face on the list of saltating faces (hs > 0): the
+// saltation layer's height, the saltation concentration and flux with the
+// fetch, probability and subgrid factors, and the over-erosion check
+// (PBSM3D.cpp:763-925), in the reference's order and rounding.
+__global__ void __launch_bounds__(kBlock) k_salt_terms(Params P, Faces G, Forcing F, FaceState S, Susp A, Members Mb) {
+    __shared__ MathTables mt;
+    math_tables_load(mt, P.mt);
+    const int64_t Tp = P.Tp;
+    const int n = *A.n_slow;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int64_t i = A.slow_list[k];
+        const Member mp = Mb.prm[Mb.face_member[i]];
+        double* fv = A.face_v;
+        const double ustar = fv[FV_USTAR * Tp + i], uth = fv[FV_UTH * Tp + i], lambda = fv[FV_LAMBDA * Tp + i];
+        double fetch = 1000;
+        if (P.use_exp_fetch || P.use_tanh_fetch) fetch = F.fetch[i];
+        const double uref = F.UR[i];
+        double snow_depth = F.sd[i];
+        snow_depth = is_nan_chm(snow_depth) ? 0 : snow_depth;
+        double swe = F.swe[i];
+        swe = is_nan_chm(swe) ? 0 : swe;
+        const double T_c = F.t[i];
+        const double t = T_c + 273.15;
+        bool saltation = true;
+        const double hs = 0.08436 * pow_t(ustar, 1.27, mt);
+        double vx, vy;
+        bearing_to_cartesian(F.dir[i], vx, vy);
+        const double ux = -vx, uy = -vy;
+        const double rho_f = std_dry_air_density(G.zc[i], t, mt);
+        const double Beta = 202.0, mB = 0.16;
+        const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
+        const double tau_n_ratio = __ddiv_rn(mbl, __dadd_rn(1.0, mbl));
+        // the bracket cancels near the threshold: no contraction here
+        const double bracket =
+            __dsub_rn(__dsub_rn(1.0, tau_n_ratio), __ddiv_rn(__dmul_rn(uth, uth), __dmul_rn(ustar, ustar)));
+        double c_salt = __dmul_rn(__ddiv_rn(rho_f, __dmul_rn(3.29, ustar)), bracket);
+        if (c_salt < 0 || isnan(c_salt)) {
+            c_salt = 0;
+            saltation = false;
+        }
+        if (P.use_exp_fetch && fetch < 500) {
+            const double fetch_ref = 500, mu = 3.0;
+            c_salt *= 1.0 - exp(-mu * fetch / fetch_ref);
+        } else if (P.use_tanh_fetch && fetch <= 300.) {
+            c_salt *= P.Lc_tanh;  // 0.5*tanh(0.01333*fetch_ref - 2)+0.5 with fetch_ref = 300
+        }
+        if (P.use_PomLi) {  // PBSM3D.cpp:848-865
+            double height_diff = smax(0.0, G.canopy[i] - snow_depth);
+            if (!P.enable_veg) height_diff = 0;
+            const double z10 = 10. + snow_depth;
+            const double u10 = z10 < kZUR ? log_scale_wind(uref, kZUR, z10, snow_depth, mp.z0) : uref;
+            const double Ah = F.psh[i];
+            const double u_mean = 11.2 + 0.365 * T_c + 0.00706 * T_c * T_c + 0.9 * log(Ah);
+            const double delta = 0.145 * T_c + 0.00196 * T_c * T_c + 4.3;
+            const double z0v = (G.stalkN[i] * G.stalkD[i] * height_diff) / 2.0;
+            const double us = u10 / sqrt((1 + 340.0 * z0v));
+            const double Pu10 = 1.0 / (1.0 + exp((sqrt(M_PI) * (u_mean - us)) / delta));
+            S.bsp[i] = Pu10;
+            c_salt *= Pu10;
+        }
+        if (P.subgrid) c_salt *= S.sub[SG_FRAC * Tp + i];  // :867-870
+        const double uhs = 2.8 * uth;
+        double Qsalt = c_salt * uhs * hs;
+        double mass = 0;
+        for (int j = 0; j < 3; ++j) {
+            const double udm = __dadd_rn(__dmul_rn(ux, G.mx[j * Tp + i]), __dmul_rn(uy, G.my[j * Tp + i]));
+            mass = __dadd_rn(mass, __dmul_rn(__dmul_rn(-G.E[j * Tp + i], Qsalt), udm));
+        }
+        mass = __dmul_rn(__ddiv_rn(mass, G.area[i]), P.dt);
+        if (mass < 0 && fabs(mass) > swe) {
+            c_salt = 0;
+            Qsalt = c_salt * uhs * hs;
+        }
+        S.Qsalt[i] = Qsalt;
+        S.saltation[i] = saltation;
+        fv[FV_HS * Tp + i] = hs;
+        fv[FV_CSALT * Tp + i] = c_salt;
     }
 }
 
@@ -888,6 +922,7 @@ void launch_assemble_suspension(Ctx& c, cudaStream_t s) {
     if (c.cfg.derive_fetch) launch_fetchr(c, s, c.Fo.dir, c.Fo.fetch);
     if (c.P.subgrid) launch_subgrid(c, s);
     k_salt_faces<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
+    k_salt_terms<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb);
     k_salt_rows<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.Fo, c.A, c.Mb);
     k_assemble_suspension<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.A, c.Mb, c.red.partials, c.sc);
     prof_end(c, s, PBSM3D_K_ASSEMBLE,
