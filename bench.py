@@ -498,10 +498,10 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
                 continue
             if isinstance(per_row, dict) and "mid" in per_row:  # polynomial steps: K-1 intermediate, 1 last
                 per_row = ((K - 1) * per_row["mid"] + per_row["last"]) / K if K > 0 else None
-            elif isinstance(per_row, dict):  # the assembly: per face, per saltating row, per row
+            elif isinstance(per_row, dict):  # per face, per saltating face and row, per row
                 L_ = rows // T
-                per_row = (per_row["per_face"] * T + per_row["per_saltating_row"] * n_slow * L_) / rows + \
-                    per_row["per_row"]
+                per_row = (per_row.get("per_face", 0.0) * T + per_row.get("per_saltating_face", 0.0) * n_slow +
+                           per_row.get("per_saltating_row", 0.0) * n_slow * L_) / rows + per_row.get("per_row", 0.0)
             if per_row is None:
                 continue
             gflops = 2.0 * per_row * rows * fig["launches"] / (fig["ms"] / 1e3) / 1e9

@@ -323,7 +323,7 @@ static int create_core(const pbsm3d_mesh_desc* mesh, const pbsm3d_config* cfg_in
     F.my = dalloc<double>(c, 3 * Tp, ok);
     F.area = dalloc<double>(c, Tp, ok);
     F.zc = dalloc<double>(c, Tp, ok);
-    F.dxn = dalloc<double>(c, 3 * Tp, ok);
+    F.depw = dalloc<double>(c, 3 * Tp, ok);
     F.canopy = dalloc<double>(c, Tp, ok);
     F.lai = dalloc<double>(c, Tp, ok);
     F.stalkN = dalloc<double>(c, Tp, ok);

@@ -69,7 +69,7 @@ struct Faces {
     double* my;       // [3][Tp]
     double* area;     // [Tp]
     double* zc;       // [Tp] centroid elevation
-    double* dxn;      // [3][Tp] centroid distance to neighbour j
+    double* depw;     // [3][Tp] deposition coupling eps E_j / |c_i - c_nb| across edge j (0 without a neighbour)
     double* canopy;   // [Tp]
     double* lai;
     double* stalkN;
@@ -153,7 +153,10 @@ enum FaceValue {
     // its factor of the particle-velocity term 3 cos(pi/4) 0.005 u_z^1.36
     // FV_LAMBDA: the roughness element density of a saltating face (pass 1
     // to its saltation terms, pass 1b)
+    // FV_UX, FV_UY: the unit wind vector -bearing_to_cartesian(dir) (pass 1
+    // to pass 1b and the deposition rows)
     FV_HS, FV_USTAR, FV_UTH, FV_CSALT, FV_QC, FV_QL, FV_EF, FV_INVLOGDEN, FV_K0, FV_K1, FV_K2, FV_Z0, FV_LAMBDA,
+    FV_UX, FV_UY,
     FV_COUNT
 };
 

@@ -257,6 +257,8 @@ __global__ void __launch_bounds__(kBlock) k_salt_faces(Params P, Faces G, Forcin
                 my[j] = G.my[j * Tp + i];
             }
             double* fv = A.face_v;
+            fv[FV_UX * Tp + i] = ux;
+            fv[FV_UY * Tp + i] = uy;
             if (saltation) {
                 fv[FV_LAMBDA * Tp + i] = lambda;
             } else {
@@ -349,9 +351,7 @@ __global__ void __launch_bounds__(kBlock) k_salt_terms(Params P, Faces G, Forcin
         const double t = T_c + 273.15;
         bool saltation = true;
         const double hs = 0.08436 * pow_t(ustar, 1.27, mt);
-        double vx, vy;
-        bearing_to_cartesian(F.dir[i], vx, vy);
-        const double ux = -vx, uy = -vy;
+        const double ux = fv[FV_UX * Tp + i], uy = fv[FV_UY * Tp + i];
         const double rho_f = std_dry_air_density(G.zc[i], t, mt);
         const double Beta = 202.0, mB = 0.16;
         const double mbl = __dmul_rn(__dmul_rn(mB, Beta), lambda);
@@ -716,7 +716,8 @@ __global__ void __launch_bounds__(kBlock) k_post(Params P, Susp A, FaceState S) 
 }
 
 __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces G, Forcing F, FaceState S, Dep D,
-                                                               Members Mb, double* partials, Scalars* sc) {
+                                                               Members Mb, const double* __restrict__ face_v,
+                                                               double* partials, Scalars* sc) {
     const int64_t Tp = P.Tp;
     double vmax = 0, vnan = 0;
     __shared__ unsigned long long mb_max[kMaxMembers];
@@ -733,9 +734,8 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
             D.x[i] = 0.0;
             continue;
         }
-        double vx, vy;
-        bearing_to_cartesian(F.dir[i], vx, vy);
-        const double ux = -vx, uy = -vy;
+        // the unit wind vector of pass 1
+        const double ux = face_v[FV_UX * Tp + i], uy = face_v[FV_UY * Tp + i];
         double dg = G.area[i];  // replace, PBSM3D.cpp:1546
         double b = 0.0;
         const double Qs_self = S.Qsusp[i], Qa_self = S.Qsalt[i];
@@ -757,9 +757,9 @@ __global__ void __launch_bounds__(kBlock) k_assemble_deposition(Params P, Faces 
             }
             double off = 0.0;
             if (nb >= 0) {
-                const double dxj = G.dxn[j * Tp + i];
-                dg += P.eps * Ej / dxj;
-                off += -P.eps * Ej / dxj;
+                const double w = G.depw[j * Tp + i];  // eps E_j / dx_j
+                dg += w;
+                off += -w;
             }
             D.off[j * Tp + i] = off;
             b += -Ej * (Qtj + Qsj) * udm;
@@ -874,18 +874,21 @@ __global__ void k_member_zero(Params P, Members Mb, double* x, const int* presen
 }
 
 // Centroid distances to neighbours (distance_UTM, coordinates.cpp:100-106).
+// The deposition rows' static couplings eps E_j / dx_j (PBSM3D.cpp:1560-1580,
+// dx the centroid distance, distance_UTM), once per mesh instead of per step.
 __global__ void k_init_static(Params P, Faces G, const double* cx, const double* cy) {
     const int64_t Tp = P.Tp;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Tp; i += (int64_t)gridDim.x * blockDim.x) {
         for (int j = 0; j < 3; ++j) {
             const int32_t nb = G.nbr[j * Tp + i];
-            double d = 2.0;
+            double w = 0.0;
             if (nb >= 0 && i < P.T) {
                 const double ddx = cx[i] - cx[nb];
                 const double ddy = cy[i] - cy[nb];
-                d = sqrt(ddx * ddx + ddy * ddy);
+                const double d = sqrt(ddx * ddx + ddy * ddy);
+                w = P.eps * G.E[j * Tp + i] / d;
             }
-            G.dxn[j * Tp + i] = d;
+            G.depw[j * Tp + i] = w;
         }
     }
 }
@@ -937,7 +940,8 @@ void launch_post_and_assemble_deposition(Ctx& c, cudaStream_t s) {
     k_post<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.A, c.S);
     prof_end(c, s, PBSM3D_K_POST, rows * 24 + T * 40);
     prof_begin(c, s);
-    k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.Mb, c.red.partials, c.sc);
+    k_assemble_deposition<<<c.grid_faces, kBlock, 0, s>>>(c.P, c.F, c.Fo, c.S, c.D, c.Mb, c.A.face_v, c.red.partials,
+                                                          c.sc);
     prof_end(c, s, PBSM3D_K_DEP_ASSEMBLE, T * 196);
 }
 
