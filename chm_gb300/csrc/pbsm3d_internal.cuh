@@ -235,7 +235,8 @@ struct MScal {
     double gamma, pad0;                    // warm-start scale (set by the host)
     int iter, done, maxit;
     unsigned counter;                      // tiles reported to the current reduction
-    int pad1[4];
+    int half;                              // FP64: the next iteration tests its half step
+    int pad1[3];
 };
 
 // Work tiles of the batched Krylov kernels: runs of at most kBlock faces

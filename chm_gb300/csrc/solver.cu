@@ -154,7 +154,10 @@ struct LatFace<float> {
     __device__ __forceinline__ Row row(int64_t k) const { return Row{uz[k], a0, a1, a2, b0, b1, b2}; }
 };
 
-enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3 };
+// DONE_HALF: stopped at the half step of a BiCGStab iteration; the column
+// kernel s applies that member's x += alpha zp, and k_bicg_t2 then marks it
+// DONE_CONVERGED (so later iterations of the batch do not apply it again).
+enum { DONE_NO = 0, DONE_CONVERGED = 1, DONE_BREAKDOWN = 2, DONE_MAXIT = 3, DONE_HALF = 4 };
 
 // z = B^{-1} u for one column, u already in smem column g[z*bd + col].
 // FP32: the Thomas sweeps on (l, ib, up), 3 operations a row.  FP64, whose
@@ -359,11 +362,13 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_p(Op
     }
 }
 
-// s = r - alpha v; zs = B^{-1} s
+// s = r - alpha v; zs = B^{-1} s.  A member that stopped at this
+// iteration's half step (FP64: xh is x) takes x += alpha zp instead.
 template <typename V, int LC>
 __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op<V> op, Tiles tl, int W, const V* __restrict__ r,
                                                         const V* __restrict__ v, V* __restrict__ s,
-                                                        V* __restrict__ zs, const MScal* __restrict__ ms) {
+                                                        V* __restrict__ zs, const MScal* __restrict__ ms,
+                                                        double* __restrict__ xh, const V* __restrict__ zp) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
     const ColLanes<LC> cl(W);
@@ -371,9 +376,19 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op
     const SliceRange br = block_slices(tl, 1 << sh);
     for (int u = br.u0; u < br.u1; ++u) {
         const int t = tl.act[u >> sh], m = tl.member[t];
-        if (ms[m].done) continue;
         const int64_t i = tl.start[t] + (int64_t)(u & ((1 << sh) - 1)) * W + cl.f;
         const bool valid = i < tl.start[t + 1];
+        if (const int d = ms[m].done) {
+            // the whole block sees the same member: no barrier is skipped
+            if (xh && d == DONE_HALF && valid) {
+                const double alpha = ms[m].alpha;
+                for (int z = cl.lane; z < op.L; z += LC) {
+                    const int64_t k = (int64_t)z * op.Tp + i;
+                    xh[k] += alpha * (double)zp[k];
+                }
+            }
+            continue;
+        }
         if (LC == 1 && !valid) continue;  // no block barrier with one lane
         const V alpha = (V)ms[m].alpha;
         if (valid)
@@ -450,11 +465,11 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
 constexpr int kLatLanes = 2;
 
 // y = u + N z for layers lane, lane + LC, ... of the column of face i, with
-// (a, y) [and (y, y)]
+// (a, y); NT = 2: and (y, y); NT = 3: and (b, y), (y, y)
 template <typename V, int NT, int LC>
 __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int lane, const V* __restrict__ u,
                                               const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
-                                              V (&acc)[2]) {
+                                              const V* __restrict__ b, V (&acc)[3]) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
     const LatFace<V> lf(op, i);
     // layers are independent here: unrolled so their loads overlap
@@ -470,16 +485,42 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int la
         if (n2 >= 0) yk += la[2] * zz[base + n2];
         y[k] = yk;
         acc[0] += a[k] * yk;
-        if (NT > 1) acc[1] += yk * yk;
+        if (NT == 2) acc[1] += yk * yk;
+        if (NT == 3) {
+            acc[1] += b[k] * yk;
+            acc[2] += yk * yk;
+        }
     }
 }
 
-// v = p + N zp; rv = (rhat, v); alpha = rho / rv
+// Below this ratio of the target to ||r||^2 the half-step norm, a difference
+// of terms of the size of ||r||^2 (FP64 sums, relative error ~1e-14), could
+// misjudge the target; the test is then left to the full step.
+constexpr double kHalfTestFloor = 1e-11;
+// The half-step iterate x + alpha zp lacks the iteration's minimal-residual
+// step, and a stop just under the target leaves more error than the full
+// steps, which usually land well below it: the half step stops only when
+// ||s|| <= 0.3 of the target (||s||^2 <= 0.09 of target2).
+constexpr double kHalfMargin2 = 0.09;
+// A half step reduces ||r||^2 by 1e-6 at most (measured 1e-2..1e-6 with the
+// polynomial preconditioner): its test (two more dot products and r read in
+// k_bicg_v) runs only once ||r||^2 is within this factor of the target.
+constexpr double kHalfWindow2 = 1e6;
+__host__ __device__ __forceinline__ int half_window(double rr, double target2) {
+    return rr <= kHalfWindow2 * target2 ? 1 : 0;
+}
+
+// v = p + N zp; rv = (rhat, v); alpha = rho / rv.  FP64 also sums (r, v) and
+// (v, v): ||s||^2 = ||r||^2 - 2 alpha (r, v) + alpha^2 (v, v) for s = r -
+// alpha v is BiCGStab's half-step test (H. A. van der Vorst, SIAM J. Sci.
+// Stat. Comput. 13, 1992, Alg. 1: stop with x + alpha zp when ||s|| meets the
+// target), which skips the iteration's second preconditioner application
+// when it passes.
 template <typename V>
 __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
                                                       const V* __restrict__ zp, V* __restrict__ v,
-                                                      const V* __restrict__ rh, MScal* ms, Scalars* sc,
-                                                      double* part) {
+                                                      const V* __restrict__ rh, const V* __restrict__ r,
+                                                      MScal* ms, Scalars* sc, double* part) {
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
@@ -488,19 +529,49 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
             a = ae;
             continue;
         }
-        V acc[2] = {0, 0};
+        // the member's half-step test (set before the launch: the same in
+        // every block of the member)
+        const bool test = sizeof(V) == 8 && ms[m].half;
+        V acc[3] = {0, 0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-            if (i < tl.start[t + 1]) lateral_apply<V, 1, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, acc);
-        }
-        V a1[1] = {acc[0]};
-        double tot[1];
-        if (member_totals<1>(a1, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0) {
-            const double rv = tot[0];
-            if (rv == 0.0 || !isfinite(rv))
-                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            if (i >= tl.start[t + 1]) continue;
+            if (test)
+                lateral_apply<V, 3, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, r, acc);
             else
-                ms[m].alpha = ms[m].rho / rv;
+                lateral_apply<V, 1, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, nullptr, acc);
+        }
+        double tot[3] = {0, 0, 0};
+        bool last;
+        if (test) {
+            last = member_totals<3>(acc, part, tl, ts, te, m, ms, tot);
+        } else {
+            V a1[1] = {acc[0]};
+            double t1[1];
+            last = member_totals<1>(a1, part, tl, ts, te, m, ms, t1);
+            tot[0] = t1[0];
+        }
+        if (last && threadIdx.x == 0) {
+            MScal& q = ms[m];
+            const double rv = tot[0];
+            if (rv == 0.0 || !isfinite(rv)) {
+                member_stop(ms, m, DONE_BREAKDOWN, sc, tl.n);
+            } else {
+                const double alpha = q.rho / rv;
+                q.alpha = alpha;
+                if (test) {
+                    // ||r||^2: rho itself on a sweep's first iteration (rhat = r)
+                    const double rr = q.iter == 0 ? q.rho : q.rnorm2;
+                    const double s2 = rr - 2.0 * alpha * tot[1] + alpha * alpha * tot[2];
+                    if (q.target2 >= kHalfTestFloor * rr && s2 <= kHalfMargin2 * q.target2) {
+                        q.rnorm2 = fmax(s2, 0.0);
+                        q.iter += 1;
+                        atomicMax(&sc->iter, q.iter);
+                        atomicAdd(&sc->counter[3], 1u);
+                        member_stop(ms, m, DONE_HALF, sc, tl.n);
+                    }
+                }
+            }
         }
         a = ae;
     }
@@ -516,17 +587,23 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
         const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
-        if (ms[m].done) {
+        if (const int d = ms[m].done) {
+            // a half-step exit's x update is in place (column kernel s, launched
+            // before): the member is converged (every block that sees it
+            // stores the same value)
+            if (d == DONE_HALF && threadIdx.x == 0) ms[m].done = DONE_CONVERGED;
             a = ae;
             continue;
         }
-        V acc[2] = {0, 0};
+        V acc[3] = {0, 0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-            if (i < tl.start[t + 1]) lateral_apply<V, 2, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, s, acc);
+            if (i < tl.start[t + 1])
+                lateral_apply<V, 2, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, s, nullptr, acc);
         }
+        V a2[2] = {acc[0], acc[1]};
         double tot[2];
-        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
+        if (member_totals<2>(a2, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
             ms[m].omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
         a = ae;
     }
@@ -568,6 +645,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_bicg_x(int64_t Tp, int L, Tiles t
             MScal& q = ms[m];
             const double rho_new = tot[0];
             q.rnorm2 = tot[1];
+            q.half = half_window(tot[1], q.target2);
             q.iter += 1;
             atomicMax(&sc->iter, q.iter);
             if (tot[1] <= q.target2)
@@ -1456,15 +1534,25 @@ void launch_col_p(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int 
     else k_bicg_p<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, p, v, zp, ms);
 }
 
+// xh: x of an FP64 solve (members stopped at the half step update it), else null
 template <typename V>
 void launch_col_s(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* r, const V* v, V* sv,
-                  V* zs, const MScal* ms) {
+                  V* zs, const MScal* ms, double* xh, const V* zp) {
     const ColGeom G = kColGeom[gi];
     const int grid = col_grid<V>(c, tl, gi, false);
     const size_t smem = (size_t)c.P.L * G.W * sizeof(V);
-    if (G.LC == 1) k_bicg_s<V, 1><<<grid, G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
-    else if (G.LC == 2) k_bicg_s<V, 2><<<grid, 2 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
-    else k_bicg_s<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms);
+    if (G.LC == 1) k_bicg_s<V, 1><<<grid, G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms, xh, zp);
+    else if (G.LC == 2) k_bicg_s<V, 2><<<grid, 2 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms, xh, zp);
+    else k_bicg_s<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms, xh, zp);
+}
+
+// x of an FP64 solve for the half-step exit, null for the FP32 inner solve
+template <typename X>
+double* half_x(X* x) {
+    if constexpr (sizeof(X) == 8)
+        return x;
+    else
+        return nullptr;
 }
 
 template <typename V, bool WRITE_W>
@@ -1532,11 +1620,14 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
     int chunk = std::max(1, std::min(16, c.bicg_hint[hint]));
     int done_iters = 0;
     const int per_it = 5 + (c.cfg.neumann > 0 ? 2 * c.cfg.neumann : 0);  // profiled launches an iteration
+    const int first_half = 2 + (c.cfg.neumann > 0 ? c.cfg.neumann : 0);  // p, the preconditioner, v
+    unsigned half_seen = 0;
     int before = 0;
     {
         int rc = read_scalars(c, s, sc);
         if (rc) return rc;
         before = c.sc_host->iter;
+        half_seen = c.sc_host->counter[3];
         if (c.sc_host->done) {
             iters = 0;
             return 0;
@@ -1564,10 +1655,12 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             prof_end(c, s, PBSM3D_K_BICG_P, rows * (8 + (op.nu ? 1 : 0)) * sv_);
             const V* up = launch_neumann<V>(c, s, op, tl, gi, p, zp, nw, nz, ms, rows, true);
             prof_begin(c, s);
-            k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
+            k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, r, ms, sc, part);
+            // (the FP64 half-step test's read of r, in the iterations near
+            // the target only, is not counted)
             prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
-            launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms);
+            launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms, half_x(x), zp);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * (7 + (op.nu ? 1 : 0)) * sv_);
             const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
@@ -1585,9 +1678,11 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         if (rc) return rc;
         const int ran = c.sc_host->iter - before;
         before = c.sc_host->iter;
-        if (timing && ran == chunk) {
+        const bool half_exit = c.sc_host->counter[3] > half_seen;
+        if (timing && ran == chunk && !half_exit) {
             // a full chunk: its time per iteration and per active face (in
-            // an ensemble later chunks carry fewer members) decides
+            // an ensemble later chunks carry fewer members) decides; one
+            // that ended at a half step did less work and is not counted
             float ms = 0;
             PBSM_CUDA_TRY(cudaEventElapsedTime(&ms, te[0], te[1]));
             tune_record(c, ms / chunk / (float)std::max<int64_t>(1, act));
@@ -1597,6 +1692,10 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
         done_iters += ran;
         const int idle = chunk - ran;
         if (idle > 0) prof_drop(c, per_it * idle);
+        // one member that stopped at a half step: the rest of that iteration
+        // (s, the second preconditioner application, t, x) did no work either
+        if (tl.n == 1 && half_exit) prof_drop(c, per_it - first_half);
+        half_seen = c.sc_host->counter[3];
         if (c.sc_host->done) break;
         if (tl.n > 1) {
             // members that stopped leave the active-tile list
@@ -1829,6 +1928,7 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
                 q.target2 = itol * itol * rr;
             } else {
                 q.target2 = tol * tol * bb;  // relative to ||b_m||
+                q.half = half_window(rr, q.target2);
             }
             q.done = conv[m] || rr == 0.0 ? DONE_CONVERGED : DONE_NO;
             ndone += q.done ? 1 : 0;
@@ -2433,6 +2533,7 @@ __global__ void k_ctl_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Ti
             q.target2 = itol * itol * rr;
         } else {
             q.target2 = tol * tol * bb;
+            q.half = half_window(rr, q.target2);
         }
         q.done = (ctl->conv[m] || rr == 0.0) ? 1 : 0;
         if (q.done) {
@@ -2447,6 +2548,7 @@ __global__ void k_ctl_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Ti
     if (threadIdx.x == 0) {
         sc->done = s_ndone == n ? 1 : 0;
         sc->counter[2] = (unsigned)s_ndone;
+        sc->counter[3] = 0u;
         sc->iter = 0;
         ctl->n_active = n - s_ndone;
         hset(h, H_OUTER, 1u);
@@ -2778,8 +2880,8 @@ void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, 
     double* part = c.tile_part;
     launch_col_p<V>(c, s, op, tl, c.geom, r, p, v, neumann_first(c, zp, nz), ms);
     const V* up = launch_neumann<V>(c, s, op, tl, c.geom, p, zp, nw, nz, ms, 0, false);
-    k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, ms, sc, part);
-    launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms);
+    k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, r, ms, sc, part);
+    launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms, half_x(x), zp);
     const V* us = launch_neumann<V>(c, s, op, tl, c.geom, sv, zs, nw, nz, ms, 0, false);
     k_bicg_t2<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
     k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);

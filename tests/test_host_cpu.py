@@ -295,3 +295,49 @@ def test_scaled_recurrence_cg_is_the_preconditioned_cg(poly):
     assert it == it_ref
     np.testing.assert_allclose(s * y, x, rtol=0, atol=1e-12 * np.abs(x).max())
     assert np.linalg.norm(b - _apply(nb, d, off, s * y)) <= 1.01 * tol * np.sqrt(bb)
+
+
+def test_bicgstab_half_step_test():
+    """k_bicg_v's FP64 half-step test (van der Vorst 1992, Alg. 1): with
+    s = r - alpha v, ||s||^2 = ||r||^2 - 2 alpha (r, v) + alpha^2 (v, v)
+    from the dot products the kernel sums, to rounding of ||r||^2; and the
+    half-step iterate x + alpha M^-1 p that the column kernel s then stores
+    leaves the true residual s.  Nonsymmetric rows (each face's couplings
+    scaled differently), right-preconditioned by Jacobi."""
+    nb, d, off, _ = _deposition_like_system()
+    rng = np.random.default_rng(11)
+    offn = off * (0.3 + 0.7 * rng.random(off.shape))
+    b = rng.standard_normal(d.size)
+
+    def A(v):
+        return _apply(nb, d, offn, v)
+
+    tol = 1e-8
+    bb = b @ b
+    x = np.zeros_like(b); r = b.copy(); rh = r.copy(); v = np.zeros_like(b); p = np.zeros_like(b)
+    rho = alpha = omega = 1.0
+    halves = 0
+    for it in range(1, 400):
+        rho_new = rh @ r
+        beta = (rho_new / rho) * (alpha / omega) if it > 1 else 0.0
+        rho = rho_new
+        p = r + beta * (p - omega * v)
+        y = p / d
+        v = A(y)
+        alpha = rho / (rh @ v)
+        rr = r @ r
+        s2 = rr - 2.0 * alpha * (r @ v) + alpha * alpha * (v @ v)
+        s = r - alpha * v
+        assert abs(s2 - s @ s) <= 1e-13 * rr, (it, s2, s @ s, rr)
+        # the stop the kernel would take at this half step: true residual = s
+        tr = b - A(x + alpha * y)
+        assert abs(tr @ tr - s @ s) <= 1e-3 * (s @ s) + 1e-26 * bb, (it, tr @ tr, s @ s)
+        halves += 1
+        z = s / d
+        t = A(z)
+        omega = (t @ s) / (t @ t)
+        x += alpha * y + omega * z
+        r = s - omega * t
+        if r @ r <= tol * tol * bb:
+            break
+    assert r @ r <= tol * tol * bb and halves >= 5
