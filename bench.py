@@ -504,7 +504,14 @@ def run_ours(args, dist: Dist, rank: int, world: int, local_rank: int) -> dict:
             per_row = tab.get(f"{cls}:fp64")
             if per_row is None or not fig["ms"]:
                 continue
-            if isinstance(per_row, dict) and "mid" in per_row:  # polynomial steps: K-1 intermediate, 1 last
+            if isinstance(per_row, dict) and "later" in per_row:
+                # residual passes: each step's first (r = b alone after a zero
+                # start), then the later ones
+                zero = VARIANTS[pname].get("warm_start", capi.X0_ZERO) == capi.X0_ZERO
+                nf = min(args.steps, fig["launches"])
+                first = per_row["first_zero_start"] if zero else per_row["first"]
+                per_row = (nf * first + (fig["launches"] - nf) * per_row["later"]) / fig["launches"]
+            elif isinstance(per_row, dict) and "mid" in per_row:  # polynomial steps: K-1 intermediate, 1 last
                 per_row = ((K - 1) * per_row["mid"] + per_row["last"]) / K if K > 0 else None
             elif isinstance(per_row, dict):  # per face, per saltating face and row, per row
                 L_ = rows // T

@@ -30,6 +30,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 
 #include "fp64_math.cuh"
 #include "pbsm3d_internal.cuh"
@@ -363,12 +364,12 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_p(Op
 }
 
 // s = r - alpha v; zs = B^{-1} s.  A member that stopped at this
-// iteration's half step (FP64: xh is x) takes x += alpha zp instead.
+// iteration's half step takes x += alpha zp instead (xh: the solve's x).
 template <typename V, int LC>
 __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op<V> op, Tiles tl, int W, const V* __restrict__ r,
                                                         const V* __restrict__ v, V* __restrict__ s,
                                                         V* __restrict__ zs, const MScal* __restrict__ ms,
-                                                        double* __restrict__ xh, const V* __restrict__ zp) {
+                                                        V* __restrict__ xh, const V* __restrict__ zp) {
     extern __shared__ unsigned char smem_raw[];
     V* g = reinterpret_cast<V*>(smem_raw);
     const ColLanes<LC> cl(W);
@@ -381,10 +382,11 @@ __global__ void __launch_bounds__(kBlock * LC, LC == 1 ? 0 : 4 / LC) k_bicg_s(Op
         if (const int d = ms[m].done) {
             // the whole block sees the same member: no barrier is skipped
             if (xh && d == DONE_HALF && valid) {
-                const double alpha = ms[m].alpha;
+                // as k_bicg_x updates x: the step in the vector precision
+                const V alpha = (V)ms[m].alpha;
                 for (int z = cl.lane; z < op.L; z += LC) {
                     const int64_t k = (int64_t)z * op.Tp + i;
-                    xh[k] += alpha * (double)zp[k];
+                    xh[k] = xh[k] + alpha * zp[k];
                 }
             }
             continue;
@@ -464,12 +466,11 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
 // launch geometry is fixed (it decides the order of the dot products' sums).
 constexpr int kLatLanes = 2;
 
-// y = u + N z for layers lane, lane + LC, ... of the column of face i, with
-// (a, y); NT = 2: and (y, y); NT = 3: and (b, y), (y, y)
-template <typename V, int NT, int LC>
+// y = u + N z for layers lane, lane + LC, ... of the column of face i; add(k,
+// y_k) folds each row into the caller's dot products
+template <typename V, int LC, typename Add>
 __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int lane, const V* __restrict__ u,
-                                              const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
-                                              const V* __restrict__ b, V (&acc)[3]) {
+                                              const V* __restrict__ zz, V* __restrict__ y, Add&& add) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
     const LatFace<V> lf(op, i);
     // layers are independent here: unrolled so their loads overlap
@@ -484,18 +485,13 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int la
         if (n1 >= 0) yk += la[1] * zz[base + n1];
         if (n2 >= 0) yk += la[2] * zz[base + n2];
         y[k] = yk;
-        acc[0] += a[k] * yk;
-        if (NT == 2) acc[1] += yk * yk;
-        if (NT == 3) {
-            acc[1] += b[k] * yk;
-            acc[2] += yk * yk;
-        }
+        add(k, yk);
     }
 }
 
-// Below this ratio of the target to ||r||^2 the half-step norm, a difference
-// of terms of the size of ||r||^2 (FP64 sums, relative error ~1e-14), could
-// misjudge the target; the test is then left to the full step.
+// The half-step norm is a difference of terms of the size of ||r||^2 (FP64
+// sums, relative error ~1e-14): below this ratio of the target to ||r||^2 it
+// could misjudge the target, and the test is left to the full step.
 constexpr double kHalfTestFloor = 1e-11;
 // The half-step iterate x + alpha zp lacks the iteration's minimal-residual
 // step, and a stop just under the target leaves more error than the full
@@ -503,25 +499,29 @@ constexpr double kHalfTestFloor = 1e-11;
 // ||s|| <= 0.3 of the target (||s||^2 <= 0.09 of target2).
 constexpr double kHalfMargin2 = 0.09;
 // A half step reduces ||r||^2 by 1e-6 at most (measured 1e-2..1e-6 with the
-// polynomial preconditioner): its test (two more dot products and r read in
-// k_bicg_v) runs only once ||r||^2 is within this factor of the target.
+// polynomial preconditioner): its test (three more dot products and r read
+// in k_bicg_v) runs only once ||r||^2 is within this factor of the target.
 constexpr double kHalfWindow2 = 1e6;
 __host__ __device__ __forceinline__ int half_window(double rr, double target2) {
     return rr <= kHalfWindow2 * target2 ? 1 : 0;
 }
 
-// v = p + N zp; rv = (rhat, v); alpha = rho / rv.  FP64 also sums (r, v) and
-// (v, v): ||s||^2 = ||r||^2 - 2 alpha (r, v) + alpha^2 (v, v) for s = r -
-// alpha v is BiCGStab's half-step test (H. A. van der Vorst, SIAM J. Sci.
-// Stat. Comput. 13, 1992, Alg. 1: stop with x + alpha zp when ||s|| meets the
-// target), which skips the iteration's second preconditioner application
-// when it passes.
+// v = p + N zp; rv = (rhat, v); alpha = rho / rv.  FP64, near the target,
+// also sums (r, v) and (v, v): ||s||^2 = ||r||^2 - 2 alpha (r, v) + alpha^2
+// (v, v) for s = r - alpha v is BiCGStab's half-step test (H. A. van der
+// Vorst, SIAM J. Sci. Stat. Comput. 13, 1992, Alg. 1: stop with x + alpha zp
+// when ||s|| meets the target), which skips the iteration's second
+// preconditioner application when it passes.  The FP32 inner solve of the
+// mixed form has no such test: its target, ~1e-8 of ||r||^2, puts nearly
+// every iteration in the window, and FP64 sums (FP32 ones cannot resolve
+// ||s||^2 there) made its v kernel 1.6x slower and the step 3% slower.
 template <typename V>
 __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_bicg_v(Op<V> op, Tiles tl, const V* __restrict__ p,
                                                       const V* __restrict__ zp, V* __restrict__ v,
                                                       const V* __restrict__ rh, const V* __restrict__ r,
                                                       MScal* ms, Scalars* sc, double* part) {
     const TileRange br = block_tiles(tl);
+    const int lane = threadIdx.x / kBlock;
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
         const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
@@ -531,24 +531,33 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
         }
         // the member's half-step test (set before the launch: the same in
         // every block of the member)
-        const bool test = sizeof(V) == 8 && ms[m].half;
-        V acc[3] = {0, 0, 0};
-        for (int t = ts; t < te; ++t) {
-            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-            if (i >= tl.start[t + 1]) continue;
-            if (test)
-                lateral_apply<V, 3, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, r, acc);
-            else
-                lateral_apply<V, 1, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, nullptr, acc);
-        }
+        bool test = false;
+        if constexpr (sizeof(V) == 8) test = ms[m].half;
         double tot[3] = {0, 0, 0};
-        bool last;
+        bool last = false;
         if (test) {
-            last = member_totals<3>(acc, part, tl, ts, te, m, ms, tot);
+            if constexpr (sizeof(V) == 8) {
+                V d[3] = {0, 0, 0};
+                for (int t = ts; t < te; ++t) {
+                    const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+                    if (i < tl.start[t + 1])
+                        lateral_apply<V, kLatLanes>(op, i, lane, p, zp, v, [&](int64_t k, V yk) {
+                            d[0] += rh[k] * yk;
+                            d[1] += r[k] * yk;
+                            d[2] += yk * yk;
+                        });
+                }
+                last = member_totals<3>(d, part, tl, ts, te, m, ms, tot);
+            }
         } else {
-            V a1[1] = {acc[0]};
+            V acc[1] = {0};
+            for (int t = ts; t < te; ++t) {
+                const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+                if (i < tl.start[t + 1])
+                    lateral_apply<V, kLatLanes>(op, i, lane, p, zp, v, [&](int64_t k, V yk) { acc[0] += rh[k] * yk; });
+            }
             double t1[1];
-            last = member_totals<1>(a1, part, tl, ts, te, m, ms, t1);
+            last = member_totals<1>(acc, part, tl, ts, te, m, ms, t1);
             tot[0] = t1[0];
         }
         if (last && threadIdx.x == 0) {
@@ -560,7 +569,8 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
                 const double alpha = q.rho / rv;
                 q.alpha = alpha;
                 if (test) {
-                    // ||r||^2: rho itself on a sweep's first iteration (rhat = r)
+                    // ||r||^2: the member's own (rho on a sweep's first
+                    // iteration, where rhat = r)
                     const double rr = q.iter == 0 ? q.rho : q.rnorm2;
                     const double s2 = rr - 2.0 * alpha * tot[1] + alpha * alpha * tot[2];
                     if (q.target2 >= kHalfTestFloor * rr && s2 <= kHalfMargin2 * q.target2) {
@@ -595,15 +605,17 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
             a = ae;
             continue;
         }
-        V acc[3] = {0, 0, 0};
+        V acc[2] = {0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x % kBlock;
             if (i < tl.start[t + 1])
-                lateral_apply<V, 2, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, s, nullptr, acc);
+                lateral_apply<V, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, [&](int64_t k, V yk) {
+                    acc[0] += s[k] * yk;
+                    acc[1] += yk * yk;
+                });
         }
-        V a2[2] = {acc[0], acc[1]};
         double tot[2];
-        if (member_totals<2>(a2, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
+        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
             ms[m].omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
         a = ae;
     }
@@ -673,12 +685,15 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2)
                                                      const double* __restrict__ b, double* __restrict__ r,
                                                      V* __restrict__ rv, V* __restrict__ rhv, V* __restrict__ pv,
                                                      V* __restrict__ vv, MScal* ms, double* part, int first,
-                                                     const int* __restrict__ sweep) {
+                                                     const int* __restrict__ sweep, int x0_zero) {
     const int64_t Tp = P.Tp, R = P.R;
     // (b, b) and (b, r) serve the first refinement sweep only (the target's
     // norm and the warm start's scale): two FP64 FMAs a row fewer after it.
     // The sweep number is the host's (first) or, in a graph, the controller's.
     const bool full = sweep ? *sweep == 0 : first != 0;
+    // the first sweep of a zero start has x = 0 (the assembly clears it):
+    // r = b without reading the bands or x
+    const bool zero_x = full && x0_zero;
     const TileRange br = block_tiles(tl);
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
@@ -690,9 +705,27 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2)
         double acc[3] = {0, 0, 0};
         // kLatLanes lanes a face column, splitting its layers (as the lateral kernels)
         const int lane = threadIdx.x / kBlock;
-        for (int t = ts; t < te; ++t) {
-            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-            if (i >= tl.start[t + 1]) continue;
+        // r_k, its copies and its share of the dot products; with_b: the
+        // first sweep's (b, b) and (b, r) too (a compile-time choice, so the
+        // later sweeps issue no FP64 instructions for them)
+        auto emit = [&](int64_t k, double rk, auto with_b) {
+            r[k] = rk;
+            if (rv) {
+                // FP32 copies rounded on the integer pipe (bit-identical to the cast)
+                const V rc = sizeof(V) == 4 ? (V)f32_rn(rk) : (V)rk;
+                rv[k] = rc;
+                rhv[k] = rc;
+                pv[k] = 0;
+                vv[k] = 0;
+            }
+            acc[0] += rk * rk;
+            if constexpr (decltype(with_b)::value) {
+                acc[1] += b[k] * b[k];
+                acc[2] += b[k] * rk;
+            }
+        };
+        // r = b - A x over the column's rows of this lane
+        auto spmv_rows = [&](int64_t i, auto with_b) {
             const int32_t nb[3] = {nbr[i], nbr[Tp + i], nbr[2 * Tp + i]};
 #pragma unroll 1
             for (int z = lane; z < P.L; z += kLatLanes) {
@@ -704,21 +737,23 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2)
                     if (nb[j] >= 0) ax += band[(j + 1) * R + k] * x[base + nb[j]];
                 if (z > 0) ax += band[4 * R + k] * x[k - Tp];
                 if (z < P.L - 1) ax += band[5 * R + k] * x[k + Tp];
-                const double rk = b[k] - ax;
-                r[k] = rk;
-                if (rv) {
-                    // FP32 copies rounded on the integer pipe (bit-identical to the cast)
-                    const V rc = sizeof(V) == 4 ? (V)f32_rn(rk) : (V)rk;
-                    rv[k] = rc;
-                    rhv[k] = rc;
-                    pv[k] = 0;
-                    vv[k] = 0;
+                emit(k, b[k] - ax, with_b);
+            }
+        };
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+            if (i >= tl.start[t + 1]) continue;
+            if (zero_x) {
+                // r = b (first sweep): rows independent, unrolled so their loads overlap
+#pragma unroll 4
+                for (int z = lane; z < P.L; z += kLatLanes) {
+                    const int64_t k = (int64_t)z * Tp + i;
+                    emit(k, b[k], std::true_type{});
                 }
-                acc[0] += rk * rk;
-                if (full) {
-                    acc[1] += b[k] * b[k];
-                    acc[2] += b[k] * rk;
-                }
+            } else if (full) {
+                spmv_rows(i, std::true_type{});
+            } else {
+                spmv_rows(i, std::false_type{});
             }
         }
         double tot[3];
@@ -1534,10 +1569,10 @@ void launch_col_p(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int 
     else k_bicg_p<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, p, v, zp, ms);
 }
 
-// xh: x of an FP64 solve (members stopped at the half step update it), else null
+// xh: the solve's x (members stopped at the half step update it)
 template <typename V>
 void launch_col_s(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* r, const V* v, V* sv,
-                  V* zs, const MScal* ms, double* xh, const V* zp) {
+                  V* zs, const MScal* ms, V* xh, const V* zp) {
     const ColGeom G = kColGeom[gi];
     const int grid = col_grid<V>(c, tl, gi, false);
     const size_t smem = (size_t)c.P.L * G.W * sizeof(V);
@@ -1546,14 +1581,6 @@ void launch_col_s(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int 
     else k_bicg_s<V, 4><<<grid, 4 * G.W, smem, s>>>(op, tl, G.W, r, v, sv, zs, ms, xh, zp);
 }
 
-// x of an FP64 solve for the half-step exit, null for the FP32 inner solve
-template <typename X>
-double* half_x(X* x) {
-    if constexpr (sizeof(X) == 8)
-        return x;
-    else
-        return nullptr;
-}
 
 template <typename V, bool WRITE_W>
 static void launch_neu_step(Ctx& c, cudaStream_t s, const Op<V>& op, const Tiles& tl, int gi, const V* u,
@@ -1660,7 +1687,7 @@ int bicgstab_iterations(Ctx& c, cudaStream_t s, MScal* ms, Scalars* sc, X* x, V*
             // the target only, is not counted)
             prof_end(c, s, PBSM3D_K_BICG_V, rows * (4 + kLatRow<V>) * sv_ + act * (12 + kLatFace<V>));
             prof_begin(c, s);
-            launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms, half_x(x), zp);
+            launch_col_s<V>(c, s, op, tl, gi, r, v, sv, neumann_first(c, zs, nz), ms, x, zp);
             prof_end(c, s, PBSM3D_K_BICG_S, rows * (7 + (op.nu ? 1 : 0)) * sv_);
             const V* us = launch_neumann<V>(c, s, op, tl, gi, sv, zs, nw, nz, ms, rows, true);
             prof_begin(c, s);
@@ -1845,13 +1872,19 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
         const int gr = std::max(1, std::min(c.grid_red[0], tl.nact));
         const int gq = std::max(1, std::min(c.grid_res, tl.nact));
         prof_begin(c, s);
+        const int x0_zero = c.cfg.warm_start == PBSM3D_X0_ZERO ? 1 : 0;
         if (c.P.mixed)
             k_residual<float><<<gq, kBlock * kLatLanes, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
-                                                    c.p32, c.v32, c.msR, part, sweeps == 0, nullptr);
+                                                    c.p32, c.v32, c.msR, part, sweeps == 0, nullptr, x0_zero);
         else
             k_residual<double><<<gq, kBlock * kLatLanes, 0, s>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh,
-                                                     c.p, c.v, c.msR, part, sweeps == 0, nullptr);
-        prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 88 : 96) + act * 12);
+                                                     c.p, c.v, c.msR, part, sweeps == 0, nullptr, x0_zero);
+        // b, r and the Krylov vectors' resets; the bands, x and the ids
+        // unless r = b (the first sweep of a zero start)
+        if (sweeps == 0 && x0_zero)
+            prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 32 : 40));
+        else
+            prof_end(c, s, PBSM3D_K_RESIDUAL, act * c.P.L * (c.P.mixed ? 88 : 96) + act * 12);
         int rc = read_members(c, s, c.msR);
         if (rc) return rc;
         if (sweeps == 0) {
@@ -1928,8 +1961,8 @@ int solve_suspension(Ctx& c, cudaStream_t s, pbsm3d_stats* st) {
                 q.target2 = itol * itol * rr;
             } else {
                 q.target2 = tol * tol * bb;  // relative to ||b_m||
-                q.half = half_window(rr, q.target2);
             }
+            q.half = half_window(rr, q.target2);
             q.done = conv[m] || rr == 0.0 ? DONE_CONVERGED : DONE_NO;
             ndone += q.done ? 1 : 0;
             init[m] = q;
@@ -2533,8 +2566,8 @@ __global__ void k_ctl_outer(StepCtl* ctl, MScal* msR, MScal* ms, Scalars* sc, Ti
             q.target2 = itol * itol * rr;
         } else {
             q.target2 = tol * tol * bb;
-            q.half = half_window(rr, q.target2);
         }
+        q.half = half_window(rr, q.target2);
         q.done = (ctl->conv[m] || rr == 0.0) ? 1 : 0;
         if (q.done) {
             atomicAdd(&s_ndone, 1);
@@ -2881,7 +2914,7 @@ void capture_bicg_iteration(Ctx& c, cudaStream_t s, const Tiles& tl, MScal* ms, 
     launch_col_p<V>(c, s, op, tl, c.geom, r, p, v, neumann_first(c, zp, nz), ms);
     const V* up = launch_neumann<V>(c, s, op, tl, c.geom, p, zp, nw, nz, ms, 0, false);
     k_bicg_v<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, up, zp, v, rh, r, ms, sc, part);
-    launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms, half_x(x), zp);
+    launch_col_s<V>(c, s, op, tl, c.geom, r, v, sv, neumann_first(c, zs, nz), ms, x, zp);
     const V* us = launch_neumann<V>(c, s, op, tl, c.geom, sv, zs, nw, nz, ms, 0, false);
     k_bicg_t2<V><<<gl, kBlock * kLatLanes, 0, s>>>(op, tl, us, zs, tv, sv, ms, part);
     k_bicg_x<V, X><<<gr, kBlock, 0, s>>>(c.P.Tp, c.P.L, tl, x, zp, zs, sv, tv, r, rh, ms, sc, part);
@@ -2897,6 +2930,7 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
     double* part = c.tile_part;
     const bool mixed = c.P.mixed;
     const int warm = c.cfg.warm_start != PBSM3D_X0_ZERO && !(c.cfg.warm_flags & 1);
+    const int x0_zero = c.cfg.warm_start == PBSM3D_X0_ZERO ? 1 : 0;
     MScal* ms = mixed ? c.ms1 : c.ms0;
     Scalars* sc = mixed ? c.sc + 1 : c.sc;
     const int start_kernels = (c.cfg.warm_start == PBSM3D_X0_LEARNED ? ((c.cfg.warm_flags & 2) ? 1 : 2) : 0) +
@@ -2908,10 +2942,10 @@ int capture_suspension(Ctx& c, StepGraph& G, const Handles& h, int depth, const 
         cudaStream_t t = G.cap[depth + 1];
         if (mixed)
             k_residual<float><<<gq, kBlock * kLatLanes, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r32, c.rh32,
-                                                    c.p32, c.v32, c.msR, part, 1, &G.ctl->sweep);
+                                                    c.p32, c.v32, c.msR, part, 1, &G.ctl->sweep, x0_zero);
         else
             k_residual<double><<<gq, kBlock * kLatLanes, 0, t>>>(c.P, tl, c.A.band, c.F.nbr, c.A.x, c.A.rhs, c.r, c.r, c.rh, c.p,
-                                                     c.v, c.msR, part, 1, &G.ctl->sweep);
+                                                     c.v, c.msR, part, 1, &G.ctl->sweep, x0_zero);
         if (warm) {
             CondBody wb;
             if (wb.begin(t, G.cap[depth + 2], h.h[H_WARM], cudaGraphCondTypeIf)) return 1;

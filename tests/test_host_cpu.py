@@ -341,3 +341,29 @@ def test_bicgstab_half_step_test():
         if r @ r <= tol * tol * bb:
             break
     assert r @ r <= tol * tol * bb and halves >= 5
+
+
+def test_half_step_norm_of_fp32_vectors():
+    """Why the mixed form's FP32 inner solve has no half-step test: near its
+    target of ~1e-8 ||r||^2, ||r - alpha v||^2 from FP32 sums of (r, r),
+    (r, v), (v, v) is off by more than its own size.  FP64 sums of the same
+    FP32 vectors (each FP32 product is exact there) would resolve it, but
+    cost the FP32 lateral kernel FP64 operations in nearly every iteration
+    (measured: the step 3% slower)."""
+    rng = np.random.default_rng(4)
+    n = 1 << 20
+    r = rng.standard_normal(n).astype(np.float32)
+    alpha = 0.37
+    v = ((r + (1e-4 * rng.standard_normal(n)).astype(np.float32)) / np.float32(alpha)).astype(np.float32)
+    r64, v64 = r.astype(np.float64), v.astype(np.float64)
+    exact = float(((r64 - alpha * v64) ** 2).sum())
+    rr = float(r64 @ r64)
+    assert 1e-9 * rr < exact < 1e-7 * rr
+    s2 = rr - 2.0 * alpha * float(r64 @ v64) + alpha * alpha * float(v64 @ v64)
+    assert abs(s2 - exact) <= 1e-4 * exact
+    # the same difference from FP32 sums (numpy's pairwise ones, more
+    # accurate than a thread's running sum) misses it by more than its size
+    rr32 = float(np.sum(r * r, dtype=np.float32))
+    s2_32 = rr32 - 2.0 * alpha * float(np.sum(r * v, dtype=np.float32)) + \
+        alpha * alpha * float(np.sum(v * v, dtype=np.float32))
+    assert abs(s2_32 - exact) > exact
