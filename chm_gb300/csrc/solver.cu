@@ -466,11 +466,12 @@ __global__ void __launch_bounds__(kBlock * LC, (LC == 1 ? 6 : LC == 2 ? 2 : 1))
 // launch geometry is fixed (it decides the order of the dot products' sums).
 constexpr int kLatLanes = 2;
 
-// y = u + N z for layers lane, lane + LC, ... of the column of face i; add(k,
-// y_k) folds each row into the caller's dot products
-template <typename V, int LC, typename Add>
+// y = u + N z for layers lane, lane + LC, ... of the column of face i, with
+// (a, y); NT = 2: and (y, y); NT = 3: and (b, y), (y, y)
+template <typename V, int NT, int LC>
 __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int lane, const V* __restrict__ u,
-                                              const V* __restrict__ zz, V* __restrict__ y, Add&& add) {
+                                              const V* __restrict__ zz, V* __restrict__ y, const V* __restrict__ a,
+                                              const V* __restrict__ b, V (&acc)[3]) {
     const int32_t n0 = op.nbr[i], n1 = op.nbr[op.Tp + i], n2 = op.nbr[2 * op.Tp + i];
     const LatFace<V> lf(op, i);
     // layers are independent here: unrolled so their loads overlap
@@ -485,13 +486,18 @@ __device__ __forceinline__ void lateral_apply(const Op<V>& op, int64_t i, int la
         if (n1 >= 0) yk += la[1] * zz[base + n1];
         if (n2 >= 0) yk += la[2] * zz[base + n2];
         y[k] = yk;
-        add(k, yk);
+        acc[0] += a[k] * yk;
+        if (NT == 2) acc[1] += yk * yk;
+        if (NT == 3) {
+            acc[1] += b[k] * yk;
+            acc[2] += yk * yk;
+        }
     }
 }
 
-// The half-step norm is a difference of terms of the size of ||r||^2 (FP64
-// sums, relative error ~1e-14): below this ratio of the target to ||r||^2 it
-// could misjudge the target, and the test is left to the full step.
+// Below this ratio of the target to ||r||^2 the half-step norm, a difference
+// of terms of the size of ||r||^2 (FP64 sums, relative error ~1e-14), could
+// misjudge the target; the test is then left to the full step.
 constexpr double kHalfTestFloor = 1e-11;
 // The half-step iterate x + alpha zp lacks the iteration's minimal-residual
 // step, and a stop just under the target leaves more error than the full
@@ -499,8 +505,8 @@ constexpr double kHalfTestFloor = 1e-11;
 // ||s|| <= 0.3 of the target (||s||^2 <= 0.09 of target2).
 constexpr double kHalfMargin2 = 0.09;
 // A half step reduces ||r||^2 by 1e-6 at most (measured 1e-2..1e-6 with the
-// polynomial preconditioner): its test (three more dot products and r read
-// in k_bicg_v) runs only once ||r||^2 is within this factor of the target.
+// polynomial preconditioner): its test (two more dot products and r read in
+// k_bicg_v) runs only once ||r||^2 is within this factor of the target.
 constexpr double kHalfWindow2 = 1e6;
 __host__ __device__ __forceinline__ int half_window(double rr, double target2) {
     return rr <= kHalfWindow2 * target2 ? 1 : 0;
@@ -521,7 +527,6 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
                                                       const V* __restrict__ rh, const V* __restrict__ r,
                                                       MScal* ms, Scalars* sc, double* part) {
     const TileRange br = block_tiles(tl);
-    const int lane = threadIdx.x / kBlock;
     for (int a = br.a0; a < br.a1;) {
         const int ts = tl.act[a], m = tl.member[ts];
         const int ae = segment_end(tl, br, a, ts, m), te = ts + (ae - a);
@@ -531,33 +536,24 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
         }
         // the member's half-step test (set before the launch: the same in
         // every block of the member)
-        bool test = false;
-        if constexpr (sizeof(V) == 8) test = ms[m].half;
+        const bool test = sizeof(V) == 8 && ms[m].half;
+        V acc[3] = {0, 0, 0};
+        for (int t = ts; t < te; ++t) {
+            const int64_t i = tl.start[t] + threadIdx.x % kBlock;
+            if (i >= tl.start[t + 1]) continue;
+            if (test)
+                lateral_apply<V, 3, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, r, acc);
+            else
+                lateral_apply<V, 1, kLatLanes>(op, i, threadIdx.x / kBlock, p, zp, v, rh, nullptr, acc);
+        }
         double tot[3] = {0, 0, 0};
-        bool last = false;
+        bool last;
         if (test) {
-            if constexpr (sizeof(V) == 8) {
-                V d[3] = {0, 0, 0};
-                for (int t = ts; t < te; ++t) {
-                    const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-                    if (i < tl.start[t + 1])
-                        lateral_apply<V, kLatLanes>(op, i, lane, p, zp, v, [&](int64_t k, V yk) {
-                            d[0] += rh[k] * yk;
-                            d[1] += r[k] * yk;
-                            d[2] += yk * yk;
-                        });
-                }
-                last = member_totals<3>(d, part, tl, ts, te, m, ms, tot);
-            }
+            last = member_totals<3>(acc, part, tl, ts, te, m, ms, tot);
         } else {
-            V acc[1] = {0};
-            for (int t = ts; t < te; ++t) {
-                const int64_t i = tl.start[t] + threadIdx.x % kBlock;
-                if (i < tl.start[t + 1])
-                    lateral_apply<V, kLatLanes>(op, i, lane, p, zp, v, [&](int64_t k, V yk) { acc[0] += rh[k] * yk; });
-            }
+            V a1[1] = {acc[0]};
             double t1[1];
-            last = member_totals<1>(acc, part, tl, ts, te, m, ms, t1);
+            last = member_totals<1>(a1, part, tl, ts, te, m, ms, t1);
             tot[0] = t1[0];
         }
         if (last && threadIdx.x == 0) {
@@ -569,8 +565,7 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
                 const double alpha = q.rho / rv;
                 q.alpha = alpha;
                 if (test) {
-                    // ||r||^2: the member's own (rho on a sweep's first
-                    // iteration, where rhat = r)
+                    // ||r||^2: rho itself on a sweep's first iteration (rhat = r)
                     const double rr = q.iter == 0 ? q.rho : q.rnorm2;
                     const double s2 = rr - 2.0 * alpha * tot[1] + alpha * alpha * tot[2];
                     if (q.target2 >= kHalfTestFloor * rr && s2 <= kHalfMargin2 * q.target2) {
@@ -605,17 +600,15 @@ __global__ void __launch_bounds__(kBlock * kLatLanes, kLatLanes == 1 ? 5 : 2) k_
             a = ae;
             continue;
         }
-        V acc[2] = {0, 0};
+        V acc[3] = {0, 0, 0};
         for (int t = ts; t < te; ++t) {
             const int64_t i = tl.start[t] + threadIdx.x % kBlock;
             if (i < tl.start[t + 1])
-                lateral_apply<V, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, [&](int64_t k, V yk) {
-                    acc[0] += s[k] * yk;
-                    acc[1] += yk * yk;
-                });
+                lateral_apply<V, 2, kLatLanes>(op, i, threadIdx.x / kBlock, u, zs, tv, s, nullptr, acc);
         }
+        V a2[2] = {acc[0], acc[1]};
         double tot[2];
-        if (member_totals<2>(acc, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
+        if (member_totals<2>(a2, part, tl, ts, te, m, ms, tot) && threadIdx.x == 0)
             ms[m].omega = tot[1] > 0 ? tot[0] / tot[1] : 0.0;
         a = ae;
     }
