@@ -247,8 +247,8 @@ typedef struct pbsm3d_outputs {
 typedef struct pbsm3d_stats {
     int32_t suspension_present;  /* ||b_susp||_inf > 1e-12 (PBSM3D.cpp:1424-1427) */
     int32_t deposition_present;  /* suspension_present && ||b_dep||_inf > 1e-12 */
-    int32_t susp_iters;          /* Krylov iterations (matrix-vector products / 2 for BiCGStab) */
-    int32_t susp_matvecs;        /* operator applications, all precisions */
+    int32_t susp_iters;          /* BiCGStab iterations; one that stops at its half step counts as one */
+    int32_t susp_matvecs;        /* operator applications, all precisions (every iteration counted whole) */
     int32_t susp_refinements;    /* MIXED: FP64 refinement sweeps */
     int32_t dep_iters;
     double susp_rel_residual;    /* final ||b-Ax||/||b|| in FP64 */
